@@ -1,0 +1,365 @@
+"""Benchmark: permutations per second of the GLM + TFCE null-distribution path.
+
+Workload (the headline configuration): two icosphere-L7 hemispheres
+(2 x 163,842 = 327,684 vertices, triangle-edge adjacency), n = 350 subjects,
+k = 5 regressors (intercept, group, age, sex, covariate), 4 contrasts x (+,-)
+x 2 hemispheres = 16 TFCE sweeps per permutation, H = 2, E = 1.  A step is one
+batch of P permutations: one glm_tstat launch and one tfce_sweep_batch launch.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--batch P]
+  python bench.py --impl reference ...   # the reference's CPU algorithm (oracle port)
+
+Prints one JSON line.  Under torchrun each rank takes a disjoint permutation
+range (no data-path collective) and rank 0 reports the whole-job rate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "perm/s at 327,684 vertices x 350 subj"
+WORKLOAD = "config2: 2 x icosphere-L7 (327,684 vertices), n=350, k=5, 4 contrasts x +/- x 2 hemispheres, H=2 E=1"
+SEED = 2
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def profile_traffic(kernel):
+    """dram bytes per launch recorded in profiles/<kernel>*.md (line
+    'dram_bytes_per_launch: <int> (<launch description>)') or None."""
+    d = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(d):
+        return None, None
+    for f in sorted(os.listdir(d)):
+        if f.startswith(kernel) and f.endswith(".md"):
+            m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)\s*\(([^)]*)\)", open(os.path.join(d, f)).read())
+            if m:
+                return float(m.group(1)), m.group(2)
+    return None, None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thr = threading.Thread(target=self._read, daemon=True)
+            self.thr.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            parts = [p.strip() for p in l.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ---------------------------------------------------------------------------
+# CPU side: the reference's algorithm (oracle port), one permutation per task
+# ---------------------------------------------------------------------------
+_W = {}
+
+
+def _cpu_init(study_args):
+    from tfce_mediation_gb300 import synth
+    st = synth.config2(**study_args)
+    _W["st"] = st
+    from oracle import oracle
+    oracle.lib()
+
+
+def _cpu_perm(p):
+    """One permutation as the reference computes it: FP64 tval_int
+    (cynumstats.pyx:59-64, chunked over vertices) then, per contrast and sign,
+    the sweep of each hemisphere scaled by max/100 and reduced
+    (pyfunc.py:107-119)."""
+    from oracle import oracle
+    st = _W["st"]
+    X = st.design()[np.random.RandomState(SEED + p).permutation(st.n)]
+    n, k = X.shape
+    invXX = np.linalg.inv(X.T @ X)
+    t = np.empty((k, st.V), np.float32)
+    for v0 in range(0, st.V, 32768):
+        y = st.Y[:, v0:v0 + 32768]
+        t[:, v0:v0 + 32768] = oracle.tval_int_ref(X, invXX, y, n, k)
+    out = []
+    for c in range(1, k):
+        for s in (1.0, -1.0):
+            best = -np.inf
+            for h in range(2):
+                a, b = st.segments[h], st.segments[h + 1]
+                off = st.offsets[a:b + 1] - st.offsets[a]
+                idx = st.indices[st.offsets[a]:st.offsets[b]] - a
+                best = max(best, oracle.tfce_max_batch(off, idx, t[c, a:b], 2.0, 1.0, sign=s,
+                                                       floor_zero=True)[0])
+            out.append(best)
+    return out
+
+
+def cpu_rate(n_perm, cores, study_args):
+    """perm/s of the oracle port over n_perm permutations on `cores` processes."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores, initializer=_cpu_init, initargs=(study_args,)) as pool:
+        pool.map(_cpu_perm, range(10_000, 10_000 + cores))  # warm: data built, libs loaded
+        t0 = time.perf_counter()
+        pool.map(_cpu_perm, range(n_perm))
+        dt = time.perf_counter() - t0
+    return n_perm / dt, dt
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    study_args = {"n": args.n, "level": args.level}
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores, initializer=_cpu_init, initargs=(study_args,)) as pool:
+        for w in range(args.warmup):
+            pool.map(_cpu_perm, range(10_000 + w * cores, 10_000 + (w + 1) * cores))
+        times = []
+        for s in range(args.steps):
+            t0 = time.perf_counter()
+            pool.map(_cpu_perm, range(s * cores, (s + 1) * cores))
+            times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = args.steps * cores / total
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "perm/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64/f32",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "perms_per_step": cores,
+                       "note": "oracle port of the reference CPU path (FP64 tval_int + C restatement of "
+                               "fast_tfce.hpp), one process per host core"},
+            "cpu_baseline": {"value": value, "unit": "perm/s", "cores": cores, "kind": "port",
+                             "sample": f"{args.steps} steps x {cores} permutations (one per process)"},
+            "e2e": {"value": value, "unit": "perm/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU side
+# ---------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+
+    from tfce_mediation_gb300 import engine as E
+    from tfce_mediation_gb300 import synth
+    from tfce_mediation_gb300.glm import DesignBatch
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    t_gen = time.perf_counter()
+    st = synth.config2(n=args.n, level=args.level)
+    gen_s = time.perf_counter() - t_gen
+    P = args.batch
+    eng = E.PermutationEngine(st.Y, st.pred_x, (st.offsets, st.indices), st.segments, 2.0, 1.0,
+                              batch=P, floor_zero=True)
+    C, S, V, n = eng.C, eng.n_seg, eng.V, eng.n
+    total_steps = args.warmup + args.steps
+    # disjoint permutation ranges per rank
+    base = rank * total_steps * P
+    perms = [E.permutations(n, SEED, base + s * P, base + (s + 1) * P) for s in range(total_steps)]
+    # device-resident design operators (inputs resident before the timed region)
+    ops = [DesignBatch(eng.X[p]).to_device() for p in perms]
+    out_max = torch.empty((total_steps, P, C, 2, S), device="cuda")
+    stream = torch.cuda.current_stream()
+    lib = eng.lib
+    from tfce_mediation_gb300 import _lib
+    from tfce_mediation_gb300.device import ptr
+
+    def step(s, ev=None):
+        pinv, Xp, invd, dof = ops[s]
+        if ev is not None:
+            ev[0].record(stream)
+        _lib.check(lib.glm_tstat(ptr(eng.Yd), V, n, V, ptr(pinv), ptr(Xp), ptr(invd), ptr(dof), P, eng.k,
+                                 ptr(eng._coef), C, ptr(eng._tbuf), V, stream.cuda_stream))
+        if ev is not None:
+            ev[1].record(stream)
+        eng.adj.sweep_batch(ptr(eng._tbuf), V, P * C, 2, None, 1, ptr(out_max[s]), None, 0,
+                            stream.cuda_stream)
+        if ev is not None:
+            ev[2].record(stream)
+
+    for s in range(args.warmup):
+        step(s)
+    torch.cuda.synchronize()
+    eng.adj.status()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        start.record(stream)
+        for s in range(args.steps):
+            step(args.warmup + s, evs[s])
+        stop.record(stream)
+        torch.cuda.synchronize()
+    eng.adj.status()
+    ms = start.elapsed_time(stop)
+    glm_ms = [e[0].elapsed_time(e[1]) for e in evs]
+    sweep_ms = [e[1].elapsed_time(e[2]) for e in evs]
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    perms_total = args.steps * P * ws
+    value = perms_total / (ms / 1000.0)
+
+    # e2e through the public API from host buffers: Y (pinned) up, permutations
+    # generated and design operators formed on the host, maxima down
+    Yh = torch.from_numpy(st.Y).pin_memory()
+    e2e_steps = max(1, min(args.steps, 3))
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for s in range(e2e_steps):
+        eng.Yd.copy_(Yh, non_blocking=True)
+        pr = E.permutations(n, SEED, 10 ** 6 + base + s * P, 10 ** 6 + base + (s + 1) * P)
+        res = eng.run_batch(pr)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0)
+    e2e_value = e2e_steps * P * ws / e2e_s
+    h2d = st.Y.nbytes + P * (2 * eng.k * n + eng.k + 1) * 4
+    d2h = P * C * 2 * S * 4
+
+    if rank != 0:
+        dist.destroy_process_group() if ws > 1 else None
+        return
+    hbm, bf16, peak_kind = measured_peaks()
+    # dominant kernel: the sweep.  Algorithmic bytes per sweep: statistic 4V +
+    # CSR offsets 4(V+1) + CSR entries 4D (per hemisphere).
+    Vh = int(st.segments[1] - st.segments[0])
+    Dh = int(st.offsets[st.segments[1]] - st.offsets[st.segments[0]])
+    bytes_per_sweep = 4 * Vh + 4 * (Vh + 1) + 4 * Dh
+    sweeps_per_launch = P * C * 2 * S
+    sweep_avg = float(np.mean(sweep_ms))
+    glm_avg = float(np.mean(glm_ms))
+    achieved = bytes_per_sweep * sweeps_per_launch / (sweep_avg / 1000) / 1e9
+    traffic, traffic_note = profile_traffic("tfce_sweep")
+    glm_flop = 4.0 * n * eng.k * V * P  # beta + residual passes, fp32 CUDA cores
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": "perm/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "perms_per_step": P, "sweeps_per_step": sweeps_per_launch,
+                   "l2": "inputs larger than L2 (Y 459 MB, t maps %d MB per step)" % (P * C * V * 4 // 2 ** 20),
+                   "parallelism": f"replicas over permutation ranges x{ws}",
+                   "data_gen_s": round(gen_s, 1)},
+        "e2e": {"value": e2e_value, "unit": "perm/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
+        "gpu_launches": 2 * args.steps,
+        "roofline": {"bound": "hbm", "kernel": "tfce_sweep_kernel", "achieved": achieved, "peak": hbm,
+                     "unit": "GB/s", "frac": achieved / hbm, "peak_source": f"{peak_kind} hbm_gbs",
+                     "traffic": traffic, "traffic_note": traffic_note,
+                     "algorithmic_bytes_per_launch": bytes_per_sweep * sweeps_per_launch,
+                     "ms_per_launch": sweep_avg,
+                     "vertex_sweeps_per_s": sweeps_per_launch * Vh / (sweep_avg / 1000)},
+        "kernels_ms_per_step": {"glm_tstat": glm_avg, "tfce_sweep": sweep_avg},
+        "glm": {"achieved_tflops_fp32": glm_flop / (glm_avg / 1000) / 1e12, "unit": "TFLOP/s"},
+        "clocks": clocks,
+    }
+    if not args.no_cpu_baseline:
+        cores = 1
+        v, dt = cpu_rate(args.cpu_perms, cores, {"n": args.n, "level": args.level})
+        line["cpu_baseline"] = {"value": v, "unit": "perm/s", "cores": cores, "kind": "port",
+                                "sample": f"{args.cpu_perms} permutations of the same workload, "
+                                          f"{dt:.1f} s, single process"}
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=64)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=350)
+    ap.add_argument("--level", type=int, default=7)
+    ap.add_argument("--cpu-perms", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,171 @@
+/*
+ * tfce_gb300.h -- C-ABI of the GB300 permutation-inference path.
+ *
+ * Plain pointers and sizes only.  "Host" arguments are ordinary host memory;
+ * "device" arguments are CUDA device pointers on the current device; `stream`
+ * is a cudaStream_t passed as void* (NULL = legacy default stream).  Every
+ * entry point returns a tfce_status; tfce_last_error() gives the message of the
+ * last failure on the calling thread.
+ *
+ * Reference interfaces replaced (paths inside trislett/TFCE_mediation):
+ *   CreateAdjSet.__init__  tfce_mediation/tfce.pyx:30-42   -> tfce_adjset_create
+ *   CreateAdjSet.run       tfce_mediation/tfce.pyx:44-45   -> tfce_adjset_run
+ *     (the sweep itself:   tfce_mediation/lib/fast_tfce.hpp:11-95)
+ *   write_perm_maxTFCE_vertex / _voxel  tfce_mediation/pyfunc.py:107-126,
+ *   write_vertStat_img / write_voxelStat_img  tfce_mediation/pyfunc.py:80-103,
+ *   tm_func.calculate_tfce / low_ram_calculate_tfce  tfce_mediation/tm_func.py:54-185
+ *                                                     -> tfce_sweep_batch
+ *   tval_int + se_of_slope  tfce_mediation/cynumstats.pyx:47-64,
+ *   calc_beta_se            tfce_mediation/cynumstats.pyx:66-74  -> glm_tstat
+ *   calc_sobelz / calc_indirect  tfce_mediation/pyfunc.py:130-162,2678-2709
+ *                                                     -> sobel_combine
+ *   calculate_fweP_vertex.find_nearest  tfce_mediation/tmanalysis/calculate_fweP_vertex.py:37-69,
+ *   calculate_fweP_voxel.find_nearest   tfce_mediation/tmanalysis/calculate_fweP_voxel.py:23-49,
+ *   tm_func.find_nearest                tfce_mediation/tm_func.py:566-573
+ *                                                     -> fwer_sort, fwer_lookup
+ */
+#ifndef TFCE_GB300_H_
+#define TFCE_GB300_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  TFCE_OK = 0,
+  TFCE_EINVAL = 1,    /* bad argument (null pointer, size, adjacency index)  */
+  TFCE_EDEVICE = 2,   /* CUDA runtime error                                    */
+  TFCE_ETIMEOUT = 3,  /* a bounded device loop hit its iteration limit         */
+  TFCE_ENOMEM = 4,    /* device allocation failed                              */
+  TFCE_ERANGE = 5     /* more thresholds than the sweep supports (maxT ~ 0)    */
+} tfce_status;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int tfce_version(void);
+/* Message of the last failure on this thread ("" if none). */
+const char* tfce_last_error(void);
+
+/* ---------------------------------------------------------------------------
+ * Adjacency sets.  A handle owns a device CSR over V vertices, optionally cut
+ * into segments (hemispheres, surfaces of a multisurface study).  Entry b in
+ * the list of a means "a is adjacent to b" exactly as the reference's
+ * adjacencyList[a] (tfce_mediation/tfce.pyx:30-42).  Entries that point
+ * outside [0, V) are rejected; self entries are dropped (the reference never
+ * unions a vertex with itself); entries whose reverse is missing are marked so
+ * the sweep applies the reference's insertion-order rule to them.
+ * ------------------------------------------------------------------------- */
+typedef struct tfce_adjset tfce_adjset;
+
+/* Host CSR (offsets[V+1], indices[offsets[V]]).  Segments: seg_offsets
+ * [n_seg+1] with seg_offsets[0] = 0, seg_offsets[n_seg] = V, or NULL for one
+ * segment; adjacency must not cross segments.  H, E: per-segment TFCE
+ * parameters (arrays of n_seg), as CreateAdjSet(H, E, adjacency) stores them. */
+int tfce_adjset_create(const int64_t* offsets, const int32_t* indices, int32_t n_vertices,
+                       const int64_t* seg_offsets, int32_t n_seg, const float* H,
+                       const float* E, tfce_adjset** out);
+void tfce_adjset_destroy(tfce_adjset* h);
+/* Replace the per-segment H/E (host arrays of n_seg). */
+int tfce_adjset_set_params(tfce_adjset* h, const float* H, const float* E);
+/* 1 if every entry has its reverse (the usual triangle-mesh / 26-neighbour
+ * case), 0 otherwise. */
+int tfce_adjset_is_symmetric(const tfce_adjset* h);
+
+/* CreateAdjSet.run(image, enhn) on host float32 arrays of length V (one
+ * segment: the whole handle).  Accumulates the sweep into enhn, as
+ * fast_tfce.hpp:82 does.  Synchronous. */
+int tfce_adjset_run(tfce_adjset* h, const float* image, float* enhn, int32_t n_vertices);
+
+/* Debug sweep of one host map through the device kernel, recording per
+ * threshold the component label (root vertex id, -1 inactive) and extent of
+ * every vertex: labels/extents are host arrays of max_steps*V; *n_steps gets
+ * the number of thresholds.  One segment handles only.  Synchronous. */
+int tfce_adjset_run_labels(tfce_adjset* h, const float* image, float* enhn, int32_t n_vertices,
+                           int32_t* labels, int32_t* extents, int32_t max_steps,
+                           int32_t* n_steps);
+
+/* Batched sweep (device pointers, stream-ordered).
+ *   stats     [n_maps][map_stride] floats, the statistic of every map laid out
+ *             over the handle's V vertices (segment s = [seg_off[s], seg_off[s+1]));
+ *   signs     1 = (+), 2 = (+,-) : every map is swept as +stat and, with 2, as -stat;
+ *   vdensity  [V] per-vertex weight or NULL (weight 1);
+ *   floor_zero nonzero: each segment's maximum is taken as at least 0, as when
+ *             a masked statistic is scattered into a zero-filled surface;
+ *   out_max   [n_maps][signs][n_seg]: max over the segment of
+ *             TFCE * (segment max / 100) * vdensity (pyfunc.py:116-118);
+ *   out_maps  [n_maps][signs][V] or NULL; out_mode 1 writes the scaled map,
+ *             out_mode 2 adds the raw sweep into out_maps (enhn semantics).
+ * Uses a device workspace that the handle grows on demand. */
+int tfce_sweep_batch(tfce_adjset* h, const float* stats, int64_t map_stride, int32_t n_maps,
+                     int32_t signs, const float* vdensity, int32_t floor_zero, float* out_max,
+                     float* out_maps, int32_t out_mode, void* stream);
+/* Synchronises `stream`, then returns (and clears) the device error word that
+ * the batched sweeps queued on this handle since the last call have set:
+ * TFCE_EINVAL (entry outside its segment), TFCE_ETIMEOUT (iteration limit),
+ * TFCE_ERANGE (threshold table overflow). */
+int tfce_sweep_status(tfce_adjset* h, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Mass-univariate OLS t for G designs against one data matrix (device).
+ *   Y       [n][ldy] float32, subjects x vertices (merge_y layout), V columns used;
+ *   pinv    [G][kmax][n]  rows of inv(X'X)X' (rows >= k_g zero), float32;
+ *   X       [G][n][kmax]  the (permuted) design, columns >= k_g zero;
+ *   invdiag [G][kmax]     diag(inv(X'X));
+ *   dof     [G]           n - k_g;
+ *   coef    [n_coef]      coefficient indices written for every design;
+ *   t_out   [G][n_coef][ldt].
+ * beta = pinv.y, RSS from the residuals y - X.beta (never from Y'Y),
+ * se = sqrt(RSS/dof * invdiag), t = beta / se  (cynumstats.pyx:28-29,47-64). */
+int glm_tstat(const float* Y, int64_t ldy, int32_t n, int64_t V, const float* pinv,
+              const float* X, const float* invdiag, const float* dof, int32_t G, int32_t kmax,
+              const int32_t* coef, int32_t n_coef, float* t_out, int64_t ldt, void* stream);
+
+/* The same fit with another output (`what`), for the one-off helpers of
+ * tfce_mediation/cynumstats.pyx:
+ *   0 t [G][n_coef][ldo]          (tval_int, :59-64)
+ *   1 beta [G][n_coef][ldo]       (cy_lin_lstsqr_mat, :28-29; calc_beta_se, :66-74)
+ *   2 se [G][n_coef][ldo]         (se_of_slope, :47-52)
+ *   3 residuals [G][n][ldo]       (resid_covars, :54-57)
+ *   4 F [G][ldo], k_g = n - dof_g, TSS about each column's mean
+ *                                 (glm_fstat gives the reference's centring)
+ *   5 RSS [G][ldo]                (cy_lin_lstsqr_mat_residual, :109-112)
+ * coef/invdiag may be NULL where the output does not use them. */
+int glm_stat(const float* Y, int64_t ldy, int32_t n, int64_t V, const float* pinv,
+             const float* X, const float* invdiag, const float* dof, int32_t G, int32_t kmax,
+             const int32_t* coef, int32_t n_coef, int32_t what, float* out, int64_t ldo,
+             void* stream);
+
+/* Model F as calcF computes it (tfce_mediation/cynumstats.pyx:31-36):
+ * ((TSS - RSS)/(k_g-1)) / (RSS/dof_g) with TSS taken around *centre (a device
+ * float; the reference centres on np.mean(y), the grand mean of the whole
+ * matrix), or around each column's mean when centre is NULL.  f_out [G][ldf]. */
+int glm_fstat(const float* Y, int64_t ldy, int32_t n, int64_t V, const float* pinv,
+              const float* X, const float* dof, int32_t G, int32_t kmax, const float* centre,
+              float* f_out, int64_t ldf, void* stream);
+
+/* Indirect-effect z from path t values (device), z[p][v] for p < P:
+ *   ta [P][lda] (or ta_scalar[P] when ta is NULL: medtype Y's linregress path),
+ *   tb [P][ldb];  alg 0 = Aroian, 1 = Sobel, 2 = Goodman (pyfunc.py:146-161). */
+int sobel_combine(const float* ta, int64_t lda, const float* ta_scalar, const float* tb,
+                  int64_t ldb, int32_t P, int64_t V, int32_t alg, float* z, int64_t ldz,
+                  void* stream);
+
+/* ---------------------------------------------------------------------------
+ * FWER.  fwer_sort sorts n doubles ascending in place (device).  fwer_lookup
+ * maps every value of an image through the sorted null of length N (the
+ * reference reads its null back from CSV text as float64):
+ *   mode 0 (calculate_fweP_*): 1-p = max(idx-1,0)/N with idx = #{null < x},
+ *           written only where x > 0 (0 elsewhere);
+ *   mode 1 (tm_func.find_nearest): p_array of the nearer neighbour rank,
+ *           for every value.
+ * image and out are double [V] (device). */
+int fwer_sort(double* values, int64_t n, void* stream);
+int fwer_lookup(const double* sorted_null, int64_t N, const double* image, int64_t V,
+                int32_t mode, double* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TFCE_GB300_H_ */

@@ -1,0 +1,366 @@
+"""ORACLE -- test infrastructure, not product code.
+
+CPU restatement of the reference's permutation-inference path.  Each function
+cites the reference lines it follows.  Only ``tests/``, ``__graft_entry__``'s
+smoke check and ``bench.py``'s CPU-baseline leg may import this module.
+
+Pinning: ``tests/test_oracle_pin.py`` checks every function here against
+golden vectors produced by the reference itself (``tests/golden/``, made by
+``tests/golden/make_golden.py`` from the reference's compiled Cython modules
+and unmodified ``pyfunc``/``tm_func``), and -- where ``oracle/_ref`` was built
+from a reference checkout -- against the reference sweep directly.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_BUILD = os.path.join(HERE, "_build")
+_LIB = None
+_REF = None
+
+_f32p = ctypes.POINTER(ctypes.c_float)
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+
+
+# --------------------------------------------------------------------------
+# native pieces
+# --------------------------------------------------------------------------
+def build() -> str:
+    """Compile the C restatement of the sweep (gcc, -O2, no -march flags so the
+    same recipe works on x86_64 and aarch64)."""
+    os.makedirs(_BUILD, exist_ok=True)
+    so = os.path.join(_BUILD, "libtfce_oracle.so")
+    src = os.path.join(HERE, "tfce_oracle.c")
+    if not (os.path.exists(so) and os.path.getmtime(so) >= os.path.getmtime(src)):
+        tmp = so + f".{os.getpid()}.tmp"
+        subprocess.check_call(["gcc", "-O2", "-std=c11", "-shared", "-fPIC", src, "-o", tmp, "-lm"])
+        os.replace(tmp, so)
+    return so
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        l = ctypes.CDLL(build())
+        l.oracle_tfce.restype = ctypes.c_int
+        l.oracle_tfce.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_int32, _i64p, _i32p,
+                                  _f32p, _f32p, _i32p, _i32p, ctypes.c_int]
+        l.oracle_tfce_max_batch.restype = ctypes.c_int
+        l.oracle_tfce_max_batch.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_int32, _i64p,
+                                            _i32p, _f32p, ctypes.c_int32, ctypes.c_float, _f32p,
+                                            ctypes.c_int, _f32p]
+        l.oracle_threshold_table.restype = ctypes.c_int
+        l.oracle_threshold_table.argtypes = [ctypes.c_float, _f32p, ctypes.c_int]
+        _LIB = l
+    return _LIB
+
+
+def ref_lib():
+    """The reference sweep itself (oracle/_ref/libref_tfce.so), when it was
+    built from a reference checkout on this machine; otherwise None."""
+    global _REF
+    if _REF is None:
+        so = os.path.join(HERE, "_ref", "libref_tfce.so")
+        if not os.path.exists(so):
+            return None
+        try:
+            l = ctypes.CDLL(so)
+        except OSError:  # built for another architecture
+            return None
+        l.ref_tfce.restype = ctypes.c_int
+        l.ref_tfce.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_int32, _i64p, _i32p,
+                               _f32p, _f32p]
+        _REF = l
+    return _REF
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t)
+
+
+def _csr(offsets, indices):
+    return (np.ascontiguousarray(offsets, dtype=np.int64),
+            np.ascontiguousarray(indices, dtype=np.int32))
+
+
+def threshold_table(maxT: float) -> np.ndarray:
+    """T = maxT, maxT - dT, ... >= 0 with dT = maxT/100, all in float32
+    (tfce_mediation/lib/fast_tfce.hpp:32-39)."""
+    buf = np.zeros(4096, np.float32)
+    n = lib().oracle_threshold_table(ctypes.c_float(maxT), _p(buf, _f32p), 4096)
+    if n < 0:
+        raise ValueError("threshold table overflow")
+    return buf[:n].copy()
+
+
+def tfce(offsets, indices, image, H, E, enhn=None):
+    """One sweep: tfce_mediation/lib/fast_tfce.hpp:11-95 as called by
+    tfce_mediation/tfce.pyx:44-45.  Accumulates into ``enhn``."""
+    offsets, indices = _csr(offsets, indices)
+    image = np.ascontiguousarray(image, dtype=np.float32)
+    V = image.shape[0]
+    if enhn is None:
+        enhn = np.zeros(V, np.float32)
+    rc = lib().oracle_tfce(H, E, V, _p(offsets, _i64p), _p(indices, _i32p), _p(image, _f32p),
+                           _p(enhn, _f32p), None, None, -1)
+    if rc < 0:
+        raise ValueError("oracle sweep failed")
+    return enhn
+
+
+def tfce_labels(offsets, indices, image, H, E):
+    """Sweep plus per-threshold component labels (root vertex id, -1 inactive)
+    and extents; (enhn, labels[L,V], extents[L,V])."""
+    offsets, indices = _csr(offsets, indices)
+    image = np.ascontiguousarray(image, dtype=np.float32)
+    V = image.shape[0]
+    finite = image[np.isfinite(image)]
+    L = len(threshold_table(float(finite.max()))) if finite.size else 0
+    enhn = np.zeros(V, np.float32)
+    labels = np.full((max(L, 1), V), -1, np.int32)
+    extents = np.zeros((max(L, 1), V), np.int32)
+    rc = lib().oracle_tfce(H, E, V, _p(offsets, _i64p), _p(indices, _i32p), _p(image, _f32p),
+                           _p(enhn, _f32p), _p(labels, _i32p), _p(extents, _i32p), -1)
+    if rc < 0:
+        raise ValueError("oracle sweep failed")
+    return enhn, labels[:rc], extents[:rc]
+
+
+def ref_tfce(offsets, indices, image, H, E, enhn=None):
+    """The reference's own sweep (needs oracle/_ref)."""
+    l = ref_lib()
+    if l is None:
+        raise RuntimeError("reference sweep not built (oracle/build_ref.py)")
+    offsets, indices = _csr(offsets, indices)
+    image = np.ascontiguousarray(image, dtype=np.float32)
+    if enhn is None:
+        enhn = np.zeros(image.shape[0], np.float32)
+    l.ref_tfce(H, E, image.shape[0], _p(offsets, _i64p), _p(indices, _i32p), _p(image, _f32p),
+               _p(enhn, _f32p))
+    return enhn
+
+
+def tfce_max_batch(offsets, indices, maps, H, E, sign=1.0, vdensity=None, floor_zero=False):
+    """Per-map scaled max, the body of tfce_mediation/pyfunc.py:107-119 for one
+    hemisphere (TFCE * max/100 * vdensity, then max)."""
+    offsets, indices = _csr(offsets, indices)
+    maps = np.ascontiguousarray(maps, dtype=np.float32)
+    if maps.ndim == 1:
+        maps = maps[None]
+    out = np.zeros(maps.shape[0], np.float32)
+    vd = None if vdensity is None else np.ascontiguousarray(vdensity, np.float32)
+    rc = lib().oracle_tfce_max_batch(H, E, maps.shape[1], _p(offsets, _i64p), _p(indices, _i32p),
+                                     _p(maps, _f32p), maps.shape[0], sign,
+                                     None if vd is None else _p(vd, _f32p), int(floor_zero),
+                                     _p(out, _f32p))
+    if rc < 0:
+        raise ValueError("oracle sweep failed")
+    return out
+
+
+# --------------------------------------------------------------------------
+# GLM: tfce_mediation/cynumstats.pyx
+# --------------------------------------------------------------------------
+def lstsqr_mat(X, y):
+    """cy_lin_lstsqr_mat: inv(X'X) X' y in FP64 (cynumstats.pyx:28-29)."""
+    X = np.asarray(X, np.float64)
+    return (np.linalg.inv(X.T.dot(X)).dot(X.T)).dot(y)
+
+
+def tval_int_ref(X, invXX, y, n, k):
+    """tval_int with the reference's precision (cynumstats.pyx:59-64): FP64
+    betas and sigma^2, SE rounded to float32 (se_of_slope, :47-52), t = FP64
+    beta / float32 SE."""
+    a = lstsqr_mat(X, y)
+    sigma2 = np.sum((y - np.dot(X, a)) ** 2, axis=0) / (n - k)
+    se = np.sqrt(sigma2[None, :] * np.diag(invXX)[:, None]).astype(np.float32)
+    return a / se
+
+
+def tval_fp64(X, y):
+    """t for every column of X, all in FP64 (the accuracy yardstick)."""
+    X = np.asarray(X, np.float64)
+    y = np.asarray(y, np.float64)
+    n, k = X.shape
+    invXX = np.linalg.inv(X.T @ X)
+    a = invXX @ (X.T @ y)
+    r = y - X @ a
+    sigma2 = np.sum(r * r, axis=0) / (n - k)
+    return a / np.sqrt(sigma2[None, :] * np.diag(invXX)[:, None])
+
+
+def calc_beta_se(x, y, n):
+    """cynumstats.pyx:66-74: design [1, x]; returns (beta[1], se float32 k x V)."""
+    X = np.column_stack([np.ones(n), x])
+    invXX = np.linalg.inv(np.dot(X.T, X))
+    k = X.shape[1]
+    a = lstsqr_mat(X, y)
+    sigma2 = np.sum((y - np.dot(X, a)) ** 2, axis=0) / (n - k)
+    se = np.sqrt(sigma2[None, :] * np.diag(invXX)[:, None]).astype(np.float32)
+    return a[1], se
+
+
+def resid_covars(x_covars, data):
+    """cynumstats.pyx:54-57 (data is V x n, returns n x V residuals)."""
+    a_c = lstsqr_mat(x_covars, data.T)
+    return data.T - np.dot(x_covars, a_c)
+
+
+def calcF(X, y, n, k):
+    """cynumstats.pyx:31-36.  TSS is taken around np.mean(y) -- the grand mean
+    of the whole matrix, not each column's mean -- as the reference does."""
+    a = lstsqr_mat(X, y)
+    resids = y - np.dot(X, a)
+    RSS = np.sum(resids ** 2, axis=0)
+    TSS = np.sum((y - np.mean(y)) ** 2, axis=0)
+    return ((TSS - RSS) / (k - 1)) / (RSS / (n - k))
+
+
+def indirect(ta, tb, alg="aroian"):
+    """Sobel/Aroian/Goodman z from path t values (pyfunc.py:146-161,
+    pyfunc.py:2678-2709)."""
+    ta = np.asarray(ta, np.float64)
+    tb = np.asarray(tb, np.float64)
+    if alg == "aroian":
+        return 1 / np.sqrt((1 / (tb ** 2)) + (1 / (ta ** 2)) + (1 / (ta ** 2 * tb ** 2)))
+    if alg == "sobel":
+        return 1 / np.sqrt((1 / (tb ** 2)) + (1 / (ta ** 2)))
+    if alg == "goodman":
+        return 1 / np.sqrt((1 / (tb ** 2)) + (1 / (ta ** 2)) - (1 / (ta ** 2 * tb ** 2)))
+    raise ValueError(alg)
+
+
+def calc_sobelz(medtype, pred_x, depend_y, merge_y, n, alg="aroian"):
+    """pyfunc.py:130-162 (medtype 'I', 'M' or 'Y')."""
+    from scipy.stats import linregress
+    if medtype == "I":
+        a_b, a_se = calc_beta_se(pred_x, merge_y, n)
+        b_b, b_se = calc_beta_se(np.column_stack([pred_x, depend_y]), merge_y, n)
+        a_se, b_se = a_se[1], b_se[1]
+    elif medtype == "M":
+        a_b, a_se = calc_beta_se(pred_x, merge_y, n)
+        b_b, b_se = calc_beta_se(np.column_stack([depend_y, pred_x]), merge_y, n)
+        a_se, b_se = a_se[1], b_se[1]
+    elif medtype == "Y":
+        lr = linregress(pred_x, depend_y)
+        a_b, a_se = lr.slope, lr.stderr
+        b_b, b_se = calc_beta_se(np.column_stack([depend_y, pred_x]), merge_y, n)
+        b_se = b_se[1]
+    else:
+        raise ValueError(medtype)
+    return indirect(a_b / a_se, b_b / b_se, alg)
+
+
+# --------------------------------------------------------------------------
+# permutations, per-permutation max, FWER
+# --------------------------------------------------------------------------
+def permutation(n, seed, p):
+    """Host-seeded index stream, the mmr-lr convention
+    (tm_func.py:147-151): RandomState(seed + p).permutation(n)."""
+    return np.random.RandomState(seed + p).permutation(n)
+
+
+def perm_max_vertex(stat, segments, H, E, vdensity=None):
+    """pyfunc.py:107-119 without the CSV: scatter, TFCE each segment
+    (hemisphere), scale by the segment's max/100 and vdensity, max over
+    segments.  segments: list of (offsets, indices, v0, v1)."""
+    best = -np.inf
+    for (off, idx, v0, v1) in segments:
+        img = np.ascontiguousarray(stat[v0:v1], np.float32)
+        enh = tfce(off, idx, img, H, E)
+        scale = img[np.isfinite(img)].max() / np.float32(100)
+        val = enh * scale
+        if vdensity is not None:
+            val = val * vdensity[v0:v1]
+        best = max(best, float(val.max()))
+    return np.float32(best)
+
+
+def fwep_vertex(tfce_values, null):
+    """1-p(FWER) as tfce_mediation/tmanalysis/calculate_fweP_vertex.py:37-69:
+    sorted null, p_array[j] = j/N, idx = searchsorted(left),
+    1-p = p_array[idx-1] (p_array[0] when idx == 0); computed where TFCE > 0."""
+    srt = np.sort(np.asarray(null, np.float64))
+    N = srt.shape[0]
+    p_array = np.arange(N, dtype=np.float64) / N
+    v = np.asarray(tfce_values)
+    out = np.zeros(v.shape, np.float64)
+    m = v > 0
+    idx = np.searchsorted(srt, v[m], side="left")
+    out[m] = p_array[np.maximum(idx - 1, 0)]
+    return out
+
+
+def find_nearest(array, value, p_array):
+    """Nearest-rank lookup of tm_func.py:566-573 / pyfunc.py:254-261."""
+    idx = np.searchsorted(array, value, side="left")
+    if idx == len(p_array):
+        return p_array[idx - 1]
+    elif math.fabs(value - array[idx - 1]) < math.fabs(value - array[idx]):
+        return p_array[idx - 1]
+    else:
+        return p_array[idx]
+
+
+def apply_mfwer(pos_images, neg_images, perm_max, position_array, weight=None, mediation=False):
+    """tm_func.py:403-491 with the permutation CSV contents passed in memory.
+
+    pos_images/neg_images: (V_total, C) scaled TFCE images; perm_max:
+    dict {(surface, contrast): 1-D array of permutation maxima}.  Returns
+    (positive_1mp, negative_1mp)."""
+    num_contrasts = pos_images.shape[1]
+    num_surf = len(position_array) - 1
+    num_perm = min(len(v) for v in perm_max.values())
+    maxvalue_array = np.zeros((num_perm, num_contrasts))
+    temp_max = np.zeros((num_perm, num_surf))
+    positive_data = np.zeros((pos_images.shape[0], num_contrasts))
+    negative_data = np.zeros((pos_images.shape[0], num_contrasts))
+    if weight == "logmasksize":
+        x = [position_array[i + 1] - position_array[i] for i in range(num_surf)]
+        weights = (np.log(x) / np.log(x).sum()) / np.mean(np.log(x) / np.log(x).sum())
+        w_temp_max = np.zeros((num_perm, num_surf))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        for c in range(num_contrasts):
+            for s in range(num_surf):
+                lp = np.log(np.asarray(perm_max[(s, c)], np.float64)[:num_perm])
+                lp[np.isinf(lp)] = 0
+                start, end = position_array[s], position_array[s + 1]
+                imgs = [(pos_images, positive_data)] + ([] if mediation else [(neg_images, negative_data)])
+                for src, dst in imgs:
+                    vm = np.log(src[start:end, c]) > 0
+                    lt = np.log(src[start:end, c][vm])
+                    lt -= lp.mean()
+                    lt /= lp.std()
+                    lt += 10
+                    dst[start:end, c][vm] = lt
+                lp -= lp.mean()
+                lp /= lp.std()
+                if weight == "logmasksize":
+                    w = lp * weights[s]
+                    w += 10
+                    w_temp_max[:, s] = w
+                lp += 10
+                temp_max[:, s] = lp
+            if weight is not None:
+                w_temp_max[np.isnan(w_temp_max)] = 0
+                mi = np.argmax(w_temp_max, axis=1)
+                mv = np.zeros(len(mi), dtype=np.float32)
+                for i in range(len(temp_max)):
+                    mv[i] = temp_max[i, mi[i]]
+                maxvalue_array[:, c] = np.sort(mv)
+            else:
+                maxvalue_array[:, c] = np.sort(temp_max.max(axis=1))
+    for c in range(num_contrasts):
+        srt = maxvalue_array[:, c]
+        p_array = np.arange(num_perm, dtype=np.float64) / num_perm
+        positive_data[:, c] = [find_nearest(srt, k, p_array) for k in positive_data[:, c]]
+        if not mediation:
+            negative_data[:, c] = [find_nearest(srt, k, p_array) for k in negative_data[:, c]]
+    return positive_data, (None if mediation else negative_data)

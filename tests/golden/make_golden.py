@@ -1,0 +1,281 @@
+"""Generate the golden vectors in tests/golden/ by running the reference itself.
+
+Run in a container that holds a reference checkout (default /root/reference,
+override with TFCE_REFERENCE_ROOT) after ``python oracle/build_ref.py``:
+
+    python tests/golden/make_golden.py
+
+It imports the reference's compiled operator modules (``tfce``, ``cynumstats``
+built into oracle/_ref/) and its unmodified ``pyfunc.py`` / ``tm_func.py`` /
+``tm_io.py`` (nibabel and matplotlib, absent here, are replaced by empty stub
+modules; none of the functions recorded touch them), calls them on small seeded
+inputs and stores inputs and outputs as compressed .npz fixtures.  The fixtures
+are what the tests compare against; the reference is not needed afterwards.
+"""
+from __future__ import annotations
+
+import importlib.util
+import os
+import sys
+import tempfile
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+REF = os.environ.get("TFCE_REFERENCE_ROOT", "/root/reference")
+sys.path.insert(0, ROOT)
+
+
+def _stub(name):
+    m = types.ModuleType(name)
+    sys.modules[name] = m
+    return m
+
+
+def load_reference():
+    for name in ["nibabel", "nibabel.freesurfer", "nibabel.freesurfer.mghformat", "matplotlib",
+                 "matplotlib.pyplot", "matplotlib.colors", "matplotlib.patches", "matplotlib.cm"]:
+        _stub(name)
+    sys.modules["matplotlib"].use = lambda *a, **k: None
+    sys.path.insert(0, os.path.join(ROOT, "oracle", "_ref"))
+    import tfce_mediation  # the oracle/_ref package holding the compiled modules
+    from tfce_mediation import cynumstats, tfce  # noqa: F401
+    mods = {}
+    for name in ["pyfunc", "tm_io", "tm_func"]:
+        path = os.path.join(REF, "tfce_mediation", f"{name}.py")
+        spec = importlib.util.spec_from_file_location(f"tfce_mediation.{name}", path)
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules[f"tfce_mediation.{name}"] = mod
+        setattr(tfce_mediation, name, mod)
+        try:
+            spec.loader.exec_module(mod)
+        except Exception as exc:  # tm_io needs more of nibabel at import time
+            print(f"note: {name} not importable ({exc!r})")
+            sys.modules.pop(f"tfce_mediation.{name}", None)
+            continue
+        mods[name] = mod
+    mods["tfce"] = sys.modules["tfce_mediation.tfce"]
+    mods["cynumstats"] = sys.modules["tfce_mediation.cynumstats"]
+    return mods
+
+
+class _OldNumpyArray(types.ModuleType):
+    """numpy as seen by code written for numpy < 1.24: np.array of ragged lists
+    gives an object array (pyfunc.create_adjac_voxel relies on it) instead of
+    raising.  Everything else is numpy itself."""
+
+    def __init__(self):
+        super().__init__("numpy_compat")
+
+    def __getattr__(self, name):
+        return getattr(np, name)
+
+    @staticmethod
+    def array(obj, *a, **k):
+        try:
+            return np.array(obj, *a, **k)
+        except ValueError:
+            out = np.empty(len(obj), dtype=object)
+            for i, x in enumerate(obj):
+                out[i] = x
+            return out
+
+
+def main():
+    from tfce_mediation_gb300 import adjacency as A
+    from tfce_mediation_gb300 import synth
+
+    R = load_reference()
+    tfce, cyn, pyfunc = R["tfce"], R["cynumstats"], R["pyfunc"]
+    pyfunc.np = _OldNumpyArray()
+    rng = np.random.default_rng(20261203)
+    out = {}
+
+    # --- adjacency builders -------------------------------------------------
+    v, f = synth.icosphere(2)
+    ref_adj = pyfunc.create_adjac_vertex(v, f)
+    off, idx = A.to_csr([sorted(s) for s in ref_adj])
+    out["adj_mesh_faces"] = f.astype(np.int32)
+    out["adj_mesh_nv"] = np.int32(v.shape[0])
+    out["adj_mesh_off"], out["adj_mesh_idx"] = off, idx
+    mask = np.zeros((7, 6, 5), bool)
+    mask[1:6, 1:5, 1:4] = True
+    mask[0, 0, 0] = True
+    mask[3, 0, 2] = True
+    mask[6, 5, 4] = True
+    out["vox_mask"] = mask
+    for dirtype in (6, 26):
+        nv = int(mask.sum())
+        adj = pyfunc.create_adjac_voxel(mask, mask.astype(np.float32), nv, dirtype=dirtype)
+        o, i = A.to_csr([list(a) for a in adj])
+        out[f"vox{dirtype}_off"], out[f"vox{dirtype}_idx"] = o, i
+    try:
+        # the tool imports the geodesic extension at module level; it is not
+        # used by create_adjac_voxel
+        if "tfce_mediation.adjacency" not in sys.modules:
+            _stub("tfce_mediation.adjacency").compute = None
+        spec = importlib.util.spec_from_file_location(
+            "tm_mmr_adj", os.path.join(REF, "tfce_mediation", "tools", "tm_mulitmodality_adjacency.py"))
+        mmr_adj = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mmr_adj)
+        for dirtype in (6, 26):
+            adj = mmr_adj.create_adjac_voxel(mask, dirtype=dirtype)
+            o, i = A.to_csr([sorted(a) for a in adj])
+            out[f"voxmmr{dirtype}_off"], out[f"voxmmr{dirtype}_idx"] = o, i
+    except Exception as exc:
+        print(f"note: mmr voxel adjacency not recorded ({exc!r})")
+
+    # --- TFCE sweeps on a level-3 icosphere ---------------------------------
+    v3, f3 = synth.icosphere(3)
+    off3, idx3 = A.mesh_csr(f3, v3.shape[0])
+    adj3 = A.from_csr(off3, idx3)
+    S = synth.smoothing_matrix(off3, idx3)
+    maps = []
+    for _ in range(4):
+        m = rng.standard_normal(v3.shape[0]).astype(np.float32)
+        for _ in range(3):
+            m = (S @ m).astype(np.float32)
+        maps.append(m * np.float32(4.0))
+    maps.append(np.round(maps[0] * 2) / 2)  # ties
+    maps.append(-np.abs(maps[1]))  # all <= 0
+    maps = np.stack(maps).astype(np.float32)
+    out["sweep_off"], out["sweep_idx"], out["sweep_maps"] = off3, idx3, maps
+    params = [(2.0, 1.0), (2.0, 0.5), (1.0, 0.67), (2.0, 2.0), (1.5, 0.75)]
+    out["sweep_params"] = np.array(params, np.float32)
+    res = np.zeros((len(params), maps.shape[0], maps.shape[1]), np.float32)
+    for pi, (H, E) in enumerate(params):
+        op = tfce.CreateAdjSet(H, E, adj3)
+        for mi in range(maps.shape[0]):
+            if maps[mi].max() == 0:
+                continue  # the reference never returns on a map whose maximum is 0
+            e = np.zeros(maps.shape[1], np.float32)
+            op.run(maps[mi].copy(), e)
+            res[pi, mi] = e
+    out["sweep_enhn"] = res
+    # accumulation into a non-zero enhn
+    op = tfce.CreateAdjSet(2.0, 1.0, adj3)
+    e0 = rng.standard_normal(maps.shape[1]).astype(np.float32)
+    e = e0.copy()
+    op.run(maps[2].copy(), e)
+    out["sweep_accum_in"], out["sweep_accum_out"] = e0, e
+
+    # --- GLM helpers ---------------------------------------------------------
+    n, V = 40, 300
+    y = rng.standard_normal((n, V)).astype(np.float32)
+    x = np.column_stack([rng.integers(0, 2, n), rng.standard_normal(n), rng.standard_normal(n)])
+    X = np.column_stack([np.ones(n), x])
+    invXX = np.linalg.inv(X.T @ X)
+    out["glm_y"], out["glm_x"] = y, x
+    out["glm_tval_int"] = cyn.tval_int(X, invXX, y, n, X.shape[1], V)
+    b, se = cyn.calc_beta_se(x[:, 0], y, n, V)
+    out["glm_cbs_beta"], out["glm_cbs_se"] = b, se
+    out["glm_lstsqr"] = cyn.cy_lin_lstsqr_mat(X, y)
+    out["glm_calcF"] = cyn.calcF(X, y, n, X.shape[1])
+    out["glm_resid_covars"] = cyn.resid_covars(X[:, :2], y.T)
+    a, rss = cyn.cy_lin_lstsqr_mat_residual(X, y)
+    out["glm_lsr_a"], out["glm_lsr_rss"] = a, rss
+    sig2 = rng.uniform(0.5, 2.0, V)
+    out["glm_sig2"] = sig2
+    out["glm_se_of_slope"] = cyn.se_of_slope(V, invXX, sig2, X.shape[1])
+
+    # --- Sobel z ---------------------------------------------------------------
+    mx = rng.integers(0, 2, n).astype(np.float64)
+    dy = rng.standard_normal(n) + 0.5 * mx
+    my = (y + 0.3 * mx[:, None] + 0.2 * dy[:, None]).astype(np.float32)
+    out["sobel_x"], out["sobel_dy"], out["sobel_y"] = mx, dy, my
+    for mt in ("I", "M", "Y"):
+        for alg in ("aroian", "sobel", "goodman"):
+            with np.errstate(all="ignore"):
+                out[f"sobel_{mt}_{alg}"] = pyfunc.calc_sobelz(mt, mx, dy, my, n, V, alg=alg)
+
+    # --- per-permutation maxima (CSV) ----------------------------------------
+    Vh = off3.shape[0] - 1
+    lh = tfce.CreateAdjSet(2.0, 1.0, adj3)
+    rh = tfce.CreateAdjSet(2.0, 1.0, adj3)
+    mask_lh = np.ones(Vh, bool)
+    mask_rh = np.ones(Vh, bool)
+    mask_rh[: Vh // 5] = False
+    nmask = int(mask_lh.sum())
+    stat = np.concatenate([maps[0], maps[1][mask_rh]]).astype(np.float64)
+    vd = A.vertex_density(adj3)
+    with tempfile.TemporaryDirectory() as td:
+        cwd = os.getcwd()
+        os.chdir(td)
+        try:
+            pyfunc.write_perm_maxTFCE_vertex("tstat_con1", stat, nmask, mask_lh, mask_rh, lh, rh)
+            pyfunc.write_perm_maxTFCE_vertex("tstat_con1", -stat, nmask, mask_lh, mask_rh, lh, rh)
+            pyfunc.write_perm_maxTFCE_vertex("tstat_con2", stat, nmask, mask_lh, mask_rh, lh, rh, vd, vd)
+            pyfunc.write_perm_maxTFCE_voxel("tstat_con1", maps[3].astype(np.float64), lh)
+            out["perm_csv_vertex1"] = np.array(open("perm_tstat_con1_TFCE_maxVertex.csv").read())
+            out["perm_csv_vertex2"] = np.array(open("perm_tstat_con2_TFCE_maxVertex.csv").read())
+            out["perm_csv_voxel1"] = np.array(open("perm_tstat_con1_TFCE_maxVoxel.csv").read())
+        finally:
+            os.chdir(cwd)
+    out["perm_stat"], out["perm_mask_rh"], out["perm_vd"] = stat, mask_rh, vd
+
+    # --- FWER lookups -----------------------------------------------------------
+    null = np.round(rng.gamma(3.0, 50.0, 200), 4)
+    img = np.concatenate([rng.gamma(3.0, 60.0, 500), np.zeros(20), null[:10], [1e6, -1.0]])
+    out["fwe_null"], out["fwe_img"] = null, img
+    srt = np.sort(null)
+    p_array = np.arange(len(srt)) / len(srt)
+    # calculate_fweP_vertex.find_nearest (restated here only to record the
+    # reference module's answer; the module itself needs nibabel at run time)
+    spec = importlib.util.spec_from_file_location(
+        "fwep_vertex", os.path.join(REF, "tfce_mediation", "tmanalysis", "calculate_fweP_vertex.py"))
+    fwepv = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(fwepv)
+    out["fwe_vertex"] = np.array([fwepv.find_nearest(srt, k, p_array) if k > 0 else 0.0 for k in img])
+    if "tm_func" in R:
+        out["fwe_nearest"] = np.array([R["tm_func"].find_nearest(srt, k, p_array) for k in img])
+    else:
+        out["fwe_nearest"] = np.array([pyfunc.find_nearest(srt, k, p_array) for k in img])
+
+    # --- apply_mfwer -------------------------------------------------------------
+    if "tm_func" in R:
+        tmf = R["tm_func"]
+        pos = [0, 40, 100, 130]
+        nperm, ncon = 50, 2
+        images = rng.gamma(2.0, 30.0, (130, 2 * ncon))
+        images[rng.random(images.shape) < 0.2] = 0.0
+        with tempfile.TemporaryDirectory() as td:
+            cwd = os.getcwd()
+            os.chdir(td)
+            try:
+                os.mkdir("output_study")
+                perm = {}
+                for s in range(3):
+                    for c in range(ncon):
+                        vals = rng.gamma(2.0 + s, 40.0, nperm)
+                        perm[(s, c)] = vals
+                        np.savetxt(f"output_study/perm_maxTFCE_surf{s}_tcon{c + 1}.csv", vals, fmt="%f")
+                for w in (None, "logmasksize"):
+                    with np.errstate(all="ignore"):
+                        p, q = tmf.apply_mfwer([images], ncon, range(3), nperm, 3, "study", pos,
+                                               [0, 1], [2, 3], weight=w)
+                    out[f"mfwer_pos_{w}"], out[f"mfwer_neg_{w}"] = p, q
+                out["mfwer_perm"] = np.stack([np.loadtxt(f"output_study/perm_maxTFCE_surf{s}_tcon{c + 1}.csv")
+                                              for s in range(3) for c in range(ncon)])
+            finally:
+                os.chdir(cwd)
+        out["mfwer_images"], out["mfwer_pos_array"] = images, np.array(pos)
+
+        # low_ram_calculate_tfce, observed (not randomised)
+        nl = 30
+        yl = rng.standard_normal((nl, Vh)).astype(np.float32)
+        for _ in range(3):
+            yl = (S @ yl.T).T.astype(np.float32)
+        xl = np.column_stack([rng.integers(0, 2, nl), rng.standard_normal(nl)])
+        maskl = np.ones(Vh, np.float32)
+        tv, tp, tn = tmf.low_ram_calculate_tfce(yl, maskl, xl, tfce.CreateAdjSet(2.0, 1.0, adj3), 1)
+        out["lr_y"], out["lr_x"], out["lr_t"], out["lr_pos"], out["lr_neg"] = yl, xl, tv, tp, tn
+
+    path = os.path.join(HERE, "reference_vectors.npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote {path} ({os.path.getsize(path)} bytes, {len(out)} arrays)")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,61 @@
+"""The C-ABI library builds for sm_103a, loads, and exports every entry point
+that include/*.h declares (no compute calls: these run without a GPU)."""
+import ctypes
+import glob
+import os
+import re
+
+from tfce_mediation_gb300 import _lib, build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\**\s+\**([a-z_][a-z0-9_]*)\s*\(",
+                             src, flags=re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for n in ("tfce_adjset_create", "tfce_adjset_run", "tfce_sweep_batch", "glm_tstat", "fwer_lookup"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _lib.load()
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_header():
+    assert declared_functions() <= set(_lib.SIGNATURES)
+
+
+def test_version_and_error_string():
+    lib = _lib.load()
+    assert lib.tfce_version() >= 100
+    assert isinstance(lib.tfce_last_error(), bytes)
+
+
+def test_invalid_arguments_are_rejected_on_host():
+    """Argument validation happens before any device work."""
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    import numpy as np
+    off = np.array([0, 1, 2], np.int64)
+    idx = np.array([1, 5], np.int32)  # 5 is out of range
+    H = np.array([2.0], np.float32)
+    E = np.array([1.0], np.float32)
+    rc = lib.tfce_adjset_create(_lib.ptr(off, _lib.c_i64p), _lib.ptr(idx, _lib.c_i32p), 2, None, 1,
+                                _lib.ptr(H, _lib.c_f32p), _lib.ptr(E, _lib.c_f32p), ctypes.byref(h))
+    assert rc == _lib.TFCE_EINVAL
+    assert b"outside" in lib.tfce_last_error()
+    assert lib.tfce_sweep_batch(None, None, 0, 0, 2, None, 0, None, None, 0, None) == _lib.TFCE_EINVAL
+    assert lib.glm_tstat(None, 1, 1, 1, None, None, None, None, 1, 1, None, 1, None, 1, None) == _lib.TFCE_EINVAL
+    assert lib.fwer_lookup(None, 0, None, 1, 0, None, None) == _lib.TFCE_EINVAL

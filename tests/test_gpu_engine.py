@@ -1,0 +1,87 @@
+"""End-to-end permutation inference on config 1 (icosphere L5, n=100, k=3)
+against the oracle pipeline on the same host-seeded permutation streams.
+
+The GPU computes t in float32, the oracle in float64, so the sweeps see maps
+that differ by ~1e-6 relative; a vertex that sits on a threshold can then
+change one increment.  Stated tolerances:
+  * per-permutation max-TFCE: relative error <= 1e-3 for every value, median
+    <= 1e-5;
+  * 1-p(FWER) maps: max |delta p| <= 0.005 (the target of the path).
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from tfce_mediation_gb300 import engine as E
+from tfce_mediation_gb300 import fwer
+
+pytestmark = pytest.mark.gpu
+
+SEED = 7
+
+
+def oracle_maxima(st, perms, contrasts=(1, 2)):
+    X = st.design()
+    out = np.zeros((perms.shape[0], len(contrasts), 2), np.float32)
+    for p in range(perms.shape[0]):
+        t = oracle.tval_fp64(X[perms[p]], st.Y)
+        for ci, c in enumerate(contrasts):
+            img = t[c].astype(np.float32)
+            for si, s in enumerate((1.0, -1.0)):
+                out[p, ci, si] = oracle.tfce_max_batch(st.offsets, st.indices, img, 2.0, 1.0, sign=s)[0]
+    return out
+
+
+@pytest.fixture(scope="module")
+def run100(config1):
+    st = config1
+    eng = E.PermutationEngine(st.Y, st.pred_x, (st.offsets, st.indices), st.segments, 2.0, 1.0, batch=32)
+    perms = E.permutations(st.n, SEED, 0, 100)
+    gpu = E.reduce_vertex(eng.run(perms=perms))
+    ref = oracle_maxima(st, perms)
+    return st, eng, perms, gpu, ref
+
+
+def test_null_maxima_match_oracle(run100):
+    st, eng, perms, gpu, ref = run100
+    rel = np.abs(gpu - ref) / np.abs(ref)
+    assert np.median(rel) <= 1e-5, np.median(rel)
+    assert rel.max() <= 1e-3, rel.max()
+
+
+def test_batching_is_invisible(run100):
+    st, eng, perms, gpu, ref = run100
+    again = E.reduce_vertex(eng.run(perms=perms[:37]))
+    np.testing.assert_array_equal(again, gpu[:37])
+
+
+def test_fwer_map_matches_oracle(run100):
+    st, eng, perms, gpu, ref = run100
+    tmaps, tfce_maps, mx = eng.observed()
+    X = st.design()
+    t_ref = oracle.tval_fp64(X, st.Y)
+    for ci in range(2):
+        null_g = E.null_distribution(gpu, ci)
+        null_o = E.null_distribution(ref, ci)
+        img = t_ref[ci + 1].astype(np.float32)
+        e = oracle.tfce(st.offsets, st.indices, img, 2.0, 1.0)
+        obs_o = e * (img.max() / np.float32(100))
+        p_g = fwer.fwep(tfce_maps[ci, 0], null_g)
+        p_o = oracle.fwep_vertex(obs_o, null_o)
+        assert np.abs(p_g - p_o).max() <= 0.005
+    # the planted effect (regressor 1) is found
+    assert fwer.fwep(tfce_maps[0, 0], E.null_distribution(gpu, 0)).max() >= 0.95
+
+
+def test_observed_maps_match_oracle(run100):
+    st, eng, perms, gpu, ref = run100
+    tmaps, tfce_maps, mx = eng.observed()
+    t_ref = oracle.tval_fp64(st.design(), st.Y)
+    err = np.abs(tmaps - t_ref[1:3]) / np.maximum(1.0, np.abs(t_ref[1:3]))
+    assert err.max() <= 1e-4
+    # feeding the GPU's own t maps to the oracle sweep reproduces the GPU TFCE bit for bit
+    for ci in range(2):
+        for si, s in enumerate((1.0, -1.0)):
+            img = (s * tmaps[ci]).astype(np.float32)
+            e = oracle.tfce(st.offsets, st.indices, img, 2.0, 1.0)
+            np.testing.assert_array_equal(tfce_maps[ci, si], e * (img.max() / np.float32(100)))

@@ -1,0 +1,177 @@
+"""TFCE sweep on the GPU against the reference (golden vectors) and the oracle.
+
+Bar: bit-exact.  The kernel adds the reference's per-threshold float
+increments to each vertex in threshold order, so TFCE values, component
+labels (as partitions) and extents must equal the reference's exactly.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from tfce_mediation_gb300 import adjacency as A
+from tfce_mediation_gb300.tfce import CreateAdjSet
+
+pytestmark = pytest.mark.gpu
+
+
+def _partition_equal(a, b):
+    """Labels equal up to renaming (and the same inactive set)."""
+    if not np.array_equal(a < 0, b < 0):
+        return False
+    m = a >= 0
+    pairs = np.unique(np.stack([a[m], b[m]]), axis=1)
+    return pairs.shape[1] == np.unique(a[m]).size == np.unique(b[m]).size
+
+
+def test_run_bitexact_vs_reference(golden):
+    off, idx, maps = golden["sweep_off"], golden["sweep_idx"], golden["sweep_maps"]
+    adj = A.from_csr(off, idx)
+    for pi, (H, E) in enumerate(golden["sweep_params"]):
+        op = CreateAdjSet(H, E, adj)
+        for mi in range(maps.shape[0]):
+            e = np.zeros(maps.shape[1], np.float32)
+            op.run(maps[mi].copy(), e)
+            np.testing.assert_array_equal(e, golden["sweep_enhn"][pi, mi], err_msg=f"H={H} E={E} map {mi}")
+
+
+def test_run_accumulates(golden):
+    op = CreateAdjSet(2.0, 1.0, (golden["sweep_off"], golden["sweep_idx"]))
+    e = golden["sweep_accum_in"].copy()
+    op.run(golden["sweep_maps"][2].copy(), e)
+    np.testing.assert_array_equal(e, golden["sweep_accum_out"])
+
+
+def test_run_argument_checks(golden):
+    op = CreateAdjSet(2.0, 1.0, (golden["sweep_off"], golden["sweep_idx"]))
+    V = op.n_vertices
+    with pytest.raises(ValueError):
+        op.run(np.zeros(V, np.float64), np.zeros(V, np.float32))
+    with pytest.raises(ValueError):
+        op.run(np.zeros((2, V), np.float32), np.zeros(V, np.float32))
+    with pytest.raises(ValueError):
+        op.run(np.zeros(2 * V, np.float32)[::2], np.zeros(V, np.float32))
+    with pytest.raises(ValueError):
+        op.run(np.zeros(V - 1, np.float32), np.zeros(V - 1, np.float32))
+    with pytest.raises(TypeError):
+        op.run([0.0] * V, np.zeros(V, np.float32))
+
+
+def _config1_maps(st, n_perm=6, seed=11):
+    X = st.design()
+    maps = []
+    for p in range(n_perm):
+        perm = np.random.RandomState(seed + p).permutation(st.n)
+        t = oracle.tval_fp64(X[perm], st.Y)
+        maps.append(t[1].astype(np.float32))
+        maps.append(t[2].astype(np.float32))
+    return np.stack(maps)
+
+
+def test_labels_and_extents_bitexact(config1):
+    st = config1
+    op = CreateAdjSet(2.0, 1.0, (st.offsets, st.indices))
+    t = oracle.tval_fp64(st.design(), st.Y)
+    for img in (t[1].astype(np.float32), (-t[1]).astype(np.float32), t[2].astype(np.float32)):
+        e_o, lab_o, ext_o = oracle.tfce_labels(st.offsets, st.indices, img, 2.0, 1.0)
+        e_g, lab_g, ext_g = op.adjacency.run_labels(img)
+        assert lab_g.shape == lab_o.shape
+        for s in range(lab_o.shape[0]):
+            assert _partition_equal(lab_o[s], lab_g[s]), f"step {s}"
+            np.testing.assert_array_equal(ext_o[s], ext_g[s])
+        np.testing.assert_array_equal(e_g, e_o)
+
+
+def test_batch_maxima_bitexact(config1):
+    import torch
+    st = config1
+    maps = _config1_maps(st)
+    adj = A.AdjacencySet((st.offsets, st.indices), 2.0, 1.0)
+    d = torch.from_numpy(maps).cuda()
+    out = torch.empty((maps.shape[0], 2, 1), device="cuda")
+    adj.sweep_batch(d.data_ptr(), st.V, maps.shape[0], 2, None, 0, out.data_ptr())
+    adj.status()
+    got = out.cpu().numpy()
+    for sgn, s in enumerate((1.0, -1.0)):
+        ref = oracle.tfce_max_batch(st.offsets, st.indices, maps, 2.0, 1.0, sign=s)
+        np.testing.assert_array_equal(got[:, sgn, 0], ref)
+
+
+def test_batch_scaled_maps_and_vdensity(config1):
+    import torch
+    st = config1
+    maps = _config1_maps(st, n_perm=2)
+    vd = A.vertex_density((st.offsets, st.indices))
+    adj = A.AdjacencySet((st.offsets, st.indices), 2.0, 1.0)
+    d = torch.from_numpy(maps).cuda()
+    vdd = torch.from_numpy(vd).cuda()
+    mx = torch.empty((maps.shape[0], 2, 1), device="cuda")
+    om = torch.empty((maps.shape[0], 2, st.V), device="cuda")
+    adj.sweep_batch(d.data_ptr(), st.V, maps.shape[0], 2, vdd.data_ptr(), 0, mx.data_ptr(),
+                    om.data_ptr(), 1)
+    adj.status()
+    for m in range(maps.shape[0]):
+        for sgn, s in enumerate((1.0, -1.0)):
+            img = (s * maps[m]).astype(np.float32)
+            e = oracle.tfce(st.offsets, st.indices, img, 2.0, 1.0)
+            ref = (e * (img.max() / np.float32(100))) * vd
+            np.testing.assert_array_equal(om[m, sgn].cpu().numpy(), ref)
+            assert mx[m, sgn, 0].item() == ref.max()
+
+
+def test_two_segments_and_floor_zero(golden):
+    """lh/rh as two segments of one launch (masked rh scattered into zeros)."""
+    import torch
+    off, idx = golden["sweep_off"], golden["sweep_idx"]
+    maps = golden["sweep_maps"]
+    Vh = off.shape[0] - 1
+    O, I, seg = A.concat_csr([(off, idx), (off, idx)])
+    adj = A.AdjacencySet((O, I), [2.0, 2.0], [1.0, 0.5], seg)
+    stat = np.concatenate([maps[0], maps[1]])[None].astype(np.float32)
+    stat[0, Vh: Vh + 50] = 0.0
+    out = torch.empty((1, 2, 2), device="cuda")
+    adj.sweep_batch(torch.from_numpy(stat).cuda().data_ptr(), 2 * Vh, 1, 2, None, 1, out.data_ptr())
+    adj.status()
+    got = out.cpu().numpy()[0]
+    for sgn, s in enumerate((1.0, -1.0)):
+        for h, E in ((0, 1.0), (1, 0.5)):
+            img = s * stat[0, h * Vh:(h + 1) * Vh]
+            ref = oracle.tfce_max_batch(off, idx, img, 2.0, E, floor_zero=True)[0]
+            assert got[sgn, h] == ref
+
+
+def test_asymmetric_lists_follow_insertion_rule():
+    """mmr voxel lists (self entries, voxel 0's one-way list) against the oracle."""
+    mask = np.zeros((9, 8, 7), bool)
+    mask[1:8, 1:7, 1:6] = True
+    mask[0, 0, 0] = True
+    off, idx = A.voxel_csr(mask, 26, "mmr")
+    adj = A.AdjacencySet((off, idx), 2.0, 1.0)
+    assert not adj.symmetric
+    rng = np.random.default_rng(3)
+    for _ in range(5):
+        img = rng.standard_normal(off.shape[0] - 1).astype(np.float32) + 0.5
+        e_g = np.zeros_like(img)
+        adj.run(img, e_g)
+        e_o = oracle.tfce(off, idx, img, 2.0, 1.0)
+        np.testing.assert_array_equal(e_g, e_o)
+
+
+def test_degenerate_maps(golden):
+    off, idx = golden["sweep_off"], golden["sweep_idx"]
+    op = CreateAdjSet(2.0, 1.0, (off, idx))
+    V = op.n_vertices
+    for img in (np.zeros(V, np.float32), -np.ones(V, np.float32),
+                np.full(V, np.nan, np.float32)):
+        e = np.ones(V, np.float32)
+        op.run(img, e)
+        np.testing.assert_array_equal(e, np.ones(V, np.float32))
+    img = golden["sweep_maps"][0].copy()
+    img[::7] = np.nan
+    e = np.zeros(V, np.float32)
+    op.run(img, e)
+    np.testing.assert_array_equal(e, oracle.tfce(off, idx, img, 2.0, 1.0))
+    single = CreateAdjSet(2.0, 1.0, [[]])
+    e = np.zeros(1, np.float32)
+    single.run(np.array([3.0], np.float32), e)
+    np.testing.assert_array_equal(e, oracle.tfce(np.array([0, 0]), np.zeros(0, np.int32),
+                                                 np.array([3.0], np.float32), 2.0, 1.0))

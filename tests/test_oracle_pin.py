@@ -1,0 +1,173 @@
+"""Pin the oracle (and the host-side builders) to the reference's own outputs.
+
+tests/golden/reference_vectors.npz was produced by tests/golden/make_golden.py
+from the reference's compiled modules and unmodified Python; every oracle
+function used by the GPU parity tests is checked against it here, on CPU.
+When oracle/_ref (the reference sweep compiled from a reference checkout) is
+present, the oracle sweep is also compared against it directly.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from tfce_mediation_gb300 import adjacency as A
+from tfce_mediation_gb300 import synth
+
+
+def test_sweep_matches_reference_bitwise(golden):
+    maps, params = golden["sweep_maps"], golden["sweep_params"]
+    for pi, (H, E) in enumerate(params):
+        for mi in range(maps.shape[0]):
+            if maps[mi].max() == 0:
+                continue
+            e = oracle.tfce(golden["sweep_off"], golden["sweep_idx"], maps[mi], float(H), float(E))
+            np.testing.assert_array_equal(e, golden["sweep_enhn"][pi, mi], err_msg=f"H={H} E={E} map {mi}")
+
+
+def test_sweep_accumulates_into_enhn(golden):
+    e = golden["sweep_accum_in"].copy()
+    oracle.tfce(golden["sweep_off"], golden["sweep_idx"], golden["sweep_maps"][2], 2.0, 1.0, enhn=e)
+    np.testing.assert_array_equal(e, golden["sweep_accum_out"])
+
+
+def test_sweep_all_nonpositive_map_is_zero(golden):
+    m = golden["sweep_maps"][5]
+    assert m.max() <= 0
+    e = oracle.tfce(golden["sweep_off"], golden["sweep_idx"], m, 2.0, 1.0)
+    assert not e.any()
+
+
+def test_threshold_table_recurrence():
+    T = oracle.threshold_table(4.2)
+    assert T[0] == np.float32(4.2)
+    dT = np.float32(4.2) / np.float32(100)
+    for a, b in zip(T[:-1], T[1:]):
+        assert b == np.float32(a - dT)
+    assert T[-1] >= 0 and np.float32(T[-1] - dT) < 0
+    assert len(T) in (100, 101)
+    assert len(oracle.threshold_table(0.0)) == 0
+    assert len(oracle.threshold_table(-1.0)) == 0
+
+
+def test_labels_are_consistent_partitions(golden):
+    m = golden["sweep_maps"][0]
+    enhn, labels, extents = oracle.tfce_labels(golden["sweep_off"], golden["sweep_idx"], m, 2.0, 1.0)
+    assert labels.shape[0] == len(oracle.threshold_table(float(m.max())))
+    for s in range(labels.shape[0]):
+        lab = labels[s]
+        act = lab >= 0
+        _, inv, cnt = np.unique(lab[act], return_inverse=True, return_counts=True)
+        np.testing.assert_array_equal(extents[s][act], cnt[inv])
+    np.testing.assert_array_equal(enhn, golden["sweep_enhn"][0, 0])
+
+
+def test_sweep_against_reference_build(golden):
+    if oracle.ref_lib() is None:
+        pytest.skip("oracle/_ref not built (no reference checkout here)")
+    st = synth.config1()
+    t = oracle.tval_fp64(st.design(), st.Y)
+    for c in (1, 2):
+        for s in (1, -1):
+            img = (s * t[c]).astype(np.float32)
+            for H, E in ((2.0, 1.0), (2.0, 0.5), (1.0, 0.67)):
+                a = oracle.tfce(st.offsets, st.indices, img, H, E)
+                b = oracle.ref_tfce(st.offsets, st.indices, img, H, E)
+                np.testing.assert_array_equal(a, b)
+
+
+def test_glm_helpers(golden):
+    y, x = golden["glm_y"], golden["glm_x"]
+    n, V = y.shape
+    X = np.column_stack([np.ones(n), x])
+    invXX = np.linalg.inv(X.T @ X)
+    np.testing.assert_array_equal(oracle.tval_int_ref(X, invXX, y, n, X.shape[1]), golden["glm_tval_int"])
+    np.testing.assert_allclose(oracle.tval_fp64(X, y), golden["glm_tval_int"], rtol=1e-6, atol=1e-6)
+    b, se = oracle.calc_beta_se(x[:, 0], y, n)
+    np.testing.assert_array_equal(b, golden["glm_cbs_beta"])
+    np.testing.assert_array_equal(se, golden["glm_cbs_se"])
+    np.testing.assert_array_equal(oracle.lstsqr_mat(X, y), golden["glm_lstsqr"])
+    np.testing.assert_allclose(oracle.calcF(X, y, n, X.shape[1]), golden["glm_calcF"], rtol=1e-12)
+    np.testing.assert_allclose(oracle.resid_covars(X[:, :2], y.T), golden["glm_resid_covars"], rtol=1e-12,
+                               atol=1e-12)
+
+
+def test_sobel(golden):
+    n = golden["sobel_x"].shape[0]
+    for mt in ("I", "M", "Y"):
+        for alg in ("aroian", "sobel", "goodman"):
+            with np.errstate(all="ignore"):
+                z = oracle.calc_sobelz(mt, golden["sobel_x"], golden["sobel_dy"], golden["sobel_y"], n, alg)
+            np.testing.assert_allclose(z, golden[f"sobel_{mt}_{alg}"], rtol=1e-12, equal_nan=True)
+
+
+def test_perm_max_csv(golden):
+    """write_perm_maxTFCE_vertex/voxel values, formatted as the reference formats them."""
+    off, idx = golden["sweep_off"], golden["sweep_idx"]
+    stat, mask_rh, vd = golden["perm_stat"], golden["perm_mask_rh"], golden["perm_vd"]
+    Vh = off.shape[0] - 1
+    nl = Vh
+
+    def full(sign, vdens=None):
+        lh = np.zeros(Vh, np.float32)
+        rh = np.zeros(Vh, np.float32)
+        lh[:] = sign * stat[:nl]
+        rh[mask_rh] = sign * stat[nl:]
+        segs = [(off, idx, 0, Vh)]
+        v = []
+        for arr in (lh, rh):
+            e = oracle.tfce(off, idx, arr, 2.0, 1.0)
+            val = e * (arr[np.isfinite(arr)].max() / np.float32(100))
+            if vdens is not None:
+                val = val * vdens
+            v.append(val.max())
+        return max(v)
+
+    lines1 = "%.4f\n%.4f\n" % (full(1), full(-1))
+    assert lines1 == str(golden["perm_csv_vertex1"])
+    assert "%.4f\n" % full(1, vd) == str(golden["perm_csv_vertex2"])
+    m3 = golden["sweep_maps"][3].astype(np.float64).astype(np.float32)
+    vox = oracle.tfce_max_batch(off, idx, m3, 2.0, 1.0)[0]
+    assert "%1.4f\n" % vox == str(golden["perm_csv_voxel1"])
+
+
+def test_fwer_lookups(golden):
+    null, img = golden["fwe_null"], golden["fwe_img"]
+    np.testing.assert_array_equal(oracle.fwep_vertex(img, null), golden["fwe_vertex"])
+    srt = np.sort(null)
+    p_array = np.arange(len(srt)) / len(srt)
+    np.testing.assert_array_equal(np.array([oracle.find_nearest(srt, k, p_array) for k in img]),
+                                  golden["fwe_nearest"])
+
+
+@pytest.mark.parametrize("weight", [None, "logmasksize"])
+def test_apply_mfwer(golden, weight):
+    images = golden["mfwer_images"]
+    perm = golden["mfwer_perm"]
+    pos = list(golden["mfwer_pos_array"])
+    pm = {}
+    k = 0
+    for s in range(3):
+        for c in range(2):
+            pm[(s, c)] = perm[k]
+            k += 1
+    p, q = oracle.apply_mfwer(images[:, [0, 1]], images[:, [2, 3]], pm, pos, weight=weight)
+    np.testing.assert_array_equal(p, golden[f"mfwer_pos_{weight}"])
+    np.testing.assert_array_equal(q, golden[f"mfwer_neg_{weight}"])
+
+
+# ---- host-side builders of the product against the reference's builders ----
+def test_mesh_adjacency_builder(golden):
+    off, idx = A.mesh_csr(golden["adj_mesh_faces"], int(golden["adj_mesh_nv"]))
+    np.testing.assert_array_equal(off, golden["adj_mesh_off"])
+    np.testing.assert_array_equal(idx, golden["adj_mesh_idx"])
+
+
+@pytest.mark.parametrize("dirtype", [6, 26])
+def test_voxel_adjacency_builders(golden, dirtype):
+    mask = golden["vox_mask"]
+    off, idx = A.voxel_csr(mask, dirtype, "pyfunc")
+    np.testing.assert_array_equal(off, golden[f"vox{dirtype}_off"])
+    np.testing.assert_array_equal(idx, golden[f"vox{dirtype}_idx"])
+    off, idx = A.voxel_csr(mask, dirtype, "mmr")
+    np.testing.assert_array_equal(off, golden[f"voxmmr{dirtype}_off"])
+    np.testing.assert_array_equal(idx, golden[f"voxmmr{dirtype}_idx"])

@@ -1,0 +1,757 @@
+// TFCE sweep over adjacency sets, batched: the GB300 replacement of
+// tfce_mediation/lib/fast_tfce.hpp:11-95 (reached through
+// tfce_mediation/tfce.pyx:44-45) and of the per-permutation scaling/max of
+// tfce_mediation/pyfunc.py:107-126.
+//
+// One work item = (map, sign, segment).  One CTA sweeps one item at a time and
+// pulls the next from a global queue (persistent grid sized to the resident
+// CTA count).  Per item:
+//   1. maxT = segment max; the threshold table T_i (float recurrence
+//      T -= maxT/100 while T >= 0, fast_tfce.hpp:34-39) and HH_i = T_i^H are
+//      built in shared memory;
+//   2. every vertex gets the step at which it activates (first i with
+//      x > T_i, strict as fast_tfce.hpp:41) and vertices are bucketed by that
+//      step (counting sort, no full sort: order inside a step does not change
+//      the partition);
+//   3. per step: (U) new vertices are unioned with active neighbours by a
+//      lock-free union-find in the bucket-position space (CAS links the
+//      larger root under the smaller, so parent[x] < x and walks end);
+//      (S) the roots that were linked this step hand their extent to their new
+//      root; (A) every active vertex adds (float)(extent^E * HH_i) to its own
+//      accumulator, in threshold order -- the reference's per-vertex
+//      arithmetic, so results are bit-identical to it;
+//   4. the map is scaled by max/100 (and vdensity), reduced to its max, and
+//      optionally written out.
+// Every walk and retry loop is bounded; a bound sets an error word and the
+// kernel runs on to its exit.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+
+namespace tfgb {
+
+constexpr int kMaxSteps = 128;
+constexpr int kSweepThreads = 512;
+constexpr uint32_t kOneWay = 0x80000000u;   // entry whose reverse entry is missing
+constexpr uint32_t kIndexMask = 0x7fffffffu;
+constexpr uint32_t kInactiveKey = 0xffffffffu;
+constexpr int kPosBits = 24;                 // key = step << 24 | position
+constexpr int32_t kMaxSegVertices = (1 << kPosBits) - 1;
+constexpr int kWalkLimit = 1 << 26;
+
+struct SweepArgs {
+  const int64_t* offsets;
+  const uint32_t* indices;
+  const float* stats;
+  int64_t map_stride;
+  int32_t n_maps;
+  int32_t n_signs;
+  int32_t n_seg;
+  const int64_t* seg_off;
+  const float* seg_H;
+  const float* seg_E;
+  const float* vdensity;
+  int32_t floor_zero;
+  float* out_max;
+  float* out_maps;
+  int32_t out_mode;
+  int32_t* labels;
+  int32_t* extents;
+  int32_t* n_steps_out;
+  int32_t label_cap;
+  char* ws;
+  int64_t ws_slot_bytes;
+  int32_t vcap;
+  int32_t* counter;
+  int32_t* err;
+  int32_t n_items;
+  const int32_t* item_order;
+};
+
+struct Slot {
+  uint32_t* key;
+  int32_t* order;
+  int32_t* parent;
+  int32_t* size;
+  float* acc;
+  int32_t* dead;
+};
+
+__host__ __device__ inline int64_t align_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
+
+__host__ __device__ inline int64_t slot_bytes(int32_t vcap) {
+  return 6 * align_up((int64_t)vcap * 4, 256);
+}
+
+__device__ inline Slot make_slot(char* base, int32_t vcap) {
+  const int64_t s = align_up((int64_t)vcap * 4, 256);
+  Slot sl;
+  sl.key = reinterpret_cast<uint32_t*>(base);
+  sl.order = reinterpret_cast<int32_t*>(base + s);
+  sl.parent = reinterpret_cast<int32_t*>(base + 2 * s);
+  sl.size = reinterpret_cast<int32_t*>(base + 3 * s);
+  sl.acc = reinterpret_cast<float*>(base + 4 * s);
+  sl.dead = reinterpret_cast<int32_t*>(base + 5 * s);
+  return sl;
+}
+
+__device__ inline void set_err(int32_t* err, int32_t code) { atomicCAS(err, 0, code); }
+
+// Root of x.  parent[] entries only ever point to smaller positions, so the
+// walk ends; the limit is a second guard.
+__device__ inline int32_t find_root(const int32_t* parent, int32_t x, int32_t* err) {
+  int32_t p = __ldcg(parent + x);
+  int it = 0;
+  while (p != x) {
+    x = p;
+    p = __ldcg(parent + x);
+    if (++it > kWalkLimit) {
+      set_err(err, kDevLoopLimit);
+      return x;
+    }
+  }
+  return x;
+}
+
+__device__ inline void unite(int32_t* parent, int32_t a, int32_t b, int32_t* dead,
+                             int32_t* n_dead, int32_t* err) {
+  for (int it = 0; it < kWalkLimit; ++it) {
+    a = find_root(parent, a, err);
+    b = find_root(parent, b, err);
+    if (a == b) return;
+    const int32_t hi = max(a, b), lo = min(a, b);
+    if (atomicCAS(parent + hi, hi, lo) == hi) {
+      const int32_t q = atomicAdd(n_dead, 1);
+      dead[q] = hi;
+      return;
+    }
+  }
+  set_err(err, kDevLoopLimit);
+}
+
+// (float)(extent^E * HH) with the reference's types: pow in double, product in
+// double, one rounding to float (fast_tfce.hpp:77).  For E == 1 the double
+// product of an integer < 2^24 and a float is exact, so one float multiply
+// rounds identically.
+__device__ inline float increment(int32_t extent, float E, int e_mode, float HH) {
+  if (e_mode == 1) return __fmul_rn(static_cast<float>(extent), HH);
+  double pe;
+  if (e_mode == 2) pe = sqrt(static_cast<double>(extent));
+  else if (e_mode == 3) pe = static_cast<double>(extent) * static_cast<double>(extent);
+  else pe = pow(static_cast<double>(extent), static_cast<double>(E));
+  return __double2float_rn(__dmul_rn(pe, static_cast<double>(HH)));
+}
+
+// HH = pow(T, H) in float (fast_tfce.hpp:70).
+__device__ inline float pow_h(float T, float H) {
+  if (H == 2.0f) return __fmul_rn(T, T);
+  if (H == 1.0f) return T;
+  return powf(T, H);
+}
+
+__device__ inline float block_max(float v, float* red) {
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = (l < (int)(blockDim.x >> 5)) ? red[l] : -INFINITY;
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (l == 0) red[0] = v;
+  }
+  __syncthreads();
+  const float r = red[0];
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(kSweepThreads, 2) tfce_sweep_kernel(SweepArgs a) {
+  __shared__ float sT[kMaxSteps];
+  __shared__ float sHH[kMaxSteps];
+  __shared__ int32_t sCnt[kMaxSteps + 1];
+  __shared__ int32_t sStart[kMaxSteps + 1];
+  __shared__ float sRed[32];
+  __shared__ int32_t sItem, sL, sNDead;
+
+  Slot sl = make_slot(a.ws + (int64_t)blockIdx.x * a.ws_slot_bytes, a.vcap);
+  const int tid = threadIdx.x, nth = blockDim.x;
+
+  for (;;) {
+    if (tid == 0) sItem = atomicAdd(a.counter, 1);
+    __syncthreads();
+    const int32_t qi = sItem;
+    __syncthreads();
+    if (qi >= a.n_items) break;
+    const int32_t item = a.item_order ? a.item_order[qi] : qi;
+    const int32_t seg = item % a.n_seg;
+    const int32_t ms = item / a.n_seg;  // map * n_signs + sign
+    const int32_t sgn = ms % a.n_signs;
+    const int32_t map = ms / a.n_signs;
+    const float sign = sgn ? -1.0f : 1.0f;
+    const int64_t v0 = a.seg_off[seg];
+    const int32_t Vs = static_cast<int32_t>(a.seg_off[seg + 1] - v0);
+    const float H = a.seg_H[seg], E = a.seg_E[seg];
+    const int e_mode = (E == 1.0f) ? 1 : (E == 0.5f) ? 2 : (E == 2.0f) ? 3 : 0;
+    const float* x = a.stats + (int64_t)map * a.map_stride + v0;
+    const float* vd = a.vdensity ? a.vdensity + v0 : nullptr;
+    float* omap = a.out_maps ? a.out_maps + (int64_t)ms * (a.seg_off[a.n_seg]) + v0 : nullptr;
+
+    // ---- 1. maximum and threshold table
+    float mx = -INFINITY;
+    for (int32_t v = tid; v < Vs; v += nth) {
+      const float xv = sign * x[v];
+      if (isfinite(xv)) mx = fmaxf(mx, xv);
+    }
+    mx = block_max(mx, sRed);
+    if (a.floor_zero) mx = fmaxf(mx, 0.0f);
+    if (tid == 0) {
+      int L = 0;
+      if (mx > 0.0f && isfinite(mx)) {
+        const float dT = __fdiv_rn(mx, 100.0f);
+        float T = mx;
+        while (T >= 0.0f) {
+          if (L >= kMaxSteps) {
+            set_err(a.err, kDevTooManySteps);
+            L = 0;
+            break;
+          }
+          sT[L] = T;
+          sHH[L] = pow_h(T, H);
+          ++L;
+          T = __fsub_rn(T, dT);
+        }
+      }
+      sL = L;
+      if (a.n_steps_out) *a.n_steps_out = L;
+    }
+    for (int i = tid; i <= kMaxSteps; i += nth) sCnt[i] = 0;
+    __syncthreads();
+    const int L = sL;
+    const float scale = isfinite(mx) ? __fdiv_rn(mx, 100.0f) : 0.0f;
+
+    // ---- 2. activation step per vertex, bucket histogram
+    for (int32_t v = tid; v < Vs; v += nth) {
+      const float xv = sign * x[v];
+      int lv = L;  // L == never active
+      if (L > 0 && xv > sT[L - 1]) {
+        int lo = 0, hi = L - 1;  // smallest i with xv > T[i]; T decreasing
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (xv > sT[mid]) hi = mid;
+          else lo = mid + 1;
+        }
+        lv = lo;
+      }
+      sl.key[v] = static_cast<uint32_t>(lv);  // provisional: step only
+      if (lv < L) {
+        const unsigned mask = __activemask();
+        const unsigned peers = __match_any_sync(mask, lv);
+        const int leader = __ffs(peers) - 1;
+        if ((tid & 31) == leader) atomicAdd(&sCnt[lv], __popc(peers));
+      }
+    }
+    __syncthreads();
+    if (tid == 0) {
+      int32_t s = 0;
+      for (int i = 0; i < L; ++i) {
+        sStart[i] = s;
+        s += sCnt[i];
+        sCnt[i] = 0;  // reused as fill cursor
+      }
+      sStart[L] = s;
+      sNDead = 0;
+    }
+    __syncthreads();
+    const int32_t n_act = sStart[L];
+    for (int32_t v = tid; v < Vs; v += nth) {
+      const int lv = static_cast<int>(sl.key[v]);
+      uint32_t key = kInactiveKey;
+      if (lv < L) {
+        const unsigned mask = __activemask();
+        const unsigned peers = __match_any_sync(mask, lv);
+        const int leader = __ffs(peers) - 1;
+        const int lane = tid & 31;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(&sCnt[lv], __popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        const int32_t p = sStart[lv] + base + __popc(peers & ((1u << lane) - 1u));
+        key = (static_cast<uint32_t>(lv) << kPosBits) | static_cast<uint32_t>(p);
+        sl.order[p] = v;
+        sl.parent[p] = p;
+        sl.size[p] = 1;
+        sl.acc[p] = (a.out_mode == 2 && omap) ? omap[v] : 0.0f;
+      }
+      sl.key[v] = key;
+    }
+    __syncthreads();
+
+    // ---- 3. threshold steps
+    for (int i = 0; i < L; ++i) {
+      const int32_t s0 = sStart[i], s1 = sStart[i + 1];
+      // (U) union newly active vertices with already-active neighbours
+      for (int32_t p = s0 + tid; p < s1; p += nth) {
+        const int32_t v = sl.order[p];
+        const int64_t e0 = a.offsets[v0 + v], e1 = a.offsets[v0 + v + 1];
+        for (int64_t e = e0; e < e1; ++e) {
+          const uint32_t raw = a.indices[e];
+          const int64_t ag = static_cast<int64_t>(raw & kIndexMask) - v0;
+          if (ag < 0 || ag >= Vs) {
+            set_err(a.err, kDevBadIndex);
+            continue;
+          }
+          const int32_t an = static_cast<int32_t>(ag);
+          const uint32_t ka = sl.key[an];
+          if (ka == kInactiveKey) continue;
+          const int la = static_cast<int>(ka >> kPosBits);
+          if (la > i) continue;
+          if (la == i && (raw & kOneWay)) {
+            // one-directional entry: effective only if the neighbour was
+            // inserted first (larger value; ties by smaller index)
+            const float xa = sign * x[an], xv = sign * x[v];
+            if (!(xa > xv || (xa == xv && an < v))) continue;
+          }
+          unite(sl.parent, p, static_cast<int32_t>(ka & ((1u << kPosBits) - 1u)), sl.dead,
+                &sNDead, a.err);
+        }
+      }
+      __syncthreads();
+      // (S) linked roots hand their extent to their final root
+      const int32_t nd = sNDead;
+      for (int32_t q = tid; q < nd; q += nth) {
+        const int32_t d = sl.dead[q];
+        const int32_t r = find_root(sl.parent, d, a.err);
+        atomicAdd(sl.size + r, __ldcg(sl.size + d));
+        __stcg(sl.parent + d, r);
+      }
+      __syncthreads();
+      if (tid == 0) sNDead = 0;
+      // (A) per-vertex increment, threshold order
+      const float HH = sHH[i];
+      for (int32_t p = tid; p < s1; p += nth) {
+        int32_t r = __ldcg(sl.parent + p);
+        if (r != p) {
+          const int32_t rr = __ldcg(sl.parent + r);
+          if (rr != r) {
+            r = find_root(sl.parent, rr, a.err);
+            __stcg(sl.parent + p, r);
+          }
+        }
+        const int32_t ext = __ldcg(sl.size + r);
+        sl.acc[p] = __fadd_rn(sl.acc[p], increment(ext, E, e_mode, HH));
+        if (a.labels && i < a.label_cap) {
+          const int32_t v = sl.order[p];
+          a.labels[(int64_t)i * Vs + v] = sl.order[r];
+          a.extents[(int64_t)i * Vs + v] = ext;
+        }
+      }
+      __syncthreads();
+    }
+
+    // ---- 4. scale, reduce, write
+    float best = (n_act < Vs) ? __fmul_rn(0.0f, scale) : -INFINITY;
+    if (a.out_mode == 1 && omap) {
+      for (int32_t v = tid; v < Vs; v += nth) {
+        const uint32_t k = sl.key[v];
+        const float t = (k == kInactiveKey) ? 0.0f : sl.acc[k & ((1u << kPosBits) - 1u)];
+        float val = __fmul_rn(t, scale);
+        if (vd) val = __fmul_rn(val, vd[v]);
+        omap[v] = val;
+        best = fmaxf(best, val);
+      }
+    } else {
+      for (int32_t p = tid; p < n_act; p += nth) {
+        const float t = sl.acc[p];
+        if (a.out_mode == 2 && omap) omap[sl.order[p]] = t;
+        float val = __fmul_rn(t, scale);
+        if (vd) val = __fmul_rn(val, vd[sl.order[p]]);
+        best = fmaxf(best, val);
+      }
+    }
+    best = block_max(best, sRed);
+    if (tid == 0 && a.out_max) a.out_max[item] = (best == -INFINITY) ? 0.0f : best;
+    __syncthreads();
+  }
+}
+
+}  // namespace tfgb
+
+// ---------------------------------------------------------------------------
+// Handle and C-ABI
+// ---------------------------------------------------------------------------
+struct tfce_adjset {
+  int device = 0;
+  int32_t V = 0;
+  int64_t D = 0;
+  int32_t n_seg = 1;
+  bool symmetric = true;
+  int32_t vmax_seg = 0;
+  std::vector<int64_t> seg_off;
+  std::vector<float> H, E;
+  int64_t* d_offsets = nullptr;
+  uint32_t* d_indices = nullptr;
+  int64_t* d_seg_off = nullptr;
+  float* d_H = nullptr;
+  float* d_E = nullptr;
+  int32_t* d_ctrl = nullptr;  // [0] queue counter, [1] error word, [2] step count
+  char* d_ws = nullptr;
+  int64_t ws_slot = 0;
+  int32_t ws_slots = 0;
+  int32_t max_slots = 0;
+  float* d_img = nullptr;
+  float* d_enh = nullptr;
+  int32_t run_cap = 0;
+  std::mutex mu;
+};
+
+namespace {
+
+int release(tfce_adjset* h) {
+  if (!h) return TFCE_OK;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaSetDevice(h->device);
+  cudaFree(h->d_offsets);
+  cudaFree(h->d_indices);
+  cudaFree(h->d_seg_off);
+  cudaFree(h->d_H);
+  cudaFree(h->d_E);
+  cudaFree(h->d_ctrl);
+  cudaFree(h->d_ws);
+  cudaFree(h->d_img);
+  cudaFree(h->d_enh);
+  cudaSetDevice(dev);
+  return TFCE_OK;
+}
+
+int resident_slots(tfce_adjset* h) {
+  if (h->max_slots) return TFCE_OK;
+  int sms = 0, per_sm = 0;
+  TFGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
+  TFGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tfgb::tfce_sweep_kernel,
+                                                          tfgb::kSweepThreads, 0));
+  h->max_slots = std::max(1, sms * std::max(1, per_sm));
+  return TFCE_OK;
+}
+
+int ensure_workspace(tfce_adjset* h, int32_t slots) {
+  const int64_t per = tfgb::slot_bytes(h->vmax_seg);
+  if (h->d_ws && h->ws_slots >= slots && h->ws_slot == per) return TFCE_OK;
+  cudaFree(h->d_ws);
+  h->d_ws = nullptr;
+  h->ws_slots = 0;
+  TFGB_CUDA(cudaMalloc(&h->d_ws, per * slots));
+  h->ws_slot = per;
+  h->ws_slots = slots;
+  return TFCE_OK;
+}
+
+int launch_sweep(tfce_adjset* h, const float* stats, int64_t map_stride, int32_t n_maps,
+                 int32_t signs, const float* vdensity, int32_t floor_zero, float* out_max,
+                 float* out_maps, int32_t out_mode, int32_t* labels, int32_t* extents,
+                 int32_t label_cap, cudaStream_t st) {
+  const int64_t items64 = (int64_t)n_maps * signs * h->n_seg;
+  TFGB_CHECK_ARG(items64 < (1LL << 31), "too many sweep items");
+  const int32_t items = static_cast<int32_t>(items64);
+  if (items == 0) return TFCE_OK;
+  int rs = resident_slots(h);
+  if (rs) return rs;
+  const int32_t slots = std::min<int32_t>(items, h->max_slots);
+  int rc = ensure_workspace(h, slots);
+  if (rc) return rc;
+  TFGB_CUDA(cudaMemsetAsync(h->d_ctrl, 0, sizeof(int32_t), st));  // queue counter only
+  tfgb::SweepArgs a{};
+  a.offsets = h->d_offsets;
+  a.indices = h->d_indices;
+  a.stats = stats;
+  a.map_stride = map_stride;
+  a.n_maps = n_maps;
+  a.n_signs = signs;
+  a.n_seg = h->n_seg;
+  a.seg_off = h->d_seg_off;
+  a.seg_H = h->d_H;
+  a.seg_E = h->d_E;
+  a.vdensity = vdensity;
+  a.floor_zero = floor_zero;
+  a.out_max = out_max;
+  a.out_maps = out_maps;
+  a.out_mode = out_mode;
+  a.labels = labels;
+  a.extents = extents;
+  a.n_steps_out = labels ? h->d_ctrl + 2 : nullptr;
+  a.label_cap = label_cap;
+  a.ws = h->d_ws;
+  a.ws_slot_bytes = h->ws_slot;
+  a.vcap = h->vmax_seg;
+  a.counter = h->d_ctrl;
+  a.err = h->d_ctrl + 1;
+  a.n_items = items;
+  a.item_order = nullptr;
+  tfgb::tfce_sweep_kernel<<<slots, tfgb::kSweepThreads, 0, st>>>(a);
+  TFGB_CUDA(cudaGetLastError());
+  return TFCE_OK;
+}
+
+// Reads and clears the sticky error word (synchronises the stream).
+int check_device_error(tfce_adjset* h, cudaStream_t st, int32_t* steps) {
+  int32_t ctrl[4];
+  TFGB_CUDA(cudaMemcpyAsync(ctrl, h->d_ctrl, sizeof(ctrl), cudaMemcpyDeviceToHost, st));
+  TFGB_CUDA(cudaStreamSynchronize(st));
+  if (steps) *steps = ctrl[2];
+  if (ctrl[1] != 0) TFGB_CUDA(cudaMemsetAsync(h->d_ctrl + 1, 0, sizeof(int32_t), st));
+  return tfgb::map_dev_err(ctrl[1]);
+}
+
+int ensure_run_buffers(tfce_adjset* h, int32_t V) {
+  if (h->run_cap >= V) return TFCE_OK;
+  cudaFree(h->d_img);
+  cudaFree(h->d_enh);
+  h->d_img = h->d_enh = nullptr;
+  h->run_cap = 0;
+  TFGB_CUDA(cudaMalloc(&h->d_img, sizeof(float) * std::max(V, 1)));
+  TFGB_CUDA(cudaMalloc(&h->d_enh, sizeof(float) * std::max(V, 1)));
+  h->run_cap = V;
+  return TFCE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tfce_adjset_create(const int64_t* offsets, const int32_t* indices, int32_t n_vertices,
+                       const int64_t* seg_offsets, int32_t n_seg, const float* H, const float* E,
+                       tfce_adjset** out) {
+  tfgb::clear_error();
+  TFGB_CHECK_ARG(out != nullptr, "out is NULL");
+  *out = nullptr;
+  TFGB_CHECK_ARG(n_vertices >= 0, "n_vertices < 0");
+  TFGB_CHECK_ARG(offsets != nullptr, "offsets is NULL");
+  TFGB_CHECK_ARG(H != nullptr && E != nullptr, "H/E is NULL");
+  if (!seg_offsets) n_seg = 1;
+  TFGB_CHECK_ARG(n_seg >= 1, "n_seg < 1");
+  const int32_t V = n_vertices;
+  TFGB_CHECK_ARG(offsets[0] == 0, "offsets[0] != 0");
+  for (int32_t v = 0; v < V; ++v) TFGB_CHECK_ARG(offsets[v + 1] >= offsets[v], "offsets not monotone");
+  const int64_t D = offsets[V];
+  TFGB_CHECK_ARG(D == 0 || indices != nullptr, "indices is NULL");
+  std::vector<int64_t> seg(n_seg + 1);
+  if (seg_offsets) {
+    for (int s = 0; s <= n_seg; ++s) seg[s] = seg_offsets[s];
+    TFGB_CHECK_ARG(seg[0] == 0 && seg[n_seg] == V, "segment offsets must span [0, V]");
+    for (int s = 0; s < n_seg; ++s) TFGB_CHECK_ARG(seg[s + 1] >= seg[s], "segment offsets not monotone");
+  } else {
+    seg[0] = 0;
+    seg[1] = V;
+  }
+  std::vector<int32_t> seg_of(V);
+  int32_t vmax = 1;
+  for (int s = 0; s < n_seg; ++s) {
+    const int64_t len = seg[s + 1] - seg[s];
+    TFGB_CHECK_ARG(len <= tfgb::kMaxSegVertices, "segment larger than 2^24-1 vertices");
+    vmax = std::max<int32_t>(vmax, static_cast<int32_t>(len));
+    for (int64_t v = seg[s]; v < seg[s + 1]; ++v) seg_of[v] = s;
+  }
+  for (int s = 0; s < n_seg; ++s) {
+    TFGB_CHECK_ARG(std::isfinite(H[s]) && std::isfinite(E[s]), "H/E must be finite");
+  }
+
+  // Clean the lists: validate, drop self entries, mark entries whose reverse
+  // is missing.  Neighbour order inside a list never changes the partition.
+  std::vector<int64_t> off(V + 1, 0);
+  std::vector<int32_t> idx;
+  idx.reserve(static_cast<size_t>(D));
+  for (int32_t v = 0; v < V; ++v) {
+    for (int64_t e = offsets[v]; e < offsets[v + 1]; ++e) {
+      const int32_t b = indices[e];
+      if (b < 0 || b >= V) {
+        tfgb::set_error("adjacency entry %d of vertex %d outside [0, %d)", b, v, V);
+        return TFCE_EINVAL;
+      }
+      if (seg_of[b] != seg_of[v]) {
+        tfgb::set_error("adjacency entry %d of vertex %d crosses segments", b, v);
+        return TFCE_EINVAL;
+      }
+      if (b != v) idx.push_back(b);
+    }
+    off[v + 1] = static_cast<int64_t>(idx.size());
+  }
+  for (int32_t v = 0; v < V; ++v) std::sort(idx.begin() + off[v], idx.begin() + off[v + 1]);
+  std::vector<uint32_t> packed(idx.size());
+  bool symmetric = true;
+  for (int32_t v = 0; v < V; ++v) {
+    for (int64_t e = off[v]; e < off[v + 1]; ++e) {
+      const int32_t b = idx[e];
+      const bool rev = std::binary_search(idx.begin() + off[b], idx.begin() + off[b + 1], v);
+      packed[e] = static_cast<uint32_t>(b) | (rev ? 0u : tfgb::kOneWay);
+      symmetric = symmetric && rev;
+    }
+  }
+
+  tfce_adjset* h = new tfce_adjset();
+  cudaGetDevice(&h->device);
+  h->V = V;
+  h->D = static_cast<int64_t>(packed.size());
+  h->n_seg = n_seg;
+  h->symmetric = symmetric;
+  h->vmax_seg = vmax;
+  h->seg_off = seg;
+  h->H.assign(H, H + n_seg);
+  h->E.assign(E, E + n_seg);
+  auto fail = [&](int rc) {
+    release(h);
+    delete h;
+    return rc;
+  };
+#define TFGB_CUDA_H(call)                                                           \
+  do {                                                                              \
+    cudaError_t _e = (call);                                                        \
+    if (_e != cudaSuccess) {                                                        \
+      tfgb::set_error("%s: %s", #call, cudaGetErrorString(_e));                     \
+      return fail(_e == cudaErrorMemoryAllocation ? TFCE_ENOMEM : TFCE_EDEVICE);    \
+    }                                                                               \
+  } while (0)
+  TFGB_CUDA_H(cudaMalloc(&h->d_offsets, sizeof(int64_t) * (V + 1)));
+  TFGB_CUDA_H(cudaMalloc(&h->d_indices, sizeof(uint32_t) * std::max<size_t>(1, packed.size())));
+  TFGB_CUDA_H(cudaMalloc(&h->d_seg_off, sizeof(int64_t) * (n_seg + 1)));
+  TFGB_CUDA_H(cudaMalloc(&h->d_H, sizeof(float) * n_seg));
+  TFGB_CUDA_H(cudaMalloc(&h->d_E, sizeof(float) * n_seg));
+  TFGB_CUDA_H(cudaMalloc(&h->d_ctrl, sizeof(int32_t) * 4));
+  TFGB_CUDA_H(cudaMemset(h->d_ctrl, 0, sizeof(int32_t) * 4));
+  TFGB_CUDA_H(cudaMemcpy(h->d_offsets, off.data(), sizeof(int64_t) * (V + 1), cudaMemcpyHostToDevice));
+  if (!packed.empty())
+    TFGB_CUDA_H(cudaMemcpy(h->d_indices, packed.data(), sizeof(uint32_t) * packed.size(),
+                           cudaMemcpyHostToDevice));
+  TFGB_CUDA_H(cudaMemcpy(h->d_seg_off, seg.data(), sizeof(int64_t) * (n_seg + 1), cudaMemcpyHostToDevice));
+  TFGB_CUDA_H(cudaMemcpy(h->d_H, H, sizeof(float) * n_seg, cudaMemcpyHostToDevice));
+  TFGB_CUDA_H(cudaMemcpy(h->d_E, E, sizeof(float) * n_seg, cudaMemcpyHostToDevice));
+#undef TFGB_CUDA_H
+  *out = h;
+  return TFCE_OK;
+}
+
+void tfce_adjset_destroy(tfce_adjset* h) {
+  if (!h) return;
+  release(h);
+  delete h;
+}
+
+int tfce_adjset_set_params(tfce_adjset* h, const float* H, const float* E) {
+  tfgb::clear_error();
+  TFGB_CHECK_ARG(h && H && E, "NULL argument");
+  std::lock_guard<std::mutex> lk(h->mu);
+  for (int s = 0; s < h->n_seg; ++s)
+    TFGB_CHECK_ARG(std::isfinite(H[s]) && std::isfinite(E[s]), "H/E must be finite");
+  h->H.assign(H, H + h->n_seg);
+  h->E.assign(E, E + h->n_seg);
+  TFGB_CUDA(cudaMemcpy(h->d_H, H, sizeof(float) * h->n_seg, cudaMemcpyHostToDevice));
+  TFGB_CUDA(cudaMemcpy(h->d_E, E, sizeof(float) * h->n_seg, cudaMemcpyHostToDevice));
+  return TFCE_OK;
+}
+
+int tfce_adjset_is_symmetric(const tfce_adjset* h) { return (h && h->symmetric) ? 1 : 0; }
+
+int tfce_adjset_run(tfce_adjset* h, const float* image, float* enhn, int32_t n_vertices) {
+  return tfce_adjset_run_labels(h, image, enhn, n_vertices, nullptr, nullptr, 0, nullptr);
+}
+
+int tfce_adjset_run_labels(tfce_adjset* h, const float* image, float* enhn, int32_t n_vertices,
+                           int32_t* labels, int32_t* extents, int32_t max_steps,
+                           int32_t* n_steps) {
+  tfgb::clear_error();
+  TFGB_CHECK_ARG(h != nullptr, "handle is NULL");
+  TFGB_CHECK_ARG(image != nullptr && enhn != nullptr, "image/enhn is NULL");
+  TFGB_CHECK_ARG(n_vertices == h->V, "array length differs from the adjacency set's vertex count");
+  TFGB_CHECK_ARG(h->n_seg == 1 || labels == nullptr, "label recording needs a one-segment handle");
+  TFGB_CHECK_ARG(labels == nullptr || (extents != nullptr && max_steps > 0), "labels need extents/max_steps");
+  std::lock_guard<std::mutex> lk(h->mu);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev != h->device) TFGB_CUDA(cudaSetDevice(h->device));
+  const int32_t V = h->V;
+  int rc = ensure_run_buffers(h, V);
+  int32_t *d_lab = nullptr, *d_ext = nullptr;
+  if (rc == TFCE_OK && V > 0) {
+    cudaStream_t st = nullptr;
+    const size_t lab_bytes = sizeof(int32_t) * (size_t)max_steps * V;
+    do {
+      if (labels) {
+        if (cudaMalloc(&d_lab, lab_bytes) != cudaSuccess || cudaMalloc(&d_ext, lab_bytes) != cudaSuccess) {
+          tfgb::set_error("label buffers: out of device memory");
+          rc = TFCE_ENOMEM;
+          break;
+        }
+        if (cudaMemset(d_lab, 0xff, lab_bytes) != cudaSuccess || cudaMemset(d_ext, 0, lab_bytes) != cudaSuccess) {
+          rc = TFCE_EDEVICE;
+          break;
+        }
+      }
+      if (cudaMemcpy(h->d_img, image, sizeof(float) * V, cudaMemcpyHostToDevice) != cudaSuccess ||
+          cudaMemcpy(h->d_enh, enhn, sizeof(float) * V, cudaMemcpyHostToDevice) != cudaSuccess) {
+        tfgb::set_error("host->device copy failed");
+        rc = TFCE_EDEVICE;
+        break;
+      }
+      rc = launch_sweep(h, h->d_img, V, 1, 1, nullptr, 0, nullptr, h->d_enh, 2, d_lab, d_ext,
+                        max_steps, st);
+      if (rc) break;
+      int32_t steps = 0;
+      rc = check_device_error(h, st, &steps);
+      if (rc) break;
+      if (cudaMemcpy(enhn, h->d_enh, sizeof(float) * V, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        tfgb::set_error("device->host copy failed");
+        rc = TFCE_EDEVICE;
+        break;
+      }
+      if (labels) {
+        const int32_t keep = std::min(steps, max_steps);
+        if (cudaMemcpy(labels, d_lab, sizeof(int32_t) * (size_t)keep * V, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(extents, d_ext, sizeof(int32_t) * (size_t)keep * V, cudaMemcpyDeviceToHost) != cudaSuccess) {
+          rc = TFCE_EDEVICE;
+          break;
+        }
+        if (steps > max_steps) {
+          tfgb::set_error("label buffer holds %d steps, sweep used %d", max_steps, steps);
+          rc = TFCE_ERANGE;
+        }
+      }
+      if (n_steps) *n_steps = steps;
+    } while (0);
+  }
+  cudaFree(d_lab);
+  cudaFree(d_ext);
+  if (dev != h->device) cudaSetDevice(dev);
+  return rc;
+}
+
+int tfce_sweep_batch(tfce_adjset* h, const float* stats, int64_t map_stride, int32_t n_maps,
+                     int32_t signs, const float* vdensity, int32_t floor_zero, float* out_max,
+                     float* out_maps, int32_t out_mode, void* stream) {
+  tfgb::clear_error();
+  TFGB_CHECK_ARG(h != nullptr, "handle is NULL");
+  TFGB_CHECK_ARG(n_maps >= 0, "n_maps < 0");
+  TFGB_CHECK_ARG(signs == 1 || signs == 2, "signs must be 1 or 2");
+  TFGB_CHECK_ARG(n_maps == 0 || stats != nullptr, "stats is NULL");
+  TFGB_CHECK_ARG(map_stride >= h->V, "map_stride < V");
+  TFGB_CHECK_ARG(out_mode >= 0 && out_mode <= 2, "out_mode must be 0, 1 or 2");
+  TFGB_CHECK_ARG(out_mode == 0 || out_maps != nullptr, "out_maps is NULL");
+  TFGB_CHECK_ARG(out_max != nullptr || out_mode != 0, "nothing to write");
+  std::lock_guard<std::mutex> lk(h->mu);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int rc = launch_sweep(h, stats, map_stride, n_maps, signs, vdensity, floor_zero, out_max,
+                        out_maps, out_mode, nullptr, nullptr, 0, st);
+  return rc;
+}
+
+// Error word of the last batched sweep on this handle (synchronises `stream`).
+int tfce_sweep_status(tfce_adjset* h, void* stream) {
+  tfgb::clear_error();
+  TFGB_CHECK_ARG(h != nullptr, "handle is NULL");
+  std::lock_guard<std::mutex> lk(h->mu);
+  return check_device_error(h, static_cast<cudaStream_t>(stream), nullptr);
+}
+
+}  // extern "C"

@@ -1,0 +1,194 @@
+"""Drop-in for the hot-path functions of ``tfce_mediation.pyfunc``.
+
+Same names, arguments, outputs and file formats as tfce_mediation/pyfunc.py;
+sweeps, regressions and indirect-effect maps run on the GPU:
+
+* create_adjac_vertex / create_adjac_voxel       (pyfunc.py:37-76)
+* write_vertStat_img / write_voxelStat_img       (pyfunc.py:80-103)
+* write_perm_maxTFCE_vertex / _voxel             (pyfunc.py:107-126)
+* calc_sobelz                                    (pyfunc.py:130-162)
+* find_nearest                                   (pyfunc.py:254-261)
+* calc_indirect, check_blocks, rand_blocks       (pyfunc.py:2678-2757)
+"""
+from __future__ import annotations
+
+import math
+import os
+
+import numpy as np
+
+from . import _lib
+from .adjacency import create_adjac_vertex, create_adjac_voxel  # noqa: F401
+from .device import dev, ptr, require_cuda, stream_handle
+from .glm import WHAT_T, DesignBatch, glm_stat
+from .io import save_mgh, save_nifti
+
+ALG = {"aroian": 0, "sobel": 1, "goodman": 2}
+
+
+def _append(path, line):
+    with open(path, "a") as fh:
+        fh.write(line + "\n")
+
+
+def _sweep_max_scaled(op, stat_full, density):
+    """Max over one hemisphere of TFCE * (max/100) * density (pyfunc.py:116-117),
+    computed by one device sweep."""
+    t = require_cuda()
+    adj = op.adjacency
+    s = dev(np.ascontiguousarray(stat_full, np.float32))
+    vd = None
+    if not (np.isscalar(density) and float(density) == 1.0):
+        vd = dev(np.ascontiguousarray(np.broadcast_to(np.asarray(density, np.float32), s.shape)))
+    out = t.empty(1, device="cuda", dtype=t.float32)
+    adj.sweep_batch(ptr(s), s.numel(), 1, 1, ptr(vd), 0, ptr(out))
+    adj.status()
+    return np.float32(out.item())
+
+
+def write_perm_maxTFCE_vertex(statname, vertStat, num_vertex, bin_mask_lh, bin_mask_rh, calcTFCE_lh,
+                              calcTFCE_rh, density_corr_lh=1, density_corr_rh=1):
+    """Scatter into zero-filled hemispheres, sweep each, scale, append the max to
+    perm_<statname>_TFCE_maxVertex.csv as %.4f (pyfunc.py:107-119)."""
+    lh = np.zeros(bin_mask_lh.shape[0], np.float32)
+    rh = np.zeros(bin_mask_rh.shape[0], np.float32)
+    lh[bin_mask_lh] = vertStat[:num_vertex]
+    rh[bin_mask_rh] = vertStat[num_vertex:]
+    m = max(_sweep_max_scaled(calcTFCE_lh, lh, density_corr_lh),
+            _sweep_max_scaled(calcTFCE_rh, rh, density_corr_rh))
+    _append("perm_%s_TFCE_maxVertex.csv" % statname, "%.4f" % m)
+
+
+def write_perm_maxTFCE_voxel(statname, voxelStat, TFCEfunc):
+    """pyfunc.py:121-126: max(TFCE) * max(stat)/100, appended as %1.4f."""
+    m = _sweep_max_scaled(TFCEfunc, np.asarray(voxelStat, np.float32), 1)
+    _append("perm_%s_TFCE_maxVoxel.csv" % statname, "%1.4f" % m)
+
+
+def _tfce_map(op, image):
+    e = np.zeros(image.shape[0], np.float32)
+    op.run(np.ascontiguousarray(image, np.float32), e)
+    return e
+
+
+def write_vertStat_img(statname, vertStat, outdata_mask, affine_mask, surf, hemi, bin_mask, TFCEfunc,
+                       all_vertex, density_corr=1, TFCE=True):
+    """pyfunc.py:80-92: TFCE image scaled by max(masked stat)/100 * density,
+    max appended to max_TFCE_contrast_values.csv, both images saved as MGH."""
+    vertStat_out = np.zeros(all_vertex).astype(np.float32, order="C")
+    vertStat_out[bin_mask] = vertStat
+    if TFCE:
+        vertStat_TFCE = _tfce_map(TFCEfunc, vertStat_out)
+        outdata_mask[:, 0, 0] = vertStat_TFCE * (vertStat[np.isfinite(vertStat)].max() / 100) * density_corr
+        _append("max_TFCE_contrast_values.csv", "%s_%s_%s,%f" % (
+            statname, surf, hemi, outdata_mask[np.isfinite(outdata_mask[:, 0, 0])].max()))
+        save_mgh(outdata_mask, affine_mask, "%s_%s_%s_TFCE.mgh" % (statname, surf, hemi))
+    outdata_mask[:, 0, 0] = vertStat_out
+    save_mgh(outdata_mask, affine_mask, "%s_%s_%s.mgh" % (statname, surf, hemi))
+
+
+def write_voxelStat_img(statname, voxelStat, out_path, data_index, affine, TFCEfunc, imgext=".nii.gz",
+                        TFCE=True):
+    """pyfunc.py:94-103."""
+    if TFCE:
+        voxelStat_out = voxelStat.astype(np.float32, order="C")
+        voxelStat_TFCE = _tfce_map(TFCEfunc, voxelStat_out)
+        out_path[data_index] = voxelStat_TFCE * (voxelStat_out.max() / 100)
+        save_nifti(out_path, affine, "%s_TFCE%s" % (statname, imgext))
+        _append("max_TFCE_contrast_values.csv", "%s,%f" % (statname, out_path.max()))
+    out_path[data_index] = voxelStat
+    save_nifti(out_path, affine, "%s%s" % (statname, imgext))
+
+
+# ---------------------------------------------------------------------------
+# mediation
+# ---------------------------------------------------------------------------
+def mediation_designs(medtype, pred_x, depend_y, n):
+    """Path-a and path-b designs of calc_sobelz (pyfunc.py:131-145); the tested
+    coefficient is column 1 of each.  For medtype 'Y' path a is a scalar
+    regression of depend_y on pred_x (scipy linregress), returned as ta."""
+    x = np.asarray(pred_x, np.float64).reshape(n, -1)
+    dy = np.asarray(depend_y, np.float64).reshape(n, -1)
+    one = np.ones((n, 1))
+    if medtype == "I":
+        return np.hstack([one, x]), np.hstack([one, x, dy]), None
+    if medtype == "M":
+        return np.hstack([one, x]), np.hstack([one, dy, x]), None
+    if medtype == "Y":
+        from scipy.stats import linregress
+        lr = linregress(np.asarray(pred_x, np.float64).ravel(), np.asarray(depend_y, np.float64).ravel())
+        return None, np.hstack([one, dy, x]), lr.slope / lr.stderr
+    raise ValueError("Invalid mediation type")
+
+
+def sobel_from_t(ta, tb, alg="aroian", ta_scalar=None):
+    """Indirect-effect z of path t maps (device tensors (P, V)) -> (P, V)."""
+    t = require_cuda()
+    P, V = tb.shape
+    z = t.empty((P, V), device="cuda", dtype=t.float32)
+    tas = None if ta_scalar is None else dev(np.asarray(ta_scalar, np.float32).reshape(P))
+    _lib.check(_lib.load().sobel_combine(ptr(ta), V, ptr(tas), ptr(tb), V, P, V, ALG[alg], ptr(z), V,
+                                         stream_handle()))
+    return z
+
+
+def calc_sobelz(medtype, pred_x, depend_y, merge_y, n, num_vertex, alg="aroian"):
+    """Sobel/Aroian/Goodman z per vertex (pyfunc.py:130-162), float64 host array."""
+    if alg not in ALG:
+        raise ValueError("Unknown indirect test algorithm")
+    Xa, Xb, ta_scalar = mediation_designs(medtype, pred_x, depend_y, n)
+    Y = np.asarray(merge_y, np.float32)
+    if ta_scalar is None:
+        tab = glm_stat(Y, DesignBatch([Xa, Xb]), WHAT_T, coef=[1])[:, 0]
+        z = sobel_from_t(tab[0:1], tab[1:2], alg)
+    else:
+        tb = glm_stat(Y, DesignBatch([Xb]), WHAT_T, coef=[1])[:, 0]
+        z = sobel_from_t(None, tb, alg, ta_scalar=[ta_scalar])
+    return z[0].cpu().numpy().astype(np.float64)
+
+
+def calc_indirect(ta, tb, alg="aroian"):
+    """pyfunc.py:2678-2709 on the device."""
+    if alg not in ALG:
+        raise ValueError("Unknown indirect test algorithm")
+    t = require_cuda()
+    ta_d = dev(np.atleast_2d(np.asarray(ta, np.float32)), t.float32)
+    tb_d = dev(np.atleast_2d(np.asarray(tb, np.float32)), t.float32)
+    z = sobel_from_t(ta_d, tb_d, alg)
+    out = z.cpu().numpy().astype(np.float64)
+    return out[0] if np.ndim(ta) == 1 else out
+
+
+# ---------------------------------------------------------------------------
+# host helpers (no device work in the reference either)
+# ---------------------------------------------------------------------------
+def find_nearest(array, value, p_array):
+    """pyfunc.py:254-261."""
+    idx = np.searchsorted(array, value, side="left")
+    if idx == len(p_array):
+        return p_array[idx - 1]
+    elif math.fabs(value - array[idx - 1]) < math.fabs(value - array[idx]):
+        return p_array[idx - 1]
+    else:
+        return p_array[idx]
+
+
+def check_blocks(block_list):
+    """pyfunc.py:2711-2731."""
+    unique_blocks = np.unique(block_list)
+    sizes = [len(block_list[block_list == b]) for b in unique_blocks]
+    eq = all(x == sizes[0] for x in sizes)
+    if not eq:
+        print("Warning: blocks are not equal. Swaping with only occur within blocks, but not among blocks.")
+    return eq
+
+
+def rand_blocks(block_list, is_equal_sizes):
+    """pyfunc.py:2733-2757 (draws from the global legacy numpy RNG, as the reference)."""
+    indexer = np.array(range(len(block_list)))
+    randindex = []
+    blocks = np.random.permutation(list(np.unique(block_list))) if is_equal_sizes is True \
+        else np.unique(block_list)
+    for block in blocks:
+        randindex.append(np.random.permutation(indexer[block_list == block]))
+    return np.concatenate(randindex)
