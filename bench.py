@@ -43,16 +43,17 @@ def measured_peaks():
 
 
 def profile_traffic(kernel):
-    """dram bytes per launch recorded in profiles/<kernel>*.md (line
-    'dram_bytes_per_launch: <int> (<launch description>)') or None."""
+    """DRAM bytes per sweep recorded from an ncu capture in
+    profiles/<kernel>*.md (line 'dram_bytes_per_sweep: <number> (<note>)'),
+    or (None, None)."""
     d = os.path.join(ROOT, "profiles")
     if not os.path.isdir(d):
         return None, None
     for f in sorted(os.listdir(d)):
         if f.startswith(kernel) and f.endswith(".md"):
-            m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)\s*\(([^)]*)\)", open(os.path.join(d, f)).read())
+            m = re.search(r"dram_bytes_per_sweep:\s*([0-9.eE+]+)\s*\(([^)]*)\)", open(os.path.join(d, f)).read())
             if m:
-                return float(m.group(1)), m.group(2)
+                return float(m.group(1)), f"{m.group(2)} [profiles/{f}]"
     return None, None
 
 
@@ -308,7 +309,8 @@ def run_gpu(args):
     sweep_avg = float(np.mean(sweep_ms))
     glm_avg = float(np.mean(glm_ms))
     achieved = bytes_per_sweep * sweeps_per_launch / (sweep_avg / 1000) / 1e9
-    traffic, traffic_note = profile_traffic("tfce_sweep")
+    per_sweep, traffic_note = profile_traffic("tfce_sweep")
+    traffic = None if per_sweep is None else per_sweep * sweeps_per_launch
     glm_flop = 4.0 * n * eng.k * V * P  # beta + residual passes, fp32 CUDA cores
     clocks = clk.summary()
     line = {
@@ -346,7 +348,7 @@ def run_gpu(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])

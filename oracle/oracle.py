@@ -52,10 +52,13 @@ def lib():
         l.oracle_tfce.restype = ctypes.c_int
         l.oracle_tfce.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_int32, _i64p, _i32p,
                                   _f32p, _f32p, _i32p, _i32p, ctypes.c_int]
+        l.oracle_tfce_mode.restype = ctypes.c_int
+        l.oracle_tfce_mode.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_int32, _i64p, _i32p,
+                                       _f32p, _f32p, _i32p, _i32p, ctypes.c_int, ctypes.c_int]
         l.oracle_tfce_max_batch.restype = ctypes.c_int
         l.oracle_tfce_max_batch.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_int32, _i64p,
                                             _i32p, _f32p, ctypes.c_int32, ctypes.c_float, _f32p,
-                                            ctypes.c_int, _f32p]
+                                            ctypes.c_int, _f32p, ctypes.c_int]
         l.oracle_threshold_table.restype = ctypes.c_int
         l.oracle_threshold_table.argtypes = [ctypes.c_float, _f32p, ctypes.c_int]
         _LIB = l
@@ -100,22 +103,26 @@ def threshold_table(maxT: float) -> np.ndarray:
     return buf[:n].copy()
 
 
-def tfce(offsets, indices, image, H, E, enhn=None):
+def tfce(offsets, indices, image, H, E, enhn=None, hh_exact=False):
     """One sweep: tfce_mediation/lib/fast_tfce.hpp:11-95 as called by
-    tfce_mediation/tfce.pyx:44-45.  Accumulates into ``enhn``."""
+    tfce_mediation/tfce.pyx:44-45.  Accumulates into ``enhn``.
+
+    hh_exact=False uses powf(T, H) for the threshold weight as the reference
+    does; hh_exact=True uses the correctly rounded power (the device's
+    arithmetic), for bit-for-bit checks of the kernel."""
     offsets, indices = _csr(offsets, indices)
     image = np.ascontiguousarray(image, dtype=np.float32)
     V = image.shape[0]
     if enhn is None:
         enhn = np.zeros(V, np.float32)
-    rc = lib().oracle_tfce(H, E, V, _p(offsets, _i64p), _p(indices, _i32p), _p(image, _f32p),
-                           _p(enhn, _f32p), None, None, -1)
+    rc = lib().oracle_tfce_mode(H, E, V, _p(offsets, _i64p), _p(indices, _i32p), _p(image, _f32p),
+                                _p(enhn, _f32p), None, None, -1, int(bool(hh_exact)))
     if rc < 0:
         raise ValueError("oracle sweep failed")
     return enhn
 
 
-def tfce_labels(offsets, indices, image, H, E):
+def tfce_labels(offsets, indices, image, H, E, hh_exact=False):
     """Sweep plus per-threshold component labels (root vertex id, -1 inactive)
     and extents; (enhn, labels[L,V], extents[L,V])."""
     offsets, indices = _csr(offsets, indices)
@@ -126,8 +133,9 @@ def tfce_labels(offsets, indices, image, H, E):
     enhn = np.zeros(V, np.float32)
     labels = np.full((max(L, 1), V), -1, np.int32)
     extents = np.zeros((max(L, 1), V), np.int32)
-    rc = lib().oracle_tfce(H, E, V, _p(offsets, _i64p), _p(indices, _i32p), _p(image, _f32p),
-                           _p(enhn, _f32p), _p(labels, _i32p), _p(extents, _i32p), -1)
+    rc = lib().oracle_tfce_mode(H, E, V, _p(offsets, _i64p), _p(indices, _i32p), _p(image, _f32p),
+                                _p(enhn, _f32p), _p(labels, _i32p), _p(extents, _i32p), -1,
+                                int(bool(hh_exact)))
     if rc < 0:
         raise ValueError("oracle sweep failed")
     return enhn, labels[:rc], extents[:rc]
@@ -147,7 +155,8 @@ def ref_tfce(offsets, indices, image, H, E, enhn=None):
     return enhn
 
 
-def tfce_max_batch(offsets, indices, maps, H, E, sign=1.0, vdensity=None, floor_zero=False):
+def tfce_max_batch(offsets, indices, maps, H, E, sign=1.0, vdensity=None, floor_zero=False,
+                   hh_exact=False):
     """Per-map scaled max, the body of tfce_mediation/pyfunc.py:107-119 for one
     hemisphere (TFCE * max/100 * vdensity, then max)."""
     offsets, indices = _csr(offsets, indices)
@@ -159,7 +168,7 @@ def tfce_max_batch(offsets, indices, maps, H, E, sign=1.0, vdensity=None, floor_
     rc = lib().oracle_tfce_max_batch(H, E, maps.shape[1], _p(offsets, _i64p), _p(indices, _i32p),
                                      _p(maps, _f32p), maps.shape[0], sign,
                                      None if vd is None else _p(vd, _f32p), int(floor_zero),
-                                     _p(out, _f32p))
+                                     _p(out, _f32p), int(bool(hh_exact)))
     if rc < 0:
         raise ValueError("oracle sweep failed")
     return out

@@ -79,9 +79,30 @@ int oracle_threshold_table(float maxT, float* T_out, int cap) {
  *   extents (n_steps x V): size of that component, 0 when inactive.
  * Returns the number of thresholds processed, or -1 on error.
  */
+/* HH at threshold T.  hh_mode 0: powf(T, H), what the reference computes
+ * (fast_tfce.hpp:70).  hh_mode 1: the correctly rounded power -- T*T for
+ * H == 2, else the double power rounded once -- which is what the device
+ * computes; the two differ only where the libm powf is off by one ulp. */
+static float oracle_hh(float T, float H, int hh_mode) {
+  if (hh_mode == 0) return powf(T, H);
+  if (H == 2.0f) return T * T;
+  if (H == 1.0f) return T;
+  return (float)pow((double)T, (double)H);
+}
+
+int oracle_tfce_mode(float H, float E, int32_t V, const int64_t* offsets,
+                     const int32_t* indices, const float* image, float* enhn,
+                     int32_t* labels, int32_t* extents, int max_steps, int hh_mode);
+
 int oracle_tfce(float H, float E, int32_t V, const int64_t* offsets,
                 const int32_t* indices, const float* image, float* enhn,
                 int32_t* labels, int32_t* extents, int max_steps) {
+  return oracle_tfce_mode(H, E, V, offsets, indices, image, enhn, labels, extents, max_steps, 0);
+}
+
+int oracle_tfce_mode(float H, float E, int32_t V, const int64_t* offsets,
+                     const int32_t* indices, const float* image, float* enhn,
+                     int32_t* labels, int32_t* extents, int max_steps, int hh_mode) {
   if (V <= 0) return 0;
   vk_t* keys = (vk_t*)malloc(sizeof(vk_t) * (size_t)V);
   int32_t* rank = (int32_t*)malloc(sizeof(int32_t) * (size_t)V);
@@ -131,7 +152,7 @@ int oracle_tfce(float H, float E, int32_t V, const int64_t* offsets,
       }
       ++j;
     }
-    const float HH = powf(Ts, H);
+    const float HH = oracle_hh(Ts, H, hh_mode);
     if (labels) for (int32_t u = 0; u < V; ++u) labels[(int64_t)s * V + u] = -1;
     if (extents) for (int32_t u = 0; u < V; ++u) extents[(int64_t)s * V + u] = 0;
     for (int32_t q = 0; q < n_act; ++q) {
@@ -161,7 +182,7 @@ fail:
 int oracle_tfce_max_batch(float H, float E, int32_t V, const int64_t* offsets,
                           const int32_t* indices, const float* maps,
                           int32_t n_maps, float sign, const float* vdensity,
-                          int floor_zero, float* out_max) {
+                          int floor_zero, float* out_max, int hh_mode) {
   float* img = (float*)malloc(sizeof(float) * (size_t)V);
   float* enh = (float*)malloc(sizeof(float) * (size_t)V);
   for (int32_t m = 0; m < n_maps; ++m) {
@@ -171,7 +192,7 @@ int oracle_tfce_max_batch(float H, float E, int32_t V, const int64_t* offsets,
       enh[i] = 0.0f;
       if (isfinite(img[i]) && img[i] > mx) mx = img[i];
     }
-    if (oracle_tfce(H, E, V, offsets, indices, img, enh, NULL, NULL, -1) < 0) {
+    if (oracle_tfce_mode(H, E, V, offsets, indices, img, enh, NULL, NULL, -1, hh_mode) < 0) {
       free(img); free(enh);
       return -1;
     }

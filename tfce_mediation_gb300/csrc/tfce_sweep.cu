@@ -146,11 +146,15 @@ __device__ inline float increment(int32_t extent, float E, int e_mode, float HH)
   return __double2float_rn(__dmul_rn(pe, static_cast<double>(HH)));
 }
 
-// HH = pow(T, H) in float (fast_tfce.hpp:70).
+// HH = pow(T, H) as a float (fast_tfce.hpp:70), correctly rounded: T*T for
+// H == 2 (exact product, one rounding), otherwise the double-precision power
+// rounded once to float.  The reference calls the host libm's powf, which is
+// not always correctly rounded (glibc: <= 0.82 ulp), so at rare thresholds
+// its HH can sit one float ulp away from this value.
 __device__ inline float pow_h(float T, float H) {
   if (H == 2.0f) return __fmul_rn(T, T);
   if (H == 1.0f) return T;
-  return powf(T, H);
+  return __double2float_rn(pow(static_cast<double>(T), static_cast<double>(H)));
 }
 
 __device__ inline float block_max(float v, float* red) {
