@@ -106,6 +106,39 @@ int tfce_sweep_batch(tfce_adjset* h, const float* stats, int64_t map_stride, int
  * TFCE_ERANGE (threshold table overflow). */
 int tfce_sweep_status(tfce_adjset* h, void* stream);
 
+/* Allocation-free form of tfce_sweep_batch.  No counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory while they sweep: a host
+ * whose device memory is reserved up front by another allocator, a real-time
+ * loop that must keep a fixed footprint, or a program that cannot take the
+ * device-wide synchronisation that cudaFree implies.  Nothing is allocated:
+ * no handle, no cudaMalloc/cudaFree.  The scratch is a 64 MiB static device
+ * array inside this library, which every process that loads the library holds
+ * on each GPU it uses until exit.
+ *
+ *   offsets [n_vertices+1] (int64), indices [n_entries] (int32): the caller's
+ *     adjacency, already on the device, in the same CSR form tfce_adjset_create
+ *     takes (it need not be symmetric; self entries are allowed);
+ *   seg_offsets [n_seg+1] (device int64), H/E [n_seg] (device float);
+ *   max_segment_vertices: an upper bound on the vertex count of every segment;
+ *     at most 2,796,160 (what one workspace slot of the 64 MiB holds) --
+ *     larger values return TFCE_ERANGE before any device work; a segment
+ *     found larger on the device returns TFCE_EINVAL;
+ *   stats, map_stride, n_maps, signs, vdensity, floor_zero, out_max: as
+ *     tfce_sweep_batch (device pointers; only the maxima are written).
+ * The first call on each device looks up the array's device address with
+ * that device current; make that first call before any stream capture.  The
+ * call returns when the sweeps have finished (it synchronises `stream`) with
+ * the device status.  All calls share the one array, which keeps the last
+ * call's contents (the queue and error words are cleared on entry): calls
+ * that overlap on the GPU -- from two threads, or on two streams -- race. */
+int tfce_sweep_batch_noalloc(const int64_t* offsets, const int32_t* indices, int32_t n_vertices,
+                             int64_t n_entries, const int64_t* seg_offsets, int32_t n_seg,
+                             int32_t max_segment_vertices, const float* H, const float* E,
+                             const float* stats, int64_t map_stride, int32_t n_maps,
+                             int32_t signs, const float* vdensity, int32_t floor_zero,
+                             float* out_max, void* stream);
+
 /* ---------------------------------------------------------------------------
  * Mass-univariate OLS t for G designs against one data matrix (device).
  *   Y       [n][ldy] float32, subjects x vertices (merge_y layout), V columns used;

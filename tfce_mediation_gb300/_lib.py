@@ -51,6 +51,10 @@ SIGNATURES = {
     "tfce_sweep_batch": (ctypes.c_int, [c_vp, c_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
                                         c_vp, ctypes.c_int32, c_vp, c_vp, ctypes.c_int32, c_vp]),
     "tfce_sweep_status": (ctypes.c_int, [c_vp, c_vp]),
+    "tfce_sweep_batch_noalloc": (ctypes.c_int, [c_vp, c_vp, ctypes.c_int32, ctypes.c_int64, c_vp,
+                                                ctypes.c_int32, ctypes.c_int32, c_vp, c_vp, c_vp,
+                                                ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, c_vp,
+                                                ctypes.c_int32, c_vp, c_vp]),
     "glm_tstat": (ctypes.c_int, [c_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int64, c_vp, c_vp,
                                  c_vp, c_vp, ctypes.c_int32, ctypes.c_int32, c_vp, ctypes.c_int32,
                                  c_vp, ctypes.c_int64, c_vp]),

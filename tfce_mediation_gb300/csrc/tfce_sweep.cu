@@ -70,6 +70,10 @@ struct SweepArgs {
   int32_t* err;
   int32_t n_items;
   const int32_t* item_order;
+  // Checked variant only (caller-provided device CSR): vertex and entry counts
+  // the kernel validates segment ranges and list extents against.
+  int32_t n_vertices;
+  int64_t n_entries;
 };
 
 struct Slot {
@@ -174,6 +178,13 @@ __device__ inline float block_max(float v, float* red) {
   return r;
 }
 
+// kChecked = false: the handle's cleaned CSR (validated on the host, entries
+// whose reverse is missing flagged).  kChecked = true: a CSR the caller keeps
+// on the device, unvalidated and unflagged -- segment ranges and list extents
+// are checked here, and the insertion-order rule is applied to every
+// same-step entry (for a symmetric pair exactly one direction passes it, so
+// the partition is the same).
+template <bool kChecked>
 __global__ void __launch_bounds__(kSweepThreads, 2) tfce_sweep_kernel(SweepArgs a) {
   __shared__ float sT[kMaxSteps];
   __shared__ float sHH[kMaxSteps];
@@ -199,6 +210,16 @@ __global__ void __launch_bounds__(kSweepThreads, 2) tfce_sweep_kernel(SweepArgs 
     const float sign = sgn ? -1.0f : 1.0f;
     const int64_t v0 = a.seg_off[seg];
     const int32_t Vs = static_cast<int32_t>(a.seg_off[seg + 1] - v0);
+    if constexpr (kChecked) {
+      const int64_t len = a.seg_off[seg + 1] - v0;
+      if (v0 < 0 || len < 0 || len > a.vcap || v0 + len > a.n_vertices) {
+        if (tid == 0) {
+          set_err(a.err, kDevBadIndex);
+          if (a.out_max) a.out_max[item] = 0.0f;
+        }
+        continue;
+      }
+    }
     const float H = a.seg_H[seg], E = a.seg_E[seg];
     const int e_mode = (E == 1.0f) ? 1 : (E == 0.5f) ? 2 : (E == 2.0f) ? 3 : 0;
     const float* x = a.stats + (int64_t)map * a.map_stride + v0;
@@ -300,7 +321,13 @@ __global__ void __launch_bounds__(kSweepThreads, 2) tfce_sweep_kernel(SweepArgs 
       // (U) union newly active vertices with already-active neighbours
       for (int32_t p = s0 + tid; p < s1; p += nth) {
         const int32_t v = sl.order[p];
-        const int64_t e0 = a.offsets[v0 + v], e1 = a.offsets[v0 + v + 1];
+        int64_t e0 = a.offsets[v0 + v], e1 = a.offsets[v0 + v + 1];
+        if constexpr (kChecked) {
+          if (e0 < 0 || e1 > a.n_entries || e1 < e0) {
+            set_err(a.err, kDevBadIndex);
+            e0 = e1 = 0;
+          }
+        }
         for (int64_t e = e0; e < e1; ++e) {
           const uint32_t raw = a.indices[e];
           const int64_t ag = static_cast<int64_t>(raw & kIndexMask) - v0;
@@ -313,7 +340,7 @@ __global__ void __launch_bounds__(kSweepThreads, 2) tfce_sweep_kernel(SweepArgs 
           if (ka == kInactiveKey) continue;
           const int la = static_cast<int>(ka >> kPosBits);
           if (la > i) continue;
-          if (la == i && (raw & kOneWay)) {
+          if (la == i && (kChecked || (raw & kOneWay))) {
             // one-directional entry: effective only if the neighbour was
             // inserted first (larger value; ties by smaller index)
             const float xa = sign * x[an], xv = sign * x[v];
@@ -436,7 +463,7 @@ int resident_slots(tfce_adjset* h) {
   if (h->max_slots) return TFCE_OK;
   int sms = 0, per_sm = 0;
   TFGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
-  TFGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tfgb::tfce_sweep_kernel,
+  TFGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tfgb::tfce_sweep_kernel<false>,
                                                           tfgb::kSweepThreads, 0));
   h->max_slots = std::max(1, sms * std::max(1, per_sm));
   return TFCE_OK;
@@ -495,7 +522,7 @@ int launch_sweep(tfce_adjset* h, const float* stats, int64_t map_stride, int32_t
   a.err = h->d_ctrl + 1;
   a.n_items = items;
   a.item_order = nullptr;
-  tfgb::tfce_sweep_kernel<<<slots, tfgb::kSweepThreads, 0, st>>>(a);
+  tfgb::tfce_sweep_kernel<false><<<slots, tfgb::kSweepThreads, 0, st>>>(a);
   TFGB_CUDA(cudaGetLastError());
   return TFCE_OK;
 }
@@ -759,3 +786,142 @@ int tfce_sweep_status(tfce_adjset* h, void* stream) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free batched sweep.
+//
+// For callers that cannot allocate device memory while they run the sweep:
+// programs whose device memory is reserved up front by another allocator (a
+// framework's caching allocator holding the whole GPU), real-time loops that
+// must keep a fixed footprint, and hosts that cannot afford the device-wide
+// synchronisation cudaFree implies.  The sweep's scratch (the per-CTA union-
+// find workspace and the queue/error words) lives in the file-scope array
+// below instead of in cudaMalloc'd memory.  Every process that loads this
+// library holds these 64 MiB on every GPU it uses, until it exits.
+// ---------------------------------------------------------------------------
+namespace tfgb {
+
+constexpr int64_t kNoAllocScratchBytes = 64LL << 20;   // 64 MiB
+constexpr int64_t kNoAllocCtrlBytes = 256;              // queue counter, error word
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+struct NoAllocDevice {
+  void* scratch = nullptr;  // device address of g_noalloc_scratch on that device
+  int max_slots = 0;        // resident CTAs of the checked kernel
+};
+
+std::mutex g_noalloc_mu;
+NoAllocDevice g_noalloc_dev[128];
+
+// Largest segment one workspace slot of the static scratch can hold.
+int32_t noalloc_max_segment() {
+  int64_t lo = 1, hi = kMaxSegVertices;
+  while (lo < hi) {  // largest v with slot_bytes(v) <= scratch - ctrl
+    const int64_t mid = (lo + hi + 1) / 2;
+    if (slot_bytes(static_cast<int32_t>(mid)) <= kNoAllocScratchBytes - kNoAllocCtrlBytes) lo = mid;
+    else hi = mid - 1;
+  }
+  return static_cast<int32_t>(lo);
+}
+
+// Per-device set-up, done by the first call on each device with that device
+// current: the host-side name of the array is not a device address, so its
+// device address is looked up once with cudaGetSymbolAddress.
+int noalloc_setup(int dev, NoAllocDevice* out) {
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (dev < 0 || dev >= 128) {
+    set_error("device ordinal %d out of range", dev);
+    return TFCE_EINVAL;
+  }
+  NoAllocDevice& d = g_noalloc_dev[dev];
+  if (!d.scratch) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+      set_error("cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
+      return TFCE_EDEVICE;
+    }
+    int sms = 0, per_sm = 0;
+    TFGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    TFGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tfce_sweep_kernel<true>,
+                                                            kSweepThreads, 0));
+    d.max_slots = std::max(1, sms * std::max(1, per_sm));
+    d.scratch = p;
+  }
+  *out = d;
+  return TFCE_OK;
+}
+
+}  // namespace tfgb
+
+extern "C" int tfce_sweep_batch_noalloc(const int64_t* offsets, const int32_t* indices,
+                                        int32_t n_vertices, int64_t n_entries,
+                                        const int64_t* seg_offsets, int32_t n_seg,
+                                        int32_t max_segment_vertices, const float* H,
+                                        const float* E, const float* stats, int64_t map_stride,
+                                        int32_t n_maps, int32_t signs, const float* vdensity,
+                                        int32_t floor_zero, float* out_max, void* stream) {
+  tfgb::clear_error();
+  TFGB_CHECK_ARG(offsets && seg_offsets && H && E && out_max, "NULL pointer");
+  TFGB_CHECK_ARG(n_entries == 0 || indices != nullptr, "indices is NULL");
+  TFGB_CHECK_ARG(n_vertices >= 0 && n_entries >= 0 && n_seg >= 1, "bad sizes");
+  TFGB_CHECK_ARG(n_maps >= 0, "n_maps < 0");
+  TFGB_CHECK_ARG(n_maps == 0 || stats != nullptr, "stats is NULL");
+  TFGB_CHECK_ARG(signs == 1 || signs == 2, "signs must be 1 or 2");
+  TFGB_CHECK_ARG(map_stride >= n_vertices, "map_stride < n_vertices");
+  TFGB_CHECK_ARG(max_segment_vertices >= 1, "max_segment_vertices < 1");
+  const int32_t cap = tfgb::noalloc_max_segment();
+  if (max_segment_vertices > cap) {
+    tfgb::set_error("segments of %d vertices exceed the static scratch: at most %d vertices per "
+                    "segment (64 MiB)", max_segment_vertices, cap);
+    return TFCE_ERANGE;
+  }
+  const int64_t items64 = (int64_t)n_maps * signs * n_seg;
+  TFGB_CHECK_ARG(items64 < (1LL << 31), "too many sweep items");
+  const int32_t items = static_cast<int32_t>(items64);
+  if (items == 0) return TFCE_OK;
+  int dev = 0;
+  TFGB_CUDA(cudaGetDevice(&dev));
+  tfgb::NoAllocDevice nd;
+  int rc = tfgb::noalloc_setup(dev, &nd);
+  if (rc) return rc;
+  const int64_t per_slot = tfgb::slot_bytes(max_segment_vertices);
+  const int64_t fit = (tfgb::kNoAllocScratchBytes - tfgb::kNoAllocCtrlBytes) / per_slot;
+  const int32_t slots = static_cast<int32_t>(std::min<int64_t>({(int64_t)items, fit, (int64_t)nd.max_slots}));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  char* base = static_cast<char*>(nd.scratch);
+  int32_t* ctrl = reinterpret_cast<int32_t*>(base);
+  // the array keeps the previous call's contents: the queue counter and the
+  // error word must start at zero; the workspace slots are rebuilt per item
+  TFGB_CUDA(cudaMemsetAsync(ctrl, 0, 4 * sizeof(int32_t), st));
+  tfgb::SweepArgs a{};
+  a.offsets = offsets;
+  a.indices = reinterpret_cast<const uint32_t*>(indices);
+  a.stats = stats;
+  a.map_stride = map_stride;
+  a.n_maps = n_maps;
+  a.n_signs = signs;
+  a.n_seg = n_seg;
+  a.seg_off = seg_offsets;
+  a.seg_H = H;
+  a.seg_E = E;
+  a.vdensity = vdensity;
+  a.floor_zero = floor_zero;
+  a.out_max = out_max;
+  a.out_maps = nullptr;
+  a.out_mode = 0;
+  a.ws = base + tfgb::kNoAllocCtrlBytes;
+  a.ws_slot_bytes = per_slot;
+  a.vcap = max_segment_vertices;
+  a.counter = ctrl;
+  a.err = ctrl + 1;
+  a.n_items = items;
+  a.n_vertices = n_vertices;
+  a.n_entries = n_entries;
+  tfgb::tfce_sweep_kernel<true><<<slots, tfgb::kSweepThreads, 0, st>>>(a);
+  TFGB_CUDA(cudaGetLastError());
+  int32_t hctrl[2] = {0, 0};
+  TFGB_CUDA(cudaMemcpyAsync(hctrl, ctrl, sizeof(hctrl), cudaMemcpyDeviceToHost, st));
+  TFGB_CUDA(cudaStreamSynchronize(st));
+  return tfgb::map_dev_err(hctrl[1]);
+}
