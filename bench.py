@@ -287,7 +287,7 @@ def run_gpu(args):
         dist.barrier()
     t0 = time.perf_counter()
     for s in range(e2e_steps):
-        eng.Yd.copy_(Yh, non_blocking=True)
+        eng.upload(Yh)
         pr = E.permutations(n, SEED, 10 ** 6 + base + s * P, 10 ** 6 + base + (s + 1) * P)
         res = eng.run_batch(pr)
     torch.cuda.synchronize()

@@ -72,6 +72,19 @@ int tfce_adjset_set_params(tfce_adjset* h, const float* H, const float* E);
  * case), 0 otherwise. */
 int tfce_adjset_is_symmetric(const tfce_adjset* h);
 
+/* How tfce_sweep_batch accumulates (the other entry points always use 0):
+ *   0  the reference's arithmetic: every active vertex adds its float
+ *      increment to a float accumulator at every threshold
+ *      (fast_tfce.hpp:72-84), so results are bit-identical to the reference
+ *      up to its libm's powf rounding (the default);
+ *   1  per-component: each live component adds its increment once per
+ *      threshold in double, and a vertex's value is resolved at the end along
+ *      the chain of components it joined; the value is the float rounding of
+ *      the exact sum of the same float increments, i.e. it differs from the
+ *      reference by the reference's own float summation error (~1e-7 rel).
+ *      Work per threshold is O(live components) instead of O(active vertices). */
+int tfce_adjset_set_accumulation(tfce_adjset* h, int32_t mode);
+
 /* CreateAdjSet.run(image, enhn) on host float32 arrays of length V (one
  * segment: the whole handle).  Accumulates the sweep into enhn, as
  * fast_tfce.hpp:82 does.  Synchronous. */

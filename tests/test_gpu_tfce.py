@@ -196,3 +196,69 @@ def test_degenerate_maps(golden):
     single.run(np.array([3.0], np.float32), e)
     np.testing.assert_array_equal(e, oracle.tfce(np.array([0, 0]), np.zeros(0, np.int32),
                                                  np.array([3.0], np.float32), 2.0, 1.0, hh_exact=True))
+
+
+COMPONENT_RTOL = 1e-5
+# Per-component sums resolve a vertex as a difference of component potentials
+# (doubles of the order of the map's largest value); vertices that enter only
+# at the last thresholds (T ~ 0) have values near 1e-10 where that
+# cancellation dominates.  Bar: |delta| <= 1e-5 |ref| + 1e-12 max|ref|.
+COMPONENT_ATOL_OF_MAX = 1e-12
+
+
+def _batch(adj, maps, signs=2, vd=None, floor_zero=0, maps_out=False):
+    import torch
+    d = torch.from_numpy(np.ascontiguousarray(maps)).cuda()
+    V = maps.shape[1]
+    mx = torch.empty((maps.shape[0], signs, adj.n_seg), device="cuda")
+    om = torch.empty((maps.shape[0], signs, V), device="cuda") if maps_out else None
+    vdd = None if vd is None else torch.from_numpy(vd).cuda()
+    adj.sweep_batch(d.data_ptr(), V, maps.shape[0], signs, None if vdd is None else vdd.data_ptr(),
+                    floor_zero, mx.data_ptr(), None if om is None else om.data_ptr(), 1 if maps_out else 0)
+    adj.status()
+    return mx.cpu().numpy(), (None if om is None else om.cpu().numpy())
+
+
+def test_component_accumulation_matches_exact(config1):
+    """Per-component accumulation: same components, exact sum of the same
+    float increments -> within 1e-5 (relative) of the reference arithmetic."""
+    st = config1
+    maps = _config1_maps(st, n_perm=4, seed=21)
+    vd = A.vertex_density((st.offsets, st.indices))
+    adj = A.AdjacencySet((st.offsets, st.indices), 2.0, 1.0)
+    mx_e, om_e = _batch(adj, maps, vd=vd, maps_out=True)
+    adj.set_accumulation("component")
+    mx_c, om_c = _batch(adj, maps, vd=vd, maps_out=True)
+    np.testing.assert_allclose(mx_c, mx_e, rtol=COMPONENT_RTOL)
+    np.testing.assert_array_equal(om_c == 0, om_e == 0)
+    for m in range(om_e.shape[0]):
+        for s in range(om_e.shape[1]):
+            ref, got = om_e[m, s], om_c[m, s]
+            tol = COMPONENT_RTOL * np.abs(ref) + COMPONENT_ATOL_OF_MAX * np.abs(ref).max()
+            assert np.all(np.abs(got - ref) <= tol), (m, s, np.max(np.abs(got - ref) - tol))
+    nz = om_e != 0
+    rel = np.abs(om_c[nz] - om_e[nz]) / np.abs(om_e[nz])
+    assert np.median(rel) <= 1e-6
+
+
+def test_component_accumulation_segments_and_asymmetric(golden):
+    off, idx = golden["sweep_off"], golden["sweep_idx"]
+    maps = golden["sweep_maps"]
+    O, I, seg = A.concat_csr([(off, idx), (off, idx)])
+    adj = A.AdjacencySet((O, I), [2.0, 1.5], [1.0, 0.5], seg)
+    stat = np.stack([np.concatenate([maps[0], maps[1]]), np.concatenate([maps[4], maps[5]])])
+    mx_e, _ = _batch(adj, stat, floor_zero=1)
+    adj.set_accumulation("component")
+    mx_c, _ = _batch(adj, stat, floor_zero=1)
+    np.testing.assert_allclose(mx_c, mx_e, rtol=COMPONENT_RTOL)
+    mask = np.zeros((9, 8, 7), bool)
+    mask[1:8, 1:7, 1:6] = True
+    mask[0, 0, 0] = True
+    o2, i2 = A.voxel_csr(mask, 26, "mmr")
+    adj2 = A.AdjacencySet((o2, i2), 2.0, 0.5)
+    rng = np.random.default_rng(9)
+    m2 = (rng.standard_normal((4, o2.shape[0] - 1)) + 0.4).astype(np.float32)
+    e_e, _ = _batch(adj2, m2)
+    adj2.set_accumulation("component")
+    e_c, _ = _batch(adj2, m2)
+    np.testing.assert_allclose(e_c, e_e, rtol=COMPONENT_RTOL)

@@ -192,6 +192,64 @@ def concat_csr(parts):
             np.asarray(segs, np.int64))
 
 
+def locality_order(offsets, indices, segments):
+    """A vertex numbering that keeps mesh neighbours close in memory: reverse
+    Cuthill-McKee inside every segment (segments stay in place).  Returns
+    `order` with new vertex u = old vertex order[u]."""
+    import scipy.sparse as sp
+    from scipy.sparse.csgraph import reverse_cuthill_mckee
+    offsets = np.asarray(offsets, np.int64)
+    indices = np.asarray(indices, np.int64)
+    order = []
+    for s in range(len(segments) - 1):
+        v0, v1 = int(segments[s]), int(segments[s + 1])
+        n = v1 - v0
+        if n == 0:
+            continue
+        e0, e1 = offsets[v0], offsets[v1]
+        loc = indices[e0:e1] - v0
+        ok = (loc >= 0) & (loc < n)
+        rows = np.repeat(np.arange(n), np.diff(offsets[v0:v1 + 1]))[ok]
+        A = sp.csr_matrix((np.ones(rows.shape[0], np.int8), (rows, loc[ok])), shape=(n, n))
+        A = ((A + A.T) > 0).astype(np.int8).tocsr()
+        order.append(np.asarray(reverse_cuthill_mckee(A, symmetric_mode=True), np.int64) + v0)
+    return np.concatenate(order) if order else np.zeros(0, np.int64)
+
+
+def is_symmetric(offsets, indices):
+    """True when every entry b in list a has a in list b (self entries aside)."""
+    import scipy.sparse as sp
+    offsets = np.asarray(offsets, np.int64)
+    indices = np.asarray(indices, np.int64)
+    V = offsets.shape[0] - 1
+    rows = np.repeat(np.arange(V), np.diff(offsets))
+    ok = (indices >= 0) & (indices < V) & (indices != rows)
+    A = sp.csr_matrix((np.ones(int(ok.sum()), np.int8), (rows[ok], indices[ok])), shape=(V, V))
+    A.data[:] = 1
+    return (A != A.T).nnz == 0
+
+
+def relabel_csr(offsets, indices, order):
+    """CSR of the same graph with vertex u_new = order[u_new] renamed; lists
+    keep their entries (renamed), out-of-range entries are kept as they are so
+    the handle still rejects them."""
+    offsets = np.asarray(offsets, np.int64)
+    indices = np.asarray(indices, np.int64)
+    V = offsets.shape[0] - 1
+    inv = np.empty(V, np.int64)
+    inv[order] = np.arange(V)
+    deg = np.diff(offsets)[order]
+    off = np.zeros(V + 1, np.int64)
+    np.cumsum(deg, out=off[1:])
+    starts = offsets[order]
+    src = np.repeat(starts - off[:-1], deg) + np.arange(int(off[-1]))
+    old = indices[src]
+    ok = (old >= 0) & (old < V)
+    new = old.copy()
+    new[ok] = inv[old[ok]]
+    return off, new.astype(np.int32)
+
+
 # ---------------------------------------------------------------------------
 # device handle
 # ---------------------------------------------------------------------------
@@ -239,6 +297,13 @@ class AdjacencySet:
         _lib.check(self._lib.tfce_adjset_set_params(self._h, _lib.ptr(Hs, _lib.c_f32p),
                                                     _lib.ptr(Es, _lib.c_f32p)))
         self.H, self.E = Hs.copy(), Es.copy()
+
+    def set_accumulation(self, mode: str):
+        """'exact' (the reference's float arithmetic, bit-identical) or
+        'component' (per-component double accumulation for batched sweeps)."""
+        code = {"exact": 0, "component": 1}[mode]
+        _lib.check(self._lib.tfce_adjset_set_accumulation(self._h, code))
+        self.accumulation = mode
 
     def run(self, image: np.ndarray, enhn: np.ndarray) -> None:
         """Sweep one host map, accumulating into enhn (float32, length V)."""

@@ -51,6 +51,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_verbose: bool = Fals
                     "-I", CSRC, "--expt-relaxed-constexpr"]
     if ptxas_verbose:
         flags += ["-Xptxas", "-v"]
+    flags += os.environ.get("TFGB_NVCC_FLAGS", "").split()
 
     def compile_one(src: str) -> str:
         obj = os.path.join(objdir, os.path.splitext(src)[0] + ".o")

@@ -25,6 +25,7 @@
 // Every walk and retry loop is bounded; a bound sets an error word and the
 // kernel runs on to its exit.
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -34,8 +35,45 @@
 
 namespace tfgb {
 
+constexpr int kMaxStepsDbg = 128;
+#ifdef TFGB_PHASE_PROFILE
+// Debug-only: clock64 cycles spent per phase, summed over items (thread 0).
+__device__ unsigned long long g_phase_cycles[8];
+#define TFGB_PHASE_MARK(k)                                              \
+  do {                                                                  \
+    if (threadIdx.x == 0) {                                             \
+      const long long _now = clock64();                                 \
+      atomicAdd(&g_phase_cycles[k], (unsigned long long)(_now - _pt));  \
+      _pt = _now;                                                       \
+    }                                                                   \
+  } while (0)
+// Debug-only event counters: [0] unite calls, [1] CAS attempts, [2] CAS
+// failures, [3] find hops, [4] halving writes, [5] list entries checked.
+__device__ unsigned long long g_dbg_counts[8];
+// Debug-only: cycles of each step's (U+S+A) by threshold index.
+__device__ unsigned long long g_step_cycles[kMaxStepsDbg];
+#define TFGB_COUNT(k, n) atomicAdd(&g_dbg_counts[k], (unsigned long long)(n))
+#else
+#define TFGB_PHASE_MARK(k) do { } while (0)
+#define TFGB_COUNT(k, n) do { } while (0)
+#endif
+
 constexpr int kMaxSteps = 128;
-constexpr int kSweepThreads = 512;
+#ifndef TFGB_SWEEP_THREADS
+#define TFGB_SWEEP_THREADS 512
+#endif
+#ifndef TFGB_SWEEP_MINBLOCKS
+#define TFGB_SWEEP_MINBLOCKS 2
+#endif
+#ifndef TFGB_UBATCH
+#define TFGB_UBATCH 6
+#endif
+#ifndef TFGB_ALANES
+#define TFGB_ALANES 4
+#endif
+constexpr int kSweepThreads = TFGB_SWEEP_THREADS;
+constexpr int kUBatch = TFGB_UBATCH;   // list entries of one vertex looked up together
+constexpr int kALanes = TFGB_ALANES;   // positions per thread per accumulation round
 constexpr uint32_t kOneWay = 0x80000000u;   // entry whose reverse entry is missing
 constexpr uint32_t kIndexMask = 0x7fffffffu;
 constexpr uint32_t kInactiveKey = 0xffffffffu;
@@ -83,6 +121,13 @@ struct Slot {
   int32_t* size;
   float* acc;
   int32_t* dead;
+  // per-component accumulation only
+  int32_t* link;     // root a dead root joined (itself while it is a root)
+  int32_t* roots_a;  // live roots after the previous threshold ...
+  int32_t* roots_b;  // ... and after this one (swapped every step)
+  double* W;         // root: increments so far; dead: potential to its link
+  uint8_t* lvl;      // activation step per vertex (255: never), 1 byte so the
+                     // neighbour activity test of the union phase stays in L1
 };
 
 __host__ __device__ inline int64_t align_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
@@ -91,9 +136,21 @@ __host__ __device__ inline int64_t slot_bytes(int32_t vcap) {
   return 6 * align_up((int64_t)vcap * 4, 256);
 }
 
+// Per-component accumulation adds link, two root lists and a double per
+// vertex to the six int32/float arrays of the exact mode.
+__host__ __device__ inline int64_t slot_bytes_lazy(int32_t vcap) {
+  return 9 * align_up((int64_t)vcap * 4, 256) + align_up((int64_t)vcap * 8, 256) +
+         align_up((int64_t)vcap, 256);
+}
+
 __device__ inline Slot make_slot(char* base, int32_t vcap) {
   const int64_t s = align_up((int64_t)vcap * 4, 256);
   Slot sl;
+  sl.link = reinterpret_cast<int32_t*>(base + 6 * s);
+  sl.roots_a = reinterpret_cast<int32_t*>(base + 7 * s);
+  sl.roots_b = reinterpret_cast<int32_t*>(base + 8 * s);
+  sl.W = reinterpret_cast<double*>(base + 9 * s);
+  sl.lvl = reinterpret_cast<uint8_t*>(base + 9 * s + align_up((int64_t)vcap * 8, 256));
   sl.key = reinterpret_cast<uint32_t*>(base);
   sl.order = reinterpret_cast<int32_t*>(base + s);
   sl.parent = reinterpret_cast<int32_t*>(base + 2 * s);
@@ -105,36 +162,66 @@ __device__ inline Slot make_slot(char* base, int32_t vcap) {
 
 __device__ inline void set_err(int32_t* err, int32_t code) { atomicCAS(err, 0, code); }
 
-// Root of x.  parent[] entries only ever point to smaller positions, so the
+// Union-find state of an item is private to the one CTA (one SM) sweeping it,
+// so loads and stores of it are relaxed at CTA scope: coherent with the
+// CTA's own CAS/atomics under the PTX memory model, and free to be served
+// from L1 (the hot roots of large components are read by every thread).
+#ifndef TFGB_STATE_GLOBAL_SCOPE
+__device__ inline int32_t ld_state(const int32_t* p) {
+  int32_t v;
+  asm volatile("ld.relaxed.cta.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ inline void st_state(int32_t* p, int32_t v) {
+  asm volatile("st.relaxed.cta.global.s32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+#else
+__device__ inline int32_t ld_state(const int32_t* p) { return __ldcg(p); }
+__device__ inline void st_state(int32_t* p, int32_t v) { __stcg(p, v); }
+#endif
+
+// Root of x, halving the path on the way: every non-root visited is
+// re-pointed to its grandparent.  Only roots are ever linked (by CAS), and a
+// non-root's new parent is one of its ancestors, so concurrent walks and links
+// stay consistent.  parent[] entries only point to smaller positions, so the
 // walk ends; the limit is a second guard.
-__device__ inline int32_t find_root(const int32_t* parent, int32_t x, int32_t* err) {
-  int32_t p = __ldcg(parent + x);
-  int it = 0;
-  while (p != x) {
-    x = p;
-    p = __ldcg(parent + x);
-    if (++it > kWalkLimit) {
-      set_err(err, kDevLoopLimit);
-      return x;
-    }
+__device__ inline int32_t find_root(int32_t* parent, int32_t x, int32_t* err) {
+  for (int it = 0; it < kWalkLimit; ++it) {
+    const int32_t p = ld_state(parent + x);
+    TFGB_COUNT(3, 1);
+    if (p == x) return x;
+    const int32_t g = ld_state(parent + p);
+    TFGB_COUNT(3, 1);
+    if (g == p) return p;
+    st_state(parent + x, g);
+    TFGB_COUNT(4, 1);
+    x = g;
   }
+  set_err(err, kDevLoopLimit);
   return x;
 }
 
-__device__ inline void unite(int32_t* parent, int32_t a, int32_t b, int32_t* dead,
-                             int32_t* n_dead, int32_t* err) {
+// Join the component of root-hint `a` with position b; returns the root of
+// the joined component (a hint: another thread may link it later).
+__device__ inline int32_t unite(int32_t* parent, int32_t a, int32_t b, int32_t* dead,
+                                int32_t* n_dead, int32_t* err) {
+  TFGB_COUNT(0, 1);
   for (int it = 0; it < kWalkLimit; ++it) {
     a = find_root(parent, a, err);
     b = find_root(parent, b, err);
-    if (a == b) return;
+    if (a == b) return a;
     const int32_t hi = max(a, b), lo = min(a, b);
-    if (atomicCAS(parent + hi, hi, lo) == hi) {
+    TFGB_COUNT(1, 1);
+    const int32_t old = atomicCAS(parent + hi, hi, lo);
+    if (old != hi) TFGB_COUNT(2, 1);
+    if (old == hi) {
       const int32_t q = atomicAdd(n_dead, 1);
       dead[q] = hi;
-      return;
+      return lo;
     }
   }
   set_err(err, kDevLoopLimit);
+  return a;
 }
 
 // (float)(extent^E * HH) with the reference's types: pow in double, product in
@@ -184,17 +271,31 @@ __device__ inline float block_max(float v, float* red) {
 // are checked here, and the insertion-order rule is applied to every
 // same-step entry (for a symmetric pair exactly one direction passes it, so
 // the partition is the same).
-template <bool kChecked>
-__global__ void __launch_bounds__(kSweepThreads, 2) tfce_sweep_kernel(SweepArgs a) {
+//
+// kLazy = false: the reference's arithmetic -- every active vertex adds its
+// float increment to its own float accumulator at every threshold, so results
+// are bit-identical to the reference sweep.  kLazy = true: per-component
+// accumulation -- each live root adds its component's increment to a double
+// once per threshold; a root that is linked keeps its potential relative to
+// the root it joins, and a vertex's value is the sum of potentials along its
+// link chain, rounded to float once.  Per threshold that is O(live
+// components) instead of O(active vertices); the result is the exact sum of
+// the same float increments, so it differs from the reference only by the
+// reference's own float summation error.
+template <bool kChecked, bool kLazy>
+__global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_sweep_kernel(SweepArgs a) {
   __shared__ float sT[kMaxSteps];
   __shared__ float sHH[kMaxSteps];
   __shared__ int32_t sCnt[kMaxSteps + 1];
   __shared__ int32_t sStart[kMaxSteps + 1];
   __shared__ float sRed[32];
-  __shared__ int32_t sItem, sL, sNDead;
+  __shared__ int32_t sItem, sL, sNDead, sNRoots, sNext;
 
   Slot sl = make_slot(a.ws + (int64_t)blockIdx.x * a.ws_slot_bytes, a.vcap);
   const int tid = threadIdx.x, nth = blockDim.x;
+#ifdef TFGB_PHASE_PROFILE
+  long long _pt = clock64();
+#endif
 
   for (;;) {
     if (tid == 0) sItem = atomicAdd(a.counter, 1);
@@ -256,6 +357,7 @@ __global__ void __launch_bounds__(kSweepThreads, 2) tfce_sweep_kernel(SweepArgs 
     }
     for (int i = tid; i <= kMaxSteps; i += nth) sCnt[i] = 0;
     __syncthreads();
+    TFGB_PHASE_MARK(0);
     const int L = sL;
     const float scale = isfinite(mx) ? __fdiv_rn(mx, 100.0f) : 0.0f;
 
@@ -290,6 +392,8 @@ __global__ void __launch_bounds__(kSweepThreads, 2) tfce_sweep_kernel(SweepArgs 
       }
       sStart[L] = s;
       sNDead = 0;
+      sNRoots = 0;
+      sNext = 0;
     }
     __syncthreads();
     const int32_t n_act = sStart[L];
@@ -309,16 +413,34 @@ __global__ void __launch_bounds__(kSweepThreads, 2) tfce_sweep_kernel(SweepArgs 
         sl.order[p] = v;
         sl.parent[p] = p;
         sl.size[p] = 1;
-        sl.acc[p] = (a.out_mode == 2 && omap) ? omap[v] : 0.0f;
+        if constexpr (kLazy) {
+          sl.W[p] = 0.0;
+          sl.link[p] = p;
+        } else {
+          sl.acc[p] = (a.out_mode == 2 && omap) ? omap[v] : 0.0f;
+        }
       }
       sl.key[v] = key;
+      if constexpr (kLazy) sl.lvl[v] = (lv < L) ? static_cast<uint8_t>(lv) : uint8_t(255);
     }
     __syncthreads();
+    TFGB_PHASE_MARK(1);
 
     // ---- 3. threshold steps
+    int32_t* cur_roots = sl.roots_a;
+    int32_t* nxt_roots = sl.roots_b;
     for (int i = 0; i < L; ++i) {
+#ifdef TFGB_PHASE_PROFILE
+      const long long _ps = clock64();
+#define TFGB_STEP_DONE() do { if (threadIdx.x == 0) atomicAdd(&g_step_cycles[i], (unsigned long long)(clock64() - _ps)); } while (0)
+#else
+#define TFGB_STEP_DONE() do { } while (0)
+#endif
       const int32_t s0 = sStart[i], s1 = sStart[i + 1];
-      // (U) union newly active vertices with already-active neighbours
+      // (U) union newly active vertices with already-active neighbours.  A
+      // vertex's list is read kUBatch entries at a time with all their key
+      // lookups issued together; the root of the vertex's component is kept
+      // as a hint between unions.
       for (int32_t p = s0 + tid; p < s1; p += nth) {
         const int32_t v = sl.order[p];
         int64_t e0 = a.offsets[v0 + v], e1 = a.offsets[v0 + v + 1];
@@ -328,62 +450,168 @@ __global__ void __launch_bounds__(kSweepThreads, 2) tfce_sweep_kernel(SweepArgs 
             e0 = e1 = 0;
           }
         }
-        for (int64_t e = e0; e < e1; ++e) {
-          const uint32_t raw = a.indices[e];
-          const int64_t ag = static_cast<int64_t>(raw & kIndexMask) - v0;
-          if (ag < 0 || ag >= Vs) {
-            set_err(a.err, kDevBadIndex);
-            continue;
+        int32_t rp = p;
+        for (int64_t eb = e0; eb < e1; eb += kUBatch) {
+          uint32_t raw[kUBatch], ka[kUBatch];
+          int32_t an[kUBatch];
+#pragma unroll
+          for (int k = 0; k < kUBatch; ++k) raw[k] = (eb + k < e1) ? a.indices[eb + k] : kIndexMask;
+          TFGB_COUNT(5, (e1 - eb < kUBatch) ? (e1 - eb) : kUBatch);
+#pragma unroll
+          for (int k = 0; k < kUBatch; ++k) {
+            const int64_t ag = static_cast<int64_t>(raw[k] & kIndexMask) - v0;
+            an[k] = static_cast<int32_t>(ag);
+            ka[k] = kInactiveKey;
+            if (eb + k < e1) {
+              if (ag < 0 || ag >= Vs) set_err(a.err, kDevBadIndex);
+              else if constexpr (kLazy) ka[k] = (sl.lvl[an[k]] <= i) ? 0u : kInactiveKey;
+              else ka[k] = sl.key[an[k]];
+            }
           }
-          const int32_t an = static_cast<int32_t>(ag);
-          const uint32_t ka = sl.key[an];
-          if (ka == kInactiveKey) continue;
-          const int la = static_cast<int>(ka >> kPosBits);
-          if (la > i) continue;
-          if (la == i && (kChecked || (raw & kOneWay))) {
-            // one-directional entry: effective only if the neighbour was
-            // inserted first (larger value; ties by smaller index)
-            const float xa = sign * x[an], xv = sign * x[v];
-            if (!(xa > xv || (xa == xv && an < v))) continue;
+          if constexpr (kLazy) {
+            // bucket positions only for the neighbours that are active
+#pragma unroll
+            for (int k = 0; k < kUBatch; ++k)
+              if (ka[k] != kInactiveKey) ka[k] = sl.key[an[k]];
           }
-          unite(sl.parent, p, static_cast<int32_t>(ka & ((1u << kPosBits) - 1u)), sl.dead,
-                &sNDead, a.err);
+#pragma unroll
+          for (int k = 0; k < kUBatch; ++k) {
+            if (ka[k] == kInactiveKey) continue;
+            const int la = static_cast<int>(ka[k] >> kPosBits);
+            if (la > i) continue;
+            if (la == i && (kChecked || (raw[k] & kOneWay))) {
+              // one-directional entry: effective only if the neighbour was
+              // inserted first (larger value; ties by smaller index)
+              const float xa = sign * x[an[k]], xv = sign * x[v];
+              if (!(xa > xv || (xa == xv && an[k] < v))) continue;
+            }
+            int32_t q = static_cast<int32_t>(ka[k] & ((1u << kPosBits) - 1u));
+            if constexpr (kLazy) {
+              // start from the neighbour's parent (an ancestor), and skip the
+              // union when it is this vertex's root and that is still a root
+              q = ld_state(sl.parent + q);
+              if (q == rp && ld_state(sl.parent + rp) == rp) continue;
+            }
+            rp = unite(sl.parent, rp, q, sl.dead, &sNDead, a.err);
+          }
         }
       }
       __syncthreads();
+      TFGB_PHASE_MARK(2);
       // (S) linked roots hand their extent to their final root
       const int32_t nd = sNDead;
       for (int32_t q = tid; q < nd; q += nth) {
         const int32_t d = sl.dead[q];
         const int32_t r = find_root(sl.parent, d, a.err);
-        atomicAdd(sl.size + r, __ldcg(sl.size + d));
-        __stcg(sl.parent + d, r);
+        atomicAdd(sl.size + r, ld_state(sl.size + d));
+        st_state(sl.parent + d, r);
+        if constexpr (kLazy) {
+          sl.link[d] = r;
+          sl.W[d] = sl.W[d] - sl.W[r];
+        }
+      }
+      if constexpr (kLazy) {
+        if (tid == 0) sNext = 0;
       }
       __syncthreads();
+      TFGB_PHASE_MARK(3);
       if (tid == 0) sNDead = 0;
-      // (A) per-vertex increment, threshold order
-      const float HH = sHH[i];
-      for (int32_t p = tid; p < s1; p += nth) {
-        int32_t r = __ldcg(sl.parent + p);
-        if (r != p) {
-          const int32_t rr = __ldcg(sl.parent + r);
-          if (rr != r) {
-            r = find_root(sl.parent, rr, a.err);
-            __stcg(sl.parent + p, r);
+      if constexpr (kLazy) {
+        // (A') every live root adds its component's increment once: the old
+        // live roots that survived this step plus the new vertices that are
+        // roots, compacted into the next list as they are visited
+        const float HHl = sHH[i];
+        const int32_t n_old = sNRoots;
+        const int32_t n_cand = n_old + (s1 - s0);
+        for (int32_t q = tid; q < n_cand; q += nth) {
+          const int32_t c = (q < n_old) ? cur_roots[q] : s0 + (q - n_old);
+          const bool is_root = (ld_state(sl.parent + c) == c);
+          if (is_root) {
+            const float inc = increment(ld_state(sl.size + c), E, e_mode, HHl);
+            sl.W[c] = sl.W[c] + static_cast<double>(inc);
+          }
+          const unsigned mask = __activemask();
+          const unsigned roots = __ballot_sync(mask, is_root);
+          if (roots) {
+            const int lane = tid & 31;
+            const int leader = __ffs(roots) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(&sNext, __popc(roots));
+            base = __shfl_sync(mask, base, leader);
+            if (is_root) nxt_roots[base + __popc(roots & ((1u << lane) - 1u))] = c;
           }
         }
-        const int32_t ext = __ldcg(sl.size + r);
-        sl.acc[p] = __fadd_rn(sl.acc[p], increment(ext, E, e_mode, HH));
-        if (a.labels && i < a.label_cap) {
-          const int32_t v = sl.order[p];
-          a.labels[(int64_t)i * Vs + v] = sl.order[r];
-          a.extents[(int64_t)i * Vs + v] = ext;
+        __syncthreads();
+        if (tid == 0) sNRoots = sNext;
+        int32_t* t_ = cur_roots;
+        cur_roots = nxt_roots;
+        nxt_roots = t_;
+        TFGB_PHASE_MARK(4);
+        TFGB_STEP_DONE();
+        continue;
+      }
+      // (A) per-vertex increment, threshold order.  Each thread takes kALanes
+      // positions per round and issues their loads together (the chain
+      // parent -> root -> extent is latency-bound otherwise).
+      const float HH = sHH[i];
+      for (int32_t base = tid; base < s1; base += kALanes * nth) {
+        int32_t pp[kALanes], rt[kALanes];
+        float ac[kALanes];
+#pragma unroll
+        for (int k = 0; k < kALanes; ++k) {
+          pp[k] = base + k * nth;
+          if (pp[k] < s1) {
+            rt[k] = ld_state(sl.parent + pp[k]);
+            ac[k] = sl.acc[pp[k]];
+          }
+        }
+        int32_t up[kALanes];
+#pragma unroll
+        for (int k = 0; k < kALanes; ++k)
+          up[k] = (pp[k] < s1 && rt[k] != pp[k]) ? ld_state(sl.parent + rt[k]) : -1;
+#pragma unroll
+        for (int k = 0; k < kALanes; ++k) {
+          if (up[k] >= 0 && up[k] != rt[k]) {
+            rt[k] = find_root(sl.parent, up[k], a.err);
+            st_state(sl.parent + pp[k], rt[k]);
+          }
+        }
+        int32_t ext[kALanes];
+#pragma unroll
+        for (int k = 0; k < kALanes; ++k)
+          if (pp[k] < s1) ext[k] = ld_state(sl.size + rt[k]);
+#pragma unroll
+        for (int k = 0; k < kALanes; ++k) {
+          if (pp[k] < s1) {
+            sl.acc[pp[k]] = __fadd_rn(ac[k], increment(ext[k], E, e_mode, HH));
+            if (a.labels && i < a.label_cap) {
+              const int32_t v = sl.order[pp[k]];
+              a.labels[(int64_t)i * Vs + v] = sl.order[rt[k]];
+              a.extents[(int64_t)i * Vs + v] = ext[k];
+            }
+          }
         }
       }
       __syncthreads();
+      TFGB_PHASE_MARK(4);
     }
 
     // ---- 4. scale, reduce, write
+    if constexpr (kLazy) {
+      // resolve every active vertex: sum of potentials along its link chain
+      for (int32_t p = tid; p < n_act; p += nth) {
+        double sum = sl.W[p];
+        int32_t c = p, l = sl.link[p];
+        for (int it = 0; l != c && it < kWalkLimit; ++it) {
+          c = l;
+          sum += sl.W[c];
+          l = sl.link[c];
+        }
+        if (a.out_mode == 2 && omap) sum += static_cast<double>(omap[sl.order[p]]);
+        sl.acc[p] = __double2float_rn(sum);
+      }
+      __syncthreads();
+    }
     float best = (n_act < Vs) ? __fmul_rn(0.0f, scale) : -INFINITY;
     if (a.out_mode == 1 && omap) {
       for (int32_t v = tid; v < Vs; v += nth) {
@@ -406,6 +634,7 @@ __global__ void __launch_bounds__(kSweepThreads, 2) tfce_sweep_kernel(SweepArgs 
     best = block_max(best, sRed);
     if (tid == 0 && a.out_max) a.out_max[item] = (best == -INFINITY) ? 0.0f : best;
     __syncthreads();
+    TFGB_PHASE_MARK(5);
   }
 }
 
@@ -436,6 +665,7 @@ struct tfce_adjset {
   float* d_img = nullptr;
   float* d_enh = nullptr;
   int32_t run_cap = 0;
+  int32_t accumulation = 0;  // 0: reference arithmetic, 1: per-component
   std::mutex mu;
 };
 
@@ -463,14 +693,19 @@ int resident_slots(tfce_adjset* h) {
   if (h->max_slots) return TFCE_OK;
   int sms = 0, per_sm = 0;
   TFGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
-  TFGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tfgb::tfce_sweep_kernel<false>,
+  TFGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tfgb::tfce_sweep_kernel<false, false>,
                                                           tfgb::kSweepThreads, 0));
   h->max_slots = std::max(1, sms * std::max(1, per_sm));
+  // tuning knob: fewer CTAs in flight (smaller L2 working set)
+  if (const char* env = std::getenv("TFCE_SWEEP_MAX_CTAS")) {
+    const int cap = std::atoi(env);
+    if (cap > 0) h->max_slots = std::min(h->max_slots, cap);
+  }
   return TFCE_OK;
 }
 
-int ensure_workspace(tfce_adjset* h, int32_t slots) {
-  const int64_t per = tfgb::slot_bytes(h->vmax_seg);
+int ensure_workspace(tfce_adjset* h, int32_t slots, bool lazy) {
+  const int64_t per = lazy ? tfgb::slot_bytes_lazy(h->vmax_seg) : tfgb::slot_bytes(h->vmax_seg);
   if (h->d_ws && h->ws_slots >= slots && h->ws_slot == per) return TFCE_OK;
   cudaFree(h->d_ws);
   h->d_ws = nullptr;
@@ -484,7 +719,7 @@ int ensure_workspace(tfce_adjset* h, int32_t slots) {
 int launch_sweep(tfce_adjset* h, const float* stats, int64_t map_stride, int32_t n_maps,
                  int32_t signs, const float* vdensity, int32_t floor_zero, float* out_max,
                  float* out_maps, int32_t out_mode, int32_t* labels, int32_t* extents,
-                 int32_t label_cap, cudaStream_t st) {
+                 int32_t label_cap, cudaStream_t st, bool lazy) {
   const int64_t items64 = (int64_t)n_maps * signs * h->n_seg;
   TFGB_CHECK_ARG(items64 < (1LL << 31), "too many sweep items");
   const int32_t items = static_cast<int32_t>(items64);
@@ -492,7 +727,7 @@ int launch_sweep(tfce_adjset* h, const float* stats, int64_t map_stride, int32_t
   int rs = resident_slots(h);
   if (rs) return rs;
   const int32_t slots = std::min<int32_t>(items, h->max_slots);
-  int rc = ensure_workspace(h, slots);
+  int rc = ensure_workspace(h, slots, lazy);
   if (rc) return rc;
   TFGB_CUDA(cudaMemsetAsync(h->d_ctrl, 0, sizeof(int32_t), st));  // queue counter only
   tfgb::SweepArgs a{};
@@ -522,7 +757,8 @@ int launch_sweep(tfce_adjset* h, const float* stats, int64_t map_stride, int32_t
   a.err = h->d_ctrl + 1;
   a.n_items = items;
   a.item_order = nullptr;
-  tfgb::tfce_sweep_kernel<false><<<slots, tfgb::kSweepThreads, 0, st>>>(a);
+  if (lazy) tfgb::tfce_sweep_kernel<false, true><<<slots, tfgb::kSweepThreads, 0, st>>>(a);
+  else tfgb::tfce_sweep_kernel<false, false><<<slots, tfgb::kSweepThreads, 0, st>>>(a);
   TFGB_CUDA(cudaGetLastError());
   return TFCE_OK;
 }
@@ -685,6 +921,15 @@ int tfce_adjset_set_params(tfce_adjset* h, const float* H, const float* E) {
 
 int tfce_adjset_is_symmetric(const tfce_adjset* h) { return (h && h->symmetric) ? 1 : 0; }
 
+int tfce_adjset_set_accumulation(tfce_adjset* h, int32_t mode) {
+  tfgb::clear_error();
+  TFGB_CHECK_ARG(h != nullptr, "handle is NULL");
+  TFGB_CHECK_ARG(mode == 0 || mode == 1, "mode must be 0 (reference) or 1 (per-component)");
+  std::lock_guard<std::mutex> lk(h->mu);
+  h->accumulation = mode;
+  return TFCE_OK;
+}
+
 int tfce_adjset_run(tfce_adjset* h, const float* image, float* enhn, int32_t n_vertices) {
   return tfce_adjset_run_labels(h, image, enhn, n_vertices, nullptr, nullptr, 0, nullptr);
 }
@@ -727,7 +972,7 @@ int tfce_adjset_run_labels(tfce_adjset* h, const float* image, float* enhn, int3
         break;
       }
       rc = launch_sweep(h, h->d_img, V, 1, 1, nullptr, 0, nullptr, h->d_enh, 2, d_lab, d_ext,
-                        max_steps, st);
+                        max_steps, st, false);
       if (rc) break;
       int32_t steps = 0;
       rc = check_device_error(h, st, &steps);
@@ -773,9 +1018,30 @@ int tfce_sweep_batch(tfce_adjset* h, const float* stats, int64_t map_stride, int
   std::lock_guard<std::mutex> lk(h->mu);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   int rc = launch_sweep(h, stats, map_stride, n_maps, signs, vdensity, floor_zero, out_max,
-                        out_maps, out_mode, nullptr, nullptr, 0, st);
+                        out_maps, out_mode, nullptr, nullptr, 0, st, h->accumulation == 1);
   return rc;
 }
+
+#ifdef TFGB_PHASE_PROFILE
+// Debug-only export: per-phase cycle sums since the last call (then cleared).
+int tfce_debug_step_cycles(unsigned long long* out128) {
+  TFGB_CUDA(cudaDeviceSynchronize());
+  TFGB_CUDA(cudaMemcpyFromSymbol(out128, tfgb::g_step_cycles, 128 * sizeof(unsigned long long)));
+  unsigned long long z[128] = {0};
+  TFGB_CUDA(cudaMemcpyToSymbol(tfgb::g_step_cycles, z, sizeof(z)));
+  return TFCE_OK;
+}
+
+int tfce_debug_phase_cycles(unsigned long long* out16) {
+  TFGB_CUDA(cudaDeviceSynchronize());
+  TFGB_CUDA(cudaMemcpyFromSymbol(out16, tfgb::g_phase_cycles, 8 * sizeof(unsigned long long)));
+  TFGB_CUDA(cudaMemcpyFromSymbol(out16 + 8, tfgb::g_dbg_counts, 8 * sizeof(unsigned long long)));
+  unsigned long long z[8] = {0};
+  TFGB_CUDA(cudaMemcpyToSymbol(tfgb::g_phase_cycles, z, sizeof(z)));
+  TFGB_CUDA(cudaMemcpyToSymbol(tfgb::g_dbg_counts, z, sizeof(z)));
+  return TFCE_OK;
+}
+#endif
 
 // Error word of the last batched sweep on this handle (synchronises `stream`).
 int tfce_sweep_status(tfce_adjset* h, void* stream) {
@@ -843,7 +1109,7 @@ int noalloc_setup(int dev, NoAllocDevice* out) {
     }
     int sms = 0, per_sm = 0;
     TFGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    TFGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tfce_sweep_kernel<true>,
+    TFGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tfce_sweep_kernel<true, false>,
                                                             kSweepThreads, 0));
     d.max_slots = std::max(1, sms * std::max(1, per_sm));
     d.scratch = p;
@@ -918,7 +1184,7 @@ extern "C" int tfce_sweep_batch_noalloc(const int64_t* offsets, const int32_t* i
   a.n_items = items;
   a.n_vertices = n_vertices;
   a.n_entries = n_entries;
-  tfgb::tfce_sweep_kernel<true><<<slots, tfgb::kSweepThreads, 0, st>>>(a);
+  tfgb::tfce_sweep_kernel<true, false><<<slots, tfgb::kSweepThreads, 0, st>>>(a);
   TFGB_CUDA(cudaGetLastError());
   int32_t hctrl[2] = {0, 0};
   TFGB_CUDA(cudaMemcpyAsync(hctrl, ctrl, sizeof(hctrl), cudaMemcpyDeviceToHost, st));

@@ -20,7 +20,7 @@ from __future__ import annotations
 import numpy as np
 
 from . import _lib
-from .adjacency import AdjacencySet
+from .adjacency import AdjacencySet, is_symmetric, locality_order, relabel_csr, to_csr
 from .device import dev, ptr, require_cuda, stream_handle
 from .glm import DesignBatch
 
@@ -40,24 +40,47 @@ class PermutationEngine:
     contrasts: coefficient indices to test (default 1..k-1: every
     non-intercept column, randomise :113-117).
     floor_zero: the segment maxima count the zero fill of masked vertices
-    (vertex path: the statistic is scattered into zero-filled hemispheres)."""
+    (vertex path: the statistic is scattered into zero-filled hemispheres).
+    accumulation: 'component' (default; per-component double sums, within
+    ~1e-7 of the reference's float sums) or 'exact' (the reference's float
+    arithmetic, bit-identical; slower).
+    reorder: renumber vertices inside every segment for memory locality
+    (reverse Cuthill-McKee); Y's columns are permuted once here and every map
+    handed back is in the caller's order.  Only symmetric adjacency is
+    renumbered (for one-way entries the tie rule depends on vertex order), so
+    results do not depend on it."""
 
     def __init__(self, Y, pred_x, adjacency, segments=None, H=2.0, E=1.0, vdensity=None,
-                 contrasts=None, floor_zero=False, batch=64, signs=2):
+                 contrasts=None, floor_zero=False, batch=64, signs=2, reorder=False,
+                 accumulation="component"):
         t = require_cuda()
         self.t = t
-        self.Yd = dev(np.asarray(Y, np.float32) if not isinstance(Y, t.Tensor) else Y, t.float32)
-        self.n, self.V = self.Yd.shape
-        px = np.asarray(pred_x, np.float64)
-        self.X = np.column_stack([np.ones(self.n), px.reshape(self.n, -1)])
-        self.k = self.X.shape[1]
+        Yh = Y if isinstance(Y, t.Tensor) else np.asarray(Y, np.float32)
+        V = Yh.shape[1]
+        self.order = None
         if isinstance(adjacency, AdjacencySet):
             self.adj = adjacency
             self.adj.set_params(H, E)
         else:
-            self.adj = AdjacencySet(adjacency, H, E, segments)
+            off, idx = to_csr(adjacency)
+            seg = np.array([0, off.shape[0] - 1], np.int64) if segments is None else np.asarray(segments)
+            if reorder and off.shape[0] - 1 == V and is_symmetric(off, idx):
+                self.order = locality_order(off, idx, seg)
+                off, idx = relabel_csr(off, idx, self.order)
+            self.adj = AdjacencySet((off, idx), H, E, seg)
+        if self.order is not None:
+            order_t = t.from_numpy(self.order)
+            Yh = (Yh[:, order_t] if isinstance(Yh, t.Tensor) else Yh[:, self.order])
+            if vdensity is not None:
+                vdensity = np.asarray(vdensity, np.float32)[self.order]
+        self.Yd = dev(Yh, t.float32)
+        self.n, self.V = self.Yd.shape
+        px = np.asarray(pred_x, np.float64)
+        self.X = np.column_stack([np.ones(self.n), px.reshape(self.n, -1)])
+        self.k = self.X.shape[1]
         if self.adj.n_vertices != self.V:
             raise ValueError(f"adjacency has {self.adj.n_vertices} vertices, data {self.V}")
+        self.adj.set_accumulation(accumulation)
         self.n_seg = self.adj.n_seg
         self.contrasts = list(range(1, self.k)) if contrasts is None else list(contrasts)
         self.C = len(self.contrasts)
@@ -95,6 +118,21 @@ class PermutationEngine:
                              int(self.floor_zero), ptr(out), None, 0, stream_handle())
         return out
 
+    def upload(self, Y_host):
+        """Copy new data (n, V) in the caller's vertex order into the resident
+        buffer (pinned host memory makes this asynchronous)."""
+        t = self.t
+        if self.order is not None:
+            if not hasattr(self, "_order_d"):
+                self._order_d = t.from_numpy(self.order).cuda()
+            staged = getattr(self, "_stage", None)
+            if staged is None or staged.shape != self.Yd.shape:
+                self._stage = staged = t.empty_like(self.Yd)
+            staged.copy_(Y_host, non_blocking=True)
+            t.index_select(staged, 1, self._order_d, out=self.Yd)
+        else:
+            self.Yd.copy_(Y_host, non_blocking=True)
+
     def run_batch(self, perms):
         """Maxima (P, C, signs, n_seg) for the permutation index rows `perms`."""
         P = perms.shape[0]
@@ -128,10 +166,24 @@ class PermutationEngine:
         self.tmaps(db, out=tm)
         maps = t.empty((self.C, self.signs, self.V), device="cuda", dtype=t.float32)
         mx = t.empty((self.C, self.signs, self.n_seg), device="cuda", dtype=t.float32)
-        self.adj.sweep_batch(ptr(tm), self.V, self.C, self.signs, ptr(self.vd), int(self.floor_zero),
-                             ptr(mx), ptr(maps), 1, stream_handle())
-        self.adj.status()
-        return tm[0].cpu().numpy(), maps.cpu().numpy(), mx.cpu().numpy()
+        # the observed image is swept once: use the reference's exact arithmetic
+        mode = getattr(self.adj, "accumulation", "exact")
+        self.adj.set_accumulation("exact")
+        try:
+            self.adj.sweep_batch(ptr(tm), self.V, self.C, self.signs, ptr(self.vd),
+                                 int(self.floor_zero), ptr(mx), ptr(maps), 1, stream_handle())
+            self.adj.status()
+        finally:
+            self.adj.set_accumulation(mode)
+        return self.to_caller(tm[0].cpu().numpy()), self.to_caller(maps.cpu().numpy()), mx.cpu().numpy()
+
+    def to_caller(self, a):
+        """Maps in the engine's internal vertex order -> the caller's order."""
+        if self.order is None:
+            return a
+        out = np.empty_like(a)
+        out[..., self.order] = a
+        return out
 
 
 def reduce_vertex(maxima):
