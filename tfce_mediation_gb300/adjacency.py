@@ -168,6 +168,31 @@ def merge_adjacency_array(adjacent_range, adjacency_array):
     return pieces
 
 
+def induced_csr(adjacency, mask):
+    """CSR of the subgraph on the vertices where `mask` is true, renumbered in
+    order; entries to vertices outside the mask are dropped.  Sweeping a masked
+    statistic on it equals sweeping the statistic scattered into a zero-filled
+    array on the full adjacency: zeros are never above a threshold >= 0, so they
+    never join a component (the max over the zero fill is kept by the
+    sweep's floor_zero option)."""
+    off, idx = to_csr(adjacency)
+    mask = np.asarray(mask, bool)
+    V = off.shape[0] - 1
+    new = np.full(V, -1, np.int64)
+    new[mask] = np.arange(int(mask.sum()))
+    rows = np.repeat(np.arange(V), np.diff(off))
+    ok = (idx >= 0) & (idx < V)
+    ok[ok] &= mask[rows[ok]] & mask[idx[ok]]
+    src, dst = new[rows[ok]], new[idx[ok]]
+    n = int(mask.sum())
+    order = np.argsort(src, kind="stable")
+    src, dst = src[order], dst[order]
+    o = np.zeros(n + 1, np.int64)
+    np.add.at(o, src + 1, 1)
+    np.cumsum(o, out=o)
+    return o, dst.astype(np.int32)
+
+
 def vertex_density(adjacency):
     """Vertex-density weight 1 - deg/max + mean/max (float32), as
     tfce_mediation/tmanalysis/STEP_1_vertex_tfce_multiple_regression.py:166-173."""

@@ -196,3 +196,105 @@ def null_distribution(maxima, contrast):
     """Interleave + and - maxima as the reference appends them to one CSV
     (randomise :115-116): (P, C, 2) -> (2P,)."""
     return np.asarray(maxima)[:, contrast, :].reshape(-1)
+
+
+class MediationEngine:
+    """Indirect-effect (Sobel/Aroian/Goodman) z + TFCE null distribution: the
+    batched form of vertex_tfce_mediation_randomise.py:79-91 and
+    tm_func.low_ram_calculate_mediation_tfce (tm_func.py:269-305).
+
+    Per permutation the reference permutes pred_x (and, for medtype 'Y', also
+    depend_y) and regresses the data on the path-a design [1, x] and the
+    path-b design ([1, x, y] for 'I', [1, y, x] for 'M' and 'Y'; pyfunc.py:131-145),
+    taking coefficient 1 of each.  Here both designs of P permutations go into
+    one glm_tstat launch (2P designs, kmax 3), sobel_combine forms z, and one
+    sweep launch gives the maxima (one sign: z >= 0 for Aroian/Sobel).  For
+    medtype 'Y' path a is a host regression of depend_y on pred_x (scipy
+    linregress), as in the reference."""
+
+    def __init__(self, Y, pred_x, depend_y, medtype, adjacency, segments=None, H=2.0, E=1.0, vdensity=None,
+                 floor_zero=False, batch=64, alg="aroian", accumulation="component"):
+        from .pyfunc import ALG
+        if medtype not in ("I", "M", "Y"):
+            raise ValueError("Invalid mediation type")
+        if alg not in ALG:
+            raise ValueError("Unknown indirect test algorithm")
+        self.inner = PermutationEngine(Y, np.zeros((np.asarray(Y).shape[0], 1)), adjacency, segments, H, E,
+                                       vdensity, contrasts=[1], floor_zero=floor_zero, batch=2 * batch, signs=1,
+                                       reorder=False, accumulation=accumulation)
+        self.t = self.inner.t
+        self.medtype, self.alg_code, self.batch = medtype, ALG[alg], int(batch)
+        self.pred_x = np.asarray(pred_x, np.float64)
+        self.depend_y = np.asarray(depend_y, np.float64)
+        self.n, self.V, self.n_seg = self.inner.n, self.inner.V, self.inner.n_seg
+        self._z = self.t.empty((self.batch, self.V), device="cuda", dtype=self.t.float32)
+        self._max = self.t.empty((self.batch, 1, self.inner.n_seg), device="cuda", dtype=self.t.float32)
+
+    def _paths(self, perms):
+        from .pyfunc import mediation_designs
+        A, B, ta = [], [], []
+        for p in perms:
+            x = self.pred_x[p]
+            dy = self.depend_y if self.medtype in ("M", "I") else self.depend_y[p]
+            Xa, Xb, tas = mediation_designs(self.medtype, x, dy, self.n)
+            A.append(Xa)
+            B.append(Xb)
+            ta.append(tas)
+        return A, B, ta
+
+    def zmaps(self, perms, out=None):
+        """Indirect-effect z maps (P, V) on the device for permutation rows."""
+        P = len(perms)
+        A, B, ta = self._paths(perms)
+        inner = self.inner
+        z = self._z[:P] if out is None else out
+        lib = inner.lib
+        if self.medtype == "Y":
+            tm = inner.tmaps(DesignBatch(B, kmax=3))  # (P, 1, V)
+            tas = dev(np.asarray(ta, np.float32))
+            _lib.check(lib.sobel_combine(None, self.V, ptr(tas), ptr(tm), self.V, P, self.V, self.alg_code,
+                                         ptr(z), self.V, stream_handle()))
+        else:
+            designs = [m for pair in zip(A, B) for m in pair]
+            tm = inner.tmaps(DesignBatch(designs, kmax=3))  # (2P, 1, V): a, b, a, b ...
+            _lib.check(lib.sobel_combine(ptr(tm), 2 * self.V, None, ptr(tm) + 4 * self.V, 2 * self.V, P,
+                                         self.V, self.alg_code, ptr(z), self.V, stream_handle()))
+        return z
+
+    def run_batch(self, perms):
+        """Maxima (P, 1, 1, n_seg) for the permutation index rows `perms`."""
+        P = len(perms)
+        if P > self.batch:
+            raise ValueError("batch larger than the engine's buffers")
+        z = self.zmaps(perms)
+        mx = self._max.view(-1)[: P * self.n_seg]
+        self.inner.adj.sweep_batch(ptr(z), self.V, P, 1, ptr(self.inner.vd), int(self.inner.floor_zero),
+                                   ptr(mx), None, 0, stream_handle())
+        out = mx.cpu().numpy().reshape(P, 1, 1, self.n_seg)
+        self.inner.adj.status()
+        return out
+
+    def run(self, n_perm=None, seed=0, start=0, stop=None, perms=None):
+        if perms is None:
+            stop = start + n_perm if stop is None else stop
+            perms = permutations(self.n, seed, start, stop)
+        out = [self.run_batch(perms[b:b + self.batch]) for b in range(0, perms.shape[0], self.batch)]
+        return np.concatenate(out) if out else np.zeros((0, 1, 1, self.n_seg), np.float32)
+
+    def observed(self):
+        """Unpermuted z map (V,) and scaled TFCE map (V,) on the host."""
+        t = self.t
+        ident = np.arange(self.n)[None]
+        z = self.zmaps(ident)[:1]
+        maps = t.empty((1, 1, self.V), device="cuda", dtype=t.float32)
+        mx = t.empty((1, 1, self.n_seg), device="cuda", dtype=t.float32)
+        adj = self.inner.adj
+        mode = getattr(adj, "accumulation", "exact")
+        adj.set_accumulation("exact")
+        try:
+            adj.sweep_batch(ptr(z), self.V, 1, 1, ptr(self.inner.vd), int(self.inner.floor_zero), ptr(mx),
+                            ptr(maps), 1, stream_handle())
+            adj.status()
+        finally:
+            adj.set_accumulation(mode)
+        return z[0].cpu().numpy(), maps[0, 0].cpu().numpy(), mx[0, 0].cpu().numpy()

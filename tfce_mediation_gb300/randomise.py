@@ -1,0 +1,298 @@
+"""Drop-ins for the reference's permutation drivers (L4 scripts).
+
+Each ``*_run(opts)`` reads the same hand-off files the reference's STEP_1
+scripts write, runs the permutations through the batched GPU engines, and
+appends the same CSV lines in the same order and format:
+
+* vertex_regress_run   -- tmanalysis/vertex_tfce_multiple_regression_randomise.py:56-118
+  (python_temp_<surface>/, output_<surface>/perm_Tstat_<surface>/perm_tstat_con<c>_TFCE_maxVertex.csv, %.4f)
+* voxel_regress_run    -- tmanalysis/voxel_tfce_multiple_regression_randomise.py:51-120
+  (python_temp/, output/perm_Tstat/perm_tstat_con<c>_TFCE_maxVoxel.csv, %1.4f)
+* vertex_mediation_run -- tmanalysis/vertex_tfce_mediation_randomise.py:48-92
+  (python_temp_med_<surface>/, perm_Zstat_<m>_TFCE_maxVertex.csv)
+* voxel_mediation_run  -- tmanalysis/voxel_tfce_mediation_randomise.py:42-77
+* mmr_lr_run           -- tm_multisurface/tm_mmr_rand_low_ram_parallel.py:166-207
+  (tmi_temp/<s>_*_temp.npy, <path>/perm_maxTFCE_surf<s>_tcon<c>.csv, %f)
+
+Permutations: the reference seeds each iteration from the clock
+(``np.random.seed(int(iter_perm*1000+time()))``); that stays the default.
+``opts.seed`` (an added, optional argument) selects the host-seeded stream
+``RandomState(seed + iter_perm).permutation(n)`` instead, which makes runs
+reproducible and shardable.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+from time import time
+
+import numpy as np
+
+from . import engine as E
+from .adjacency import induced_csr, concat_csr, to_csr
+
+
+def _load(path):
+    return np.load(path, allow_pickle=True)
+
+
+def _perm_rows(n, start, stop, seed):
+    rows = []
+    for it in range(start, stop):
+        if seed is None:
+            np.random.seed(int(it * 1000 + time()))
+            rows.append(np.random.permutation(list(range(n))))
+        else:
+            rows.append(np.random.RandomState(seed + it).permutation(n))
+    return np.asarray(rows)
+
+
+def _append(path, lines):
+    with open(path, "a") as fh:
+        fh.write("".join(l + "\n" for l in lines))
+
+
+def _vd(v, mask):
+    if np.isscalar(v) or np.ndim(v) == 0:
+        return np.full(int(np.sum(mask)), float(v), np.float32)
+    return np.asarray(v, np.float32)[np.asarray(mask, bool)]
+
+
+def _hemispheres(adj_lh, adj_rh, mask_lh, mask_rh):
+    o1, i1 = induced_csr(adj_lh, mask_lh)
+    o2, i2 = induced_csr(adj_rh, mask_rh)
+    return concat_csr([(o1, i1), (o2, i2)])
+
+
+def parser_common(ap, surface=True):
+    ap.add_argument("-r", "--range", nargs=2, type=int, required=True, metavar=("INT", "INT"))
+    if surface:
+        ap.add_argument("-s", "--surface", nargs=1, required=True, metavar=("STR",))
+    ap.add_argument("--seed", nargs=1, type=int, default=None,
+                    help="host-seeded permutation stream RandomState(seed + i) (default: clock seeding)")
+    ap.add_argument("--batch", type=int, default=64)
+    return ap
+
+
+def vertex_regress_parser(ap=None):
+    ap = parser_common(ap or argparse.ArgumentParser(description="Vertex-wise GLM + TFCE permutations (GPU)"))
+    ap.add_argument("-v", "--specifyvars", nargs=2, type=int, metavar=("INT", "INT"))
+    ap.add_argument("-e", "--exchangeblock", nargs=1, metavar=("*.csv",))
+    return ap
+
+
+def _designs_for(X, n, start, stop, opts, seed):
+    """Permuted designs of the reference loop (randomise :90-105), including the
+    in-place cumulative -v column permutation and exchange blocks."""
+    out = []
+    X = X.copy()
+    block_list = None
+    if getattr(opts, "exchangeblock", None):
+        block_list = np.genfromtxt(opts.exchangeblock[0], dtype=str)
+        indexer = np.array(range(len(block_list)))
+    for it in range(start, stop):
+        if seed is None:
+            np.random.seed(int(it * 1000 + time()))
+            rng = np.random
+        else:
+            rng = np.random.RandomState(seed + it)
+        if getattr(opts, "specifyvars", None):
+            a, b = opts.specifyvars[0], opts.specifyvars[1] + 1
+            X[:, a:b] = X[:, a:b][rng.permutation(list(range(n)))]
+            out.append(X.copy())
+        elif block_list is not None:
+            randindex = [rng.permutation(indexer[block_list == blk])
+                         for blk in rng.permutation(list(np.unique(block_list)))]
+            out.append(X[np.concatenate(randindex)])
+        else:
+            out.append(X[rng.permutation(list(range(n)))])
+    return np.stack(out)
+
+
+def _run_designs(eng, designs, batch):
+    from .glm import DesignBatch
+    res = []
+    for b in range(0, designs.shape[0], batch):
+        db = DesignBatch(designs[b:b + batch])
+        tm = eng.tmaps(db)
+        mx = eng.sweep_max(tm, db.G * eng.C)
+        res.append(mx.cpu().numpy().reshape(db.G, eng.C, eng.signs, eng.n_seg))
+        eng.adj.status()
+    return np.concatenate(res)
+
+
+def vertex_regress_run(opts):
+    start, stop = int(opts.range[0]), int(opts.range[1]) + 1
+    surface = str(opts.surface[0])
+    seed = opts.seed[0] if getattr(opts, "seed", None) else None
+    d = "python_temp_%s" % surface
+    ny = _load(f"{d}/merge_y.npy")
+    num_vertex_lh = int(_load(f"{d}/num_vertex_lh.npy"))
+    mask_lh, mask_rh = _load(f"{d}/bin_mask_lh.npy"), _load(f"{d}/bin_mask_rh.npy")
+    n = int(_load(f"{d}/num_subjects.npy"))
+    pred_x = _load(f"{d}/pred_x.npy")
+    adj_lh, adj_rh = _load(f"{d}/adjac_lh.npy"), _load(f"{d}/adjac_rh.npy")
+    optstfce = _load(f"{d}/optstfce.npy")
+    vd_lh, vd_rh = _load(f"{d}/vdensity_lh.npy"), _load(f"{d}/vdensity_rh.npy")
+    off, idx, seg = _hemispheres(adj_lh, adj_rh, mask_lh, mask_rh)
+    vd = np.concatenate([_vd(vd_lh, mask_lh), _vd(vd_rh, mask_rh)])
+    X = np.column_stack([np.ones(n), pred_x])
+    k = X.shape[1]
+    if getattr(opts, "specifyvars", None):
+        ncon = opts.specifyvars[1] + 1 - opts.specifyvars[0]
+    else:
+        ncon = k - 1
+    eng = E.PermutationEngine(ny, pred_x, (off, idx), seg, float(optstfce[0]), float(optstfce[1]),
+                              vdensity=vd, contrasts=list(range(1, ncon + 1)), floor_zero=True,
+                              batch=getattr(opts, "batch", 64))
+    designs = _designs_for(X, n, start, stop, opts, seed)
+    maxima = _run_designs(eng, designs, eng.batch).max(axis=-1)  # (P, C, 2)
+    out = "output_%s/perm_Tstat_%s" % (surface, surface)
+    os.makedirs(out, exist_ok=True)
+    for c in range(ncon):
+        lines = []
+        for p in range(maxima.shape[0]):
+            lines += ["%.4f" % maxima[p, c, 0], "%.4f" % maxima[p, c, 1]]
+        _append(os.path.join(out, "perm_tstat_con%d_TFCE_maxVertex.csv" % (c + 1)), lines)
+    return maxima
+
+
+def voxel_regress_run(opts):
+    start, stop = int(opts.range[0]), int(opts.range[1]) + 1
+    seed = opts.seed[0] if getattr(opts, "seed", None) else None
+    n = int(_load("python_temp/num_subjects.npy"))
+    ny = _load("python_temp/raw_nonzero_corr.npy").T
+    pred_x = _load("python_temp/pred_x.npy")
+    adjac = _load("python_temp/adjac.npy")
+    ancova = int(_load("python_temp/ancova.npy"))
+    optstfce = _load("python_temp/optstfce.npy")
+    off, idx = to_csr(adjac)
+    X = np.column_stack([np.ones(n), pred_x])
+    k = X.shape[1]
+    out = "output/perm_Tstat"
+    os.makedirs(out, exist_ok=True)
+    if ancova == 1:
+        return voxel_ftest_run(ny, X, (off, idx), optstfce, start, stop, seed, out)
+    if getattr(opts, "specifyvars", None):
+        ncon = opts.specifyvars[1] + 1 - opts.specifyvars[0]
+    else:
+        ncon = k - 1
+    eng = E.PermutationEngine(np.ascontiguousarray(ny, np.float32), pred_x, (off, idx), None,
+                              float(optstfce[0]), float(optstfce[1]), contrasts=list(range(1, ncon + 1)),
+                              batch=getattr(opts, "batch", 64))
+    designs = _designs_for(X, n, start, stop, opts, seed)
+    maxima = _run_designs(eng, designs, eng.batch)[..., 0]  # (P, C, 2)
+    for c in range(ncon):
+        lines = []
+        for p in range(maxima.shape[0]):
+            lines += ["%1.4f" % maxima[p, c, 0], "%1.4f" % maxima[p, c, 1]]
+        _append(os.path.join(out, "perm_tstat_con%d_TFCE_maxVoxel.csv" % (c + 1)), lines)
+    return maxima
+
+
+def voxel_ftest_run(ny, X, adjacency, optstfce, start, stop, seed, out):
+    """The voxel --ftest (ancova) branch (voxel_…randomise.py:79-89): twice the
+    permutations, sqrt(max(F,0)) swept with one sign."""
+    import torch
+
+    from .adjacency import AdjacencySet
+    from .device import ptr, stream_handle
+    from .glm import DesignBatch, glm_fstat
+    n = X.shape[0]
+    adj = AdjacencySet(adjacency, float(optstfce[0]), float(optstfce[1]))
+    adj.set_accumulation("component")
+    Yd = torch.from_numpy(np.ascontiguousarray(ny, np.float32)).cuda()
+    centre = float(np.mean(ny))
+    lines = []
+    perms = _perm_rows(n, start, int((stop - 1) * 2 + 1), seed)
+    for b in range(0, perms.shape[0], 64):
+        db = DesignBatch(X[perms[b:b + 64]])
+        F = glm_fstat(Yd, db, centre=centre)
+        F = torch.sqrt(torch.clamp(F, min=0.0)).contiguous()
+        mx = torch.empty(db.G, device="cuda")
+        adj.sweep_batch(ptr(F), F.shape[1], db.G, 1, None, 0, ptr(mx), None, 0, stream_handle())
+        adj.status()
+        lines += ["%1.4f" % v for v in mx.cpu().numpy()]
+    _append(os.path.join(out, "perm_fstat_TFCE_maxVoxel.csv"), lines)
+    return np.asarray([float(l) for l in lines])
+
+
+def mediation_parser(ap=None, surface=True):
+    ap = parser_common(ap or argparse.ArgumentParser(description="Mediation + TFCE permutations (GPU)"),
+                       surface=surface)
+    ap.add_argument("-m", "--medtype", nargs=1, choices=["M", "Y", "I"], required=True)
+    return ap
+
+
+def vertex_mediation_run(opts):
+    start, stop = int(opts.range[0]), int(opts.range[1]) + 1
+    medtype, surface = str(opts.medtype[0]), str(opts.surface[0])
+    seed = opts.seed[0] if getattr(opts, "seed", None) else None
+    d = "python_temp_med_%s" % surface
+    y = _load(f"{d}/merge_y.npy")
+    mask_lh, mask_rh = _load(f"{d}/bin_mask_lh.npy"), _load(f"{d}/bin_mask_rh.npy")
+    n = int(_load(f"{d}/num_subjects.npy"))
+    pred_x, depend_y = _load(f"{d}/pred_x.npy"), _load(f"{d}/depend_y.npy")
+    adj_lh, adj_rh = _load(f"{d}/adjac_lh.npy"), _load(f"{d}/adjac_rh.npy")
+    optstfce = _load(f"{d}/optstfce.npy")
+    vd_lh, vd_rh = _load(f"{d}/vdensity_lh.npy"), _load(f"{d}/vdensity_rh.npy")
+    off, idx, seg = _hemispheres(adj_lh, adj_rh, mask_lh, mask_rh)
+    vd = np.concatenate([_vd(vd_lh, mask_lh), _vd(vd_rh, mask_rh)])
+    eng = E.MediationEngine(y, pred_x, depend_y, medtype, (off, idx), seg, float(optstfce[0]),
+                            float(optstfce[1]), vdensity=vd, floor_zero=True, batch=getattr(opts, "batch", 64))
+    maxima = eng.run(perms=_perm_rows(n, start, stop, seed))[:, 0, 0, :].max(axis=-1)
+    out = "output_med_%s/perm_SobelZ_%s" % (surface, medtype)
+    os.makedirs(out, exist_ok=True)
+    _append(os.path.join(out, "perm_Zstat_%s_TFCE_maxVertex.csv" % medtype), ["%.4f" % m for m in maxima])
+    return maxima
+
+
+def voxel_mediation_run(opts):
+    start, stop = int(opts.range[0]), int(opts.range[1]) + 1
+    medtype = str(opts.medtype[0])
+    seed = opts.seed[0] if getattr(opts, "seed", None) else None
+    n = int(_load("python_temp/num_subjects.npy"))
+    ny = _load("python_temp/raw_nonzero_corr.npy").T
+    pred_x, depend_y = _load("python_temp/pred_x.npy"), _load("python_temp/depend_y.npy")
+    adjac = _load("python_temp/adjac.npy")
+    optstfce = _load("python_temp/optstfce.npy")
+    eng = E.MediationEngine(np.ascontiguousarray(ny, np.float32), pred_x, depend_y, medtype, to_csr(adjac), None,
+                            float(optstfce[0]), float(optstfce[1]), batch=getattr(opts, "batch", 64))
+    maxima = eng.run(perms=_perm_rows(n, start, stop, seed))[:, 0, 0, 0]
+    out = "output/perm_SobelZ"
+    os.makedirs(out, exist_ok=True)
+    _append(os.path.join(out, "perm_Zstat_%s_TFCE_maxVoxel.csv" % medtype), ["%1.4f" % m for m in maxima])
+    return maxima
+
+
+def mmr_lr_run(surf_num, perm_range, seed, path, H, E_, pred_x=None, mediation=None, batch=64):
+    """One surface of mmr-lr (tm_mmr_rand_low_ram_parallel.py:166-207): reads
+    tmi_temp/<s>_{adjacency,mask,data,vdensity}_temp.npy; the permutation of
+    iteration p is RandomState(p + seed) (tm_func.py:147-151) for every surface,
+    so the study-wide maxima line up across surfaces."""
+    adjacency = _load("tmi_temp/%d_adjacency_temp.npy" % surf_num)
+    mask = _load("tmi_temp/%d_mask_temp.npy" % surf_num)
+    data = _load("tmi_temp/%d_data_temp.npy" % surf_num)
+    vdensity = _load("tmi_temp/%d_vdensity_temp.npy" % surf_num)
+    n = data.shape[0]
+    m = np.asarray(mask).ravel() == 1
+    off, idx = induced_csr(adjacency, m) if m.shape[0] == len(adjacency) and not m.all() else to_csr(adjacency)
+    vd = _vd(vdensity, np.ones(data.shape[1], bool)) if np.ndim(vdensity) else None
+    perms = _perm_rows(n, perm_range[0], perm_range[1] + 1, seed)
+    floor = not m.all()
+    if mediation is None:
+        eng = E.PermutationEngine(np.ascontiguousarray(data, np.float32), pred_x, (off, idx), None, H, E_,
+                                  vdensity=vd, floor_zero=floor, batch=batch)
+        maxima = eng.run(perms=perms)[..., 0]  # (P, C, 2)
+        for c in range(maxima.shape[1]):
+            lines = []
+            for p in range(maxima.shape[0]):
+                lines += ["%f" % maxima[p, c, 0], "%f" % maxima[p, c, 1]]
+            _append(os.path.join(path, "perm_maxTFCE_surf%d_tcon%d.csv" % (surf_num, c + 1)), lines)
+        return maxima
+    medtype, mx, dy = mediation
+    eng = E.MediationEngine(np.ascontiguousarray(data, np.float32), mx, dy, medtype, (off, idx), None, H, E_,
+                            vdensity=vd, floor_zero=floor, batch=batch)
+    maxima = eng.run(perms=perms)[:, 0, 0, 0]
+    _append(os.path.join(path, "perm_maxTFCE_surf%d_%s_zstat.csv" % (surf_num, medtype)), ["%f" % v for v in maxima])
+    return maxima
