@@ -85,3 +85,14 @@ def test_observed_maps_match_oracle(run100):
             img = (s * tmaps[ci]).astype(np.float32)
             e = oracle.tfce(st.offsets, st.indices, img, 2.0, 1.0, hh_exact=True)
             np.testing.assert_array_equal(tfce_maps[ci, si], e * (img.max() / np.float32(100)))
+
+
+def test_graph_runner_matches_uncaptured(config1):
+    st = config1
+    eng = E.PermutationEngine(st.Y, st.pred_x, (st.offsets, st.indices), st.segments, 2.0, 1.0, batch=16)
+    perms = E.permutations(st.n, 13, 0, 16 * 5 + 7)  # 5 full captured batches + a partial one
+    a = eng.run(perms=perms)
+    b = eng.run_graph(perms=perms)
+    np.testing.assert_array_equal(a, b)
+    c = eng.run_graph(perms=perms)  # replays again
+    np.testing.assert_array_equal(a, c)

@@ -1,0 +1,101 @@
+"""Choice of P (permutations per launch) for a permutation engine.
+
+Each candidate P is timed on the device (CUDA events, after a warm-up launch)
+for the GLM + sweep of one batch; the one with the highest permutations per
+second wins.  Good values fill the persistent sweep grid evenly: one launch
+has P x contrasts x signs x segments sweep items spread over the resident
+CTAs (2 per SM), so P where that count is a multiple of the CTA count avoids
+a ragged last wave.  Results are cached per (GPU, n, k, V, entries, segments,
+contrasts, signs) in ~/.cache/tfce_mediation_gb300/autotune.json.
+"""
+from __future__ import annotations
+
+import json
+import os
+
+import numpy as np
+
+CACHE = os.path.join(os.path.expanduser("~"), ".cache", "tfce_mediation_gb300", "autotune.json")
+
+
+def _key(eng):
+    import torch
+    name = torch.cuda.get_device_name()
+    return "|".join(str(x) for x in (name, eng.n, eng.k, eng.V, eng.adj.n_entries, eng.n_seg, eng.C, eng.signs))
+
+
+def _load():
+    try:
+        with open(CACHE) as fh:
+            return json.load(fh)
+    except Exception:
+        return {}
+
+
+def _save(d):
+    try:
+        os.makedirs(os.path.dirname(CACHE), exist_ok=True)
+        tmp = CACHE + f".{os.getpid()}"
+        with open(tmp, "w") as fh:
+            json.dump(d, fh, indent=1)
+        os.replace(tmp, CACHE)
+    except OSError:
+        pass
+
+
+def candidates(eng, max_p=256):
+    """Batch sizes whose sweep items fill whole waves of the resident CTAs,
+    plus the powers of two."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    ctas = 2 * sms
+    per_perm = eng.C * eng.signs * eng.n_seg
+    out = {16, 32, 64, 128, 256}
+    for waves in range(1, 64):
+        items = waves * ctas
+        if items % per_perm == 0:
+            out.add(items // per_perm)
+    return sorted(p for p in out if 4 <= p <= max_p)
+
+
+def time_batch(eng, P, seed=12345, repeats=3):
+    """Milliseconds per batch of P permutations (GLM + sweep), device time."""
+    import torch
+    from .engine import permutations
+    from .glm import DesignBatch
+    perms = permutations(eng.n, seed, 0, P)
+    ops = DesignBatch(eng.X[perms])
+    t = torch.empty((P, eng.C, eng.V), device="cuda", dtype=torch.float32)
+    mx = torch.empty(P * eng.C * eng.signs * eng.n_seg, device="cuda", dtype=torch.float32)
+    eng.tmaps(ops, out=t)
+    eng.sweep_max(t, P * eng.C, out=mx)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(repeats):
+        eng.tmaps(ops, out=t)
+        eng.sweep_max(t, P * eng.C, out=mx)
+    b.record()
+    torch.cuda.synchronize()
+    eng.adj.status()
+    return a.elapsed_time(b) / repeats
+
+
+def choose_batch(eng, max_p=256, use_cache=True):
+    """Best P for this engine's problem (cached)."""
+    key = _key(eng)
+    cache = _load() if use_cache else {}
+    if key in cache:
+        return int(cache[key]["P"])
+    results = {}
+    for P in candidates(eng, max_p):
+        try:
+            ms = time_batch(eng, P)
+        except RuntimeError:
+            continue
+        results[P] = P / ms * 1000.0
+    best = max(results, key=results.get)
+    cache[key] = {"P": best, "perm_per_s": results}
+    if use_cache:
+        _save(cache)
+    return best

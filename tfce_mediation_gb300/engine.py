@@ -34,6 +34,8 @@ class PermutationEngine:
     """Mass-univariate GLM + TFCE null distribution on one GPU.
 
     Y: (n, V) float32 data (subjects x vertices, concatenated segments).
+    batch: permutations per launch, or "auto" (timed candidates, cached;
+    tfce_mediation_gb300.autotune).
     pred_x: (n, k-1) regressors; the design is [1, pred_x] (randomise :88).
     adjacency: (offsets, indices) CSR over V, or an AdjacencySet.
     segments: vertex offsets of the segments (hemispheres / surfaces).
@@ -87,14 +89,21 @@ class PermutationEngine:
         self.signs = signs
         self.floor_zero = bool(floor_zero)
         self.vd = None if vdensity is None else dev(np.asarray(vdensity, np.float32))
-        self.batch = int(batch)
+        self.lib = _lib.load()
         self._coef = dev(np.asarray(self.contrasts, np.int32))
+        if batch == "auto":
+            from .autotune import choose_batch
+            batch = choose_batch(self)
+        self.batch = int(batch)
+        self._alloc_buffers()
+
+    def _alloc_buffers(self):
+        t = self.t
         self._tbuf = t.empty((self.batch, self.C, self.V), device="cuda", dtype=t.float32)
         self._maxbuf = t.empty((self.batch, self.C, self.signs, self.n_seg), device="cuda",
                                dtype=t.float32)
         self._host_max = t.empty((self.batch, self.C, self.signs, self.n_seg), dtype=t.float32,
                                  pin_memory=True)
-        self.lib = _lib.load()
 
     # -- device steps -------------------------------------------------------
     def _designs(self, perms):
@@ -156,6 +165,91 @@ class PermutationEngine:
         for b in range(0, perms.shape[0], self.batch):
             out.append(self.run_batch(perms[b:b + self.batch]))
         return np.concatenate(out) if out else np.zeros((0, self.C, self.signs, self.n_seg), np.float32)
+
+    # -- CUDA-graph path ----------------------------------------------------
+    def _graph_slot(self, P):
+        """One captured batch: pinned design operators -> device, glm_tstat,
+        the sweep (counter reset included), maxima -> pinned host memory."""
+        t = self.t
+        n, kmax = self.n, self.k
+        slot = {"P": P}
+        slot["h_pinv"] = t.empty((P, kmax, n), dtype=t.float32, pin_memory=True)
+        slot["h_X"] = t.empty((P, n, kmax), dtype=t.float32, pin_memory=True)
+        slot["h_invd"] = t.empty((P, kmax), dtype=t.float32, pin_memory=True)
+        slot["h_dof"] = t.empty((P,), dtype=t.float32, pin_memory=True)
+        slot["h_max"] = t.empty((P, self.C, self.signs, self.n_seg), dtype=t.float32, pin_memory=True)
+        for key in ("pinv", "X", "invd", "dof"):
+            slot["d_" + key] = t.empty(slot["h_" + key].shape, device="cuda", dtype=t.float32)
+        slot["d_t"] = t.empty((P, self.C, self.V), device="cuda", dtype=t.float32)
+        slot["d_max"] = t.empty((P, self.C, self.signs, self.n_seg), device="cuda", dtype=t.float32)
+
+        def body():
+            for key in ("pinv", "X", "invd", "dof"):
+                slot["d_" + key].copy_(slot["h_" + key], non_blocking=True)
+            _lib.check(self.lib.glm_tstat(ptr(self.Yd), self.V, n, self.V, ptr(slot["d_pinv"]),
+                                          ptr(slot["d_X"]), ptr(slot["d_invd"]), ptr(slot["d_dof"]), P, kmax,
+                                          ptr(self._coef), self.C, ptr(slot["d_t"]), self.V, stream_handle()))
+            self.adj.sweep_batch(ptr(slot["d_t"]), self.V, P * self.C, self.signs, ptr(self.vd),
+                                 int(self.floor_zero), ptr(slot["d_max"]), None, 0, stream_handle())
+            slot["h_max"].copy_(slot["d_max"], non_blocking=True)
+
+        # warm-up outside capture (allocates the sweep workspace), then capture
+        side = t.cuda.Stream()
+        side.wait_stream(t.cuda.current_stream())
+        with t.cuda.stream(side):
+            body()
+        t.cuda.current_stream().wait_stream(side)
+        t.cuda.synchronize()
+        self.adj.status()
+        g = t.cuda.CUDAGraph()
+        with t.cuda.graph(g):
+            body()
+        slot["graph"] = g
+        slot["event"] = t.cuda.Event()
+        return slot
+
+    def _fill(self, slot, perms):
+        db = DesignBatch(self.X[perms])
+        P = perms.shape[0]
+        slot["h_pinv"].numpy()[:P] = db.pinv64
+        slot["h_X"].numpy()[:P] = db.X64
+        slot["h_invd"].numpy()[:P] = db.invdiag64
+        slot["h_dof"].numpy()[:P] = db.dof
+
+    def run_graph(self, n_perm=None, seed=0, start=0, stop=None, perms=None):
+        """Same result as run(), through two captured batch graphs replayed in
+        turn: while one batch runs on the GPU the host forms the next batch's
+        design inverses.  A final partial batch runs uncaptured."""
+        t = self.t
+        if perms is None:
+            stop = start + n_perm if stop is None else stop
+            perms = permutations(self.n, seed, start, stop)
+        P = self.batch
+        full = perms.shape[0] // P
+        if not hasattr(self, "_slots") or self._slots[0]["P"] != P:
+            self._slots = [self._graph_slot(P), self._graph_slot(P)]
+        out = []
+        pending = None
+        for b in range(full):
+            slot = self._slots[b % 2]
+            if slot.get("busy"):
+                slot["event"].synchronize()
+                out.append((slot["order"], slot["h_max"].numpy().copy()))
+                slot["busy"] = False
+            self._fill(slot, perms[b * P:(b + 1) * P])
+            slot["graph"].replay()
+            slot["event"].record()
+            slot["busy"], slot["order"] = True, b
+        for slot in self._slots:
+            if slot.get("busy"):
+                slot["event"].synchronize()
+                out.append((slot["order"], slot["h_max"].numpy().copy()))
+                slot["busy"] = False
+        self.adj.status()
+        res = [m for _, m in sorted(out, key=lambda x: x[0])]
+        if perms.shape[0] > full * P:
+            res.append(self.run_batch(perms[full * P:]))
+        return np.concatenate(res) if res else np.zeros((0, self.C, self.signs, self.n_seg), np.float32)
 
     def observed(self):
         """Unpermuted t maps (C, V) and scaled TFCE maps (C, signs, V) as host arrays
