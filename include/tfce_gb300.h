@@ -210,6 +210,34 @@ int fwer_sort(double* values, int64_t n, void* stream);
 int fwer_lookup(const double* sorted_null, int64_t N, const double* image, int64_t V,
                 int32_t mode, double* out, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Learned null-tail surrogate: kernels of a small MLP (no counterpart in the
+ * reference, whose only tail model is the gamma / Johnson-SB fit of
+ * bin/tm_maths:522-553).  Row-major matrices, device pointers.
+ *   mlp_gemm:      C[M][N] = op(A)[M][K] . op(B)[K][N] (+ bias[N]) (+ C when
+ *                  accumulate); act 1 applies GELU (erf form) and stores the
+ *                  pre-activation in preact (nullable);
+ *   mlp_gemm_bf16: forward GEMM with bfloat16 A and B, FP32 accumulation;
+ *   mlp_to_bf16:   float -> bfloat16 (round to nearest even);
+ *   mlp_gelu_backward: dz = dy * GELU'(z);
+ *   mlp_bias_grad: db[c] = sum_r dz[r][c];
+ *   mlp_mse_loss:  loss = mean(w_c (y - t)^2), dy = 2 w_c (y - t) / n;
+ *   mlp_adam_step: Adam with bias correction and decoupled weight decay. */
+int mlp_gemm(int32_t transA, int32_t transB, int32_t M, int32_t N, int32_t K, const float* A,
+             int32_t lda, const float* B, int32_t ldb, float* C, int32_t ldc, const float* bias,
+             int32_t act, float* preact, int32_t accumulate, void* stream);
+int mlp_gemm_bf16(int32_t transA, int32_t transB, int32_t M, int32_t N, int32_t K, const void* A,
+                  int32_t lda, const void* B, int32_t ldb, float* C, int32_t ldc, const float* bias,
+                  int32_t act, void* stream);
+int mlp_to_bf16(const float* x, void* y, int64_t n, void* stream);
+int mlp_gelu_backward(const float* dy, const float* z, float* dz, int64_t n, void* stream);
+int mlp_bias_grad(const float* dz, int32_t rows, int32_t cols, float* db, void* stream);
+int mlp_mse_loss(const float* y, const float* t, const float* col_weight, int64_t n, int32_t cols,
+                 float* dy, float* loss, void* stream);
+int mlp_adam_step(float* param, const float* grad, float* m, float* v, int64_t n, float lr,
+                  float beta1, float beta2, float eps, int32_t step, float weight_decay,
+                  void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -71,6 +71,18 @@ SIGNATURES = {
     "fwer_sort": (ctypes.c_int, [c_vp, ctypes.c_int64, c_vp]),
     "fwer_lookup": (ctypes.c_int, [c_vp, ctypes.c_int64, c_vp, ctypes.c_int64, ctypes.c_int32,
                                    c_vp, c_vp]),
+    "mlp_gemm": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                c_vp, ctypes.c_int32, c_vp, ctypes.c_int32, c_vp, ctypes.c_int32, c_vp,
+                                ctypes.c_int32, c_vp, ctypes.c_int32, c_vp]),
+    "mlp_gemm_bf16": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                     ctypes.c_int32, c_vp, ctypes.c_int32, c_vp, ctypes.c_int32, c_vp,
+                                     ctypes.c_int32, c_vp, ctypes.c_int32, c_vp]),
+    "mlp_to_bf16": (ctypes.c_int, [c_vp, c_vp, ctypes.c_int64, c_vp]),
+    "mlp_gelu_backward": (ctypes.c_int, [c_vp, c_vp, c_vp, ctypes.c_int64, c_vp]),
+    "mlp_bias_grad": (ctypes.c_int, [c_vp, ctypes.c_int32, ctypes.c_int32, c_vp, c_vp]),
+    "mlp_mse_loss": (ctypes.c_int, [c_vp, c_vp, c_vp, ctypes.c_int64, ctypes.c_int32, c_vp, c_vp, c_vp]),
+    "mlp_adam_step": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, ctypes.c_int64, ctypes.c_float, ctypes.c_float,
+                                     ctypes.c_float, ctypes.c_float, ctypes.c_int32, ctypes.c_float, c_vp]),
 }
 
 
