@@ -190,6 +190,26 @@ int glm_fstat(const float* Y, int64_t ldy, int32_t n, int64_t V, const float* pi
               const float* X, const float* dof, int32_t G, int32_t kmax, const float* centre,
               float* f_out, int64_t ldf, void* stream);
 
+/* Tensor-core (tcgen05) form of glm_tstat, split BF16: every operand is
+ * hi = bf16(x), lo = bf16(x - hi); beta = P_hi.Y_hi + P_hi.Y_lo + P_lo.Y_hi
+ * with FP32 accumulation in tensor memory (three tcgen05.mma per 16-deep
+ * step), then residuals y - X.beta, RSS, SE and t on the CUDA cores.
+ *   glm_split_bf16: dst_hi/lo [rows][ld_dst] from src [rows][cols] (row
+ *     stride ld_src), or from src [cols][rows] with transpose = 1 (to turn
+ *     Y [n][V] into the per-vertex rows [V][n_pad]); zero past cols;
+ *     ld_dst a multiple of 8;
+ *   glm_tstat_tc: y_hi/lo [V][n_pad], p_hi/lo [G*8][n_pad] (8 rows per
+ *     design, rows >= k_g zero), n_pad a multiple of 32 and <= 640, X /
+ *     invdiag / dof / coef / t_out as glm_tstat; err: a device int32 that
+ *     receives TFCE_ETIMEOUT's device code if an MMA completion wait runs
+ *     out (it is bounded). */
+int glm_split_bf16(const float* src, int64_t ld_src, int32_t transpose, int64_t rows, int32_t cols,
+                   int32_t ld_dst, void* hi, void* lo, void* stream);
+int glm_tstat_tc(const void* y_hi, const void* y_lo, int32_t n, int32_t n_pad, int64_t V,
+                 const void* p_hi, const void* p_lo, const float* X, const float* invdiag,
+                 const float* dof, int32_t G, int32_t kmax, const int32_t* coef, int32_t n_coef,
+                 float* t_out, int64_t ldt, int32_t* err, void* stream);
+
 /* Indirect-effect z from path t values (device), z[p][v] for p < P:
  *   ta [P][lda] (or ta_scalar[P] when ta is NULL: medtype Y's linregress path),
  *   tb [P][ldb];  alg 0 = Aroian, 1 = Sobel, 2 = Goodman (pyfunc.py:146-161). */

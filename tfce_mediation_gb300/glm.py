@@ -103,3 +103,67 @@ def glm_fstat(Y, designs, centre=None, stream=None):
     _lib.check(_lib.load().glm_fstat(ptr(Yd), V, n, V, ptr(pinv), ptr(Xp), ptr(dof), db.G, db.kmax,
                                      ptr(c), ptr(out), V, stream_handle(stream)))
     return out
+
+
+class TensorCoreOperands:
+    """Split-BF16 operands of the tcgen05 GLM (glm_tstat_tc): the data once,
+    as per-vertex rows [V][n_pad] (hi and lo), and each batch's stacked
+    pseudoinverses as [G*8][n_pad] (hi and lo)."""
+
+    def __init__(self, Yd):
+        t = require_cuda()
+        self.t = t
+        self.n, self.V = Yd.shape
+        self.n_pad = (self.n + 31) // 32 * 32
+        if self.n_pad > 640:
+            raise ValueError("the tensor-core GLM holds at most 640 subjects per tile")
+        self.y_hi = t.empty((self.V, self.n_pad), dtype=t.bfloat16, device="cuda")
+        self.y_lo = t.empty_like(self.y_hi)
+        self.lib = _lib.load()
+        _lib.check(self.lib.glm_split_bf16(ptr(Yd), self.V, 1, self.V, self.n, self.n_pad, ptr(self.y_hi),
+                                           ptr(self.y_lo), stream_handle()))
+        self.err = t.zeros(1, dtype=t.int32, device="cuda")
+
+    def stacked(self, db: DesignBatch):
+        """Host float32 [G][8][n_pad] of the pseudoinverse rows (zero padded)."""
+        P8 = np.zeros((db.G, 8, self.n_pad), np.float32)
+        P8[:, :db.kmax, :db.n] = db.pinv64
+        return P8
+
+    def split(self, P8_dev, G, p_hi=None, p_lo=None):
+        t = self.t
+        p_hi = t.empty((G * 8, self.n_pad), dtype=t.bfloat16, device="cuda") if p_hi is None else p_hi
+        p_lo = t.empty_like(p_hi) if p_lo is None else p_lo
+        _lib.check(self.lib.glm_split_bf16(ptr(P8_dev), self.n_pad, 0, G * 8, self.n_pad, self.n_pad, ptr(p_hi),
+                                           ptr(p_lo), stream_handle()))
+        return p_hi, p_lo
+
+    def tstat(self, p_hi, p_lo, X, invd, dof, G, kmax, coef_d, n_coef, out, ldt):
+        _lib.check(self.lib.glm_tstat_tc(ptr(self.y_hi), ptr(self.y_lo), self.n, self.n_pad, self.V, ptr(p_hi),
+                                         ptr(p_lo), ptr(X), ptr(invd), ptr(dof), G, kmax, ptr(coef_d), n_coef,
+                                         ptr(out), ldt, ptr(self.err), stream_handle()))
+
+    def status(self):
+        e = int(self.err.item())
+        if e:
+            self.err.zero_()
+            raise RuntimeError("tensor-core GLM: MMA completion wait ran out (device code %d)" % e)
+
+
+def glm_tstat_tc(Y, designs, coef, ops=None):
+    """t maps (G, n_coef, V) through the tcgen05 split-BF16 GLM."""
+    t = require_cuda()
+    Yd = dev(Y, t.float32)
+    ops = ops or TensorCoreOperands(Yd)
+    db = designs if isinstance(designs, DesignBatch) else DesignBatch(designs)
+    if db.kmax > 8:
+        raise ValueError("at most 8 regressors per design")
+    P8 = dev(ops.stacked(db))
+    p_hi, p_lo = ops.split(P8, db.G)
+    _, Xp, invd, dof = db.to_device()
+    coef_d = dev(np.asarray(coef, np.int32))
+    out = t.empty((db.G, len(coef), ops.V), device="cuda", dtype=t.float32)
+    ops.tstat(p_hi, p_lo, Xp, invd, dof, db.G, db.kmax, coef_d, len(coef), out, ops.V)
+    t.cuda.synchronize()
+    ops.status()
+    return out
