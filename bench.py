@@ -224,7 +224,8 @@ def run_gpu(args):
     st = synth.config2(n=args.n, level=args.level)
     gen_s = time.perf_counter() - t_gen
     eng = E.PermutationEngine(st.Y, st.pred_x, (st.offsets, st.indices), st.segments, 2.0, 1.0,
-                              batch="auto" if args.batch == 0 else args.batch, floor_zero=True)
+                              batch="auto" if args.batch == 0 else args.batch, floor_zero=True,
+                              precision=args.precision)
     P = eng.batch
     C, S, V, n = eng.C, eng.n_seg, eng.V, eng.n
     total_steps = args.warmup + args.steps
@@ -232,7 +233,18 @@ def run_gpu(args):
     base = rank * total_steps * P
     perms = [E.permutations(n, SEED, base + s * P, base + (s + 1) * P) for s in range(total_steps)]
     # device-resident design operators (inputs resident before the timed region)
-    ops = [DesignBatch(eng.X[p]).to_device() for p in perms]
+    tc = eng._tc
+    from tfce_mediation_gb300.device import dev
+    if tc is not None:
+        ops = []
+        for p in perms:
+            db = DesignBatch(eng.X[p])
+            P8, U, Xt = tc.host_operands(db)
+            ops.append((dev(P8), dev(U), dev(Xt), dev(db.invdiag64.astype(np.float32)),
+                        dev(db.dof.astype(np.float32))))
+        pt_buf = tc.tile_designs(ops[0][0], P, eng.k)
+    else:
+        ops = [DesignBatch(eng.X[p]).to_device() for p in perms]
     out_max = torch.empty((total_steps, P, C, 2, S), device="cuda")
     stream = torch.cuda.current_stream()
     lib = eng.lib
@@ -240,11 +252,16 @@ def run_gpu(args):
     from tfce_mediation_gb300.device import ptr
 
     def step(s, ev=None):
-        pinv, Xp, invd, dof = ops[s]
         if ev is not None:
             ev[0].record(stream)
-        _lib.check(lib.glm_tstat(ptr(eng.Yd), V, n, V, ptr(pinv), ptr(Xp), ptr(invd), ptr(dof), P, eng.k,
-                                 ptr(eng._coef), C, ptr(eng._tbuf), V, stream.cuda_stream))
+        if tc is not None:
+            P8d, Ud, Xtd, invd, dof = ops[s]
+            tc.tile_designs(P8d, P, eng.k, out=pt_buf)
+            tc.tstat(pt_buf, Ud, Xtd, invd, dof, P, eng.k, eng._coef, C, eng._tbuf, V)
+        else:
+            pinv, Xp, invd, dof = ops[s]
+            _lib.check(lib.glm_tstat(ptr(eng.Yd), V, n, V, ptr(pinv), ptr(Xp), ptr(invd), ptr(dof), P, eng.k,
+                                     ptr(eng._coef), C, ptr(eng._tbuf), V, stream.cuda_stream))
         if ev is not None:
             ev[1].record(stream)
         eng.adj.sweep_batch(ptr(eng._tbuf), V, P * C, 2, None, 1, ptr(out_max[s]), None, 0,
@@ -255,7 +272,7 @@ def run_gpu(args):
     for s in range(args.warmup):
         step(s)
     torch.cuda.synchronize()
-    eng.adj.status()
+    eng.status()
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
     if ws > 1:
         dist.barrier()
@@ -267,7 +284,7 @@ def run_gpu(args):
             step(args.warmup + s, evs[s])
         stop.record(stream)
         torch.cuda.synchronize()
-    eng.adj.status()
+    eng.status()
     ms = start.elapsed_time(stop)
     glm_ms = [e[0].elapsed_time(e[1]) for e in evs]
     sweep_ms = [e[1].elapsed_time(e[2]) for e in evs]
@@ -303,13 +320,20 @@ def run_gpu(args):
     eng.run_graph(perms=job_perms)
     torch.cuda.synchronize()
     job_value = job_perms.shape[0] * ws / (time.perf_counter() - t0)
-    h2d = st.Y.nbytes + P * (2 * eng.k * n + eng.k + 1) * 4
+    slot = eng._slots[0]
+    h2d = st.Y.nbytes + sum(v.numel() * v.element_size() for k_, v in slot.items()
+                            if k_.startswith("h_") and k_ != "h_max")
     d2h = P * C * 2 * S * 4
 
     if rank != 0:
         dist.destroy_process_group() if ws > 1 else None
         return
     hbm, bf16, peak_kind = measured_peaks()
+    bf16_sus = bf16
+    try:
+        bf16_sus = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("bf16_tflops_sustained", bf16)
+    except (OSError, ValueError):
+        pass
     # dominant kernel: the sweep.  Algorithmic bytes per sweep: statistic 4V +
     # CSR offsets 4(V+1) + CSR entries 4D (per hemisphere).
     Vh = int(st.segments[1] - st.segments[0])
@@ -321,12 +345,31 @@ def run_gpu(args):
     achieved = bytes_per_sweep * sweeps_per_launch / (sweep_avg / 1000) / 1e9
     per_sweep, traffic_note = profile_traffic("tfce_sweep")
     traffic = None if per_sweep is None else per_sweep * sweeps_per_launch
-    glm_flop = 4.0 * n * eng.k * V * P  # beta + residual passes, fp32 CUDA cores
     clocks = clk.summary()
+    if tc is not None:
+        # split-BF16 GEMM: 3 MMAs of M=V, N=8 rows per design, K=n_pad; residual
+        # epilogue: (k+1) FP32 FMAs per vertex, design and subject
+        mma_flop = 2.0 * 3 * V * 8 * tc.padded(P, eng.k) * tc.n_pad
+        epi_flop = 2.0 * (eng.k + 1) * n * V * P
+        glm_info = {"precision": "bf16x3", "kernels": "tile_split_kernel + glm_tc_kernel<%d>" % eng.k,
+                    "ms_per_launch": glm_avg,
+                    "tensor_tflops_issued": mma_flop / (glm_avg / 1000) / 1e12,
+                    "tensor_peak_tflops": bf16_sus,
+                    "tensor_frac": mma_flop / (glm_avg / 1000) / 1e12 / bf16_sus,
+                    "peak_source": f"{peak_kind} bf16_tflops_sustained (kernel timed inside a long step)",
+                    "epilogue_fp32_tflops": epi_flop / (glm_avg / 1000) / 1e12,
+                    "note": "tensor FLOPs count the three split-BF16 products on 8 padded rows per design"}
+        launches = 3 * args.steps
+    else:
+        glm_flop = 4.0 * n * eng.k * V * P  # beta + residual passes, FP32 CUDA cores
+        glm_info = {"precision": "fp32", "kernels": "glm_tstat_kernel", "ms_per_launch": glm_avg,
+                    "achieved_tflops_fp32": glm_flop / (glm_avg / 1000) / 1e12}
+        launches = 2 * args.steps
     line = {
         "metric": METRIC, "value": value, "unit": "perm/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if tc is None else "f32+bf16x3",
+        "data": "synthetic",
         "config": {"workload": WORKLOAD, "perms_per_step": P, "sweeps_per_step": sweeps_per_launch,
                    "l2": "inputs larger than L2 (Y 459 MB, t maps %d MB per step)" % (P * C * V * 4 // 2 ** 20),
                    "parallelism": f"replicas over permutation ranges x{ws}",
@@ -337,15 +380,15 @@ def run_gpu(args):
                         "captured GLM + sweep, maxima -> host"},
         "job_api": {"value": job_value, "unit": "perm/s",
                     "note": "PermutationEngine.run_graph over %d permutations, Y resident" % (8 * P)},
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": "tfce_sweep_kernel", "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm, "peak_source": f"{peak_kind} hbm_gbs",
                      "traffic": traffic, "traffic_note": traffic_note,
                      "algorithmic_bytes_per_launch": bytes_per_sweep * sweeps_per_launch,
                      "ms_per_launch": sweep_avg,
                      "vertex_sweeps_per_s": sweeps_per_launch * Vh / (sweep_avg / 1000)},
-        "kernels_ms_per_step": {"glm_tstat": glm_avg, "tfce_sweep": sweep_avg},
-        "glm": {"achieved_tflops_fp32": glm_flop / (glm_avg / 1000) / 1e12, "unit": "TFLOP/s"},
+        "kernels_ms_per_step": {"glm": glm_avg, "tfce_sweep": sweep_avg},
+        "glm": glm_info,
         "clocks": clocks,
     }
     if not args.no_cpu_baseline:
@@ -370,6 +413,8 @@ def main():
     ap.add_argument("--level", type=int, default=7)
     ap.add_argument("--cpu-perms", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", default="bf16x3", choices=["bf16x3", "fp32"],
+                    help="GLM arithmetic: tensor-core split BF16 or FP32 CUDA cores")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

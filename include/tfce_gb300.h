@@ -190,25 +190,41 @@ int glm_fstat(const float* Y, int64_t ldy, int32_t n, int64_t V, const float* pi
               const float* X, const float* dof, int32_t G, int32_t kmax, const float* centre,
               float* f_out, int64_t ldf, void* stream);
 
-/* Tensor-core (tcgen05) form of glm_tstat, split BF16: every operand is
- * hi = bf16(x), lo = bf16(x - hi); beta = P_hi.Y_hi + P_hi.Y_lo + P_lo.Y_hi
- * with FP32 accumulation in tensor memory (three tcgen05.mma per 16-deep
- * step), then residuals y - X.beta, RSS, SE and t on the CUDA cores.
- *   glm_split_bf16: dst_hi/lo [rows][ld_dst] from src [rows][cols] (row
- *     stride ld_src), or from src [cols][rows] with transpose = 1 (to turn
- *     Y [n][V] into the per-vertex rows [V][n_pad]); zero past cols;
- *     ld_dst a multiple of 8;
- *   glm_tstat_tc: y_hi/lo [V][n_pad], p_hi/lo [G*8][n_pad] (8 rows per
- *     design, rows >= k_g zero), n_pad a multiple of 32 and <= 640, X /
+/* Tensor-core (tcgen05) form of glm_tstat (same t as cynumstats.pyx:28-64),
+ * split BF16: every GEMM operand is hi = bf16(x), lo = bf16(x - hi);
+ * beta = Y_hi.P_hi + Y_hi.P_lo + Y_lo.P_hi with FP32 accumulation in tensor
+ * memory (three tcgen05.mma per 16-deep step; M = 128 vertices, N = 8 rows
+ * per design), then the residuals y - X.beta (FP32 data), RSS, SE and t on
+ * the CUDA cores.
+ *   glm_tc_design_block(kmax): designs per tile DB (32 for kmax <= 5, else
+ *     16); -1 for kmax outside [1, 8];
+ *   glm_tile_bytes(rows, row_block, n_pad): bytes of a pre-tiled operand;
+ *   glm_col_mean: mean[v] = FP64 mean over the n rows of Y [n][ldy] (the
+ *     per-vertex centre of the data);
+ *   glm_tile_split: dst = the split-BF16 tiles of src [rows][cols] (row
+ *     stride ld_src; transpose = 1: src stored [cols][rows], the data n x V)
+ *     minus row_shift[row] when row_shift is not NULL, in row blocks of
+ *     row_block (128 for the data, DB*8 for the stacked pseudoinverse rows
+ *     [G_pad*8][n_pad], rows >= k_g of a design zero) and 16-deep K steps,
+ *     n_pad a multiple of 16 >= cols, zero fill;
+ *   glm_tstat_tc: y_tiles (row block 128, centred on y_shift when that is not
+ *     NULL) and p_tiles (row block DB*8) from glm_tile_split; u_rows
+ *     [G_pad][kmax] = pinv(X_d).1 (needed with y_shift: beta = beta_c +
+ *     y_shift[v] u_d); Y the FP32 data [n][ldy]; x_rows
+ *     [ceil(G/DB)][n_sc][kmax][DB] float, the NEGATED design rows (design d of
+ *     block b, row i at [b][i][j][d], zero padded; n_sc a multiple of 32 >= n);
  *     invdiag / dof / coef / t_out as glm_tstat; err: a device int32 that
- *     receives TFCE_ETIMEOUT's device code if an MMA completion wait runs
- *     out (it is bounded). */
-int glm_split_bf16(const float* src, int64_t ld_src, int32_t transpose, int64_t rows, int32_t cols,
-                   int32_t ld_dst, void* hi, void* lo, void* stream);
-int glm_tstat_tc(const void* y_hi, const void* y_lo, int32_t n, int32_t n_pad, int64_t V,
-                 const void* p_hi, const void* p_lo, const float* X, const float* invdiag,
-                 const float* dof, int32_t G, int32_t kmax, const int32_t* coef, int32_t n_coef,
-                 float* t_out, int64_t ldt, int32_t* err, void* stream);
+ *     receives TFCE_ETIMEOUT's device code if a copy or MMA completion wait
+ *     runs out (all are bounded).  Tiles and x_rows 16-byte aligned. */
+int glm_tc_design_block(int32_t kmax);
+int64_t glm_tile_bytes(int64_t rows, int32_t row_block, int32_t n_pad);
+int glm_col_mean(const float* Y, int64_t ldy, int32_t n, int64_t V, float* mean, void* stream);
+int glm_tile_split(const float* src, int64_t ld_src, int32_t transpose, int64_t rows, int32_t cols,
+                   const float* row_shift, int32_t row_block, int32_t n_pad, void* dst, void* stream);
+int glm_tstat_tc(const void* y_tiles, const float* y_shift, const float* Y, int64_t ldy, int32_t n,
+                 int32_t n_pad, int64_t V, const void* p_tiles, const float* u_rows, const float* x_rows,
+                 int32_t n_sc, const float* invdiag, const float* dof, int32_t G, int32_t kmax,
+                 const int32_t* coef, int32_t n_coef, float* t_out, int64_t ldt, int32_t* err, void* stream);
 
 /* Indirect-effect z from path t values (device), z[p][v] for p < P:
  *   ta [P][lda] (or ta_scalar[P] when ta is NULL: medtype Y's linregress path),

@@ -1,11 +1,13 @@
 """End-to-end permutation inference on config 1 (icosphere L5, n=100, k=3)
 against the oracle pipeline on the same host-seeded permutation streams.
 
-The GPU computes t in float32, the oracle in float64, so the sweeps see maps
-that differ by ~1e-6 relative; a vertex that sits on a threshold can then
-change one increment.  Stated tolerances:
+The GPU computes t in FP32 arithmetic (precision 'fp32', ~1e-6 relative to
+FP64) or as a split-BF16 tensor-core GEMM with FP32 accumulation ('bf16x3',
+~3e-5), the oracle in float64, so the sweeps see maps that differ slightly; a
+vertex that sits on a threshold can then change one increment.  Stated
+tolerances:
   * per-permutation max-TFCE: relative error <= 1e-3 for every value, median
-    <= 1e-5;
+    <= 1e-5 ('fp32') / 1e-4 ('bf16x3');
   * 1-p(FWER) maps: max |delta p| <= 0.005 (the target of the path).
 """
 import numpy as np
@@ -32,20 +34,30 @@ def oracle_maxima(st, perms, contrasts=(1, 2)):
     return out
 
 
+MEDIAN_BAR = {"fp32": 1e-5, "bf16x3": 1e-4}
+
+
 @pytest.fixture(scope="module")
-def run100(config1):
+def ref100(config1):
+    perms = E.permutations(config1.n, SEED, 0, 100)
+    return perms, oracle_maxima(config1, perms)
+
+
+@pytest.fixture(scope="module", params=["bf16x3", "fp32"])
+def run100(config1, ref100, request):
     st = config1
-    eng = E.PermutationEngine(st.Y, st.pred_x, (st.offsets, st.indices), st.segments, 2.0, 1.0, batch=32)
-    perms = E.permutations(st.n, SEED, 0, 100)
+    eng = E.PermutationEngine(st.Y, st.pred_x, (st.offsets, st.indices), st.segments, 2.0, 1.0, batch=32,
+                              precision=request.param)
+    perms, ref = ref100
     gpu = E.reduce_vertex(eng.run(perms=perms))
-    ref = oracle_maxima(st, perms)
     return st, eng, perms, gpu, ref
 
 
 def test_null_maxima_match_oracle(run100):
     st, eng, perms, gpu, ref = run100
     rel = np.abs(gpu - ref) / np.abs(ref)
-    assert np.median(rel) <= 1e-5, np.median(rel)
+    print(eng.precision, "median", np.median(rel), "max", rel.max())
+    assert np.median(rel) <= MEDIAN_BAR[eng.precision], np.median(rel)
     assert rel.max() <= 1e-3, rel.max()
 
 
@@ -87,9 +99,11 @@ def test_observed_maps_match_oracle(run100):
             np.testing.assert_array_equal(tfce_maps[ci, si], e * (img.max() / np.float32(100)))
 
 
-def test_graph_runner_matches_uncaptured(config1):
+@pytest.mark.parametrize("precision", ["bf16x3", "fp32"])
+def test_graph_runner_matches_uncaptured(config1, precision):
     st = config1
-    eng = E.PermutationEngine(st.Y, st.pred_x, (st.offsets, st.indices), st.segments, 2.0, 1.0, batch=16)
+    eng = E.PermutationEngine(st.Y, st.pred_x, (st.offsets, st.indices), st.segments, 2.0, 1.0, batch=16,
+                              precision=precision)
     perms = E.permutations(st.n, 13, 0, 16 * 5 + 7)  # 5 full captured batches + a partial one
     a = eng.run(perms=perms)
     b = eng.run_graph(perms=perms)

@@ -1,12 +1,13 @@
-"""tcgen05 split-BF16 GLM against the FP32 CUDA-core GLM and the FP64 oracle.
+"""tcgen05 split-BF16 GLM (glm_tstat_tc) against the FP64 oracle.
 
-Bar: |t_tc - t_fp64| <= 2e-4 * max(1, |t|) (split BF16 drops the lo.lo term,
-~2^-16 relative per product, and the residual pass reads y = hi + lo)."""
+Bar: |t_tc - t_fp64| <= 2e-4 * max(1, |t|).  Split BF16 represents each
+operand to ~2^-17 relative and drops the lo.lo product, so the betas carry
+~1e-5 relative error; the residual pass reads the FP32 data."""
 import numpy as np
 import pytest
 
 from oracle import oracle
-from tfce_mediation_gb300.glm import WHAT_T, DesignBatch, glm_stat, glm_tstat_tc
+from tfce_mediation_gb300.glm import WHAT_T, DesignBatch, TensorCoreOperands, glm_stat, glm_tstat_tc
 
 pytestmark = pytest.mark.gpu
 
@@ -17,11 +18,51 @@ def _err(a, ref):
     return float(np.max(np.abs(np.asarray(a, np.float64) - ref) / np.maximum(1.0, np.abs(ref))))
 
 
-@pytest.mark.parametrize("n,V,G", [(100, 10242, 40), (350, 4000, 33), (57, 777, 16)])
-def test_tc_vs_fp32_and_fp64(n, V, G):
+def _split(x):
+    import torch
+    xt = torch.from_numpy(np.ascontiguousarray(x, np.float32))
+    hi = xt.to(torch.bfloat16)
+    lo = (xt - hi.float()).to(torch.bfloat16)
+    return hi.view(torch.int16).numpy(), lo.view(torch.int16).numpy()
+
+
+def test_tile_layout_matches_definition():
+    """Device tiles of a [rows][cols] matrix against the documented byte layout."""
+    import torch
+    from tfce_mediation_gb300 import _lib
+    from tfce_mediation_gb300.device import ptr
+    lib = _lib.load()
+    rng = np.random.default_rng(5)
+    rows, cols, rb, n_pad = 300, 37, 128, 48
+    A = rng.standard_normal((rows, cols)).astype(np.float32)
+    shift = rng.standard_normal(rows).astype(np.float32)
+    nbytes = lib.glm_tile_bytes(rows, rb, n_pad)
+    for transpose, with_shift in ((0, False), (1, False), (1, True)):
+        src = torch.from_numpy(A.T.copy() if transpose else A).cuda()
+        sh = torch.from_numpy(shift).cuda() if with_shift else None
+        ld = rows if transpose else cols
+        dst = torch.zeros(nbytes, dtype=torch.uint8, device="cuda")
+        _lib.check(lib.glm_tile_split(ptr(src), ld, transpose, rows, cols, ptr(sh), rb, n_pad, ptr(dst), None))
+        got = dst.cpu().view(torch.int16).numpy()
+        Ap = np.zeros(((rows + rb - 1) // rb * rb, n_pad), np.float32)
+        Ap[:rows, :cols] = (A - shift[:, None]) if with_shift else A
+        hi, lo = _split(Ap)
+        KS = n_pad // 16
+        exp = np.zeros_like(got)
+        for R in range(Ap.shape[0]):
+            for c in range(n_pad):
+                base = ((R // rb * KS + c // 16) * 2) * rb * 16 + ((c % 16) // 8) * rb * 8 + (R % rb) * 8 + c % 8
+                exp[base] = hi[R, c]
+                exp[base + rb * 16] = lo[R, c]
+        np.testing.assert_array_equal(got, exp)
+
+
+@pytest.mark.parametrize("n,V,G", [(100, 10242, 40), (350, 4000, 33), (57, 777, 16), (350, 20000, 64)])
+def test_tc_vs_fp64(n, V, G):
     rng = np.random.default_rng(n + V)
     Y = rng.standard_normal((n, V)).astype(np.float32)
     Y[:, : V // 3] += 0.4 * rng.standard_normal(n)[:, None].astype(np.float32)
+    Y += 3.0  # an offset: the residual pass must not lose it
     X = np.column_stack([np.ones(n), rng.integers(0, 2, n), rng.standard_normal((n, 3))])
     perms = np.stack([rng.permutation(n) for _ in range(G)])
     db = DesignBatch(X[perms])
@@ -37,11 +78,57 @@ def test_tc_vs_fp32_and_fp64(n, V, G):
     assert e_tc <= TOL, e_tc
 
 
-def test_tc_mixed_k_designs():
-    rng = np.random.default_rng(9)
+@pytest.mark.parametrize("ks", [(2, 3, 5, 8, 4), (6, 7, 6), (1, 1, 2)])
+def test_tc_mixed_k_designs(ks):
+    rng = np.random.default_rng(sum(ks))
     n, V = 120, 3000
     Y = rng.standard_normal((n, V)).astype(np.float32)
-    mats = [np.column_stack([np.ones(n), rng.standard_normal((n, k - 1))]) for k in (2, 3, 5, 8, 4)]
-    t_tc = glm_tstat_tc(Y, DesignBatch(mats), [1]).cpu().numpy()
+    mats = [np.column_stack([np.ones(n), rng.standard_normal((n, k - 1))]) if k > 1 else np.ones((n, 1))
+            for k in ks]
+    coef = [0] if min(ks) == 1 else [0, 1]
+    t_tc = glm_tstat_tc(Y, DesignBatch(mats), coef).cpu().numpy()
     for g, Xg in enumerate(mats):
-        assert _err(t_tc[g, 0], oracle.tval_fp64(Xg, Y)[1]) <= TOL
+        ref = oracle.tval_fp64(Xg, Y)[coef]
+        assert _err(t_tc[g], ref) <= TOL, (g, _err(t_tc[g], ref))
+
+
+def test_tc_many_blocks_kmax7():
+    """kmax 7: 16 designs per tile, 70 designs = 5 design blocks."""
+    rng = np.random.default_rng(11)
+    n, V, G = 200, 5000, 70
+    Y = rng.standard_normal((n, V)).astype(np.float32)
+    X = np.column_stack([np.ones(n), rng.standard_normal((n, 6))])
+    perms = np.stack([rng.permutation(n) for _ in range(G)])
+    ops = TensorCoreOperands(__import__("torch").from_numpy(Y).cuda())
+    t_tc = glm_tstat_tc(Y, DesignBatch(X[perms]), [1, 6], ops=ops).cpu().numpy()
+    for g in range(0, G, 7):
+        ref = oracle.tval_fp64(X[perms[g]], Y)[[1, 6]]
+        assert _err(t_tc[g], ref) <= TOL
+    assert int(ops.err.item()) == 0
+
+
+@pytest.mark.parametrize("offset", [0.0, 25.0, 1000.0])
+def test_tc_offset_data(offset):
+    """Data far from zero (mean/SD up to 1000): the per-vertex centring keeps
+    the split error on the data's spread."""
+    rng = np.random.default_rng(21)
+    n, V, G = 150, 3000, 20
+    Y = (offset + rng.standard_normal((n, V))).astype(np.float32)
+    X = np.column_stack([np.ones(n), rng.standard_normal((n, 2))])
+    perms = np.stack([rng.permutation(n) for _ in range(G)])
+    t_tc = glm_tstat_tc(Y, DesignBatch(X[perms]), [1, 2]).cpu().numpy()
+    for g in range(G):
+        ref = oracle.tval_fp64(X[perms[g]], Y.astype(np.float64))[[1, 2]]
+        assert _err(t_tc[g], ref) <= TOL, (offset, g, _err(t_tc[g], ref))
+
+
+def test_tc_no_intercept_design():
+    """Designs without a constant column: beta = beta_c + mean * pinv(X).1 is
+    still exact."""
+    rng = np.random.default_rng(8)
+    n, V = 90, 2000
+    Y = (5.0 + rng.standard_normal((n, V))).astype(np.float32)
+    mats = [rng.standard_normal((n, 3)) + 1.0 for _ in range(5)]
+    t_tc = glm_tstat_tc(Y, DesignBatch(mats), [0, 1, 2]).cpu().numpy()
+    for g, Xg in enumerate(mats):
+        assert _err(t_tc[g], oracle.tval_fp64(Xg, Y)[[0, 1, 2]]) <= TOL

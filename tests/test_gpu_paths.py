@@ -1,9 +1,10 @@
 """Mediation, voxel and multisurface paths on the GPU against the oracle and
 the reference's own outputs (golden vectors).
 
-Tolerances: the GPU computes t/z in float32 and the oracle in float64, so
-sweeps see maps that differ by ~1e-6 relative.  Per-permutation maxima:
-relative error <= 1e-3 (median <= 1e-5); TFCE images: |delta| <= 1e-3 * max.
+Tolerances: the engines compute the permutation t maps with the split-BF16
+tensor-core GLM (~3e-5 relative to FP64; z inherits it), the oracle in
+float64, so sweeps see maps that differ slightly.  Per-permutation maxima:
+relative error <= 1e-3 (median <= 1e-4); TFCE images: |delta| <= 1e-3 * max.
 """
 import os
 
@@ -20,7 +21,8 @@ pytestmark = pytest.mark.gpu
 
 def _assert_maxima(got, ref):
     rel = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-12)
-    assert np.median(rel) <= 1e-5, np.median(rel)
+    print("maxima: median", np.median(rel), "max", rel.max())
+    assert np.median(rel) <= 1e-4, np.median(rel)
     assert rel.max() <= 1e-3, rel.max()
 
 

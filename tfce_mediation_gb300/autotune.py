@@ -21,7 +21,8 @@ CACHE = os.path.join(os.path.expanduser("~"), ".cache", "tfce_mediation_gb300", 
 def _key(eng):
     import torch
     name = torch.cuda.get_device_name()
-    return "|".join(str(x) for x in (name, eng.n, eng.k, eng.V, eng.adj.n_entries, eng.n_seg, eng.C, eng.signs))
+    return "|".join(str(x) for x in (name, eng.n, eng.k, eng.V, eng.adj.n_entries, eng.n_seg, eng.C, eng.signs,
+                                     getattr(eng, "precision", "fp32")))
 
 
 def _load():
@@ -77,7 +78,7 @@ def time_batch(eng, P, seed=12345, repeats=3):
         eng.sweep_max(t, P * eng.C, out=mx)
     b.record()
     torch.cuda.synchronize()
-    eng.adj.status()
+    eng.status()
     return a.elapsed_time(b) / repeats
 
 

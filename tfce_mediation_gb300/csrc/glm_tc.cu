@@ -1,22 +1,44 @@
-// Tensor-core (tcgen05) form of the permuted-design GLM: the stacked
-// pseudoinverses of G designs, P = [G*8][n] (rows of inv(X'X)X', padded to 8
-// rows per design), times the data Y [n][V], as one GEMM per 64-vertex tile
-// with an FP32 accumulator in tensor memory, followed by the residual / RSS /
-// SE / t epilogue on the CUDA cores (cynumstats.pyx:28-29, 47-64: RSS from the
-// residuals y - X.beta, never from Y'Y).
+// Tensor-core (tcgen05) form of the permuted-design GLM.
 //
-// Precision: split BF16 -- every operand is stored as hi = bf16(x) and
-// lo = bf16(x - hi), and beta = P_hi.Y_hi + P_hi.Y_lo + P_lo.Y_hi is
-// accumulated in FP32 by three tcgen05.mma kind::f16 per 16-deep K step
-// (the dropped P_lo.Y_lo term is ~2^-16 relative).  The residual pass uses
-// y = hi + lo.
+// One launch computes t maps for G designs over V vertices:
+//   beta_d = pinv(X_d) y            (cynumstats.pyx:28-29, np.dot(pinv, y))
+//   r      = y - X_d beta_d         (cynumstats.pyx:47-64: the residuals)
+//   t      = beta_j / sqrt(r'r / dof * inv(X'X)_jj)
+// The betas of all designs are one GEMM, D[v][d*8+j] = sum_i Y[v][i] P[d*8+j][i],
+// with M = 128 vertices (tensor-memory lanes), N = 8 pseudoinverse rows per
+// design (up to 32 designs: N = 256), K = subjects.  The epilogue forms the
+// residuals from y and X_d on the CUDA cores (RSS from the residuals, never
+// from Y'Y) and writes t.
 //
-// Per CTA (256 threads, one 64-vertex tile): the tile of Y (hi and lo,
-// K-major, no swizzle, 8x16-byte core matrices) stays in shared memory; for
-// each group of 16 designs (M = 128 rows) the pseudoinverse rows stream
-// through a 32-deep K chunk, thread 0 issues the MMAs, tcgen05.commit
-// arrives on an mbarrier (bounded wait), warps 0-3 read the accumulator with
-// tcgen05.ld into shared memory and all warps run the epilogue.
+// Precision: split BF16.  Both operands are stored as hi = bf16(x) and
+// lo = bf16(x - hi); each 16-deep K step issues hi.hi + hi.lo + lo.hi
+// (tcgen05.mma kind::f16, FP32 accumulation in tensor memory).  The dropped
+// lo.lo term and the split's rounding are ~2^-17 relative per product.  The
+// residual pass reads the FP32 data.  The data is centred per vertex (FP64
+// mean) before the split, so the split error scales with the data's spread,
+// not its mean; the epilogue restores beta = beta_c + mean_v * pinv(X_d).1,
+// which is exact for any design.
+//
+// Operands are pre-tiled in HBM (glm_tile_split) so that one K step of a
+// tile is a contiguous chunk: one cp.async.bulk per operand per pipeline
+// stage, completing on an mbarrier.  In shared memory each chunk is the
+// K-major no-swizzle layout of 8-row x 16-byte core matrices:
+//   [hi|lo][k-block 0..1][row][8 elements]
+// so a descriptor has LBO (next 8 K elements) = rows*16 bytes and SBO (next
+// 8 rows) = 128 bytes.
+//
+// Per CTA (256 threads, 2 CTAs per SM so one CTA's MMAs overlap the other's
+// epilogue): thread 0 runs the 4-stage copy/MMA pipeline.  The accumulator is
+// then drained (warp w reads TMEM lanes 32*(w%4).., design half w/4) into
+// shared memory and re-read transposed: lane = design, each thread a run of
+// DB/2 vertices with their betas in registers.  Subjects stream through
+// shared memory in chunks of 32 (cp.async, double buffered): the design rows
+// are a conflict-free per-lane load, y a broadcast; residual and RSS use
+// packed FP32x2 FMAs over vertex pairs.
+//
+// Every wait is bounded (globaltimer, 2 s): on expiry the kernel records
+// kDevLoopLimit in *err, waits (bounded) for its own copies in flight,
+// frees its tensor memory and returns.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -26,17 +48,42 @@
 namespace tfgb {
 
 constexpr int kTcThreads = 256;
-constexpr int kTcN = 64;        // vertices per CTA (MMA N)
-constexpr int kTcM = 128;       // design rows per MMA (16 designs x 8)
-constexpr int kTcKPad = 8;      // rows per design in the stacked operand
-constexpr int kTcKC = 32;       // K elements per A chunk (2 MMA K steps)
-constexpr int kTcMaxN = 640;    // subjects supported by the shared-memory tile
-constexpr int kBetaLd = kTcN + 1;
-constexpr long long kTcWaitLimit = 1LL << 26;
+constexpr int kTcM = 128;           // vertices per tile (MMA M, TMEM lanes)
+constexpr int kTcRowsPerDesign = 8; // pseudoinverse rows per design (kmax <= 8)
+constexpr int kTcK = 16;            // subjects per MMA K step / pipeline stage
+constexpr int kTcStages = 4;
+constexpr int kTcSubjChunk = 32;    // subjects per epilogue X chunk
+constexpr uint64_t kTcWaitNs = 2000000000ull;
+
+__host__ __device__ constexpr int tc_dpt(int kmax) { return kmax <= 5 ? 16 : 8; }  // designs per thread
+__host__ __device__ constexpr int tc_db(int kmax) { return 2 * tc_dpt(kmax); }     // designs per tile
+__host__ __device__ constexpr int tc_n(int kmax) { return tc_db(kmax) * kTcRowsPerDesign; }
+__host__ __device__ constexpr int tc_y_stage() { return kTcM * kTcK * 2 * 2; }          // 8 KB
+__host__ __device__ constexpr int tc_p_stage(int kmax) { return tc_n(kmax) * kTcK * 2 * 2; }
+__host__ __device__ constexpr int tc_stage(int kmax) { return tc_y_stage() + tc_p_stage(kmax); }
+__host__ __device__ constexpr int tc_xchunk(int kmax) { return kTcSubjChunk * kmax * tc_db(kmax) * 4; }
+__host__ __device__ constexpr int tc_ychunk() { return kTcSubjChunk * kTcM * 4; }
+constexpr int kTcBld = kTcM + 1;  // row stride (floats) of the drained betas
+__host__ __device__ constexpr int tc_beta_bytes(int kmax) { return tc_db(kmax) * kmax * kTcBld * 4; }
+__host__ __device__ constexpr int tc_cmax(int a, int b) { return a > b ? a : b; }
+// the stage ring, the drained betas and the subject chunks share one area
+__host__ __device__ constexpr int tc_area(int kmax) {
+  return (tc_cmax(tc_cmax(kTcStages * tc_stage(kmax), tc_beta_bytes(kmax)),
+                  2 * (tc_xchunk(kmax) + tc_ychunk())) + 127) / 128 * 128;
+}
+__host__ __device__ constexpr int tc_smem(int kmax) { return tc_area(kmax) + 128; }
+static_assert(tc_smem(5) <= 113 * 1024 && tc_smem(8) <= 113 * 1024 && tc_smem(4) <= 113 * 1024,
+              "two CTAs per SM");
 
 // --- PTX wrappers -----------------------------------------------------------
 __device__ inline uint32_t smem_addr(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ inline uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
 }
 
 // tcgen05 shared-memory matrix descriptor, K-major, no swizzle:
@@ -86,282 +133,446 @@ __device__ inline bool mbar_try_wait(uint32_t mbar, uint32_t phase) {
   return ok != 0;
 }
 
+// Bounded wait on an mbarrier phase; false when the time limit ran out.
+__device__ inline bool mbar_wait(uint32_t mbar, uint32_t phase) {
+  if (mbar_try_wait(mbar, phase)) return true;
+  const uint64_t t0 = global_ns();
+  while (!mbar_try_wait(mbar, phase)) {
+    if (global_ns() - t0 > kTcWaitNs) return false;
+  }
+  return true;
+}
+
+__device__ inline void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+
+__device__ inline void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+      "l"(src), "r"(bytes), "r"(mbar)
+      : "memory");
+}
+
+__device__ inline void cp_async16(uint32_t dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ inline void cp_async4(uint32_t dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ inline void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ inline void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 __device__ inline void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ inline void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ inline void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-__device__ inline void tmem_ld16(uint32_t taddr, float* out) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
+__device__ inline void tmem_ld8(uint32_t taddr, float* out) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-  for (int i = 0; i < 16; ++i) out[i] = __uint_as_float(r[i]);
+  for (int i = 0; i < 8; ++i) out[i] = __uint_as_float(r[i]);
 }
 
-// --- operand preparation --------------------------------------------------
-// dst_hi/lo [rows][ld_dst] = split of src [rows][cols] (row stride ld_src),
-// zero past cols.  Optional transpose: src is [cols][rows] (Y stored n x V).
-__global__ void split_bf16_kernel(const float* __restrict__ src, int64_t ld_src, int transpose, int64_t rows,
-                                  int cols, int ld_dst, __nv_bfloat16* __restrict__ hi,
-                                  __nv_bfloat16* __restrict__ lo) {
-  const int64_t total = rows * ld_dst;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r = i / ld_dst;
-    const int c = static_cast<int>(i % ld_dst);
-    float x = 0.0f;
-    if (c < cols) x = transpose ? src[(int64_t)c * ld_src + r] : src[r * ld_src + c];
-    const __nv_bfloat16 h = __float2bfloat16_rn(x);
-    hi[i] = h;
-    lo[i] = __float2bfloat16_rn(x - __bfloat162float(h));
+// --- operand pre-tiling -------------------------------------------------------
+// dst = the split-BF16 tiles of a [rows][cols] FP32 matrix (row stride ld_src;
+// transpose: the source is stored [cols][rows], e.g. the data n x V):
+//   byte offset of (row R, col c) = ((R/RB * KS + c/16) * 2 + part) * RB*32
+//                                   + ((c%16)/8) * RB*16 + (R%RB) * 16 + (c%8) * 2
+// with KS = n_pad/16 and zero fill past rows / cols; row_shift (optional)
+// is subtracted from every element of its row first.  One thread writes the
+// 8 columns of one (row, k-block): 16 bytes hi and 16 bytes lo.
+__global__ void tile_split_kernel(const float* __restrict__ src, int64_t ld_src, int transpose, int64_t rows,
+                                  int cols, const float* __restrict__ row_shift, int rb, int ks_count,
+                                  int64_t n_blk, __nv_bfloat16* __restrict__ dst) {
+  const int64_t total = n_blk * ks_count * 2 * rb;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int r = static_cast<int>(idx % rb);
+    int64_t rest = idx / rb;
+    const int kb = static_cast<int>(rest % 2);
+    rest /= 2;
+    const int ks = static_cast<int>(rest % ks_count);
+    const int64_t blk = rest / ks_count;
+    const int64_t R = blk * rb + r;
+    const int c0 = ks * kTcK + kb * 8;
+    const float sh = (row_shift != nullptr && R < rows) ? row_shift[R] : 0.0f;
+    __align__(16) __nv_bfloat16 h[8];
+    __align__(16) __nv_bfloat16 l[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int c = c0 + e;
+      float x = 0.0f;
+      if (R < rows && c < cols) x = (transpose ? src[(int64_t)c * ld_src + R] : src[R * ld_src + c]) - sh;
+      h[e] = __float2bfloat16_rn(x);
+      l[e] = __float2bfloat16_rn(x - __bfloat162float(h[e]));
+    }
+    const int64_t base = ((blk * ks_count + ks) * 2) * (int64_t)rb * kTcK + (int64_t)kb * rb * 8 + (int64_t)r * 8;
+    *reinterpret_cast<uint4*>(dst + base) = *reinterpret_cast<const uint4*>(h);
+    *reinterpret_cast<uint4*>(dst + base + (int64_t)rb * kTcK) = *reinterpret_cast<const uint4*>(l);
   }
 }
 
-// --- the GEMM + epilogue ----------------------------------------------------
+// Per-column FP64 mean of Y [n][ldy] (the per-vertex centre of the data).
+__global__ void col_mean_kernel(const float* __restrict__ Y, int64_t ldy, int n, int64_t V, float* __restrict__ mean) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s += Y[(int64_t)i * ldy + v];
+    mean[v] = static_cast<float>(s / n);
+  }
+}
+
+// --- the GEMM + residual epilogue -----------------------------------------------
 struct TcArgs {
-  const __nv_bfloat16* y_hi;  // [V][n_pad]
-  const __nv_bfloat16* y_lo;
-  const __nv_bfloat16* p_hi;  // [G*8][n_pad]
-  const __nv_bfloat16* p_lo;
-  const float* X;             // [G][n][kmax]
-  const float* invdiag;       // [G][kmax]
-  const float* dof;           // [G]
+  const __nv_bfloat16* yt;  // pre-tiled data, 128-vertex row blocks
+  const __nv_bfloat16* pt;  // pre-tiled pseudoinverse rows, DB*8-row blocks
+  const float* xt;          // [n_db][n_sc][kmax][DB] negated design rows (zero padded)
+  const float* Y;           // FP32 data [n][ldy]
+  const float* shift;       // per-vertex centre subtracted before the split (or null)
+  const float* u;           // [G_pad][kmax] pinv(X_d).1 (with shift)
+  const float* invdiag;     // [G][kmax]
+  const float* dof;         // [G]
   const int32_t* coef;
-  float* t_out;               // [G][n_coef][ldt]
-  int64_t ldt;
-  int64_t V;
-  int32_t n, n_pad, G, kmax, n_coef;
+  float* t_out;             // [G][n_coef][ldt]
+  int64_t ldy, ldt, V;
+  int32_t n, n_sc, ks_count, G, n_db, n_coef;
   int32_t* err;
 };
 
-// Shared memory layout (bytes): [0, A) A chunk hi+lo, then the Y tile hi+lo,
-// then beta, then the mbarrier and the TMEM address.  A comes first so that
-// every descriptor-addressed read stays inside this CTA's allocation.
-__host__ __device__ inline int tc_a_bytes() { return 2 * kTcM * kTcKC * 2; }
-__host__ __device__ inline int tc_y_bytes(int n_pad) { return 2 * kTcN * n_pad * 2; }
-__host__ __device__ inline int tc_beta_bytes() { return kTcM * kBetaLd * 4; }
-__host__ __device__ inline int tc_smem_bytes(int n_pad) {
-  return tc_a_bytes() + tc_y_bytes(n_pad) + tc_beta_bytes() + 64;
-}
-
-__global__ void __launch_bounds__(kTcThreads, 1) glm_tc_kernel(TcArgs a) {
+template <int KMAX>
+__global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
+  constexpr int DPT = tc_dpt(KMAX);
+  constexpr int DB = tc_db(KMAX);
+  constexpr int N = tc_n(KMAX);
+  constexpr int YS = tc_y_stage();
+  constexpr int PS = tc_p_stage(KMAX);
+  constexpr int ST = tc_stage(KMAX);
+  constexpr int XC = tc_xchunk(KMAX);
   extern __shared__ __align__(1024) unsigned char sm[];
-  unsigned char* sA = sm;                                       // hi: [0, A/2), lo: [A/2, A)
-  unsigned char* sY = sm + tc_a_bytes();                        // hi then lo
-  float* sBeta = reinterpret_cast<float*>(sm + tc_a_bytes() + tc_y_bytes(a.n_pad));
-  uint64_t* sBar = reinterpret_cast<uint64_t*>(sm + tc_a_bytes() + tc_y_bytes(a.n_pad) + tc_beta_bytes());
-  uint32_t* sTmem = reinterpret_cast<uint32_t*>(sBar + 1);
-  const int tid = threadIdx.x, warp = tid / 32;
-  const int64_t v0 = (int64_t)blockIdx.x * kTcN;
-  const int kb_total = a.n_pad / 8;
-  const int a_half = kTcM * kTcKC * 2;
-  const int y_half = kTcN * a.n_pad * 2;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + tc_area(KMAX));  // full[4], empty[4], done
+  uint32_t* sTmem = reinterpret_cast<uint32_t*>(bars + 2 * kTcStages + 1);
+  int* sFail = reinterpret_cast<int*>(sTmem + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int64_t vb = blockIdx.x / a.n_db;
+  const int db = static_cast<int>(blockIdx.x % a.n_db);
+  const uint32_t sbase = smem_addr(sm);
+  const uint32_t full0 = smem_addr(bars), empty0 = full0 + 8 * kTcStages, done = full0 + 16 * kTcStages;
 
-  // TMEM: 64 fp32 columns (one N = 64 accumulator), allocated by warp 0
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(smem_addr(sTmem))
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(sTmem)),
+                 "n"(N)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    mbar_init(smem_addr(sBar), 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  // Y tile -> core-matrix layout: (kb, nb) at (kb*8 + nb)*128, row v%8 at +16*(v%8)
-  for (int i = tid; i < kTcN * kb_total; i += kTcThreads) {
-    const int v = i / kb_total, kb = i % kb_total;
-    const int off = (kb * 8 + v / 8) * 128 + (v % 8) * 16;
-    uint4 h = make_uint4(0, 0, 0, 0), l = make_uint4(0, 0, 0, 0);
-    if (v0 + v < a.V) {
-      h = *reinterpret_cast<const uint4*>(a.y_hi + (v0 + v) * a.n_pad + kb * 8);
-      l = *reinterpret_cast<const uint4*>(a.y_lo + (v0 + v) * a.n_pad + kb * 8);
+    for (int s = 0; s < kTcStages; ++s) {
+      mbar_init(full0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, 1);
     }
-    *reinterpret_cast<uint4*>(sY + off) = h;
-    *reinterpret_cast<uint4*>(sY + y_half + off) = l;
+    mbar_init(done, 1);
+    *sFail = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *sTmem;
-  const uint32_t bar = smem_addr(sBar);
-  const uint32_t idesc = make_idesc(kTcM, kTcN);
-  const uint32_t aBase = smem_addr(sA), yBase = smem_addr(sY);
-  uint32_t phase = 0;
-  const int n_mt = (a.G * kTcKPad + kTcM - 1) / kTcM;
+  const int KS = a.ks_count;
 
-  for (int mt = 0; mt < n_mt; ++mt) {
-    for (int kc = 0; kc < a.n_pad / kTcKC; ++kc) {
-      // A chunk: rows of this M tile, K [kc*32, kc*32+32): (kb, mb) at (kb*16 + mb)*128
-      for (int i = tid; i < kTcM * (kTcKC / 8); i += kTcThreads) {
-        const int r = i / (kTcKC / 8), kb = i % (kTcKC / 8);
-        const int64_t gr = (int64_t)mt * kTcM + r;
-        const int off = (kb * 16 + r / 8) * 128 + (r % 8) * 16;
-        uint4 h = make_uint4(0, 0, 0, 0), l = make_uint4(0, 0, 0, 0);
-        if (gr < (int64_t)a.G * kTcKPad) {
-          h = *reinterpret_cast<const uint4*>(a.p_hi + gr * a.n_pad + kc * kTcKC + kb * 8);
-          l = *reinterpret_cast<const uint4*>(a.p_lo + gr * a.n_pad + kc * kTcKC + kb * 8);
-        }
-        *reinterpret_cast<uint4*>(sA + off) = h;
-        *reinterpret_cast<uint4*>(sA + a_half + off) = l;
+  // ---- copy / MMA pipeline (one thread) ----
+  if (tid == 0) {
+    const unsigned char* ysrc = reinterpret_cast<const unsigned char*>(a.yt) + (vb * KS) * (int64_t)YS;
+    const unsigned char* psrc = reinterpret_cast<const unsigned char*>(a.pt) + ((int64_t)db * KS) * (int64_t)PS;
+    const uint32_t idesc = make_idesc(kTcM, N);
+    int issued = 0;  // K steps whose copies were issued
+    bool ok = true;
+    for (; issued < kTcStages && issued < KS; ++issued) {
+      const uint32_t dst = sbase + issued * ST, fb = full0 + 8 * issued;
+      mbar_expect_tx(fb, YS + PS);
+      bulk_g2s(dst, ysrc + (int64_t)issued * YS, YS, fb);
+      bulk_g2s(dst + YS, psrc + (int64_t)issued * PS, PS, fb);
+    }
+    int ks = 0;  // K steps whose copies were consumed
+    for (; ks < KS; ++ks) {
+      const int s = ks % kTcStages;
+      if (!mbar_wait(full0 + 8 * s, (ks / kTcStages) & 1)) {
+        ok = false;
+        break;
       }
-      fence_proxy_async();
-      __syncthreads();
-      if (tid == 0) {
-        tc_fence_after();
-#pragma unroll
-        for (int s = 0; s < kTcKC / 16; ++s) {
-          const int q = kc * (kTcKC / 16) + s;  // global 16-deep K step
-          const uint64_t ah = make_desc(aBase + s * 2 * 2048, 2048, 128);
-          const uint64_t al = make_desc(aBase + a_half + s * 2 * 2048, 2048, 128);
-          const uint64_t bh = make_desc(yBase + q * 2 * 1024, 1024, 128);
-          const uint64_t bl = make_desc(yBase + y_half + q * 2 * 1024, 1024, 128);
-          mma_bf16(tmem, ah, bh, idesc, (kc | s) ? 1u : 0u);
-          mma_bf16(tmem, ah, bl, idesc, 1u);
-          mma_bf16(tmem, al, bh, idesc, 1u);
-        }
-        mma_commit(bar);
-      }
-      // bounded wait for the MMAs of this chunk (they also free the A buffer)
-      long long it = 0;
-      while (!mbar_try_wait(bar, phase)) {
-        if (++it > kTcWaitLimit) {
-          if (tid == 0) atomicCAS(a.err, 0, kDevLoopLimit);
+      tc_fence_after();
+      const uint32_t st = sbase + s * ST;
+      const uint64_t ah = make_desc(st, kTcM * 16, 128);
+      const uint64_t al = make_desc(st + YS / 2, kTcM * 16, 128);
+      const uint64_t bh = make_desc(st + YS, N * 16, 128);
+      const uint64_t bl = make_desc(st + YS + PS / 2, N * 16, 128);
+      mma_bf16(tmem, ah, bh, idesc, ks > 0 ? 1u : 0u);
+      mma_bf16(tmem, ah, bl, idesc, 1u);
+      mma_bf16(tmem, al, bh, idesc, 1u);
+      mma_commit(empty0 + 8 * s);
+      // refill the stage of step ks-1 (its MMAs are queued ahead of this step's)
+      if (ks >= 1 && issued < KS) {
+        const int kp = ks - 1, sp = kp % kTcStages;
+        if (!mbar_wait(empty0 + 8 * sp, (kp / kTcStages) & 1)) {
+          ok = false;
+          ++ks;
           break;
         }
-      }
-      phase ^= 1u;
-      tc_fence_after();
-      __syncthreads();
-    }
-    // accumulator -> shared (warps 0-3 own TMEM lanes 32w..32w+31 = rows)
-    if (warp < 4) {
-      float buf[16];
-#pragma unroll
-      for (int c = 0; c < kTcN / 16; ++c) {
-        tmem_ld16(tmem + (static_cast<uint32_t>(warp * 32) << 16) + c * 16, buf);
-        const int row = warp * 32 + (tid % 32);
-#pragma unroll
-        for (int j = 0; j < 16; ++j) sBeta[row * kBetaLd + c * 16 + j] = buf[j];
+        const uint32_t dst = sbase + sp * ST, fb = full0 + 8 * sp;
+        mbar_expect_tx(fb, YS + PS);
+        bulk_g2s(dst, ysrc + (int64_t)issued * YS, YS, fb);
+        bulk_g2s(dst + YS, psrc + (int64_t)issued * PS, PS, fb);
+        ++issued;
       }
     }
-    tc_fence_before();
-    __syncthreads();
-    // epilogue: 16 designs x 64 vertices, 4 vertices per thread
-    {
-      const int d = tid / 16;
-      const int vb = (tid % 16) * 4;
-      const int64_t g = (int64_t)mt * (kTcM / kTcKPad) + d;
-      if (g < a.G) {
-        const int kmax = a.kmax;
-        float beta[kTcKPad][4];
-#pragma unroll
-        for (int j = 0; j < kTcKPad; ++j)
-#pragma unroll
-          for (int c = 0; c < 4; ++c) beta[j][c] = (j < kmax) ? sBeta[(d * kTcKPad + j) * kBetaLd + vb + c] : 0.0f;
-        float rss[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        const float* xg = a.X + g * a.n * kmax;
-        const __nv_bfloat16* yh = reinterpret_cast<const __nv_bfloat16*>(sY);
-        const __nv_bfloat16* yl = reinterpret_cast<const __nv_bfloat16*>(sY + y_half);
-        for (int s = 0; s < a.n; ++s) {
-          float xv[kTcKPad];
-#pragma unroll
-          for (int j = 0; j < kTcKPad; ++j) xv[j] = (j < kmax) ? __ldg(xg + (int64_t)s * kmax + j) : 0.0f;
-          const int kb = s / 8, kk = s % 8;
-#pragma unroll
-          for (int c = 0; c < 4; ++c) {
-            const int v = vb + c;
-            const int e = ((kb * 8 + v / 8) * 128 + (v % 8) * 16) / 2 + kk;
-            float r = __bfloat162float(yh[e]) + __bfloat162float(yl[e]);
-#pragma unroll
-            for (int j = 0; j < kTcKPad; ++j) r = fmaf(-xv[j], beta[j][c], r);
-            rss[c] = fmaf(r, r, rss[c]);
-          }
-        }
-        const float inv_dof = 1.0f / a.dof[g];
-        for (int ci = 0; ci < a.n_coef; ++ci) {
-          const int j = a.coef[ci];
-          const float dj = a.invdiag[g * kmax + j];
-          float* dst = a.t_out + (g * a.n_coef + ci) * a.ldt + v0 + vb;
-#pragma unroll
-          for (int c = 0; c < 4; ++c) {
-            if (v0 + vb + c < a.V) {
-              float bj = 0.0f;
-#pragma unroll
-              for (int jj = 0; jj < kTcKPad; ++jj)
-                if (jj == j) bj = beta[jj][c];
-              dst[c] = bj / sqrtf(rss[c] * inv_dof * dj);
-            }
-          }
-        }
-      }
+    mma_commit(done);
+    if (!ok) {
+      atomicCAS(a.err, 0, kDevLoopLimit);
+      *sFail = 1;
+      // copies issued but not consumed: wait (bounded) until they have landed
+      for (int qq = ks; qq < issued; ++qq) mbar_wait(full0 + 8 * (qq % kTcStages), (qq / kTcStages) & 1);
     }
-    __syncthreads();
-    tc_fence_after();
+  }
+  __syncwarp();
+  if (!mbar_wait(done, 0)) {
+    if (lane == 0) atomicCAS(a.err, 0, kDevLoopLimit);
+    *sFail = 1;
+  }
+  tc_fence_after();
+  fence_proxy_async();
+  __syncthreads();
+  const bool failed = *sFail != 0;
+
+  // ---- drain: TMEM lane = vertex -> sB[(d*KMAX + j)*kTcBld + vertex] ----
+  float* sB = reinterpret_cast<float*>(sm);
+  if (!failed) {
+    const int q = warp & 3, half = warp >> 2;
+    const int vl = q * 32 + lane;
+#pragma unroll
+    for (int dd = 0; dd < DPT; ++dd) {
+      float t8[8];
+      tmem_ld8(tmem + (static_cast<uint32_t>(q * 32) << 16) + (half * DPT + dd) * kTcRowsPerDesign, t8);
+#pragma unroll
+      for (int j = 0; j < KMAX; ++j) sB[((half * DPT + dd) * KMAX + j) * kTcBld + vl] = t8[j];
+    }
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 0) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem) : "memory");
+
+  // ---- residual pass: lane = design d, thread = VT consecutive vertices ----
+  constexpr int VT = DB / 2;
+  constexpr int YC = tc_ychunk();
+  static_assert((kTcThreads / DB) * VT == kTcM, "threads cover the tile");
+  const int d = tid % DB, vg = tid / DB;
+  const int g = db * DB + d;
+  const int vl0 = vg * VT;
+  const int64_t v0 = vb * kTcM + vl0;
+  float2 bp[VT / 2][KMAX];
+  float2 rss[VT / 2];
+  {
+    float u[KMAX];
+#pragma unroll
+    for (int j = 0; j < KMAX; ++j) u[j] = (a.shift != nullptr) ? __ldg(a.u + g * KMAX + j) : 0.0f;
+#pragma unroll
+    for (int vv = 0; vv < VT; ++vv) {
+      const float m = (a.shift != nullptr && v0 + vv < a.V) ? __ldg(a.shift + v0 + vv) : 0.0f;
+#pragma unroll
+      for (int j = 0; j < KMAX; ++j) {
+        const float bv = failed ? 0.0f : fmaf(m, u[j], sB[(d * KMAX + j) * kTcBld + vl0 + vv]);
+        if (vv & 1) bp[vv / 2][j].y = bv; else bp[vv / 2][j].x = bv;
+      }
+    }
+#pragma unroll
+    for (int p = 0; p < VT / 2; ++p) rss[p] = make_float2(0.0f, 0.0f);
   }
+  __syncthreads();  // the beta area becomes the chunk buffers
+
+  const int n_chunks = a.n_sc / kTcSubjChunk;
+  const float* xsrc = a.xt + (int64_t)db * a.n_sc * KMAX * DB;
+  const int64_t vt0 = vb * kTcM;
+  auto load_chunk = [&](int c) {
+    const uint32_t dst = sbase + (c & 1) * (XC + YC);
+    const float* src = xsrc + (int64_t)c * kTcSubjChunk * KMAX * DB;
+    for (int i = tid; i < XC / 16; i += kTcThreads) cp_async16(dst + i * 16, src + i * 4);
+    for (int e = tid; e < kTcSubjChunk * kTcM; e += kTcThreads) {
+      const int i = c * kTcSubjChunk + e / kTcM;
+      const int64_t v = vt0 + e % kTcM;
+      const bool ok = i < a.n && v < a.V;
+      cp_async4(dst + XC + e * 4, ok ? a.Y + (int64_t)i * a.ldy + v : a.Y, ok ? 4u : 0u);
+    }
+    cp_async_commit();
+  };
+  if (!failed) {
+    load_chunk(0);
+    for (int c = 0; c < n_chunks; ++c) {
+      // chunk c+1 streams into the other buffer while chunk c is used
+      if (c + 1 < n_chunks) {
+        load_chunk(c + 1);
+        cp_async_wait<1>();
+      } else {
+        cp_async_wait<0>();
+      }
+      __syncthreads();
+      const float* xs = reinterpret_cast<const float*>(sm + (c & 1) * (XC + YC));
+      const float* ys = xs + XC / 4;
+#pragma unroll 2
+      for (int ii = 0; ii < kTcSubjChunk; ++ii) {
+        float2 xj[KMAX];
+#pragma unroll
+        for (int j = 0; j < KMAX; ++j) {
+          const float x = xs[(ii * KMAX + j) * DB + d];
+          xj[j] = make_float2(x, x);
+        }
+        const float4* yr = reinterpret_cast<const float4*>(ys + ii * kTcM + vl0);
+#pragma unroll
+        for (int q4 = 0; q4 < VT / 4; ++q4) {
+          const float4 yv = yr[q4];
+          float2 r0 = make_float2(yv.x, yv.y), r1 = make_float2(yv.z, yv.w);
+#pragma unroll
+          for (int j = 0; j < KMAX; ++j) {
+            r0 = __ffma2_rn(xj[j], bp[2 * q4][j], r0);
+            r1 = __ffma2_rn(xj[j], bp[2 * q4 + 1][j], r1);
+          }
+          rss[2 * q4] = __ffma2_rn(r0, r0, rss[2 * q4]);
+          rss[2 * q4 + 1] = __ffma2_rn(r1, r1, rss[2 * q4 + 1]);
+        }
+      }
+      __syncthreads();
+    }
+    if (g < a.G) {
+      const float inv_dof = 1.0f / __ldg(a.dof + g);
+      for (int ci = 0; ci < a.n_coef; ++ci) {
+        const int j = __ldg(a.coef + ci);
+        const float dj = __ldg(a.invdiag + g * KMAX + j);
+        float* dst = a.t_out + ((int64_t)g * a.n_coef + ci) * a.ldt + v0;
+#pragma unroll
+        for (int vv = 0; vv < VT; ++vv) {
+          if (v0 + vv < a.V) {
+            float bj = 0.0f;
+#pragma unroll
+            for (int jj = 0; jj < KMAX; ++jj)
+              if (jj == j) bj = (vv & 1) ? bp[vv / 2][jj].y : bp[vv / 2][jj].x;
+            const float rs = (vv & 1) ? rss[vv / 2].y : rss[vv / 2].x;
+            dst[vv] = bj / sqrtf(rs * inv_dof * dj);
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(N) : "memory");
+  }
+}
+
+template <int KMAX>
+static int launch_tc(const TcArgs& a, int64_t n_vb, cudaStream_t stream) {
+  const int smem = tc_smem(KMAX);
+  TFGB_CUDA(cudaFuncSetAttribute(glm_tc_kernel<KMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  const int64_t grid = n_vb * a.n_db;
+  glm_tc_kernel<KMAX><<<static_cast<unsigned>(grid), kTcThreads, smem, stream>>>(a);
+  TFGB_CUDA(cudaGetLastError());
+  return TFCE_OK;
 }
 
 }  // namespace tfgb
 
 extern "C" {
 
-int glm_split_bf16(const float* src, int64_t ld_src, int32_t transpose, int64_t rows, int32_t cols,
-                   int32_t ld_dst, void* hi, void* lo, void* stream) {
+int glm_tc_design_block(int32_t kmax) {
+  if (kmax < 1 || kmax > tfgb::kTcRowsPerDesign) return -1;
+  return tfgb::tc_db(kmax);
+}
+
+int64_t glm_tile_bytes(int64_t rows, int32_t row_block, int32_t n_pad) {
+  if (rows < 0 || row_block <= 0 || n_pad <= 0 || n_pad % tfgb::kTcK) return -1;
+  const int64_t blocks = (rows + row_block - 1) / row_block;
+  return blocks * row_block * (int64_t)n_pad * 4;  // hi + lo, 2 bytes each
+}
+
+int glm_col_mean(const float* Y, int64_t ldy, int32_t n, int64_t V, float* mean, void* stream) {
   tfgb::clear_error();
-  TFGB_CHECK_ARG(src && hi && lo, "NULL pointer");
-  TFGB_CHECK_ARG(rows >= 0 && cols >= 0 && ld_dst >= cols && ld_dst % 8 == 0, "bad sizes");
-  if (rows == 0) return TFCE_OK;
-  const int64_t total = rows * ld_dst;
-  const unsigned blocks = static_cast<unsigned>(std::min<int64_t>((total + 255) / 256, 152 * 32));
-  tfgb::split_bf16_kernel<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
-      src, ld_src, transpose, rows, cols, ld_dst, static_cast<__nv_bfloat16*>(hi),
-      static_cast<__nv_bfloat16*>(lo));
+  TFGB_CHECK_ARG(Y && mean, "NULL pointer");
+  TFGB_CHECK_ARG(n > 0 && V >= 0 && ldy >= V, "bad sizes");
+  if (V == 0) return TFCE_OK;
+  const unsigned blocks = static_cast<unsigned>(std::min<int64_t>((V + 255) / 256, 152 * 16));
+  tfgb::col_mean_kernel<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(Y, ldy, n, V, mean);
   TFGB_CUDA(cudaGetLastError());
   return TFCE_OK;
 }
 
-int glm_tstat_tc(const void* y_hi, const void* y_lo, int32_t n, int32_t n_pad, int64_t V, const void* p_hi,
-                 const void* p_lo, const float* X, const float* invdiag, const float* dof, int32_t G,
-                 int32_t kmax, const int32_t* coef, int32_t n_coef, float* t_out, int64_t ldt, int32_t* err,
-                 void* stream) {
+int glm_tile_split(const float* src, int64_t ld_src, int32_t transpose, int64_t rows, int32_t cols,
+                   const float* row_shift, int32_t row_block, int32_t n_pad, void* dst, void* stream) {
   tfgb::clear_error();
-  TFGB_CHECK_ARG(y_hi && y_lo && p_hi && p_lo && X && invdiag && dof && coef && t_out && err, "NULL pointer");
-  TFGB_CHECK_ARG(n > 0 && n_pad >= n && n_pad % tfgb::kTcKC == 0, "n_pad must be >= n and a multiple of 32");
-  TFGB_CHECK_ARG(n_pad <= tfgb::kTcMaxN, "more than 640 subjects: use glm_tstat");
-  TFGB_CHECK_ARG(kmax >= 1 && kmax <= tfgb::kTcKPad, "kmax must be in [1, 8]");
-  TFGB_CHECK_ARG(n_coef >= 1 && V >= 0 && G >= 0 && ldt >= V, "bad sizes");
+  TFGB_CHECK_ARG(src && dst, "NULL pointer");
+  TFGB_CHECK_ARG(rows >= 0 && cols >= 0 && n_pad >= cols && n_pad % tfgb::kTcK == 0,
+                 "n_pad must be >= cols and a multiple of 16");
+  TFGB_CHECK_ARG(row_block > 0 && row_block % 8 == 0 && row_block <= 256,
+                 "row_block must be a multiple of 8 in [8, 256]");
+  if (rows == 0) return TFCE_OK;
+  const int64_t n_blk = (rows + row_block - 1) / row_block;
+  const int ks = n_pad / tfgb::kTcK;
+  const int64_t total = n_blk * ks * 2 * row_block;
+  const unsigned blocks = static_cast<unsigned>(std::min<int64_t>((total + 255) / 256, 152 * 16));
+  tfgb::tile_split_kernel<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      src, ld_src, transpose, rows, cols, row_shift, row_block, ks, n_blk, static_cast<__nv_bfloat16*>(dst));
+  TFGB_CUDA(cudaGetLastError());
+  return TFCE_OK;
+}
+
+int glm_tstat_tc(const void* y_tiles, const float* y_shift, const float* Y, int64_t ldy, int32_t n,
+                 int32_t n_pad, int64_t V, const void* p_tiles, const float* u_rows, const float* x_rows,
+                 int32_t n_sc, const float* invdiag, const float* dof, int32_t G, int32_t kmax,
+                 const int32_t* coef, int32_t n_coef, float* t_out, int64_t ldt, int32_t* err, void* stream) {
+  tfgb::clear_error();
+  TFGB_CHECK_ARG(y_tiles && Y && p_tiles && x_rows && invdiag && dof && coef && t_out && err, "NULL pointer");
+  TFGB_CHECK_ARG(!y_shift || u_rows, "a centred data operand needs u_rows");
+  TFGB_CHECK_ARG(n > 0 && n_pad >= n && n_pad % tfgb::kTcK == 0, "n_pad must be >= n and a multiple of 16");
+  TFGB_CHECK_ARG(n_sc >= n && n_sc % tfgb::kTcSubjChunk == 0, "n_sc must be >= n and a multiple of 32");
+  TFGB_CHECK_ARG(kmax >= 1 && kmax <= tfgb::kTcRowsPerDesign, "kmax must be in [1, 8]");
+  TFGB_CHECK_ARG(n_coef >= 1 && V >= 0 && G >= 0 && ldt >= V && ldy >= V, "bad sizes");
+  TFGB_CHECK_ARG(reinterpret_cast<uintptr_t>(y_tiles) % 16 == 0 && reinterpret_cast<uintptr_t>(p_tiles) % 16 == 0 &&
+                     reinterpret_cast<uintptr_t>(x_rows) % 16 == 0,
+                 "tiles and design rows must be 16-byte aligned");
   if (V == 0 || G == 0) return TFCE_OK;
-  const int smem = tfgb::tc_smem_bytes(n_pad);
-  TFGB_CUDA(cudaFuncSetAttribute(tfgb::glm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   tfgb::TcArgs a{};
-  a.y_hi = static_cast<const __nv_bfloat16*>(y_hi);
-  a.y_lo = static_cast<const __nv_bfloat16*>(y_lo);
-  a.p_hi = static_cast<const __nv_bfloat16*>(p_hi);
-  a.p_lo = static_cast<const __nv_bfloat16*>(p_lo);
-  a.X = X;
+  a.yt = static_cast<const __nv_bfloat16*>(y_tiles);
+  a.pt = static_cast<const __nv_bfloat16*>(p_tiles);
+  a.xt = x_rows;
+  a.Y = Y;
+  a.shift = y_shift;
+  a.u = u_rows;
   a.invdiag = invdiag;
   a.dof = dof;
   a.coef = coef;
   a.t_out = t_out;
+  a.ldy = ldy;
   a.ldt = ldt;
   a.V = V;
   a.n = n;
-  a.n_pad = n_pad;
+  a.n_sc = n_sc;
+  a.ks_count = n_pad / tfgb::kTcK;
   a.G = G;
-  a.kmax = kmax;
+  a.n_db = (G + tfgb::tc_db(kmax) - 1) / tfgb::tc_db(kmax);
   a.n_coef = n_coef;
   a.err = err;
-  const unsigned grid = static_cast<unsigned>((V + tfgb::kTcN - 1) / tfgb::kTcN);
-  tfgb::glm_tc_kernel<<<grid, tfgb::kTcThreads, smem, static_cast<cudaStream_t>(stream)>>>(a);
-  TFGB_CUDA(cudaGetLastError());
-  return TFCE_OK;
+  const int64_t n_vb = (V + tfgb::kTcM - 1) / tfgb::kTcM;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  switch (kmax) {
+    case 1: return tfgb::launch_tc<1>(a, n_vb, st);
+    case 2: return tfgb::launch_tc<2>(a, n_vb, st);
+    case 3: return tfgb::launch_tc<3>(a, n_vb, st);
+    case 4: return tfgb::launch_tc<4>(a, n_vb, st);
+    case 5: return tfgb::launch_tc<5>(a, n_vb, st);
+    case 6: return tfgb::launch_tc<6>(a, n_vb, st);
+    case 7: return tfgb::launch_tc<7>(a, n_vb, st);
+    default: return tfgb::launch_tc<8>(a, n_vb, st);
+  }
 }
 
 }  // extern "C"

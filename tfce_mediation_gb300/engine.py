@@ -7,7 +7,9 @@ tfce_mediation/tm_func.py:144-185 and 269-305).
 Per launch, P permutations:
   1. host: permutation indices RandomState(seed + p).permutation(n) and, in
      float64, each permuted design's inv(X'X) X' and diag(inv(X'X));
-  2. device: one glm_tstat launch -> t maps [P][C][V] (float32, resident);
+  2. device: one GLM launch -> t maps [P][C][V] (float32, resident): the
+     tcgen05 split-BF16 GEMM with the fused residual epilogue (precision
+     'bf16x3', default) or the FP32 CUDA-core kernel ('fp32');
   3. device: one tfce_sweep_batch launch over P x C maps x (+,-) x segments
      -> the scaled per-segment maximum of every sweep;
   4. host: max over segments (hemispheres) gives the reference's per-permutation
@@ -22,7 +24,7 @@ import numpy as np
 from . import _lib
 from .adjacency import AdjacencySet, is_symmetric, locality_order, relabel_csr, to_csr
 from .device import dev, ptr, require_cuda, stream_handle
-from .glm import DesignBatch
+from .glm import DesignBatch, TensorCoreOperands
 
 
 def permutations(n, seed, start, stop):
@@ -46,6 +48,10 @@ class PermutationEngine:
     accumulation: 'component' (default; per-component double sums, within
     ~1e-7 of the reference's float sums) or 'exact' (the reference's float
     arithmetic, bit-identical; slower).
+    precision: GLM arithmetic of the permutation t maps: 'bf16x3' (default;
+    tensor cores, split BF16 with FP32 accumulation, t within ~3e-5 relative
+    of FP64) or 'fp32' (CUDA cores, ~1e-6).  The observed (unpermuted) t map
+    always uses 'fp32'.
     reorder: renumber vertices inside every segment for memory locality
     (reverse Cuthill-McKee); Y's columns are permuted once here and every map
     handed back is in the caller's order.  Only symmetric adjacency is
@@ -54,8 +60,11 @@ class PermutationEngine:
 
     def __init__(self, Y, pred_x, adjacency, segments=None, H=2.0, E=1.0, vdensity=None,
                  contrasts=None, floor_zero=False, batch=64, signs=2, reorder=False,
-                 accumulation="component"):
+                 accumulation="component", precision="bf16x3"):
         t = require_cuda()
+        if precision not in ("bf16x3", "fp32"):
+            raise ValueError("precision must be 'bf16x3' (tensor cores) or 'fp32' (CUDA cores)")
+        self.precision = precision
         self.t = t
         Yh = Y if isinstance(Y, t.Tensor) else np.asarray(Y, np.float32)
         V = Yh.shape[1]
@@ -91,6 +100,7 @@ class PermutationEngine:
         self.vd = None if vdensity is None else dev(np.asarray(vdensity, np.float32))
         self.lib = _lib.load()
         self._coef = dev(np.asarray(self.contrasts, np.int32))
+        self._tc = TensorCoreOperands(self.Yd) if precision == "bf16x3" else None
         if batch == "auto":
             from .autotune import choose_batch
             batch = choose_batch(self)
@@ -109,10 +119,18 @@ class PermutationEngine:
     def _designs(self, perms):
         return DesignBatch(self.X[perms])
 
-    def tmaps(self, designs: DesignBatch, out=None):
+    def tmaps(self, designs: DesignBatch, out=None, precision=None):
         """t maps [G][C][V] for a DesignBatch (device tensor)."""
         G = designs.G
         out = self._tbuf[:G] if out is None else out
+        if (precision or self.precision) == "bf16x3":
+            tc = self._tc if self._tc is not None else TensorCoreOperands(self.Yd)
+            self._tc = tc
+            P8, U, Xt = tc.host_operands(designs)
+            pt = tc.tile_designs(dev(P8), G, designs.kmax)
+            tc.tstat(pt, dev(U), dev(Xt), dev(designs.invdiag64.astype(np.float32)),
+                     dev(designs.dof.astype(np.float32)), G, designs.kmax, self._coef, self.C, out, self.V)
+            return out
         pinv, Xp, invd, dof = designs.to_device()
         _lib.check(self.lib.glm_tstat(ptr(self.Yd), self.V, self.n, self.V, ptr(pinv), ptr(Xp),
                                       ptr(invd), ptr(dof), G, designs.kmax, ptr(self._coef),
@@ -141,6 +159,14 @@ class PermutationEngine:
             t.index_select(staged, 1, self._order_d, out=self.Yd)
         else:
             self.Yd.copy_(Y_host, non_blocking=True)
+        if self._tc is not None:
+            self._tc.retile()
+
+    def status(self):
+        """Raise if a device wait of the last launches ran out (sweep or GLM)."""
+        self.adj.status()
+        if self._tc is not None:
+            self._tc.status()
 
     def run_batch(self, perms):
         """Maxima (P, C, signs, n_seg) for the permutation index rows `perms`."""
@@ -152,7 +178,7 @@ class PermutationEngine:
         hm = self._host_max.view(-1)[: mx.numel()]
         hm.copy_(mx, non_blocking=True)
         self.t.cuda.current_stream().synchronize()
-        self.adj.status()
+        self.status()
         return hm.numpy().reshape(P, self.C, self.signs, self.n_seg).copy()
 
     def run(self, n_perm=None, seed=0, start=0, stop=None, perms=None):
@@ -172,23 +198,40 @@ class PermutationEngine:
         the sweep (counter reset included), maxima -> pinned host memory."""
         t = self.t
         n, kmax = self.n, self.k
+        tc = self._tc
         slot = {"P": P}
-        slot["h_pinv"] = t.empty((P, kmax, n), dtype=t.float32, pin_memory=True)
-        slot["h_X"] = t.empty((P, n, kmax), dtype=t.float32, pin_memory=True)
+        if tc is not None:
+            Gp, DB = tc.padded(P, kmax), tc.block(kmax)
+            keys = ("P8", "U", "Xt", "invd", "dof")
+            slot["h_P8"] = t.empty((Gp * 8, tc.n_pad), dtype=t.float32, pin_memory=True)
+            slot["h_U"] = t.empty((Gp, kmax), dtype=t.float32, pin_memory=True)
+            slot["h_Xt"] = t.empty((Gp // DB, tc.n_sc, kmax, DB), dtype=t.float32, pin_memory=True)
+            slot["d_pt"] = t.empty(int(self.lib.glm_tile_bytes(Gp * 8, DB * 8, tc.n_pad)), dtype=t.uint8,
+                                   device="cuda")
+        else:
+            keys = ("pinv", "X", "invd", "dof")
+            slot["h_pinv"] = t.empty((P, kmax, n), dtype=t.float32, pin_memory=True)
+            slot["h_X"] = t.empty((P, n, kmax), dtype=t.float32, pin_memory=True)
         slot["h_invd"] = t.empty((P, kmax), dtype=t.float32, pin_memory=True)
         slot["h_dof"] = t.empty((P,), dtype=t.float32, pin_memory=True)
         slot["h_max"] = t.empty((P, self.C, self.signs, self.n_seg), dtype=t.float32, pin_memory=True)
-        for key in ("pinv", "X", "invd", "dof"):
+        for key in keys:
             slot["d_" + key] = t.empty(slot["h_" + key].shape, device="cuda", dtype=t.float32)
         slot["d_t"] = t.empty((P, self.C, self.V), device="cuda", dtype=t.float32)
         slot["d_max"] = t.empty((P, self.C, self.signs, self.n_seg), device="cuda", dtype=t.float32)
 
         def body():
-            for key in ("pinv", "X", "invd", "dof"):
+            for key in keys:
                 slot["d_" + key].copy_(slot["h_" + key], non_blocking=True)
-            _lib.check(self.lib.glm_tstat(ptr(self.Yd), self.V, n, self.V, ptr(slot["d_pinv"]),
-                                          ptr(slot["d_X"]), ptr(slot["d_invd"]), ptr(slot["d_dof"]), P, kmax,
-                                          ptr(self._coef), self.C, ptr(slot["d_t"]), self.V, stream_handle()))
+            if tc is not None:
+                tc.tile_designs(slot["d_P8"], P, kmax, out=slot["d_pt"])
+                tc.tstat(slot["d_pt"], slot["d_U"], slot["d_Xt"], slot["d_invd"], slot["d_dof"], P, kmax,
+                         self._coef, self.C, slot["d_t"], self.V)
+            else:
+                _lib.check(self.lib.glm_tstat(ptr(self.Yd), self.V, n, self.V, ptr(slot["d_pinv"]),
+                                              ptr(slot["d_X"]), ptr(slot["d_invd"]), ptr(slot["d_dof"]), P,
+                                              kmax, ptr(self._coef), self.C, ptr(slot["d_t"]), self.V,
+                                              stream_handle()))
             self.adj.sweep_batch(ptr(slot["d_t"]), self.V, P * self.C, self.signs, ptr(self.vd),
                                  int(self.floor_zero), ptr(slot["d_max"]), None, 0, stream_handle())
             slot["h_max"].copy_(slot["d_max"], non_blocking=True)
@@ -200,7 +243,7 @@ class PermutationEngine:
             body()
         t.cuda.current_stream().wait_stream(side)
         t.cuda.synchronize()
-        self.adj.status()
+        self.status()
         g = t.cuda.CUDAGraph()
         with t.cuda.graph(g):
             body()
@@ -211,8 +254,11 @@ class PermutationEngine:
     def _fill(self, slot, perms):
         db = DesignBatch(self.X[perms])
         P = perms.shape[0]
-        slot["h_pinv"].numpy()[:P] = db.pinv64
-        slot["h_X"].numpy()[:P] = db.X64
+        if self._tc is not None:
+            self._tc.host_operands(db, P8=slot["h_P8"].numpy(), U=slot["h_U"].numpy(), Xt=slot["h_Xt"].numpy())
+        else:
+            slot["h_pinv"].numpy()[:P] = db.pinv64
+            slot["h_X"].numpy()[:P] = db.X64
         slot["h_invd"].numpy()[:P] = db.invdiag64
         slot["h_dof"].numpy()[:P] = db.dof
 
@@ -245,7 +291,7 @@ class PermutationEngine:
                 slot["event"].synchronize()
                 out.append((slot["order"], slot["h_max"].numpy().copy()))
                 slot["busy"] = False
-        self.adj.status()
+        self.status()
         res = [m for _, m in sorted(out, key=lambda x: x[0])]
         if perms.shape[0] > full * P:
             res.append(self.run_batch(perms[full * P:]))
@@ -257,7 +303,7 @@ class PermutationEngine:
         t = self.t
         db = DesignBatch(self.X[None])
         tm = t.empty((1, self.C, self.V), device="cuda", dtype=t.float32)
-        self.tmaps(db, out=tm)
+        self.tmaps(db, out=tm, precision="fp32")
         maps = t.empty((self.C, self.signs, self.V), device="cuda", dtype=t.float32)
         mx = t.empty((self.C, self.signs, self.n_seg), device="cuda", dtype=t.float32)
         # the observed image is swept once: use the reference's exact arithmetic
@@ -307,7 +353,7 @@ class MediationEngine:
     linregress), as in the reference."""
 
     def __init__(self, Y, pred_x, depend_y, medtype, adjacency, segments=None, H=2.0, E=1.0, vdensity=None,
-                 floor_zero=False, batch=64, alg="aroian", accumulation="component"):
+                 floor_zero=False, batch=64, alg="aroian", accumulation="component", precision="bf16x3"):
         from .pyfunc import ALG
         if medtype not in ("I", "M", "Y"):
             raise ValueError("Invalid mediation type")
@@ -315,7 +361,7 @@ class MediationEngine:
             raise ValueError("Unknown indirect test algorithm")
         self.inner = PermutationEngine(Y, np.zeros((np.asarray(Y).shape[0], 1)), adjacency, segments, H, E,
                                        vdensity, contrasts=[1], floor_zero=floor_zero, batch=2 * batch, signs=1,
-                                       reorder=False, accumulation=accumulation)
+                                       reorder=False, accumulation=accumulation, precision=precision)
         self.t = self.inner.t
         self.medtype, self.alg_code, self.batch = medtype, ALG[alg], int(batch)
         self.pred_x = np.asarray(pred_x, np.float64)
@@ -365,7 +411,7 @@ class MediationEngine:
         self.inner.adj.sweep_batch(ptr(z), self.V, P, 1, ptr(self.inner.vd), int(self.inner.floor_zero),
                                    ptr(mx), None, 0, stream_handle())
         out = mx.cpu().numpy().reshape(P, 1, 1, self.n_seg)
-        self.inner.adj.status()
+        self.inner.status()
         return out
 
     def run(self, n_perm=None, seed=0, start=0, stop=None, perms=None):

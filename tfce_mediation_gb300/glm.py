@@ -106,64 +106,105 @@ def glm_fstat(Y, designs, centre=None, stream=None):
 
 
 class TensorCoreOperands:
-    """Split-BF16 operands of the tcgen05 GLM (glm_tstat_tc): the data once,
-    as per-vertex rows [V][n_pad] (hi and lo), and each batch's stacked
-    pseudoinverses as [G*8][n_pad] (hi and lo)."""
+    """Operands of the tensor-core GLM (glm_tstat_tc).
 
-    def __init__(self, Yd):
+    The data is centred per vertex (FP64 mean), split into BF16 hi/lo and
+    pre-tiled once (128-vertex row blocks of Y', 16-subject K steps).  Per
+    design batch: the stacked pseudoinverse rows [G_pad*8][n_pad] (tiled on
+    the device), u = pinv(X_d).1 [G_pad][kmax] (restores the betas of the
+    uncentred data) and the negated design rows [G_pad/DB][n_sc][kmax][DB]
+    for the residual epilogue."""
+
+    ROW_BLOCK = 128
+
+    def __init__(self, Yd, centre=True):
         t = require_cuda()
         self.t = t
-        self.n, self.V = Yd.shape
-        self.n_pad = (self.n + 31) // 32 * 32
-        if self.n_pad > 640:
-            raise ValueError("the tensor-core GLM holds at most 640 subjects per tile")
-        self.y_hi = t.empty((self.V, self.n_pad), dtype=t.bfloat16, device="cuda")
-        self.y_lo = t.empty_like(self.y_hi)
         self.lib = _lib.load()
-        _lib.check(self.lib.glm_split_bf16(ptr(Yd), self.V, 1, self.V, self.n, self.n_pad, ptr(self.y_hi),
-                                           ptr(self.y_lo), stream_handle()))
+        self.Yd = Yd
+        self.n, self.V = Yd.shape
+        self.n_pad = (self.n + 15) // 16 * 16
+        self.n_sc = (self.n + 31) // 32 * 32
+        nbytes = int(self.lib.glm_tile_bytes(self.V, self.ROW_BLOCK, self.n_pad))
+        self.yt = t.empty(nbytes, dtype=t.uint8, device="cuda")
+        self.shift = t.empty(self.V, dtype=t.float32, device="cuda") if centre else None
         self.err = t.zeros(1, dtype=t.int32, device="cuda")
+        self.retile()
 
-    def stacked(self, db: DesignBatch):
-        """Host float32 [G][8][n_pad] of the pseudoinverse rows (zero padded)."""
-        P8 = np.zeros((db.G, 8, self.n_pad), np.float32)
-        P8[:, :db.kmax, :db.n] = db.pinv64
-        return P8
+    def retile(self):
+        """Centre, split and tile the resident data again (after new data was copied in)."""
+        if self.shift is not None:
+            _lib.check(self.lib.glm_col_mean(ptr(self.Yd), self.V, self.n, self.V, ptr(self.shift),
+                                             stream_handle()))
+        _lib.check(self.lib.glm_tile_split(ptr(self.Yd), self.V, 1, self.V, self.n, ptr(self.shift),
+                                           self.ROW_BLOCK, self.n_pad, ptr(self.yt), stream_handle()))
 
-    def split(self, P8_dev, G, p_hi=None, p_lo=None):
+    def block(self, kmax):
+        return int(self.lib.glm_tc_design_block(kmax))
+
+    def padded(self, G, kmax):
+        DB = self.block(kmax)
+        return (G + DB - 1) // DB * DB
+
+    def host_operands(self, db: DesignBatch, P8=None, U=None, Xt=None):
+        """Host float32 operands of a DesignBatch: stacked pseudoinverse rows
+        (G_pad*8, n_pad), u = pinv.1 (G_pad, kmax) and negated design rows
+        (G_pad/DB, n_sc, kmax, DB); written into P8 / U / Xt when given (e.g.
+        pinned buffers of exactly those sizes)."""
+        G, kmax, n = db.G, db.kmax, db.n
+        DB = self.block(kmax)
+        Gp = self.padded(G, kmax)
+        p = np.zeros((Gp, 8, self.n_pad), np.float32) if P8 is None else P8.reshape(Gp, 8, self.n_pad)
+        if P8 is not None:
+            p[...] = 0.0
+        p[:G, :kmax, :n] = db.pinv64
+        u = np.zeros((Gp, kmax), np.float32) if U is None else U.reshape(Gp, kmax)
+        u[...] = 0.0
+        u[:G] = db.pinv64.sum(axis=2)
+        x = np.zeros((Gp // DB, self.n_sc, kmax, DB), np.float32) if Xt is None else \
+            Xt.reshape(Gp // DB, self.n_sc, kmax, DB)
+        xg = np.zeros((Gp, self.n_sc, kmax), np.float32)
+        xg[:G, :n] = -db.X64
+        x[...] = xg.reshape(Gp // DB, DB, self.n_sc, kmax).transpose(0, 2, 3, 1)
+        return p.reshape(Gp * 8, self.n_pad), u, x
+
+    def tile_designs(self, P8_dev, G, kmax, out=None):
+        """Device tiles of stacked pseudoinverse rows P8_dev (G_pad*8, n_pad)."""
         t = self.t
-        p_hi = t.empty((G * 8, self.n_pad), dtype=t.bfloat16, device="cuda") if p_hi is None else p_hi
-        p_lo = t.empty_like(p_hi) if p_lo is None else p_lo
-        _lib.check(self.lib.glm_split_bf16(ptr(P8_dev), self.n_pad, 0, G * 8, self.n_pad, self.n_pad, ptr(p_hi),
-                                           ptr(p_lo), stream_handle()))
-        return p_hi, p_lo
+        rows = self.padded(G, kmax) * 8
+        rb = self.block(kmax) * 8
+        nbytes = int(self.lib.glm_tile_bytes(rows, rb, self.n_pad))
+        out = t.empty(nbytes, dtype=t.uint8, device="cuda") if out is None else out
+        _lib.check(self.lib.glm_tile_split(ptr(P8_dev), self.n_pad, 0, rows, self.n_pad, None, rb, self.n_pad,
+                                           ptr(out), stream_handle()))
+        return out
 
-    def tstat(self, p_hi, p_lo, X, invd, dof, G, kmax, coef_d, n_coef, out, ldt):
-        _lib.check(self.lib.glm_tstat_tc(ptr(self.y_hi), ptr(self.y_lo), self.n, self.n_pad, self.V, ptr(p_hi),
-                                         ptr(p_lo), ptr(X), ptr(invd), ptr(dof), G, kmax, ptr(coef_d), n_coef,
-                                         ptr(out), ldt, ptr(self.err), stream_handle()))
+    def tstat(self, p_tiles, u_rows, x_rows, invd, dof, G, kmax, coef_d, n_coef, out, ldt):
+        _lib.check(self.lib.glm_tstat_tc(ptr(self.yt), ptr(self.shift), ptr(self.Yd), self.V, self.n, self.n_pad,
+                                         self.V, ptr(p_tiles), ptr(u_rows), ptr(x_rows), self.n_sc, ptr(invd),
+                                         ptr(dof), G, kmax, ptr(coef_d), n_coef, ptr(out), ldt, ptr(self.err),
+                                         stream_handle()))
 
     def status(self):
         e = int(self.err.item())
         if e:
             self.err.zero_()
-            raise RuntimeError("tensor-core GLM: MMA completion wait ran out (device code %d)" % e)
+            raise RuntimeError("tensor-core GLM: a copy or MMA completion wait ran out (device code %d)" % e)
 
 
-def glm_tstat_tc(Y, designs, coef, ops=None):
-    """t maps (G, n_coef, V) through the tcgen05 split-BF16 GLM."""
+def glm_tstat_tc(Y, designs, coef, ops=None, centre=True):
+    """t maps (G, n_coef, V) through the tcgen05 split-BF16 GLM (glm_tstat_tc)."""
     t = require_cuda()
-    Yd = dev(Y, t.float32)
-    ops = ops or TensorCoreOperands(Yd)
     db = designs if isinstance(designs, DesignBatch) else DesignBatch(designs)
-    if db.kmax > 8:
-        raise ValueError("at most 8 regressors per design")
-    P8 = dev(ops.stacked(db))
-    p_hi, p_lo = ops.split(P8, db.G)
-    _, Xp, invd, dof = db.to_device()
+    ops = ops or TensorCoreOperands(dev(Y, t.float32), centre=centre)
+    P8, U, Xt = ops.host_operands(db)
+    pt = ops.tile_designs(dev(P8), db.G, db.kmax)
+    u, xt = dev(U), dev(Xt)
+    invd = dev(db.invdiag64.astype(np.float32))
+    dof = dev(db.dof.astype(np.float32))
     coef_d = dev(np.asarray(coef, np.int32))
     out = t.empty((db.G, len(coef), ops.V), device="cuda", dtype=t.float32)
-    ops.tstat(p_hi, p_lo, Xp, invd, dof, db.G, db.kmax, coef_d, len(coef), out, ops.V)
+    ops.tstat(pt, u, xt, invd, dof, db.G, db.kmax, coef_d, len(coef), out, ops.V)
     t.cuda.synchronize()
     ops.status()
     return out
