@@ -203,17 +203,18 @@ class PermutationEngine:
         if tc is not None:
             Gp, DB = tc.padded(P, kmax), tc.block(kmax)
             keys = ("P8", "U", "Xt", "invd", "dof")
-            slot["h_P8"] = t.empty((Gp * 8, tc.n_pad), dtype=t.float32, pin_memory=True)
-            slot["h_U"] = t.empty((Gp, kmax), dtype=t.float32, pin_memory=True)
-            slot["h_Xt"] = t.empty((Gp // DB, tc.n_sc, kmax, DB), dtype=t.float32, pin_memory=True)
+            slot["h_P8"] = t.zeros((Gp * 8, tc.n_pad), dtype=t.float32, pin_memory=True)
+            slot["h_U"] = t.zeros((Gp, kmax), dtype=t.float32, pin_memory=True)
+            slot["h_Xt"] = t.zeros((Gp // DB, tc.n_sc, kmax, DB), dtype=t.float32, pin_memory=True)
             slot["d_pt"] = t.empty(int(self.lib.glm_tile_bytes(Gp * 8, DB * 8, tc.n_pad)), dtype=t.uint8,
                                    device="cuda")
         else:
             keys = ("pinv", "X", "invd", "dof")
-            slot["h_pinv"] = t.empty((P, kmax, n), dtype=t.float32, pin_memory=True)
-            slot["h_X"] = t.empty((P, n, kmax), dtype=t.float32, pin_memory=True)
-        slot["h_invd"] = t.empty((P, kmax), dtype=t.float32, pin_memory=True)
-        slot["h_dof"] = t.empty((P,), dtype=t.float32, pin_memory=True)
+            slot["h_pinv"] = t.zeros((P, kmax, n), dtype=t.float32, pin_memory=True)
+            slot["h_X"] = t.zeros((P, n, kmax), dtype=t.float32, pin_memory=True)
+        # the capture warm-up runs on these before the first fill: a harmless design
+        slot["h_invd"] = t.ones((P, kmax), dtype=t.float32, pin_memory=True)
+        slot["h_dof"] = t.ones((P,), dtype=t.float32, pin_memory=True)
         slot["h_max"] = t.empty((P, self.C, self.signs, self.n_seg), dtype=t.float32, pin_memory=True)
         for key in keys:
             slot["d_" + key] = t.empty(slot["h_" + key].shape, device="cuda", dtype=t.float32)
