@@ -72,6 +72,9 @@ constexpr int kMaxSteps = 128;
 #define TFGB_ALANES 4
 #endif
 constexpr int kSweepThreads = TFGB_SWEEP_THREADS;
+#ifndef TFGB_BATCHED_UNION
+#define TFGB_BATCHED_UNION 1
+#endif
 constexpr int kUBatch = TFGB_UBATCH;   // list entries of one vertex looked up together
 constexpr int kALanes = TFGB_ALANES;   // positions per thread per accumulation round
 constexpr uint32_t kOneWay = 0x80000000u;   // entry whose reverse entry is missing
@@ -474,6 +477,86 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
             for (int k = 0; k < kUBatch; ++k)
               if (ka[k] != kInactiveKey) ka[k] = sl.key[an[k]];
           }
+#if TFGB_BATCHED_UNION
+          // Batched union: the roots of all effective neighbours in this
+          // batch (and of the vertex's own component) are walked in lockstep,
+          // one round of loads per hop, then every distinct root other than
+          // the smallest is linked under it.  A link is a CAS that succeeds
+          // only on a root; a lost race falls back to the general unite.
+          int32_t cur[kUBatch];
+#pragma unroll
+          for (int k = 0; k < kUBatch; ++k) {
+            cur[k] = -1;
+            if (ka[k] == kInactiveKey) continue;
+            const int la = static_cast<int>(ka[k] >> kPosBits);
+            if (la > i) continue;
+            if (la == i && (kChecked || (raw[k] & kOneWay))) {
+              // one-directional entry: effective only if the neighbour was
+              // inserted first (larger value; ties by smaller index)
+              const float xa = sign * x[an[k]], xv = sign * x[v];
+              if (!(xa > xv || (xa == xv && an[k] < v))) continue;
+            }
+            cur[k] = static_cast<int32_t>(ka[k] & ((1u << kPosBits) - 1u));
+          }
+          bool any = false;
+#pragma unroll
+          for (int k = 0; k < kUBatch; ++k) any |= (cur[k] >= 0);
+          if (!any) continue;
+          int32_t rr = rp;
+          for (int it = 0;; ++it) {
+            if (it >= kWalkLimit) {
+              set_err(a.err, kDevLoopLimit);
+              break;
+            }
+            int32_t par[kUBatch];
+#pragma unroll
+            for (int k = 0; k < kUBatch; ++k) par[k] = (cur[k] >= 0) ? ld_state(sl.parent + cur[k]) : cur[k];
+            const int32_t pr = ld_state(sl.parent + rr);
+            bool walking = (pr != rr);
+#pragma unroll
+            for (int k = 0; k < kUBatch; ++k) walking |= (par[k] != cur[k]);
+            if (!walking) break;
+            int32_t gp[kUBatch];
+#pragma unroll
+            for (int k = 0; k < kUBatch; ++k) gp[k] = (par[k] != cur[k]) ? ld_state(sl.parent + par[k]) : par[k];
+            const int32_t gr = (pr != rr) ? ld_state(sl.parent + pr) : pr;
+#pragma unroll
+            for (int k = 0; k < kUBatch; ++k) {
+              if (par[k] != cur[k]) {
+                if (gp[k] != par[k]) st_state(sl.parent + cur[k], gp[k]);  // halve the path
+                cur[k] = gp[k];
+              }
+            }
+            if (pr != rr) {
+              if (gr != pr) st_state(sl.parent + rr, gr);
+              rr = gr;
+            }
+          }
+          int32_t tgt = rr;
+#pragma unroll
+          for (int k = 0; k < kUBatch; ++k)
+            if (cur[k] >= 0) tgt = min(tgt, cur[k]);
+          // distinct roots other than the target, each linked once; the
+          // CASes are issued together, their results read afterwards
+          int32_t lk[kUBatch + 1], old[kUBatch + 1];
+          lk[0] = (rr != tgt) ? rr : -1;
+#pragma unroll
+          for (int k = 0; k < kUBatch; ++k) {
+            bool keep = cur[k] >= 0 && cur[k] != tgt && cur[k] != rr;
+#pragma unroll
+            for (int j = 0; j < k; ++j) keep &= (cur[j] != cur[k]);
+            lk[k + 1] = keep ? cur[k] : -1;
+          }
+#pragma unroll
+          for (int m = 0; m <= kUBatch; ++m) old[m] = (lk[m] >= 0) ? atomicCAS(sl.parent + lk[m], lk[m], tgt) : -1;
+#pragma unroll
+          for (int m = 0; m <= kUBatch; ++m) {
+            if (lk[m] < 0) continue;
+            if (old[m] == lk[m]) sl.dead[atomicAdd(&sNDead, 1)] = lk[m];
+            else tgt = unite(sl.parent, tgt, lk[m], sl.dead, &sNDead, a.err);
+          }
+          rp = tgt;
+#else
 #pragma unroll
           for (int k = 0; k < kUBatch; ++k) {
             if (ka[k] == kInactiveKey) continue;
@@ -494,6 +577,7 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
             }
             rp = unite(sl.parent, rp, q, sl.dead, &sNDead, a.err);
           }
+#endif
         }
       }
       __syncthreads();
