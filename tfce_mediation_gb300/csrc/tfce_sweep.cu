@@ -69,14 +69,21 @@ constexpr int kMaxSteps = 128;
 #define TFGB_UBATCH 6
 #endif
 #ifndef TFGB_ALANES
-#define TFGB_ALANES 4
+#define TFGB_ALANES 2
 #endif
 constexpr int kSweepThreads = TFGB_SWEEP_THREADS;
+#ifndef TFGB_U_GRAB
+#define TFGB_U_GRAB 1
+#endif
 #ifndef TFGB_BATCHED_UNION
 #define TFGB_BATCHED_UNION 1
 #endif
 constexpr int kUBatch = TFGB_UBATCH;   // list entries of one vertex looked up together
 constexpr int kALanes = TFGB_ALANES;   // positions per thread per accumulation round
+#ifndef TFGB_SLANES
+#define TFGB_SLANES 2
+#endif
+constexpr int kSLanes = TFGB_SLANES;   // dead roots per thread per size round
 constexpr uint32_t kOneWay = 0x80000000u;   // entry whose reverse entry is missing
 constexpr uint32_t kIndexMask = 0x7fffffffu;
 constexpr uint32_t kInactiveKey = 0xffffffffu;
@@ -129,8 +136,6 @@ struct Slot {
   int32_t* roots_a;  // live roots after the previous threshold ...
   int32_t* roots_b;  // ... and after this one (swapped every step)
   double* W;         // root: increments so far; dead: potential to its link
-  uint8_t* lvl;      // activation step per vertex (255: never), 1 byte so the
-                     // neighbour activity test of the union phase stays in L1
 };
 
 __host__ __device__ inline int64_t align_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
@@ -142,8 +147,7 @@ __host__ __device__ inline int64_t slot_bytes(int32_t vcap) {
 // Per-component accumulation adds link, two root lists and a double per
 // vertex to the six int32/float arrays of the exact mode.
 __host__ __device__ inline int64_t slot_bytes_lazy(int32_t vcap) {
-  return 9 * align_up((int64_t)vcap * 4, 256) + align_up((int64_t)vcap * 8, 256) +
-         align_up((int64_t)vcap, 256);
+  return 9 * align_up((int64_t)vcap * 4, 256) + align_up((int64_t)vcap * 8, 256);
 }
 
 __device__ inline Slot make_slot(char* base, int32_t vcap) {
@@ -153,7 +157,6 @@ __device__ inline Slot make_slot(char* base, int32_t vcap) {
   sl.roots_a = reinterpret_cast<int32_t*>(base + 7 * s);
   sl.roots_b = reinterpret_cast<int32_t*>(base + 8 * s);
   sl.W = reinterpret_cast<double*>(base + 9 * s);
-  sl.lvl = reinterpret_cast<uint8_t*>(base + 9 * s + align_up((int64_t)vcap * 8, 256));
   sl.key = reinterpret_cast<uint32_t*>(base);
   sl.order = reinterpret_cast<int32_t*>(base + s);
   sl.parent = reinterpret_cast<int32_t*>(base + 2 * s);
@@ -292,7 +295,7 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
   __shared__ int32_t sCnt[kMaxSteps + 1];
   __shared__ int32_t sStart[kMaxSteps + 1];
   __shared__ float sRed[32];
-  __shared__ int32_t sItem, sL, sNDead, sNRoots, sNext;
+  __shared__ int32_t sItem, sL, sNDead, sNRoots, sNext, sGrab;
 
   Slot sl = make_slot(a.ws + (int64_t)blockIdx.x * a.ws_slot_bytes, a.vcap);
   const int tid = threadIdx.x, nth = blockDim.x;
@@ -327,6 +330,7 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
     const float H = a.seg_H[seg], E = a.seg_E[seg];
     const int e_mode = (E == 1.0f) ? 1 : (E == 0.5f) ? 2 : (E == 2.0f) ? 3 : 0;
     const float* x = a.stats + (int64_t)map * a.map_stride + v0;
+    const int64_t seg_e0 = a.offsets[v0];
     const float* vd = a.vdensity ? a.vdensity + v0 : nullptr;
     float* omap = a.out_maps ? a.out_maps + (int64_t)ms * (a.seg_off[a.n_seg]) + v0 : nullptr;
 
@@ -397,6 +401,7 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
       sNDead = 0;
       sNRoots = 0;
       sNext = 0;
+      sGrab = 0;
     }
     __syncthreads();
     const int32_t n_act = sStart[L];
@@ -419,12 +424,17 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
         if constexpr (kLazy) {
           sl.W[p] = 0.0;
           sl.link[p] = p;
+          // the vertex's list (start relative to the segment's, degree) by
+          // position, so the union phase reads it without a dependent load;
+          // -1: out of the packed range, read the offsets
+          const int64_t e0 = a.offsets[v0 + v], deg = a.offsets[v0 + v + 1] - e0, rel = e0 - seg_e0;
+          reinterpret_cast<int32_t*>(sl.acc)[p] =
+              (deg <= 63 && rel >= 0 && rel < (int64_t(1) << 25)) ? static_cast<int32_t>((rel << 6) | deg) : -1;
         } else {
           sl.acc[p] = (a.out_mode == 2 && omap) ? omap[v] : 0.0f;
         }
       }
       sl.key[v] = key;
-      if constexpr (kLazy) sl.lvl[v] = (lv < L) ? static_cast<uint8_t>(lv) : uint8_t(255);
     }
     __syncthreads();
     TFGB_PHASE_MARK(1);
@@ -444,9 +454,24 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
       // vertex's list is read kUBatch entries at a time with all their key
       // lookups issued together; the root of the vertex's component is kept
       // as a hint between unions.
+#if TFGB_U_GRAB
+      // each thread takes the next unprocessed vertex of the step from a
+      // shared cursor, so threads with short walks do not wait for slow ones
+      for (int32_t p = atomicAdd(&sGrab, 1); p < s1; p = atomicAdd(&sGrab, 1)) {
+#else
       for (int32_t p = s0 + tid; p < s1; p += nth) {
-        const int32_t v = sl.order[p];
-        int64_t e0 = a.offsets[v0 + v], e1 = a.offsets[v0 + v + 1];
+#endif
+        int32_t v = -1;  // the vertex: read when needed
+        int64_t e0, e1;
+        const int32_t pk = kLazy ? reinterpret_cast<const int32_t*>(sl.acc)[p] : -1;
+        if (pk >= 0) {
+          e0 = seg_e0 + (pk >> 6);
+          e1 = e0 + (pk & 63);
+        } else {
+          v = sl.order[p];
+          e0 = a.offsets[v0 + v];
+          e1 = a.offsets[v0 + v + 1];
+        }
         if constexpr (kChecked) {
           if (e0 < 0 || e1 > a.n_entries || e1 < e0) {
             set_err(a.err, kDevBadIndex);
@@ -467,15 +492,8 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
             ka[k] = kInactiveKey;
             if (eb + k < e1) {
               if (ag < 0 || ag >= Vs) set_err(a.err, kDevBadIndex);
-              else if constexpr (kLazy) ka[k] = (sl.lvl[an[k]] <= i) ? 0u : kInactiveKey;
               else ka[k] = sl.key[an[k]];
             }
-          }
-          if constexpr (kLazy) {
-            // bucket positions only for the neighbours that are active
-#pragma unroll
-            for (int k = 0; k < kUBatch; ++k)
-              if (ka[k] != kInactiveKey) ka[k] = sl.key[an[k]];
           }
 #if TFGB_BATCHED_UNION
           // Batched union: the roots of all effective neighbours in this
@@ -493,6 +511,7 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
             if (la == i && (kChecked || (raw[k] & kOneWay))) {
               // one-directional entry: effective only if the neighbour was
               // inserted first (larger value; ties by smaller index)
+              if (v < 0) v = sl.order[p];
               const float xa = sign * x[an[k]], xv = sign * x[v];
               if (!(xa > xv || (xa == xv && an[k] < v))) continue;
             }
@@ -565,6 +584,7 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
             if (la == i && (kChecked || (raw[k] & kOneWay))) {
               // one-directional entry: effective only if the neighbour was
               // inserted first (larger value; ties by smaller index)
+              if (v < 0) v = sl.order[p];
               const float xa = sign * x[an[k]], xv = sign * x[v];
               if (!(xa > xv || (xa == xv && an[k] < v))) continue;
             }
@@ -581,17 +601,62 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
         }
       }
       __syncthreads();
+      if (tid == 0) sGrab = s1;  // the next step's first position
       TFGB_PHASE_MARK(2);
-      // (S) linked roots hand their extent to their final root
+      // (S) linked roots hand their extent to their final root.  Each thread
+      // takes kSLanes dead roots per round and walks them in lockstep.
       const int32_t nd = sNDead;
-      for (int32_t q = tid; q < nd; q += nth) {
-        const int32_t d = sl.dead[q];
-        const int32_t r = find_root(sl.parent, d, a.err);
-        atomicAdd(sl.size + r, ld_state(sl.size + d));
-        st_state(sl.parent + d, r);
-        if constexpr (kLazy) {
-          sl.link[d] = r;
-          sl.W[d] = sl.W[d] - sl.W[r];
+      for (int32_t q0 = tid; q0 < nd; q0 += kSLanes * nth) {
+        int32_t d[kSLanes], c[kSLanes];
+#pragma unroll
+        for (int k = 0; k < kSLanes; ++k) {
+          const int32_t q = q0 + k * nth;
+          d[k] = (q < nd) ? sl.dead[q] : -1;
+          c[k] = d[k];
+        }
+        for (int it = 0;; ++it) {
+          if (it >= kWalkLimit) {
+            set_err(a.err, kDevLoopLimit);
+            break;
+          }
+          int32_t par[kSLanes];
+#pragma unroll
+          for (int k = 0; k < kSLanes; ++k) par[k] = (c[k] >= 0) ? ld_state(sl.parent + c[k]) : c[k];
+          bool walking = false;
+#pragma unroll
+          for (int k = 0; k < kSLanes; ++k) walking |= (par[k] != c[k]);
+          if (!walking) break;
+          int32_t gp[kSLanes];
+#pragma unroll
+          for (int k = 0; k < kSLanes; ++k) gp[k] = (par[k] != c[k]) ? ld_state(sl.parent + par[k]) : par[k];
+#pragma unroll
+          for (int k = 0; k < kSLanes; ++k) {
+            if (par[k] != c[k]) {
+              if (gp[k] != par[k]) st_state(sl.parent + c[k], gp[k]);  // halve the path
+              c[k] = gp[k];
+            }
+          }
+        }
+        int32_t sz[kSLanes];
+        double wd[kSLanes], wr[kSLanes];
+#pragma unroll
+        for (int k = 0; k < kSLanes; ++k) {
+          if (d[k] < 0) continue;
+          sz[k] = ld_state(sl.size + d[k]);
+          if constexpr (kLazy) {
+            wd[k] = sl.W[d[k]];
+            wr[k] = sl.W[c[k]];
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < kSLanes; ++k) {
+          if (d[k] < 0) continue;
+          atomicAdd(sl.size + c[k], sz[k]);
+          st_state(sl.parent + d[k], c[k]);
+          if constexpr (kLazy) {
+            sl.link[d[k]] = c[k];
+            sl.W[d[k]] = wd[k] - wr[k];
+          }
         }
       }
       if constexpr (kLazy) {
@@ -607,22 +672,39 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
         const float HHl = sHH[i];
         const int32_t n_old = sNRoots;
         const int32_t n_cand = n_old + (s1 - s0);
-        for (int32_t q = tid; q < n_cand; q += nth) {
-          const int32_t c = (q < n_old) ? cur_roots[q] : s0 + (q - n_old);
-          const bool is_root = (ld_state(sl.parent + c) == c);
-          if (is_root) {
-            const float inc = increment(ld_state(sl.size + c), E, e_mode, HHl);
-            sl.W[c] = sl.W[c] + static_cast<double>(inc);
+        for (int32_t q0 = tid; q0 < n_cand; q0 += kALanes * nth) {
+          int32_t c[kALanes];
+          bool is_root[kALanes];
+#pragma unroll
+          for (int k = 0; k < kALanes; ++k) {
+            const int32_t q = q0 + k * nth;
+            c[k] = (q >= n_cand) ? -1 : (q < n_old) ? cur_roots[q] : s0 + (q - n_old);
           }
+#pragma unroll
+          for (int k = 0; k < kALanes; ++k) is_root[k] = (c[k] >= 0) && (ld_state(sl.parent + c[k]) == c[k]);
+          int32_t sz[kALanes];
+          double w[kALanes];
+#pragma unroll
+          for (int k = 0; k < kALanes; ++k) {
+            if (!is_root[k]) continue;
+            sz[k] = ld_state(sl.size + c[k]);
+            w[k] = sl.W[c[k]];
+          }
+#pragma unroll
+          for (int k = 0; k < kALanes; ++k)
+            if (is_root[k]) sl.W[c[k]] = w[k] + static_cast<double>(increment(sz[k], E, e_mode, HHl));
           const unsigned mask = __activemask();
-          const unsigned roots = __ballot_sync(mask, is_root);
-          if (roots) {
-            const int lane = tid & 31;
-            const int leader = __ffs(roots) - 1;
-            int base = 0;
-            if (lane == leader) base = atomicAdd(&sNext, __popc(roots));
-            base = __shfl_sync(mask, base, leader);
-            if (is_root) nxt_roots[base + __popc(roots & ((1u << lane) - 1u))] = c;
+          const int lane = tid & 31;
+#pragma unroll
+          for (int k = 0; k < kALanes; ++k) {
+            const unsigned roots = __ballot_sync(mask, is_root[k]);
+            if (roots) {
+              const int leader = __ffs(roots) - 1;
+              int base = 0;
+              if (lane == leader) base = atomicAdd(&sNext, __popc(roots));
+              base = __shfl_sync(mask, base, leader);
+              if (is_root[k]) nxt_roots[base + __popc(roots & ((1u << lane) - 1u))] = c[k];
+            }
           }
         }
         __syncthreads();
@@ -722,6 +804,15 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
   }
 }
 
+// Per-component accumulation with the union-find indexed by VERTEX: a
+// neighbour's activity is its 1-byte activation step and its union-find
+// entry is parent[neighbour] itself, so the union phase touches the level
+// array (V bytes per item) and the vertex-indexed parent array, whose entries
+// for mesh neighbours share cache sectors.  Links put the larger vertex index
+// under the smaller (parent[x] <= x, walks end).  The component partition,
+// extents and increments are those of the position-indexed kernel; only the
+// representative of a component differs, which the per-component potentials
+// do not depend on.
 }  // namespace tfgb
 
 // ---------------------------------------------------------------------------
