@@ -15,7 +15,11 @@
 //      the partition);
 //   3. per step: (U) new vertices are unioned with active neighbours by a
 //      lock-free union-find in the bucket-position space (CAS links the
-//      larger root under the smaller, so parent[x] < x and walks end);
+//      larger root under the smaller, so parent[x] < x and walks end).  A
+//      thread takes the next new vertex from a shared cursor, walks the roots
+//      of all its effective neighbours in lockstep (one round of loads per
+//      hop, path halving) and links every distinct root under the smallest
+//      with CASes issued together; a lost race falls back to a general unite;
 //      (S) the roots that were linked this step hand their extent to their new
 //      root; (A) every active vertex adds (float)(extent^E * HH_i) to its own
 //      accumulator, in threshold order -- the reference's per-vertex
@@ -74,9 +78,6 @@ constexpr int kMaxSteps = 128;
 constexpr int kSweepThreads = TFGB_SWEEP_THREADS;
 #ifndef TFGB_U_GRAB
 #define TFGB_U_GRAB 1
-#endif
-#ifndef TFGB_BATCHED_UNION
-#define TFGB_BATCHED_UNION 1
 #endif
 constexpr int kUBatch = TFGB_UBATCH;   // list entries of one vertex looked up together
 constexpr int kALanes = TFGB_ALANES;   // positions per thread per accumulation round
@@ -295,7 +296,7 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
   __shared__ int32_t sCnt[kMaxSteps + 1];
   __shared__ int32_t sStart[kMaxSteps + 1];
   __shared__ float sRed[32];
-  __shared__ int32_t sItem, sL, sNDead, sNRoots, sNext, sGrab;
+  __shared__ int32_t sItem, sL, sNDead, sNRoots, sNext, sGrab, sGrabS, sGrabA;
 
   Slot sl = make_slot(a.ws + (int64_t)blockIdx.x * a.ws_slot_bytes, a.vcap);
   const int tid = threadIdx.x, nth = blockDim.x;
@@ -402,6 +403,7 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
       sNRoots = 0;
       sNext = 0;
       sGrab = 0;
+      sGrabS = 0;
     }
     __syncthreads();
     const int32_t n_act = sStart[L];
@@ -495,7 +497,6 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
               else ka[k] = sl.key[an[k]];
             }
           }
-#if TFGB_BATCHED_UNION
           // Batched union: the roots of all effective neighbours in this
           // batch (and of the vertex's own component) are walked in lockstep,
           // one round of loads per hop, then every distinct root other than
@@ -575,29 +576,6 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
             else tgt = unite(sl.parent, tgt, lk[m], sl.dead, &sNDead, a.err);
           }
           rp = tgt;
-#else
-#pragma unroll
-          for (int k = 0; k < kUBatch; ++k) {
-            if (ka[k] == kInactiveKey) continue;
-            const int la = static_cast<int>(ka[k] >> kPosBits);
-            if (la > i) continue;
-            if (la == i && (kChecked || (raw[k] & kOneWay))) {
-              // one-directional entry: effective only if the neighbour was
-              // inserted first (larger value; ties by smaller index)
-              if (v < 0) v = sl.order[p];
-              const float xa = sign * x[an[k]], xv = sign * x[v];
-              if (!(xa > xv || (xa == xv && an[k] < v))) continue;
-            }
-            int32_t q = static_cast<int32_t>(ka[k] & ((1u << kPosBits) - 1u));
-            if constexpr (kLazy) {
-              // start from the neighbour's parent (an ancestor), and skip the
-              // union when it is this vertex's root and that is still a root
-              q = ld_state(sl.parent + q);
-              if (q == rp && ld_state(sl.parent + rp) == rp) continue;
-            }
-            rp = unite(sl.parent, rp, q, sl.dead, &sNDead, a.err);
-          }
-#endif
         }
       }
       __syncthreads();
@@ -606,11 +584,11 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
       // (S) linked roots hand their extent to their final root.  Each thread
       // takes kSLanes dead roots per round and walks them in lockstep.
       const int32_t nd = sNDead;
-      for (int32_t q0 = tid; q0 < nd; q0 += kSLanes * nth) {
+      for (int32_t q0 = atomicAdd(&sGrabS, kSLanes); q0 < nd; q0 = atomicAdd(&sGrabS, kSLanes)) {
         int32_t d[kSLanes], c[kSLanes];
 #pragma unroll
         for (int k = 0; k < kSLanes; ++k) {
-          const int32_t q = q0 + k * nth;
+          const int32_t q = q0 + k;
           d[k] = (q < nd) ? sl.dead[q] : -1;
           c[k] = d[k];
         }
@@ -660,11 +638,17 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
         }
       }
       if constexpr (kLazy) {
-        if (tid == 0) sNext = 0;
+        if (tid == 0) {
+          sNext = 0;
+          sGrabA = 0;
+        }
       }
       __syncthreads();
       TFGB_PHASE_MARK(3);
-      if (tid == 0) sNDead = 0;
+      if (tid == 0) {
+        sNDead = 0;
+        sGrabS = 0;  // read again only after two more barriers
+      }
       if constexpr (kLazy) {
         // (A') every live root adds its component's increment once: the old
         // live roots that survived this step plus the new vertices that are
@@ -672,12 +656,12 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
         const float HHl = sHH[i];
         const int32_t n_old = sNRoots;
         const int32_t n_cand = n_old + (s1 - s0);
-        for (int32_t q0 = tid; q0 < n_cand; q0 += kALanes * nth) {
+        for (int32_t q0 = atomicAdd(&sGrabA, kALanes); q0 < n_cand; q0 = atomicAdd(&sGrabA, kALanes)) {
           int32_t c[kALanes];
           bool is_root[kALanes];
 #pragma unroll
           for (int k = 0; k < kALanes; ++k) {
-            const int32_t q = q0 + k * nth;
+            const int32_t q = q0 + k;
             c[k] = (q >= n_cand) ? -1 : (q < n_old) ? cur_roots[q] : s0 + (q - n_old);
           }
 #pragma unroll
