@@ -162,9 +162,18 @@ def _cpu_perm(p):
     return out
 
 
+def _one_thread_per_process():
+    """BLAS / OpenMP thread counts of 1 for the worker processes (spawned
+    children read these when their numpy loads), so `cores` processes use
+    exactly `cores` host cores, as independent single-threaded jobs do."""
+    for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS", "NUMEXPR_NUM_THREADS"):
+        os.environ[var] = "1"
+
+
 def cpu_rate(n_perm, cores, study_args):
     """perm/s of the oracle port over n_perm permutations on `cores` processes."""
     import multiprocessing as mp
+    _one_thread_per_process()
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores, initializer=_cpu_init, initargs=(study_args,)) as pool:
         pool.map(_cpu_perm, range(10_000, 10_000 + cores))  # warm: data built, libs loaded
@@ -181,6 +190,7 @@ def run_reference(args):
     cores = os.cpu_count() or 1
     study_args = {"n": args.n, "level": args.level}
     import multiprocessing as mp
+    _one_thread_per_process()
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores, initializer=_cpu_init, initargs=(study_args,)) as pool:
         for w in range(args.warmup):
@@ -198,7 +208,7 @@ def run_reference(args):
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "perms_per_step": cores,
                        "note": "oracle port of the reference CPU path (FP64 tval_int + C restatement of "
-                               "fast_tfce.hpp), one process per host core"},
+                               "fast_tfce.hpp), one single-threaded process per host core"},
             "cpu_baseline": {"value": value, "unit": "perm/s", "cores": cores, "kind": "port",
                              "sample": f"{args.steps} steps x {cores} permutations (one per process)"},
             "e2e": {"value": value, "unit": "perm/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -343,6 +353,30 @@ def run_gpu(args):
     sweep_avg = float(np.mean(sweep_ms))
     glm_avg = float(np.mean(glm_ms))
     achieved = bytes_per_sweep * sweeps_per_launch / (sweep_avg / 1000) / 1e9
+    # work rate of the reference algorithm: sum over thresholds of the active
+    # vertices (its per-threshold pass over every active vertex), from a host
+    # sample of this step's t maps and the same float threshold recurrence
+    upd = []
+    tsample = eng._tbuf[: min(P, 4)].reshape(-1, V).cpu().numpy()
+    for m in tsample:
+        for sgn in (1.0, -1.0):
+            for h in range(S):
+                a_, b_ = int(st.segments[h]), int(st.segments[h + 1])
+                xs = (sgn * m[a_:b_]).astype(np.float32)
+                mx = max(float(xs.max()), 0.0)
+                if mx <= 0.0:
+                    upd.append(0)
+                    continue
+                T = [np.float32(mx)]
+                dT = np.float32(mx) / np.float32(100.0)
+                while True:
+                    nxt = np.float32(T[-1] - dT)
+                    if nxt < 0:
+                        break
+                    T.append(nxt)
+                T = np.asarray(T, np.float32)
+                upd.append(int(sum(int(np.count_nonzero(xs > t_)) for t_ in T)))
+    updates_per_sweep = float(np.mean(upd))
     per_sweep, traffic_note = profile_traffic("tfce_sweep")
     traffic = None if per_sweep is None else per_sweep * sweeps_per_launch
     clocks = clk.summary()
@@ -386,7 +420,9 @@ def run_gpu(args):
                      "traffic": traffic, "traffic_note": traffic_note,
                      "algorithmic_bytes_per_launch": bytes_per_sweep * sweeps_per_launch,
                      "ms_per_launch": sweep_avg,
-                     "vertex_sweeps_per_s": sweeps_per_launch * Vh / (sweep_avg / 1000)},
+                     "vertex_sweeps_per_s": sweeps_per_launch * Vh / (sweep_avg / 1000),
+                     "vertex_threshold_updates_per_sweep": updates_per_sweep,
+                     "vertex_threshold_updates_per_s": updates_per_sweep * sweeps_per_launch / (sweep_avg / 1000)},
         "kernels_ms_per_step": {"glm": glm_avg, "tfce_sweep": sweep_avg},
         "glm": glm_info,
         "clocks": clocks,
