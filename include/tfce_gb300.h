@@ -225,6 +225,21 @@ int glm_tstat_tc(const void* y_tiles, const float* y_shift, const float* Y, int6
                  int32_t n_pad, int64_t V, const void* p_tiles, const float* u_rows, const float* x_rows,
                  int32_t n_sc, const float* invdiag, const float* dof, int32_t G, int32_t kmax,
                  const int32_t* coef, int32_t n_coef, float* t_out, int64_t ldt, int32_t* err, void* stream);
+/* glm_stat_tc: glm_tstat_tc with a choice of epilogue output (t_out rows [G][n_coef][ldt]):
+ *   mode 0: t of the coefficients coef[0..n_coef) (= glm_tstat_tc);
+ *   mode 1: RSS from the residuals, one row per design (n_coef, coef ignored);
+ *   mode 2: partial F of n_coef column groups, coef = (start, width) pairs over
+ *     the design's columns: F = (RSS without the group - RSS) / width / (RSS/dof),
+ *     the reference's glm_typeI drop-one F (tm/pyfunc.py:2282-2400), with the
+ *     extra sum of squares in its exact form b_S' inv(inv(X'X)_SS) b_S; wmat
+ *     [G][w_stride] holds, per design, the groups' inv(inv(X'X)_SS) blocks
+ *     (row-major, concatenated in group order).  A group outside [0, kmax)
+ *     yields NaN. */
+int glm_stat_tc(const void* y_tiles, const float* y_shift, const float* Y, int64_t ldy, int32_t n,
+                int32_t n_pad, int64_t V, const void* p_tiles, const float* u_rows, const float* x_rows,
+                int32_t n_sc, const float* invdiag, const float* dof, int32_t G, int32_t kmax, int32_t mode,
+                const int32_t* coef, int32_t n_coef, const float* wmat, int32_t w_stride, float* t_out,
+                int64_t ldt, int32_t* err, void* stream);
 
 /* Indirect-effect z from path t values (device), z[p][v] for p < P:
  *   ta [P][lda] (or ta_scalar[P] when ta is NULL: medtype Y's linregress path),

@@ -205,6 +205,66 @@ def tval_fp64(X, y):
     return a / np.sqrt(sigma2[None, :] * np.diag(invXX)[:, None])
 
 
+def glm_typeI(endog, exog, dmy_covariates=None, rand_array=None):
+    """glm_typeI with output_fvalues and output_tvalues (tm/pyfunc.py:2282-2400):
+    design [1, exog..., covariates] (rows permuted by rand_array), model F
+    ((SS_Total - RSS)/(k-1)) / (RSS/(n-k)) with SS_Total around each column's
+    mean (formed in the data's own type, float32 for the reference's data),
+    the drop-one F of every exogenous variable from the refit without its
+    columns, and t of every coefficient with the SE rounded to float32
+    (se_of_slope).  Returns (F_model, F_var (n_var, V), T (k, V))."""
+    y = np.asarray(endog, np.float64)
+    n = y.shape[0]
+    kvars, cols = [], [np.ones(n)]
+    for var in exog:
+        var = np.asarray(var, np.float64)
+        kvars.append(1 if var.ndim == 1 else var.shape[1])
+        cols.append(var.reshape(n, -1))
+    if dmy_covariates is not None:
+        cols.append(np.asarray(dmy_covariates, np.float64).reshape(n, -1))
+    X = np.column_stack(cols)
+    if rand_array is not None:
+        X = X[np.asarray(rand_array)]
+    k = X.shape[1]
+
+    def rss(Xm):
+        a = np.linalg.lstsq(Xm, y, rcond=None)[0]
+        r = y - Xm @ a
+        return a, np.sum(r * r, axis=0)
+
+    # SS_Total in the data's own type, as numpy forms it for float32 data
+    y_in = np.asarray(endog)
+    ss_total = np.sum((y_in - np.mean(y_in, 0)) ** 2, 0).astype(np.float64)
+    a, rss_full = rss(X)
+    ms_res = rss_full / (n - k)
+    F_model = ((ss_total - rss_full) / (k - 1)) / ms_res
+    F_var, start = [], 1
+    for kv in kvars:
+        _, rss_red = rss(np.delete(X, np.s_[start:start + kv], 1))
+        F_var.append((rss_red - rss_full) / (ms_res * kv))
+        start += kv
+    invXX = np.linalg.inv(X.T @ X)
+    se = np.sqrt((rss_full / (n - k))[None, :] * np.diag(invXX)[:, None]).astype(np.float32)
+    return F_model, np.asarray(F_var), a / se
+
+
+def partial_f_fp64(X, y, groups):
+    """Drop-one F of column groups [(start, width), ...] of design X, FP64,
+    from the refits without each group (the yardstick of glm_stat_tc mode 2)."""
+    X = np.asarray(X, np.float64)
+    y = np.asarray(y, np.float64)
+    n, k = X.shape
+
+    def rss(Xm):
+        a = np.linalg.lstsq(Xm, y, rcond=None)[0]
+        r = y - Xm @ a
+        return np.sum(r * r, axis=0)
+
+    full = rss(X)
+    return np.asarray([(rss(np.delete(X, np.s_[s0:s0 + w], 1)) - full) / w / (full / (n - k))
+                       for s0, w in groups])
+
+
 def calc_beta_se(x, y, n):
     """cynumstats.pyx:66-74: design [1, x]; returns (beta[1], se float32 k x V)."""
     X = np.column_stack([np.ones(n), x])

@@ -272,6 +272,24 @@ def main():
         tv, tp, tn = tmf.low_ram_calculate_tfce(yl, maskl, xl, tfce.CreateAdjSet(2.0, 1.0, adj3), 1)
         out["lr_y"], out["lr_x"], out["lr_t"], out["lr_pos"], out["lr_neg"] = yl, xl, tv, tp, tn
 
+    # glm_typeI (tm-models GLM): drop-one F per exogenous variable, model F
+    # and t, observed and with a fixed permutation of the design rows
+    nt, Vt = 60, 40
+    yt = rng.standard_normal((nt, Vt)).astype(np.float32) + 2.0
+    fac = rng.integers(0, 3, nt)
+    ex0 = np.column_stack([(fac == 1), (fac == 2)]).astype(np.float64)
+    ex1 = rng.standard_normal(nt)
+    cov = rng.standard_normal((nt, 1))
+    yt[:, :10] += (0.8 * ex1)[:, None].astype(np.float32)
+    yt[:, 10:20] += (0.6 * ex0[:, 0])[:, None].astype(np.float32)
+    permt = np.random.RandomState(77).permutation(nt)
+    for tag, ra in (("obs", None), ("perm", permt)):
+        Fm, Fv, Tv = pyfunc.glm_typeI(yt, [ex0, ex1], dmy_covariates=cov, output_fvalues=True,
+                                  output_tvalues=True, verbose=False, rand_array=ra)
+        out[f"typeI_F_{tag}"], out[f"typeI_Fvar_{tag}"], out[f"typeI_T_{tag}"] = Fm, np.asarray(Fv), Tv
+    out["typeI_y"], out["typeI_ex0"], out["typeI_ex1"] = yt, ex0, ex1
+    out["typeI_cov"], out["typeI_perm"] = cov, permt
+
     path = os.path.join(HERE, "reference_vectors.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({os.path.getsize(path)} bytes, {len(out)} arrays)")

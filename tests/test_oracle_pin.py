@@ -171,3 +171,23 @@ def test_voxel_adjacency_builders(golden, dirtype):
     off, idx = A.voxel_csr(mask, dirtype, "mmr")
     np.testing.assert_array_equal(off, golden[f"voxmmr{dirtype}_off"])
     np.testing.assert_array_equal(idx, golden[f"voxmmr{dirtype}_idx"])
+
+
+@pytest.mark.parametrize("tag", ["obs", "perm"])
+def test_glm_typeI(golden, tag):
+    """The FP64 restatement of glm_typeI against the reference's own outputs
+    (model F, drop-one F per variable, t with float32 SE)."""
+    ra = None if tag == "obs" else golden["typeI_perm"]
+    F, Fv, T = oracle.glm_typeI(golden["typeI_y"], [golden["typeI_ex0"], golden["typeI_ex1"]],
+                                dmy_covariates=golden["typeI_cov"], rand_array=ra)
+    np.testing.assert_allclose(F, golden[f"typeI_F_{tag}"], rtol=1e-9)
+    np.testing.assert_allclose(Fv, golden[f"typeI_Fvar_{tag}"], rtol=1e-8, atol=1e-10)
+    np.testing.assert_allclose(T, golden[f"typeI_T_{tag}"], rtol=1e-12)
+
+
+def test_partial_f_is_glm_typeI_drop_one(golden):
+    y = golden["typeI_y"]
+    n = y.shape[0]
+    X = np.column_stack([np.ones(n), golden["typeI_ex0"], golden["typeI_ex1"], golden["typeI_cov"]])
+    Fv = oracle.partial_f_fp64(X, y, [(1, 2), (3, 1)])
+    np.testing.assert_allclose(Fv, golden["typeI_Fvar_obs"], rtol=1e-8, atol=1e-10)

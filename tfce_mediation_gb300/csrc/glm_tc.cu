@@ -66,14 +66,19 @@ __host__ __device__ constexpr int tc_ychunk() { return kTcSubjChunk * kTcM * 4; 
 constexpr int kTcBld = kTcM + 1;  // row stride (floats) of the drained betas
 __host__ __device__ constexpr int tc_beta_bytes(int kmax) { return tc_db(kmax) * kmax * kTcBld * 4; }
 __host__ __device__ constexpr int tc_cmax(int a, int b) { return a > b ? a : b; }
-// the stage ring, the drained betas and the subject chunks share one area
+// partial-F epilogue: every thread's betas and RSS (DB/2 vertices x (kmax+1) floats)
+__host__ __device__ constexpr int tc_fslice_bytes(int kmax) { return 256 * (tc_db(kmax) / 2) * (kmax + 1) * 4; }
+// the stage ring, the drained betas, the subject chunks and the partial-F
+// slices share one area
 __host__ __device__ constexpr int tc_area(int kmax) {
-  return (tc_cmax(tc_cmax(kTcStages * tc_stage(kmax), tc_beta_bytes(kmax)),
-                  2 * (tc_xchunk(kmax) + tc_ychunk())) + 127) / 128 * 128;
+  return (tc_cmax(tc_cmax(tc_cmax(kTcStages * tc_stage(kmax), tc_beta_bytes(kmax)),
+                          2 * (tc_xchunk(kmax) + tc_ychunk())),
+                  tc_fslice_bytes(kmax)) + 127) / 128 * 128;
 }
 __host__ __device__ constexpr int tc_smem(int kmax) { return tc_area(kmax) + 128; }
 static_assert(tc_smem(5) <= 113 * 1024 && tc_smem(8) <= 113 * 1024 && tc_smem(4) <= 113 * 1024,
               "two CTAs per SM");
+
 
 // --- PTX wrappers -----------------------------------------------------------
 __device__ inline uint32_t smem_addr(const void* p) {
@@ -238,10 +243,11 @@ struct TcArgs {
   const float* u;           // [G_pad][kmax] pinv(X_d).1 (with shift)
   const float* invdiag;     // [G][kmax]
   const float* dof;         // [G]
-  const int32_t* coef;
+  const int32_t* coef;      // mode 0: coefficient indices; mode 2: (start, width) per column group
+  const float* wmat;        // mode 2: [G][w_stride] inverse blocks of inv(X'X) per group
   float* t_out;             // [G][n_coef][ldt]
   int64_t ldy, ldt, V;
-  int32_t n, n_sc, ks_count, G, n_db, n_coef;
+  int32_t n, n_sc, ks_count, G, n_db, n_coef, mode, w_stride;
   int32_t* err;
 };
 
@@ -444,7 +450,8 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
       }
       __syncthreads();
     }
-    if (g < a.G) {
+    if (g < a.G && a.mode == 0) {
+      // t of each requested coefficient
       const float inv_dof = 1.0f / __ldg(a.dof + g);
       for (int ci = 0; ci < a.n_coef; ++ci) {
         const int j = __ldg(a.coef + ci);
@@ -461,6 +468,44 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
             dst[vv] = bj / sqrtf(rs * inv_dof * dj);
           }
         }
+      }
+    } else if (g < a.G && a.mode == 1) {
+      // residual sum of squares (from the residuals)
+      float* dst = a.t_out + (int64_t)g * a.ldt + v0;
+#pragma unroll
+      for (int vv = 0; vv < VT; ++vv)
+        if (v0 + vv < a.V) dst[vv] = (vv & 1) ? rss[vv / 2].y : rss[vv / 2].x;
+    } else if (g < a.G && a.mode == 2) {
+      // partial F of each column group S (the F of dropping S from the
+      // design): (RSS_without_S - RSS) / |S| / (RSS / dof), with the extra sum
+      // of squares in its exact Wald form b_S' inv(inv(X'X)_SS) b_S -- no
+      // difference of two residual sums
+      // this thread's betas and RSS go to its own slice of the (now free)
+      // shared area, so the group loops index them at run time
+      float* mine = reinterpret_cast<float*>(sm) + tid * VT * (KMAX + 1);
+#pragma unroll
+      for (int vv = 0; vv < VT; ++vv) {
+#pragma unroll
+        for (int jj = 0; jj < KMAX; ++jj) mine[vv * (KMAX + 1) + jj] = (vv & 1) ? bp[vv / 2][jj].y : bp[vv / 2][jj].x;
+        mine[vv * (KMAX + 1) + KMAX] = (vv & 1) ? rss[vv / 2].y : rss[vv / 2].x;
+      }
+      const float dof = __ldg(a.dof + g);
+      const float* wg = a.wmat + (int64_t)g * a.w_stride;
+      int woff = 0;
+      for (int gi = 0; gi < a.n_coef; ++gi) {
+        const int s0 = __ldg(a.coef + 2 * gi), kv = __ldg(a.coef + 2 * gi + 1);
+        const bool ok = s0 >= 0 && kv >= 1 && s0 + kv <= KMAX;
+        float* dst = a.t_out + ((int64_t)g * a.n_coef + gi) * a.ldt + v0;
+        for (int vv = 0; vv < VT; ++vv) {
+          if (v0 + vv >= a.V) break;
+          const float* bv = mine + vv * (KMAX + 1);
+          float q = 0.0f;
+          for (int ja = 0; ok && ja < kv; ++ja)
+            for (int jc = 0; jc < kv; ++jc)
+              q = fmaf(bv[s0 + ja] * __ldg(wg + woff + ja * kv + jc), bv[s0 + jc], q);
+          dst[vv] = ok ? (q / static_cast<float>(kv)) / (bv[KMAX] / dof) : __int_as_float(0x7fc00000);
+        }
+        woff += kv * kv;
       }
     }
   }
@@ -525,17 +570,22 @@ int glm_tile_split(const float* src, int64_t ld_src, int32_t transpose, int64_t 
   return TFCE_OK;
 }
 
-int glm_tstat_tc(const void* y_tiles, const float* y_shift, const float* Y, int64_t ldy, int32_t n,
-                 int32_t n_pad, int64_t V, const void* p_tiles, const float* u_rows, const float* x_rows,
-                 int32_t n_sc, const float* invdiag, const float* dof, int32_t G, int32_t kmax,
-                 const int32_t* coef, int32_t n_coef, float* t_out, int64_t ldt, int32_t* err, void* stream) {
+int glm_stat_tc(const void* y_tiles, const float* y_shift, const float* Y, int64_t ldy, int32_t n,
+                int32_t n_pad, int64_t V, const void* p_tiles, const float* u_rows, const float* x_rows,
+                int32_t n_sc, const float* invdiag, const float* dof, int32_t G, int32_t kmax, int32_t mode,
+                const int32_t* coef, int32_t n_coef, const float* wmat, int32_t w_stride, float* t_out,
+                int64_t ldt, int32_t* err, void* stream) {
   tfgb::clear_error();
-  TFGB_CHECK_ARG(y_tiles && Y && p_tiles && x_rows && invdiag && dof && coef && t_out && err, "NULL pointer");
+  TFGB_CHECK_ARG(y_tiles && Y && p_tiles && x_rows && invdiag && dof && t_out && err, "NULL pointer");
+  TFGB_CHECK_ARG(mode == 1 || coef != nullptr, "coef is NULL");
   TFGB_CHECK_ARG(!y_shift || u_rows, "a centred data operand needs u_rows");
   TFGB_CHECK_ARG(n > 0 && n_pad >= n && n_pad % tfgb::kTcK == 0, "n_pad must be >= n and a multiple of 16");
   TFGB_CHECK_ARG(n_sc >= n && n_sc % tfgb::kTcSubjChunk == 0, "n_sc must be >= n and a multiple of 32");
   TFGB_CHECK_ARG(kmax >= 1 && kmax <= tfgb::kTcRowsPerDesign, "kmax must be in [1, 8]");
-  TFGB_CHECK_ARG(n_coef >= 1 && V >= 0 && G >= 0 && ldt >= V && ldy >= V, "bad sizes");
+  TFGB_CHECK_ARG(mode >= 0 && mode <= 2, "mode must be 0 (t), 1 (RSS) or 2 (partial F)");
+  TFGB_CHECK_ARG(mode == 1 || n_coef >= 1, "n_coef must be >= 1");
+  TFGB_CHECK_ARG(mode != 2 || (wmat != nullptr && w_stride >= 1), "partial F needs wmat");
+  TFGB_CHECK_ARG(V >= 0 && G >= 0 && ldt >= V && ldy >= V, "bad sizes");
   TFGB_CHECK_ARG(reinterpret_cast<uintptr_t>(y_tiles) % 16 == 0 && reinterpret_cast<uintptr_t>(p_tiles) % 16 == 0 &&
                      reinterpret_cast<uintptr_t>(x_rows) % 16 == 0,
                  "tiles and design rows must be 16-byte aligned");
@@ -550,6 +600,7 @@ int glm_tstat_tc(const void* y_tiles, const float* y_shift, const float* Y, int6
   a.invdiag = invdiag;
   a.dof = dof;
   a.coef = coef;
+  a.wmat = wmat;
   a.t_out = t_out;
   a.ldy = ldy;
   a.ldt = ldt;
@@ -559,7 +610,9 @@ int glm_tstat_tc(const void* y_tiles, const float* y_shift, const float* Y, int6
   a.ks_count = n_pad / tfgb::kTcK;
   a.G = G;
   a.n_db = (G + tfgb::tc_db(kmax) - 1) / tfgb::tc_db(kmax);
-  a.n_coef = n_coef;
+  a.n_coef = (mode == 1) ? 1 : n_coef;
+  a.mode = mode;
+  a.w_stride = w_stride;
   a.err = err;
   const int64_t n_vb = (V + tfgb::kTcM - 1) / tfgb::kTcM;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -573,6 +626,14 @@ int glm_tstat_tc(const void* y_tiles, const float* y_shift, const float* Y, int6
     case 7: return tfgb::launch_tc<7>(a, n_vb, st);
     default: return tfgb::launch_tc<8>(a, n_vb, st);
   }
+}
+
+int glm_tstat_tc(const void* y_tiles, const float* y_shift, const float* Y, int64_t ldy, int32_t n,
+                 int32_t n_pad, int64_t V, const void* p_tiles, const float* u_rows, const float* x_rows,
+                 int32_t n_sc, const float* invdiag, const float* dof, int32_t G, int32_t kmax,
+                 const int32_t* coef, int32_t n_coef, float* t_out, int64_t ldt, int32_t* err, void* stream) {
+  return glm_stat_tc(y_tiles, y_shift, Y, ldy, n, n_pad, V, p_tiles, u_rows, x_rows, n_sc, invdiag, dof, G, kmax, 0,
+                     coef, n_coef, nullptr, 0, t_out, ldt, err, stream);
 }
 
 }  // extern "C"

@@ -48,6 +48,10 @@ class PermutationEngine:
     accumulation: 'component' (default; per-component double sums, within
     ~1e-7 of the reference's float sums) or 'exact' (the reference's float
     arithmetic, bit-identical; slower).
+    f_groups: [(start, width), ...] column groups of the design: the maps are
+    then the drop-one F of each group (glm_typeI's F per variable,
+    tm/pyfunc.py:2282-2400, as tm_models_randomise.py:205-210 permutes it),
+    swept with one sign; needs precision 'bf16x3'.
     precision: GLM arithmetic of the permutation t maps: 'bf16x3' (default;
     tensor cores, split BF16 with FP32 accumulation, t within ~3e-5 relative
     of FP64) or 'fp32' (CUDA cores, ~1e-6).  The observed (unpermuted) t map
@@ -60,11 +64,16 @@ class PermutationEngine:
 
     def __init__(self, Y, pred_x, adjacency, segments=None, H=2.0, E=1.0, vdensity=None,
                  contrasts=None, floor_zero=False, batch=64, signs=2, reorder=False,
-                 accumulation="component", precision="bf16x3"):
+                 accumulation="component", precision="bf16x3", f_groups=None):
         t = require_cuda()
         if precision not in ("bf16x3", "fp32"):
             raise ValueError("precision must be 'bf16x3' (tensor cores) or 'fp32' (CUDA cores)")
         self.precision = precision
+        self.f_groups = None if f_groups is None else [(int(a), int(b)) for a, b in f_groups]
+        if self.f_groups is not None:
+            if precision != "bf16x3":
+                raise ValueError("partial-F maps run on the tensor-core GLM (precision='bf16x3')")
+            signs = 1
         self.t = t
         Yh = Y if isinstance(Y, t.Tensor) else np.asarray(Y, np.float32)
         V = Yh.shape[1]
@@ -94,12 +103,18 @@ class PermutationEngine:
         self.adj.set_accumulation(accumulation)
         self.n_seg = self.adj.n_seg
         self.contrasts = list(range(1, self.k)) if contrasts is None else list(contrasts)
+        if self.f_groups is not None:
+            for s0, w in self.f_groups:
+                if s0 < 1 or w < 1 or s0 + w > self.k:
+                    raise ValueError(f"column group ({s0}, {w}) outside the design's {self.k} columns")
+            self.contrasts = list(range(len(self.f_groups)))
         self.C = len(self.contrasts)
         self.signs = signs
         self.floor_zero = bool(floor_zero)
         self.vd = None if vdensity is None else dev(np.asarray(vdensity, np.float32))
         self.lib = _lib.load()
-        self._coef = dev(np.asarray(self.contrasts, np.int32))
+        self._coef = dev(np.asarray(self.contrasts if self.f_groups is None else self.f_groups,
+                                    np.int32).reshape(-1))
         self._tc = TensorCoreOperands(self.Yd) if precision == "bf16x3" else None
         if batch == "auto":
             from .autotune import choose_batch
@@ -128,8 +143,12 @@ class PermutationEngine:
             self._tc = tc
             P8, U, Xt = tc.host_operands(designs)
             pt = tc.tile_designs(dev(P8), G, designs.kmax)
-            tc.tstat(pt, dev(U), dev(Xt), dev(designs.invdiag64.astype(np.float32)),
-                     dev(designs.dof.astype(np.float32)), G, designs.kmax, self._coef, self.C, out, self.V)
+            mode, wmat = 0, None
+            if self.f_groups is not None:
+                mode, wmat = 2, dev(designs.group_blocks(self.f_groups))
+            tc.stat(mode, pt, dev(U), dev(Xt), dev(designs.invdiag64.astype(np.float32)),
+                    dev(designs.dof.astype(np.float32)), G, designs.kmax, self._coef, self.C, out, self.V,
+                    wmat=wmat)
             return out
         pinv, Xp, invd, dof = designs.to_device()
         _lib.check(self.lib.glm_tstat(ptr(self.Yd), self.V, self.n, self.V, ptr(pinv), ptr(Xp),
@@ -202,7 +221,10 @@ class PermutationEngine:
         slot = {"P": P}
         if tc is not None:
             Gp, DB = tc.padded(P, kmax), tc.block(kmax)
-            keys = ("P8", "U", "Xt", "invd", "dof")
+            keys = ("P8", "U", "Xt", "invd", "dof") + (("W",) if self.f_groups is not None else ())
+            if self.f_groups is not None:
+                slot["h_W"] = t.zeros((P, sum(w * w for _, w in self.f_groups)), dtype=t.float32,
+                                      pin_memory=True)
             slot["h_P8"] = t.zeros((Gp * 8, tc.n_pad), dtype=t.float32, pin_memory=True)
             slot["h_U"] = t.zeros((Gp, kmax), dtype=t.float32, pin_memory=True)
             slot["h_Xt"] = t.zeros((Gp // DB, tc.n_sc, kmax, DB), dtype=t.float32, pin_memory=True)
@@ -226,8 +248,9 @@ class PermutationEngine:
                 slot["d_" + key].copy_(slot["h_" + key], non_blocking=True)
             if tc is not None:
                 tc.tile_designs(slot["d_P8"], P, kmax, out=slot["d_pt"])
-                tc.tstat(slot["d_pt"], slot["d_U"], slot["d_Xt"], slot["d_invd"], slot["d_dof"], P, kmax,
-                         self._coef, self.C, slot["d_t"], self.V)
+                tc.stat(2 if self.f_groups is not None else 0, slot["d_pt"], slot["d_U"], slot["d_Xt"],
+                        slot["d_invd"], slot["d_dof"], P, kmax, self._coef, self.C, slot["d_t"], self.V,
+                        wmat=slot.get("d_W"))
             else:
                 _lib.check(self.lib.glm_tstat(ptr(self.Yd), self.V, n, self.V, ptr(slot["d_pinv"]),
                                               ptr(slot["d_X"]), ptr(slot["d_invd"]), ptr(slot["d_dof"]), P,
@@ -257,6 +280,8 @@ class PermutationEngine:
         P = perms.shape[0]
         if self._tc is not None:
             self._tc.host_operands(db, P8=slot["h_P8"].numpy(), U=slot["h_U"].numpy(), Xt=slot["h_Xt"].numpy())
+            if self.f_groups is not None:
+                slot["h_W"].numpy()[:P] = db.group_blocks(self.f_groups)
         else:
             slot["h_pinv"].numpy()[:P] = db.pinv64
             slot["h_X"].numpy()[:P] = db.X64
@@ -304,7 +329,8 @@ class PermutationEngine:
         t = self.t
         db = DesignBatch(self.X[None])
         tm = t.empty((1, self.C, self.V), device="cuda", dtype=t.float32)
-        self.tmaps(db, out=tm, precision="fp32")
+        # the observed map: FP32 CUDA-core t (partial F exists on the tensor-core GLM only)
+        self.tmaps(db, out=tm, precision="fp32" if self.f_groups is None else None)
         maps = t.empty((self.C, self.signs, self.V), device="cuda", dtype=t.float32)
         mx = t.empty((self.C, self.signs, self.n_seg), device="cuda", dtype=t.float32)
         # the observed image is swept once: use the reference's exact arithmetic

@@ -55,7 +55,31 @@ class DesignBatch:
                 invdiag[g, :k] = np.diag(inv if invXX is None else np.asarray(invXX[g], np.float64))
         self.G, self.n, self.kmax, self.ks = G, n, kmax, ks
         self.pinv64, self.X64, self.invdiag64 = pinv, Xp, invdiag
+        self._mats = mats
         self.dof = np.asarray([n - k for k in ks], np.float64)
+
+    def inverse(self):
+        """(G, kmax, kmax) inv(X'X) per design (zero padded), FP64."""
+        if getattr(self, "_inv64", None) is None:
+            inv = np.zeros((self.G, self.kmax, self.kmax), np.float64)
+            for g, m in enumerate(self._mats):
+                k = m.shape[1]
+                inv[g, :k, :k] = np.linalg.inv(m.T @ m)
+            self._inv64 = inv
+        return self._inv64
+
+    def group_blocks(self, groups):
+        """(G, sum w^2) float32: per design, inv(inv(X'X)_SS) of every column
+        group S = (start, width), row-major, concatenated -- the Wald form of
+        the extra sum of squares of dropping S."""
+        inv = self.inverse()
+        out = np.zeros((self.G, sum(w * w for _, w in groups)), np.float64)
+        for g in range(self.G):
+            o = 0
+            for s0, w in groups:
+                out[g, o:o + w * w] = np.linalg.inv(inv[g, s0:s0 + w, s0:s0 + w]).ravel()
+                o += w * w
+        return out.astype(np.float32)
 
     def to_device(self):
         return (dev(self.pinv64.astype(np.float32)), dev(self.X64.astype(np.float32)),
@@ -180,10 +204,16 @@ class TensorCoreOperands:
         return out
 
     def tstat(self, p_tiles, u_rows, x_rows, invd, dof, G, kmax, coef_d, n_coef, out, ldt):
-        _lib.check(self.lib.glm_tstat_tc(ptr(self.yt), ptr(self.shift), ptr(self.Yd), self.V, self.n, self.n_pad,
-                                         self.V, ptr(p_tiles), ptr(u_rows), ptr(x_rows), self.n_sc, ptr(invd),
-                                         ptr(dof), G, kmax, ptr(coef_d), n_coef, ptr(out), ldt, ptr(self.err),
-                                         stream_handle()))
+        self.stat(0, p_tiles, u_rows, x_rows, invd, dof, G, kmax, coef_d, n_coef, out, ldt)
+
+    def stat(self, mode, p_tiles, u_rows, x_rows, invd, dof, G, kmax, coef_d, n_coef, out, ldt, wmat=None):
+        """mode 0: t of coefficients coef_d; 1: RSS; 2: partial F of the column
+        groups coef_d = (start, width) pairs, wmat from DesignBatch.group_blocks."""
+        w_stride = 0 if wmat is None else int(wmat.shape[-1])
+        _lib.check(self.lib.glm_stat_tc(ptr(self.yt), ptr(self.shift), ptr(self.Yd), self.V, self.n, self.n_pad,
+                                        self.V, ptr(p_tiles), ptr(u_rows), ptr(x_rows), self.n_sc, ptr(invd),
+                                        ptr(dof), G, kmax, mode, ptr(coef_d), n_coef, ptr(wmat), w_stride,
+                                        ptr(out), ldt, ptr(self.err), stream_handle()))
 
     def status(self):
         e = int(self.err.item())
@@ -208,3 +238,34 @@ def glm_tstat_tc(Y, designs, coef, ops=None, centre=True):
     t.cuda.synchronize()
     ops.status()
     return out
+
+
+def glm_stat_tc(Y, designs, mode, coef=None, groups=None, ops=None):
+    """Tensor-core GLM outputs for a DesignBatch: mode 't' -> (G, len(coef), V)
+    t maps; 'rss' -> (G, V) residual sums of squares; 'f' -> (G, len(groups), V)
+    partial F of the column groups [(start, width), ...] (glm_typeI's drop-one
+    F, tm/pyfunc.py:2282-2400)."""
+    t = require_cuda()
+    db = designs if isinstance(designs, DesignBatch) else DesignBatch(designs)
+    ops = ops or TensorCoreOperands(dev(Y, t.float32))
+    P8, U, Xt = ops.host_operands(db)
+    pt = ops.tile_designs(dev(P8), db.G, db.kmax)
+    u, xt = dev(U), dev(Xt)
+    invd = dev(db.invdiag64.astype(np.float32))
+    dof = dev(db.dof.astype(np.float32))
+    wmat = None
+    if mode == "t":
+        m, rows, coef_d = 0, len(coef), dev(np.asarray(coef, np.int32))
+    elif mode == "rss":
+        m, rows, coef_d = 1, 1, None
+    elif mode == "f":
+        m, rows = 2, len(groups)
+        coef_d = dev(np.asarray(groups, np.int32).reshape(-1))
+        wmat = dev(db.group_blocks(groups))
+    else:
+        raise ValueError("mode must be 't', 'rss' or 'f'")
+    out = t.empty((db.G, rows, ops.V), device="cuda", dtype=t.float32)
+    ops.stat(m, pt, u, xt, invd, dof, db.G, db.kmax, coef_d, rows, out, ops.V, wmat=wmat)
+    t.cuda.synchronize()
+    ops.status()
+    return out[:, 0] if mode == "rss" else out

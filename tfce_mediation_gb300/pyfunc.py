@@ -192,3 +192,97 @@ def rand_blocks(block_list, is_equal_sizes):
     for block in blocks:
         randindex.append(np.random.permutation(indexer[block_list == block]))
     return np.concatenate(randindex)
+
+
+def _typeI_design(n, exog, dmy_covariates):
+    """[1, exog variables..., covariates] and the column widths of the exog
+    variables (pyfunc.py:2305-2317)."""
+    kvars, cols = [], [np.ones((n, 1))]
+    for var in exog:
+        var = np.asarray(var, np.float64)
+        kvars.append(1 if var.ndim == 1 else var.shape[1])
+        cols.append(var.reshape(n, -1))
+    if dmy_covariates is not None:
+        cols.append(np.asarray(dmy_covariates, np.float64).reshape(n, -1))
+    return np.column_stack(cols), kvars
+
+
+def glm_typeI(endog, exog, dmy_covariates=None, output_fvalues=True, output_tvalues=False, output_pvalues=False,
+              verbose=True, rand_array=None, use_reduced_residuals=False, output_reduced_residuals=False,
+              exog_names=None):
+    """Generalised ANCOVA of the tm-models path, pyfunc.py:2282-2400, on the GPU.
+
+    endog (n, V) or (n,); exog: list of (n,) / (n, k_i) dummy-coded variables;
+    the design is [1, exog..., dmy_covariates], rows permuted by rand_array.
+    Returns the reference's tuples: F (model), the drop-one F of every exog
+    variable, t of every coefficient, P values (scipy, as the reference),
+    reduced residuals.  Model F and t run on the FP32 CUDA-core GLM (TSS around
+    each column's mean); the drop-one F runs on the tensor-core GLM in its
+    exact Wald form (glm_stat_tc mode 2: no difference of residual sums)."""
+    from .glm import WHAT_RESID, glm_fstat, glm_stat_tc
+    y = np.asarray(endog)
+    one = y.ndim == 1
+    Y = np.ascontiguousarray(y.reshape(y.shape[0], -1), np.float32)
+    n = Y.shape[0]
+    X, kvars = _typeI_design(n, exog, dmy_covariates)
+    if rand_array is not None:
+        if use_reduced_residuals:
+            Y = glm_stat(Y, DesignBatch([X]), WHAT_RESID)[0].cpu().numpy()
+        X = X[np.asarray(rand_array)]
+    reduced_data = None
+    if output_reduced_residuals:
+        reduced_data = glm_stat(Y, DesignBatch([X]), WHAT_RESID)[0].cpu().numpy()
+    k = X.shape[1]
+    df_between, df_within, df_total = k - 1, n - k, n - 1
+    db = DesignBatch([X])
+
+    Fvalues = Fvar = Tvalues = None
+    Pvar = []
+    if output_fvalues:
+        Fvalues = glm_fstat(Y, db)[0].cpu().numpy()
+        if verbose:
+            print("Source\t\tDF\tF(Max)")
+            print("Model\t\t(%d,%d)\t%.2f" % (df_between, df_within, Fvalues.max()))
+        groups, start = [], 1
+        for kv in kvars:
+            groups.append((start, kv))
+            start += kv
+        Fvar = glm_stat_tc(Y, db, "f", groups=groups)[0].cpu().numpy()
+        for i, col in enumerate(kvars):
+            if verbose:
+                name = exog_names[i] if exog_names is not None else "Exog%d" % (i + 1)
+                print("%s\t\t(%d,%d)\t%.2f" % (name, col, df_within, Fvar[i].max()))
+    if output_tvalues:
+        Tvalues = glm_stat(Y, db, WHAT_T)[0].cpu().numpy()
+    if one:
+        Fvalues = None if Fvalues is None else Fvalues[0]
+        Fvar = None if Fvar is None else Fvar[:, 0]
+        Tvalues = None if Tvalues is None else Tvalues[:, 0]
+    if output_fvalues and output_pvalues:
+        from scipy.stats import f as fdist
+        Pvar = [fdist.sf(Fvar[i], col, df_within) for i, col in enumerate(kvars)]
+    if output_tvalues and output_fvalues:
+        if output_pvalues:
+            from scipy.stats import f as fdist
+            from scipy.stats import t as tdist
+            return (Fvalues, np.array(Fvar), Tvalues, fdist.sf(Fvalues, df_between, df_within), np.array(Pvar),
+                    tdist.sf(np.abs(Tvalues), df_total) * 2)
+        if output_reduced_residuals:
+            return (Fvalues, np.array(Fvar), Tvalues, reduced_data)
+        return (Fvalues, np.array(Fvar), Tvalues)
+    if output_tvalues:
+        if output_pvalues:
+            from scipy.stats import t as tdist
+            return (Tvalues, tdist.sf(np.abs(Tvalues), df_total) * 2)
+        if output_reduced_residuals:
+            return (Tvalues, reduced_data)
+        return Tvalues
+    if output_fvalues:
+        if output_pvalues:
+            from scipy.stats import f as fdist
+            return (Fvalues, np.array(Fvar), fdist.sf(Fvalues, df_between, df_within), np.array(Pvar))
+        if output_reduced_residuals:
+            return (Fvalues, np.array(Fvar), reduced_data)
+        return (Fvalues, np.array(Fvar))
+    print("No output has been selected")
+    return None
