@@ -94,3 +94,53 @@ def test_engine_f_mode_vs_oracle(config1):
     print("F-mode maxima: median", np.median(rel), "max", rel.max())
     assert np.median(rel) <= 1e-4
     assert rel.max() <= 1e-3
+
+
+def test_tm_models_glm_driver_volume(tmp_path, monkeypatch):
+    """tm_models_randomise GLM branch drop-in on a small volume: the CSV lines
+    against the oracle pipeline (FP64 glm_typeI + C sweep) on the same
+    host-seeded permutations."""
+    import argparse
+    from tfce_mediation_gb300 import adjacency as A
+    from tfce_mediation_gb300 import randomise
+    rng = np.random.default_rng(33)
+    mask = np.zeros((10, 9, 8), bool)
+    mask[1:9, 1:8, 1:7] = True
+    off, idx = A.voxel_csr(mask, 26, "pyfunc")
+    V, n = int(mask.sum()), 40
+    fac = rng.integers(0, 2, n).astype(np.float64)
+    age = rng.standard_normal(n)
+    cov = rng.standard_normal((n, 1))
+    data = rng.standard_normal((n, V)).astype(np.float32)
+    data[:, :60] += (0.7 * age)[:, None].astype(np.float32)
+    d = tmp_path / "tmtemp_GLM_volume"
+    d.mkdir()
+    np.save(d / "exog_flat.npy", np.column_stack([fac, age]))
+    np.save(d / "exog_shape.npy", np.array([1, 1]))
+    np.save(d / "varnames.npy", np.array(["group", "age"]))
+    np.save(d / "gstat.npy", np.array("both"))
+    np.save(d / "data.npy", data)
+    np.save(d / "optstfce.npy", np.array([2.0, 0.5]))
+    np.save(d / "dmy_covariates.npy", cov)
+    adj = np.empty(V, dtype=object)
+    for v in range(V):
+        adj[v] = np.asarray(idx[off[v]:off[v + 1]], np.int64)
+    np.save(d / "adjac.npy", adj, allow_pickle=True)
+    monkeypatch.chdir(tmp_path)
+    opts = argparse.Namespace(range=[0, 5], surface=None, exchangeblock=None, seed=[11], batch=4)
+    randomise.tm_models_glm_run(opts)
+    out = tmp_path / "output_GLM_volume" / "perm_GLM"
+    F_csv = {nm: np.loadtxt(out / f"perm_Fstat_{nm}_TFCE_maxVoxel.csv") for nm in ("group", "age")}
+    T_csv = [np.loadtxt(out / f"perm_Tstat_con{c}_TFCE_maxVoxel.csv") for c in (1, 2)]
+    for p in range(6):
+        perm = np.random.RandomState(11 + p).permutation(n)
+        Fm, Fv, T = oracle.glm_typeI(data, [fac, age], dmy_covariates=cov, rand_array=perm)
+        for j, nm in enumerate(("group", "age")):
+            img = Fv[j].astype(np.float32)
+            ref = oracle.tfce_max_batch(off, idx, img, 2.0, 0.5)[0]
+            assert abs(F_csv[nm][p] - ref) <= 1e-3 * abs(ref) + 1e-3, (nm, p, F_csv[nm][p], ref)
+        for c in (1, 2):
+            for si, s in enumerate((1.0, -1.0)):
+                ref = oracle.tfce_max_batch(off, idx, T[c].astype(np.float32), 2.0, 0.5, sign=s)[0]
+                got = T_csv[c - 1][2 * p + si]
+                assert abs(got - ref) <= 1e-3 * abs(ref) + 1e-3, (c, p, s, got, ref)

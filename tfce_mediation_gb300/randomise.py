@@ -13,6 +13,9 @@ appends the same CSV lines in the same order and format:
 * voxel_mediation_run  -- tmanalysis/voxel_tfce_mediation_randomise.py:42-77
 * mmr_lr_run           -- tm_multisurface/tm_mmr_rand_low_ram_parallel.py:166-207
   (tmi_temp/<s>_*_temp.npy, <path>/perm_maxTFCE_surf<s>_tcon<c>.csv, %f)
+* tm_models_glm_run    -- tmanalysis/tm_models_randomise.py:76-92,193-274 (the GLM branch:
+  tmtemp_GLM_<surface|volume>/, output_GLM_<..>/perm_GLM/perm_Fstat_<var>_TFCE_max*.csv
+  and perm_Tstat_con<c>_TFCE_max*.csv)
 
 Permutations: the reference seeds each iteration from the clock
 (``np.random.seed(int(iter_perm*1000+time()))``); that stays the default.
@@ -117,7 +120,7 @@ def _run_designs(eng, designs, batch):
         tm = eng.tmaps(db)
         mx = eng.sweep_max(tm, db.G * eng.C)
         res.append(mx.cpu().numpy().reshape(db.G, eng.C, eng.signs, eng.n_seg))
-        eng.adj.status()
+        eng.status()
     return np.concatenate(res)
 
 
@@ -296,3 +299,85 @@ def mmr_lr_run(surf_num, perm_range, seed, path, H, E_, pred_x=None, mediation=N
     maxima = eng.run(perms=perms)[:, 0, 0, 0]
     _append(os.path.join(path, "perm_maxTFCE_surf%d_%s_zstat.csv" % (surf_num, medtype)), ["%f" % v for v in maxima])
     return maxima
+
+
+def tm_models_glm_parser(ap=None):
+    ap = ap or argparse.ArgumentParser(description="tm-models GLM permutations (GPU)")
+    ap.add_argument("-r", "--range", nargs=2, type=int, required=True, metavar=("INT", "INT"))
+    ap.add_argument("-s", "--surface", nargs=1, default=None, metavar=("STR",))
+    ap.add_argument("-e", "--exchangeblock", nargs=1, metavar=("*.csv",))
+    ap.add_argument("--seed", nargs=1, type=int, default=None,
+                    help="host-seeded permutation stream RandomState(seed + i) (default: clock seeding)")
+    ap.add_argument("--batch", type=int, default=64)
+    return ap
+
+
+def tm_models_glm_run(opts):
+    """The GLM branch of tm_models_randomise.py (:76-92, :193-274): per
+    permutation of the design rows, glm_typeI's drop-one F of every exog
+    variable (gstat 'f') and/or t of every exog column with both signs
+    (gstat 't'), TFCE maxima appended to the reference's CSVs.  F maps run on
+    the engine's partial-F mode (one sign, as the reference TFCEs F)."""
+    start, stop = int(opts.range[0]), int(opts.range[1]) + 1
+    seed = opts.seed[0] if getattr(opts, "seed", None) else None
+    surface = str(opts.surface[0]) if getattr(opts, "surface", None) else None
+    tempdir = "tmtemp_GLM_%s" % surface if surface else "tmtemp_GLM_volume"
+    outdir = "output_GLM_%s/perm_GLM" % surface if surface else "output_GLM_volume/perm_GLM"
+    exog_flat = _load(f"{tempdir}/exog_flat.npy")
+    exog_shape = [int(c) for c in _load(f"{tempdir}/exog_shape.npy")]
+    varnames = _load(f"{tempdir}/varnames.npy")
+    gstat = str(_load(f"{tempdir}/gstat.npy"))
+    data = _load(f"{tempdir}/data.npy")
+    optstfce = _load(f"{tempdir}/optstfce.npy")
+    cov = _load(f"{tempdir}/dmy_covariates.npy")
+    cov = None if np.all(cov) is None else np.asarray(cov, np.float64)
+    n = data.shape[0]
+    pred_x = exog_flat if cov is None else np.column_stack([exog_flat, cov])
+    X = np.column_stack([np.ones(n), pred_x])
+    groups, s0 = [], 1
+    for w in exog_shape:
+        groups.append((s0, w))
+        s0 += w
+    numcon = sum(exog_shape)
+    H, E_ = float(optstfce[0]), float(optstfce[1])
+    if surface:
+        num_vertex_lh = int(_load(f"{tempdir}/num_vertex_lh.npy"))
+        mask_lh, mask_rh = _load(f"{tempdir}/mask_lh.npy"), _load(f"{tempdir}/mask_rh.npy")
+        adj_lh, adj_rh = _load(f"{tempdir}/adjac_lh.npy"), _load(f"{tempdir}/adjac_rh.npy")
+        vd_lh, vd_rh = _load(f"{tempdir}/vdensity_lh.npy"), _load(f"{tempdir}/vdensity_rh.npy")
+        off, idx, seg = _hemispheres(adj_lh, adj_rh, mask_lh, mask_rh)
+        vd = np.concatenate([_vd(vd_lh, mask_lh), _vd(vd_rh, mask_rh)])
+        kw = dict(segments=seg, vdensity=vd, floor_zero=True)
+        fmt, suffix = "%.4f", "maxVertex"
+        del num_vertex_lh
+    else:
+        off, idx = to_csr(_load(f"{tempdir}/adjac.npy"))
+        kw = dict(segments=None)
+        fmt, suffix = "%1.4f", "maxVoxel"
+    Y = np.ascontiguousarray(data, np.float32)
+    batch = getattr(opts, "batch", 64)
+    designs = _designs_for(X, n, start, stop, opts, seed)
+    os.makedirs(outdir, exist_ok=True)
+    out = {}
+
+    def reduce(m):
+        return m.max(axis=-1) if surface else m[..., 0]
+
+    if gstat != "f":
+        eng = E.PermutationEngine(Y, pred_x, (off, idx), H=H, E=E_, contrasts=list(range(1, numcon + 1)),
+                                  batch=batch, **kw)
+        mt = reduce(_run_designs(eng, designs, eng.batch))  # (P, numcon, 2)
+        for c in range(numcon):
+            lines = []
+            for p in range(mt.shape[0]):
+                lines += [fmt % mt[p, c, 0], fmt % mt[p, c, 1]]
+            _append(os.path.join(outdir, "perm_Tstat_con%d_TFCE_%s.csv" % (c + 1, suffix)), lines)
+        out["t"] = mt
+    if gstat != "t":
+        eng = E.PermutationEngine(Y, pred_x, (off, idx), H=H, E=E_, f_groups=groups, batch=batch, **kw)
+        mf = reduce(_run_designs(eng, designs, eng.batch))  # (P, n_var, 1)
+        for j in range(len(groups)):
+            _append(os.path.join(outdir, "perm_Fstat_%s_TFCE_%s.csv" % (varnames[j], suffix)),
+                    [fmt % mf[p, j, 0] for p in range(mf.shape[0])])
+        out["f"] = mf
+    return out
