@@ -110,3 +110,25 @@ def test_graph_runner_matches_uncaptured(config1, precision):
     np.testing.assert_array_equal(a, b)
     c = eng.run_graph(perms=perms)  # replays again
     np.testing.assert_array_equal(a, c)
+
+
+def test_run_stream_with_new_data_per_step(config1):
+    """run_stream: new host data at chosen steps takes effect exactly from
+    that step (stream order), short batches are padded inside the graph."""
+    import torch
+    st = config1
+    Y2 = (st.Y[::-1].copy() + 0.1).astype(np.float32)
+    kw = dict(segments=st.segments, H=2.0, E=1.0, batch=8)
+    eng = E.PermutationEngine(st.Y, st.pred_x, (st.offsets, st.indices), **kw)
+    e1 = E.PermutationEngine(st.Y, st.pred_x, (st.offsets, st.indices), **kw)
+    e2 = E.PermutationEngine(Y2, st.pred_x, (st.offsets, st.indices), **kw)
+    perms = E.permutations(st.n, 31, 0, 29)
+    P1 = torch.from_numpy(st.Y).pin_memory()
+    P2 = torch.from_numpy(Y2).pin_memory()
+    steps = [(None, perms[0:8]), (P2, perms[8:16]), (None, perms[16:24]), (P1, perms[24:29])]
+    got = eng.run_stream(steps)
+    assert [g.shape[0] for g in got] == [8, 8, 8, 5]
+    np.testing.assert_allclose(got[0], e1.run(perms=perms[0:8]), rtol=1e-6)
+    np.testing.assert_allclose(got[1], e2.run(perms=perms[8:16]), rtol=1e-6)
+    np.testing.assert_allclose(got[2], e2.run(perms=perms[16:24]), rtol=1e-6)
+    np.testing.assert_allclose(got[3], e1.run(perms=perms[24:29]), rtol=1e-6)

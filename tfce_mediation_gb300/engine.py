@@ -291,37 +291,63 @@ class PermutationEngine:
     def run_graph(self, n_perm=None, seed=0, start=0, stop=None, perms=None):
         """Same result as run(), through two captured batch graphs replayed in
         turn: while one batch runs on the GPU the host forms the next batch's
-        design inverses.  A final partial batch runs uncaptured."""
-        t = self.t
+        design inverses (run_stream over the batches)."""
         if perms is None:
             stop = start + n_perm if stop is None else stop
             perms = permutations(self.n, seed, start, stop)
         P = self.batch
-        full = perms.shape[0] // P
+        res = self.run_stream((None, perms[b:b + P]) for b in range(0, perms.shape[0], P))
+        return np.concatenate(res) if res else np.zeros((0, self.C, self.signs, self.n_seg), np.float32)
+
+    def run_stream(self, steps):
+        """The pipelined public entry: one batch per item of `steps`, each a
+        pair (data, perms) -- data: new (n, V) host data in the caller's
+        vertex order (pinned memory keeps the copy asynchronous) or None to
+        keep the resident data; perms: at most `batch` permutation index rows.
+        Two captured batch graphs are replayed in turn.  The host forms a
+        batch's design operators while the GPU runs the previous batch; new
+        data is copied and re-tiled in stream order, after the previous
+        batch's kernels and before this batch's; each batch's maxima come back
+        when its slot is reused or at the end.  A short batch is padded with
+        its last row inside the captured graph and the padding discarded.
+        Returns the per-batch maxima, (rows, C, signs, n_seg) each."""
+        P = self.batch
         if not hasattr(self, "_slots") or self._slots[0]["P"] != P:
             self._slots = [self._graph_slot(P), self._graph_slot(P)]
-        out = []
-        pending = None
-        for b in range(full):
-            slot = self._slots[b % 2]
+        results = {}
+
+        def collect(slot):
+            slot["event"].synchronize()
+            results[slot["order"]] = slot["h_max"].numpy()[: slot["rows"]].copy()
+            slot["busy"] = False
+
+        n_steps = 0
+        for s_, (data, perms) in enumerate(steps):
+            perms = np.asarray(perms)
+            rows = perms.shape[0]
+            if rows == 0:
+                results[s_] = np.zeros((0, self.C, self.signs, self.n_seg), np.float32)
+                n_steps = s_ + 1
+                continue
+            if rows > P:
+                raise ValueError("a step has more permutations than the engine's batch")
+            if rows < P:
+                perms = np.concatenate([perms, np.repeat(perms[-1:], P - rows, axis=0)])
+            slot = self._slots[s_ % 2]
             if slot.get("busy"):
-                slot["event"].synchronize()
-                out.append((slot["order"], slot["h_max"].numpy().copy()))
-                slot["busy"] = False
-            self._fill(slot, perms[b * P:(b + 1) * P])
+                collect(slot)
+            self._fill(slot, perms)
+            if data is not None:
+                self.upload(data)
             slot["graph"].replay()
             slot["event"].record()
-            slot["busy"], slot["order"] = True, b
+            slot["busy"], slot["order"], slot["rows"] = True, s_, rows
+            n_steps = s_ + 1
         for slot in self._slots:
             if slot.get("busy"):
-                slot["event"].synchronize()
-                out.append((slot["order"], slot["h_max"].numpy().copy()))
-                slot["busy"] = False
+                collect(slot)
         self.status()
-        res = [m for _, m in sorted(out, key=lambda x: x[0])]
-        if perms.shape[0] > full * P:
-            res.append(self.run_batch(perms[full * P:]))
-        return np.concatenate(res) if res else np.zeros((0, self.C, self.signs, self.n_seg), np.float32)
+        return [results[i] for i in range(n_steps)]
 
     def observed(self):
         """Unpermuted t maps (C, V) and scaled TFCE maps (C, signs, V) as host arrays
