@@ -224,11 +224,19 @@ __global__ void tile_split_kernel(const float* __restrict__ src, int64_t ld_src,
   }
 }
 
-// Per-column FP64 mean of Y [n][ldy] (the per-vertex centre of the data).
+// Per-column mean of Y [n][ldy] (the per-vertex centre of the data): FP32
+// sums of 16-row blocks accumulated in FP64 (the centre only has to be close
+// to the mean -- the GLM restores the betas with the same value -- and FP64
+// adds are scarce on this part).
 __global__ void col_mean_kernel(const float* __restrict__ Y, int64_t ldy, int n, int64_t V, float* __restrict__ mean) {
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (int64_t)gridDim.x * blockDim.x) {
     double s = 0.0;
-    for (int i = 0; i < n; ++i) s += Y[(int64_t)i * ldy + v];
+    for (int i0 = 0; i0 < n; i0 += 16) {
+      float b = 0.0f;
+      const int i1 = min(n, i0 + 16);
+      for (int i = i0; i < i1; ++i) b += __ldg(Y + (int64_t)i * ldy + v);
+      s += static_cast<double>(b);
+    }
     mean[v] = static_cast<float>(s / n);
   }
 }
