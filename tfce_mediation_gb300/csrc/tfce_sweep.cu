@@ -39,7 +39,6 @@
 
 namespace tfgb {
 
-constexpr int kMaxStepsDbg = 128;
 #ifdef TFGB_PHASE_PROFILE
 // Debug-only: clock64 cycles spent per phase, summed over items (thread 0).
 __device__ unsigned long long g_phase_cycles[8];
@@ -55,7 +54,7 @@ __device__ unsigned long long g_phase_cycles[8];
 // failures, [3] find hops, [4] halving writes, [5] list entries checked.
 __device__ unsigned long long g_dbg_counts[8];
 // Debug-only: cycles of each step's (U+S+A) by threshold index.
-__device__ unsigned long long g_step_cycles[kMaxStepsDbg];
+__device__ unsigned long long g_step_cycles[128];
 #define TFGB_COUNT(k, n) atomicAdd(&g_dbg_counts[k], (unsigned long long)(n))
 #else
 #define TFGB_PHASE_MARK(k) do { } while (0)
@@ -76,9 +75,6 @@ constexpr int kMaxSteps = 128;
 #define TFGB_ALANES 2
 #endif
 constexpr int kSweepThreads = TFGB_SWEEP_THREADS;
-#ifndef TFGB_U_GRAB
-#define TFGB_U_GRAB 1
-#endif
 constexpr int kUBatch = TFGB_UBATCH;   // list entries of one vertex looked up together
 constexpr int kALanes = TFGB_ALANES;   // positions per thread per accumulation round
 #ifndef TFGB_SLANES
@@ -456,13 +452,9 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
       // vertex's list is read kUBatch entries at a time with all their key
       // lookups issued together; the root of the vertex's component is kept
       // as a hint between unions.
-#if TFGB_U_GRAB
       // each thread takes the next unprocessed vertex of the step from a
       // shared cursor, so threads with short walks do not wait for slow ones
       for (int32_t p = atomicAdd(&sGrab, 1); p < s1; p = atomicAdd(&sGrab, 1)) {
-#else
-      for (int32_t p = s0 + tid; p < s1; p += nth) {
-#endif
         int32_t v = -1;  // the vertex: read when needed
         int64_t e0, e1;
         const int32_t pk = kLazy ? reinterpret_cast<const int32_t*>(sl.acc)[p] : -1;
