@@ -205,9 +205,10 @@ __device__ inline int32_t find_root(int32_t* parent, int32_t x, int32_t* err) {
 }
 
 // Join the component of root-hint `a` with position b; returns the root of
-// the joined component (a hint: another thread may link it later).
+// the joined component (a hint: another thread may link it later).  A linked
+// root older than fresh_lo is appended to the dead list.
 __device__ inline int32_t unite(int32_t* parent, int32_t a, int32_t b, int32_t* dead,
-                                int32_t* n_dead, int32_t* err) {
+                                int32_t* n_dead, int32_t fresh_lo, int32_t* err) {
   TFGB_COUNT(0, 1);
   for (int it = 0; it < kWalkLimit; ++it) {
     a = find_root(parent, a, err);
@@ -218,8 +219,9 @@ __device__ inline int32_t unite(int32_t* parent, int32_t a, int32_t b, int32_t* 
     const int32_t old = atomicCAS(parent + hi, hi, lo);
     if (old != hi) TFGB_COUNT(2, 1);
     if (old == hi) {
-      const int32_t q = atomicAdd(n_dead, 1);
-      dead[q] = hi;
+      // roots activated at this step (positions >= fresh_lo) are found by the
+      // size phase in the step's own position range; older ones are listed
+      if (hi < fresh_lo) dead[atomicAdd(n_dead, 1)] = hi;
       return lo;
     }
   }
@@ -564,8 +566,11 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
 #pragma unroll
           for (int m = 0; m <= kUBatch; ++m) {
             if (lk[m] < 0) continue;
-            if (old[m] == lk[m]) sl.dead[atomicAdd(&sNDead, 1)] = lk[m];
-            else tgt = unite(sl.parent, tgt, lk[m], sl.dead, &sNDead, a.err);
+            if (old[m] == lk[m]) {
+              if (lk[m] < s0) sl.dead[atomicAdd(&sNDead, 1)] = lk[m];  // new roots: found by (S) in [s0, s1)
+            } else {
+              tgt = unite(sl.parent, tgt, lk[m], sl.dead, &sNDead, s0, a.err);
+            }
           }
           rp = tgt;
         }
@@ -573,16 +578,25 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
       __syncthreads();
       if (tid == 0) sGrab = s1;  // the next step's first position
       TFGB_PHASE_MARK(2);
-      // (S) linked roots hand their extent to their final root.  Each thread
-      // takes kSLanes dead roots per round and walks them in lockstep.
+      // (S) linked roots hand their extent to their final root: the listed
+      // older roots and the positions of this step that are no longer roots.
+      // Each thread takes kSLanes of them per round and walks them in
+      // lockstep from their parents; parent[d] is rewritten only when the
+      // final root is not already its parent.
       const int32_t nd = sNDead;
-      for (int32_t q0 = atomicAdd(&sGrabS, kSLanes); q0 < nd; q0 = atomicAdd(&sGrabS, kSLanes)) {
-        int32_t d[kSLanes], c[kSLanes];
+      const int32_t nsp = nd + (s1 - s0);
+      for (int32_t q0 = atomicAdd(&sGrabS, kSLanes); q0 < nsp; q0 = atomicAdd(&sGrabS, kSLanes)) {
+        int32_t d[kSLanes], c[kSLanes], pd[kSLanes];
 #pragma unroll
         for (int k = 0; k < kSLanes; ++k) {
           const int32_t q = q0 + k;
-          d[k] = (q < nd) ? sl.dead[q] : -1;
-          c[k] = d[k];
+          d[k] = (q < nd) ? sl.dead[q] : (q < nsp ? s0 + (q - nd) : -1);
+        }
+#pragma unroll
+        for (int k = 0; k < kSLanes; ++k) {
+          pd[k] = (d[k] >= 0) ? ld_state(sl.parent + d[k]) : -1;
+          if (pd[k] == d[k]) d[k] = -1;  // still a root
+          c[k] = (d[k] >= 0) ? pd[k] : -1;
         }
         for (int it = 0;; ++it) {
           if (it >= kWalkLimit) {
@@ -622,7 +636,7 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
         for (int k = 0; k < kSLanes; ++k) {
           if (d[k] < 0) continue;
           atomicAdd(sl.size + c[k], sz[k]);
-          st_state(sl.parent + d[k], c[k]);
+          if (c[k] != pd[k]) st_state(sl.parent + d[k], c[k]);
           if constexpr (kLazy) {
             sl.link[d[k]] = c[k];
             sl.W[d[k]] = wd[k] - wr[k];
