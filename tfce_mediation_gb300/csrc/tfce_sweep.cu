@@ -18,10 +18,11 @@
 //      larger root under the smaller, so parent[x] < x and walks end).  A
 //      thread takes the next new vertex from a shared cursor, walks the roots
 //      of all its effective neighbours in lockstep (one round of loads per
-//      hop, path halving) and links every distinct root under the smallest
-//      with CASes issued together; a lost race falls back to a general unite;
-//      (S) the roots that were linked this step hand their extent to their new
-//      root; (A) every active vertex adds (float)(extent^E * HH_i) to its own
+//      hop; path halving in the exact mode) and links every distinct root
+//      under the smallest with CASes issued together; a lost race falls back
+//      to a general unite; (S) the roots that were linked this step hand their
+//      extent to their final root and point at it; (A) every active vertex
+//      adds (float)(extent^E * HH_i) to its own
 //      accumulator, in threshold order -- the reference's per-vertex
 //      arithmetic, so results are bit-identical to it;
 //   4. the map is scaled by max/100 (and vdensity), reduced to its max, and
@@ -129,10 +130,9 @@ struct Slot {
   float* acc;
   int32_t* dead;
   // per-component accumulation only
-  int32_t* link;     // root a dead root joined (itself while it is a root)
   int32_t* roots_a;  // live roots after the previous threshold ...
   int32_t* roots_b;  // ... and after this one (swapped every step)
-  double* W;         // root: increments so far; dead: potential to its link
+  double* W;         // root: increments so far; dead: potential to its parent (the root it joined)
 };
 
 __host__ __device__ inline int64_t align_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
@@ -141,19 +141,18 @@ __host__ __device__ inline int64_t slot_bytes(int32_t vcap) {
   return 6 * align_up((int64_t)vcap * 4, 256);
 }
 
-// Per-component accumulation adds link, two root lists and a double per
-// vertex to the six int32/float arrays of the exact mode.
+// Per-component accumulation adds two root lists and a double per vertex to
+// the six int32/float arrays of the exact mode.
 __host__ __device__ inline int64_t slot_bytes_lazy(int32_t vcap) {
-  return 9 * align_up((int64_t)vcap * 4, 256) + align_up((int64_t)vcap * 8, 256);
+  return 8 * align_up((int64_t)vcap * 4, 256) + align_up((int64_t)vcap * 8, 256);
 }
 
 __device__ inline Slot make_slot(char* base, int32_t vcap) {
   const int64_t s = align_up((int64_t)vcap * 4, 256);
   Slot sl;
-  sl.link = reinterpret_cast<int32_t*>(base + 6 * s);
-  sl.roots_a = reinterpret_cast<int32_t*>(base + 7 * s);
-  sl.roots_b = reinterpret_cast<int32_t*>(base + 8 * s);
-  sl.W = reinterpret_cast<double*>(base + 9 * s);
+  sl.roots_a = reinterpret_cast<int32_t*>(base + 6 * s);
+  sl.roots_b = reinterpret_cast<int32_t*>(base + 7 * s);
+  sl.W = reinterpret_cast<double*>(base + 8 * s);
   sl.key = reinterpret_cast<uint32_t*>(base);
   sl.order = reinterpret_cast<int32_t*>(base + s);
   sl.parent = reinterpret_cast<int32_t*>(base + 2 * s);
@@ -188,6 +187,7 @@ __device__ inline void st_state(int32_t* p, int32_t v) { __stcg(p, v); }
 // non-root's new parent is one of its ancestors, so concurrent walks and links
 // stay consistent.  parent[] entries only point to smaller positions, so the
 // walk ends; the limit is a second guard.
+template <bool kHalve = true>
 __device__ inline int32_t find_root(int32_t* parent, int32_t x, int32_t* err) {
   for (int it = 0; it < kWalkLimit; ++it) {
     const int32_t p = ld_state(parent + x);
@@ -196,7 +196,7 @@ __device__ inline int32_t find_root(int32_t* parent, int32_t x, int32_t* err) {
     const int32_t g = ld_state(parent + p);
     TFGB_COUNT(3, 1);
     if (g == p) return p;
-    st_state(parent + x, g);
+    if (kHalve) st_state(parent + x, g);
     TFGB_COUNT(4, 1);
     x = g;
   }
@@ -207,12 +207,13 @@ __device__ inline int32_t find_root(int32_t* parent, int32_t x, int32_t* err) {
 // Join the component of root-hint `a` with position b; returns the root of
 // the joined component (a hint: another thread may link it later).  A linked
 // root older than fresh_lo is appended to the dead list.
+template <bool kHalve = true>
 __device__ inline int32_t unite(int32_t* parent, int32_t a, int32_t b, int32_t* dead,
                                 int32_t* n_dead, int32_t fresh_lo, int32_t* err) {
   TFGB_COUNT(0, 1);
   for (int it = 0; it < kWalkLimit; ++it) {
-    a = find_root(parent, a, err);
-    b = find_root(parent, b, err);
+    a = find_root<kHalve>(parent, a, err);
+    b = find_root<kHalve>(parent, b, err);
     if (a == b) return a;
     const int32_t hi = max(a, b), lo = min(a, b);
     TFGB_COUNT(1, 1);
@@ -283,7 +284,8 @@ __device__ inline float block_max(float v, float* red) {
 // accumulation -- each live root adds its component's increment to a double
 // once per threshold; a root that is linked keeps its potential relative to
 // the root it joins, and a vertex's value is the sum of potentials along its
-// link chain, rounded to float once.  Per threshold that is O(live
+// parent chain (no path halving in this mode, so a dead root's parent stays
+// the root it joined), rounded to float once.  Per threshold that is O(live
 // components) instead of O(active vertices); the result is the exact sum of
 // the same float increments, so it differs from the reference only by the
 // reference's own float summation error.
@@ -298,6 +300,10 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
 
   Slot sl = make_slot(a.ws + (int64_t)blockIdx.x * a.ws_slot_bytes, a.vcap);
   const int tid = threadIdx.x, nth = blockDim.x;
+  // Per-component mode keeps every dead root's parent at the root it joined
+  // (no path halving), so parent[] is also the chain of the potentials; the
+  // exact mode halves paths.
+  constexpr bool kHalve = !kLazy;
 #ifdef TFGB_PHASE_PROFILE
   long long _pt = clock64();
 #endif
@@ -423,7 +429,6 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
         sl.size[p] = 1;
         if constexpr (kLazy) {
           sl.W[p] = 0.0;
-          sl.link[p] = p;
           // the vertex's list (start relative to the segment's, degree) by
           // position, so the union phase reads it without a dependent load;
           // -1: out of the packed range, read the offsets
@@ -537,12 +542,12 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
 #pragma unroll
             for (int k = 0; k < kUBatch; ++k) {
               if (par[k] != cur[k]) {
-                if (gp[k] != par[k]) st_state(sl.parent + cur[k], gp[k]);  // halve the path
+                if (kHalve && gp[k] != par[k]) st_state(sl.parent + cur[k], gp[k]);  // halve the path
                 cur[k] = gp[k];
               }
             }
             if (pr != rr) {
-              if (gr != pr) st_state(sl.parent + rr, gr);
+              if (kHalve && gr != pr) st_state(sl.parent + rr, gr);
               rr = gr;
             }
           }
@@ -569,7 +574,7 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
             if (old[m] == lk[m]) {
               if (lk[m] < s0) sl.dead[atomicAdd(&sNDead, 1)] = lk[m];  // new roots: found by (S) in [s0, s1)
             } else {
-              tgt = unite(sl.parent, tgt, lk[m], sl.dead, &sNDead, s0, a.err);
+              tgt = unite<kHalve>(sl.parent, tgt, lk[m], sl.dead, &sNDead, s0, a.err);
             }
           }
           rp = tgt;
@@ -616,7 +621,7 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
 #pragma unroll
           for (int k = 0; k < kSLanes; ++k) {
             if (par[k] != c[k]) {
-              if (gp[k] != par[k]) st_state(sl.parent + c[k], gp[k]);  // halve the path
+              if (kHalve && gp[k] != par[k]) st_state(sl.parent + c[k], gp[k]);  // halve the path
               c[k] = gp[k];
             }
           }
@@ -638,7 +643,6 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
           atomicAdd(sl.size + c[k], sz[k]);
           if (c[k] != pd[k]) st_state(sl.parent + d[k], c[k]);
           if constexpr (kLazy) {
-            sl.link[d[k]] = c[k];
             sl.W[d[k]] = wd[k] - wr[k];
           }
         }
@@ -754,14 +758,14 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
 
     // ---- 4. scale, reduce, write
     if constexpr (kLazy) {
-      // resolve every active vertex: sum of potentials along its link chain
+      // resolve every active vertex: sum of potentials along its parent chain
       for (int32_t p = tid; p < n_act; p += nth) {
         double sum = sl.W[p];
-        int32_t c = p, l = sl.link[p];
+        int32_t c = p, l = sl.parent[p];
         for (int it = 0; l != c && it < kWalkLimit; ++it) {
           c = l;
           sum += sl.W[c];
-          l = sl.link[c];
+          l = sl.parent[c];
         }
         if (a.out_mode == 2 && omap) sum += static_cast<double>(omap[sl.order[p]]);
         sl.acc[p] = __double2float_rn(sum);
