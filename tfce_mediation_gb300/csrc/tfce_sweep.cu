@@ -122,6 +122,15 @@ struct SweepArgs {
   int64_t n_entries;
 };
 
+// Per-component mode: the increments so far (root) or the potential to the
+// root joined (dead root) and the extent of a position, in one 16-byte record
+// so that the size and accumulation phases touch one sector per position.
+struct alignas(16) Rec {
+  double w;
+  int32_t size;
+  int32_t pad;
+};
+
 struct Slot {
   uint32_t* key;
   int32_t* order;
@@ -132,7 +141,7 @@ struct Slot {
   // per-component accumulation only
   int32_t* roots_a;  // live roots after the previous threshold ...
   int32_t* roots_b;  // ... and after this one (swapped every step)
-  double* W;         // root: increments so far; dead: potential to its parent (the root it joined)
+  Rec* rec;          // {W, extent} per position
 };
 
 __host__ __device__ inline int64_t align_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
@@ -141,10 +150,10 @@ __host__ __device__ inline int64_t slot_bytes(int32_t vcap) {
   return 6 * align_up((int64_t)vcap * 4, 256);
 }
 
-// Per-component accumulation adds two root lists and a double per vertex to
-// the six int32/float arrays of the exact mode.
+// Per-component accumulation adds two root lists and a 16-byte {W, extent}
+// record per vertex to the six int32/float arrays of the exact mode.
 __host__ __device__ inline int64_t slot_bytes_lazy(int32_t vcap) {
-  return 8 * align_up((int64_t)vcap * 4, 256) + align_up((int64_t)vcap * 8, 256);
+  return 8 * align_up((int64_t)vcap * 4, 256) + align_up((int64_t)vcap * 16, 256);
 }
 
 __device__ inline Slot make_slot(char* base, int32_t vcap) {
@@ -152,7 +161,7 @@ __device__ inline Slot make_slot(char* base, int32_t vcap) {
   Slot sl;
   sl.roots_a = reinterpret_cast<int32_t*>(base + 6 * s);
   sl.roots_b = reinterpret_cast<int32_t*>(base + 7 * s);
-  sl.W = reinterpret_cast<double*>(base + 8 * s);
+  sl.rec = reinterpret_cast<Rec*>(base + 8 * s);
   sl.key = reinterpret_cast<uint32_t*>(base);
   sl.order = reinterpret_cast<int32_t*>(base + s);
   sl.parent = reinterpret_cast<int32_t*>(base + 2 * s);
@@ -426,9 +435,8 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
         key = (static_cast<uint32_t>(lv) << kPosBits) | static_cast<uint32_t>(p);
         sl.order[p] = v;
         sl.parent[p] = p;
-        sl.size[p] = 1;
         if constexpr (kLazy) {
-          sl.W[p] = 0.0;
+          sl.rec[p] = Rec{0.0, 1, 0};
           // the vertex's list (start relative to the segment's, degree) by
           // position, so the union phase reads it without a dependent load;
           // -1: out of the packed range, read the offsets
@@ -436,6 +444,7 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
           reinterpret_cast<int32_t*>(sl.acc)[p] =
               (deg <= 63 && rel >= 0 && rel < (int64_t(1) << 25)) ? static_cast<int32_t>((rel << 6) | deg) : -1;
         } else {
+          sl.size[p] = 1;
           sl.acc[p] = (a.out_mode == 2 && omap) ? omap[v] : 0.0f;
         }
       }
@@ -631,19 +640,23 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
 #pragma unroll
         for (int k = 0; k < kSLanes; ++k) {
           if (d[k] < 0) continue;
-          sz[k] = ld_state(sl.size + d[k]);
           if constexpr (kLazy) {
-            wd[k] = sl.W[d[k]];
-            wr[k] = sl.W[c[k]];
+            const Rec rd = sl.rec[d[k]];
+            sz[k] = rd.size;
+            wd[k] = rd.w;
+            wr[k] = sl.rec[c[k]].w;
+          } else {
+            sz[k] = ld_state(sl.size + d[k]);
           }
         }
 #pragma unroll
         for (int k = 0; k < kSLanes; ++k) {
           if (d[k] < 0) continue;
-          atomicAdd(sl.size + c[k], sz[k]);
+          if constexpr (kLazy) atomicAdd(&sl.rec[c[k]].size, sz[k]);
+          else atomicAdd(sl.size + c[k], sz[k]);
           if (c[k] != pd[k]) st_state(sl.parent + d[k], c[k]);
           if constexpr (kLazy) {
-            sl.W[d[k]] = wd[k] - wr[k];
+            sl.rec[d[k]].w = wd[k] - wr[k];
           }
         }
       }
@@ -681,12 +694,13 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
 #pragma unroll
           for (int k = 0; k < kALanes; ++k) {
             if (!is_root[k]) continue;
-            sz[k] = ld_state(sl.size + c[k]);
-            w[k] = sl.W[c[k]];
+            const Rec rc = sl.rec[c[k]];
+            sz[k] = rc.size;
+            w[k] = rc.w;
           }
 #pragma unroll
           for (int k = 0; k < kALanes; ++k)
-            if (is_root[k]) sl.W[c[k]] = w[k] + static_cast<double>(increment(sz[k], E, e_mode, HHl));
+            if (is_root[k]) sl.rec[c[k]].w = w[k] + static_cast<double>(increment(sz[k], E, e_mode, HHl));
           const unsigned mask = __activemask();
           const int lane = tid & 31;
 #pragma unroll
@@ -760,11 +774,11 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
     if constexpr (kLazy) {
       // resolve every active vertex: sum of potentials along its parent chain
       for (int32_t p = tid; p < n_act; p += nth) {
-        double sum = sl.W[p];
+        double sum = sl.rec[p].w;
         int32_t c = p, l = sl.parent[p];
         for (int it = 0; l != c && it < kWalkLimit; ++it) {
           c = l;
-          sum += sl.W[c];
+          sum += sl.rec[c].w;
           l = sl.parent[c];
         }
         if (a.out_mode == 2 && omap) sum += static_cast<double>(omap[sl.order[p]]);
