@@ -73,13 +73,13 @@ constexpr int kMaxSteps = 128;
 #define TFGB_UBATCH 6
 #endif
 #ifndef TFGB_ALANES
-#define TFGB_ALANES 2
+#define TFGB_ALANES 1
 #endif
 constexpr int kSweepThreads = TFGB_SWEEP_THREADS;
 constexpr int kUBatch = TFGB_UBATCH;   // list entries of one vertex looked up together
 constexpr int kALanes = TFGB_ALANES;   // positions per thread per accumulation round
 #ifndef TFGB_SLANES
-#define TFGB_SLANES 2
+#define TFGB_SLANES 1
 #endif
 constexpr int kSLanes = TFGB_SLANES;   // dead roots per thread per size round
 constexpr uint32_t kOneWay = 0x80000000u;   // entry whose reverse entry is missing
