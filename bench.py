@@ -249,7 +249,7 @@ def run_gpu(args):
         ops = []
         for p in perms:
             db = DesignBatch(eng.X[p])
-            P8, U, Xt = tc.host_operands(db)
+            P8, U, Xt = tc.host_operands(db, centred=eng._centred)
             ops.append((dev(P8), dev(U), dev(Xt), dev(db.invdiag64.astype(np.float32)),
                         dev(db.dof.astype(np.float32))))
         pt_buf = tc.tile_designs(ops[0][0], P, eng.k)
@@ -267,7 +267,7 @@ def run_gpu(args):
         if tc is not None:
             P8d, Ud, Xtd, invd, dof = ops[s]
             tc.tile_designs(P8d, P, eng.k, out=pt_buf)
-            tc.tstat(pt_buf, Ud, Xtd, invd, dof, P, eng.k, eng._coef, C, eng._tbuf, V)
+            tc.stat(0, pt_buf, Ud, Xtd, invd, dof, P, eng.k, eng._coef, C, eng._tbuf, V, centred=eng._centred)
         else:
             pinv, Xp, invd, dof = ops[s]
             _lib.check(lib.glm_tstat(ptr(eng.Yd), V, n, V, ptr(pinv), ptr(Xp), ptr(invd), ptr(dof), P, eng.k,
@@ -383,9 +383,10 @@ def run_gpu(args):
     clocks = clk.summary()
     if tc is not None:
         # split-BF16 GEMM: 3 MMAs of M=V, N=8 rows per design, K=n_pad; residual
-        # epilogue: (k+1) FP32 FMAs per vertex, design and subject
+        # epilogue: (k+1) FP32 FMAs per vertex, design and subject (k with the
+        # centred form)
         mma_flop = 2.0 * 3 * V * 8 * tc.padded(P, eng.k) * tc.n_pad
-        epi_flop = 2.0 * (eng.k + 1) * n * V * P
+        epi_flop = 2.0 * (eng.k + (0 if eng._centred else 1)) * n * V * P
         glm_info = {"precision": "bf16x3", "kernels": "tile_split_kernel + glm_tc_kernel<%d>" % eng.k,
                     "ms_per_launch": glm_avg,
                     "tensor_tflops_issued": mma_flop / (glm_avg / 1000) / 1e12,

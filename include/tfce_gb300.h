@@ -234,8 +234,17 @@ int glm_tstat_tc(const void* y_tiles, const float* y_shift, const float* Y, int6
  *     extra sum of squares in its exact form b_S' inv(inv(X'X)_SS) b_S; wmat
  *     [G][w_stride] holds, per design, the groups' inv(inv(X'X)_SS) blocks
  *     (row-major, concatenated in group order).  A group outside [0, kmax)
- *     yields NaN. */
-int glm_stat_tc(const void* y_tiles, const float* y_shift, const float* Y, int64_t ldy, int32_t n,
+ *     yields NaN.
+ *   Y_centred (optional): Y minus its per-vertex centre (glm_col_center with
+ *     y_shift); only for designs whose first column is all ones and whose
+ *     x_rows hold the other columns minus their means: the residuals are then
+ *     formed without the intercept term (one FMA fewer per vertex, design and
+ *     subject); coefficient 0 is then not available (t of it, or a group
+ *     holding it, is returned as 0). */
+int glm_col_center(const float* Y, int64_t ldy, int32_t n, int64_t V, const float* centre, float* out,
+                   void* stream);
+int glm_stat_tc(const void* y_tiles, const float* y_shift, const float* Y, const float* Y_centred, int64_t ldy,
+                int32_t n,
                 int32_t n_pad, int64_t V, const void* p_tiles, const float* u_rows, const float* x_rows,
                 int32_t n_sc, const float* invdiag, const float* dof, int32_t G, int32_t kmax, int32_t mode,
                 const int32_t* coef, int32_t n_coef, const float* wmat, int32_t w_stride, float* t_out,

@@ -80,10 +80,14 @@ def test_voxel_engine_E_half_vs_oracle():
 
 def test_multisurface_segments_per_segment_HE():
     """Uneven surfaces plus a voxel skeleton in one launch, own H/E each
-    (mmr-lr semantics, one permutation stream for all surfaces)."""
+    (mmr-lr semantics, one permutation stream for all surfaces).  The t maps
+    come from the FP32 GLM (~1e-6 of FP64) so that the per-value bar tests the
+    segment handling: on segments of a few hundred vertices one vertex moving
+    across a threshold under the split-BF16 GLM's ~2e-5 can move a maximum by
+    more than 1e-3."""
     st = synth.config4_mmr(seed=5, n=40, levels=[2, 3, 2, 4], skeleton_voxels=600, passes=3)
     eng = E.PermutationEngine(st.Y, st.pred_x, (st.offsets, st.indices), st.segments, st.H, st.E,
-                              floor_zero=False, batch=6)
+                              floor_zero=False, batch=6, precision="fp32")
     perms = E.permutations(st.n, 77, 0, 6)
     got = eng.run(perms=perms)  # (P, C, 2, S)
     X = st.design()

@@ -73,7 +73,8 @@ SIGNATURES = {
     "glm_tstat_tc": (ctypes.c_int, [c_vp, c_vp, c_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
                                     ctypes.c_int64, c_vp, c_vp, c_vp, ctypes.c_int32, c_vp, c_vp, ctypes.c_int32,
                                     ctypes.c_int32, c_vp, ctypes.c_int32, c_vp, ctypes.c_int64, c_vp, c_vp]),
-    "glm_stat_tc": (ctypes.c_int, [c_vp, c_vp, c_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
+    "glm_col_center": (ctypes.c_int, [c_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int64, c_vp, c_vp, c_vp]),
+    "glm_stat_tc": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
                                    ctypes.c_int64, c_vp, c_vp, c_vp, ctypes.c_int32, c_vp, c_vp, ctypes.c_int32,
                                    ctypes.c_int32, ctypes.c_int32, c_vp, ctypes.c_int32, c_vp, ctypes.c_int32,
                                    c_vp, ctypes.c_int64, c_vp, c_vp]),

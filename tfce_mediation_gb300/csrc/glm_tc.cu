@@ -241,12 +241,24 @@ __global__ void col_mean_kernel(const float* __restrict__ Y, int64_t ldy, int n,
   }
 }
 
+// out = Y minus each column's centre (the data centred per vertex).
+__global__ void col_center_kernel(const float* __restrict__ Y, int64_t ldy, int n, int64_t V,
+                                  const float* __restrict__ centre, float* __restrict__ out) {
+  const int64_t total = (int64_t)n * V;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / V, v = e % V;
+    out[i * ldy + v] = Y[i * ldy + v] - centre[v];
+  }
+}
+
 // --- the GEMM + residual epilogue -----------------------------------------------
 struct TcArgs {
   const __nv_bfloat16* yt;  // pre-tiled data, 128-vertex row blocks
   const __nv_bfloat16* pt;  // pre-tiled pseudoinverse rows, DB*8-row blocks
   const float* xt;          // [n_db][n_sc][kmax][DB] negated design rows (zero padded)
   const float* Y;           // FP32 data [n][ldy]
+  const float* Yc;          // data minus its per-vertex centre (or null): with it every design has an
+                            // intercept and its rows come centred, so residuals skip the intercept term
   const float* shift;       // per-vertex centre subtracted before the split (or null)
   const float* u;           // [G_pad][kmax] pinv(X_d).1 (with shift)
   const float* invdiag;     // [G][kmax]
@@ -259,8 +271,11 @@ struct TcArgs {
   int32_t* err;
 };
 
-template <int KMAX>
+template <int KMAX, bool kCentred>
 __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
+  // centred form: r = (y - c) - Xc b[1..] for designs with an intercept
+  // (column means removed from the other columns; c the data's centre)
+  constexpr int J0 = kCentred ? 1 : 0;
   constexpr int DPT = tc_dpt(KMAX);
   constexpr int DB = tc_db(KMAX);
   constexpr int N = tc_n(KMAX);
@@ -397,7 +412,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
       const float m = (a.shift != nullptr && v0 + vv < a.V) ? __ldg(a.shift + v0 + vv) : 0.0f;
 #pragma unroll
       for (int j = 0; j < KMAX; ++j) {
-        const float bv = failed ? 0.0f : fmaf(m, u[j], sB[(d * KMAX + j) * kTcBld + vl0 + vv]);
+        const float bv = (failed || j < J0) ? 0.0f : fmaf(m, u[j], sB[(d * KMAX + j) * kTcBld + vl0 + vv]);
         if (vv & 1) bp[vv / 2][j].y = bv; else bp[vv / 2][j].x = bv;
       }
     }
@@ -417,7 +432,8 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
       const int i = c * kTcSubjChunk + e / kTcM;
       const int64_t v = vt0 + e % kTcM;
       const bool ok = i < a.n && v < a.V;
-      cp_async4(dst + XC + e * 4, ok ? a.Y + (int64_t)i * a.ldy + v : a.Y, ok ? 4u : 0u);
+      const float* ysrc = kCentred ? a.Yc : a.Y;
+      cp_async4(dst + XC + e * 4, ok ? ysrc + (int64_t)i * a.ldy + v : ysrc, ok ? 4u : 0u);
     }
     cp_async_commit();
   };
@@ -438,7 +454,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
       for (int ii = 0; ii < kTcSubjChunk; ++ii) {
         float2 xj[KMAX];
 #pragma unroll
-        for (int j = 0; j < KMAX; ++j) {
+        for (int j = J0; j < KMAX; ++j) {
           const float x = xs[(ii * KMAX + j) * DB + d];
           xj[j] = make_float2(x, x);
         }
@@ -448,7 +464,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
           const float4 yv = yr[q4];
           float2 r0 = make_float2(yv.x, yv.y), r1 = make_float2(yv.z, yv.w);
 #pragma unroll
-          for (int j = 0; j < KMAX; ++j) {
+          for (int j = J0; j < KMAX; ++j) {
             r0 = __ffma2_rn(xj[j], bp[2 * q4][j], r0);
             r1 = __ffma2_rn(xj[j], bp[2 * q4 + 1][j], r1);
           }
@@ -470,7 +486,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
           if (v0 + vv < a.V) {
             float bj = 0.0f;
 #pragma unroll
-            for (int jj = 0; jj < KMAX; ++jj)
+            for (int jj = J0; jj < KMAX; ++jj)
               if (jj == j) bj = (vv & 1) ? bp[vv / 2][jj].y : bp[vv / 2][jj].x;
             const float rs = (vv & 1) ? rss[vv / 2].y : rss[vv / 2].x;
             dst[vv] = bj / sqrtf(rs * inv_dof * dj);
@@ -494,7 +510,8 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
 #pragma unroll
       for (int vv = 0; vv < VT; ++vv) {
 #pragma unroll
-        for (int jj = 0; jj < KMAX; ++jj) mine[vv * (KMAX + 1) + jj] = (vv & 1) ? bp[vv / 2][jj].y : bp[vv / 2][jj].x;
+        for (int jj = 0; jj < KMAX; ++jj)
+          mine[vv * (KMAX + 1) + jj] = (jj < J0) ? 0.0f : ((vv & 1) ? bp[vv / 2][jj].y : bp[vv / 2][jj].x);
         mine[vv * (KMAX + 1) + KMAX] = (vv & 1) ? rss[vv / 2].y : rss[vv / 2].x;
       }
       const float dof = __ldg(a.dof + g);
@@ -526,9 +543,14 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
 template <int KMAX>
 static int launch_tc(const TcArgs& a, int64_t n_vb, cudaStream_t stream) {
   const int smem = tc_smem(KMAX);
-  TFGB_CUDA(cudaFuncSetAttribute(glm_tc_kernel<KMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   const int64_t grid = n_vb * a.n_db;
-  glm_tc_kernel<KMAX><<<static_cast<unsigned>(grid), kTcThreads, smem, stream>>>(a);
+  if (a.Yc != nullptr) {
+    TFGB_CUDA(cudaFuncSetAttribute(glm_tc_kernel<KMAX, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    glm_tc_kernel<KMAX, true><<<static_cast<unsigned>(grid), kTcThreads, smem, stream>>>(a);
+  } else {
+    TFGB_CUDA(cudaFuncSetAttribute(glm_tc_kernel<KMAX, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    glm_tc_kernel<KMAX, false><<<static_cast<unsigned>(grid), kTcThreads, smem, stream>>>(a);
+  }
   TFGB_CUDA(cudaGetLastError());
   return TFCE_OK;
 }
@@ -559,6 +581,19 @@ int glm_col_mean(const float* Y, int64_t ldy, int32_t n, int64_t V, float* mean,
   return TFCE_OK;
 }
 
+int glm_col_center(const float* Y, int64_t ldy, int32_t n, int64_t V, const float* centre, float* out,
+                   void* stream) {
+  tfgb::clear_error();
+  TFGB_CHECK_ARG(Y && centre && out, "NULL pointer");
+  TFGB_CHECK_ARG(n > 0 && V >= 0 && ldy >= V, "bad sizes");
+  if (V == 0) return TFCE_OK;
+  const int64_t total = (int64_t)n * V;
+  const unsigned blocks = static_cast<unsigned>(std::min<int64_t>((total + 255) / 256, 152 * 32));
+  tfgb::col_center_kernel<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(Y, ldy, n, V, centre, out);
+  TFGB_CUDA(cudaGetLastError());
+  return TFCE_OK;
+}
+
 int glm_tile_split(const float* src, int64_t ld_src, int32_t transpose, int64_t rows, int32_t cols,
                    const float* row_shift, int32_t row_block, int32_t n_pad, void* dst, void* stream) {
   tfgb::clear_error();
@@ -578,7 +613,8 @@ int glm_tile_split(const float* src, int64_t ld_src, int32_t transpose, int64_t 
   return TFCE_OK;
 }
 
-int glm_stat_tc(const void* y_tiles, const float* y_shift, const float* Y, int64_t ldy, int32_t n,
+int glm_stat_tc(const void* y_tiles, const float* y_shift, const float* Y, const float* Y_centred, int64_t ldy,
+                int32_t n,
                 int32_t n_pad, int64_t V, const void* p_tiles, const float* u_rows, const float* x_rows,
                 int32_t n_sc, const float* invdiag, const float* dof, int32_t G, int32_t kmax, int32_t mode,
                 const int32_t* coef, int32_t n_coef, const float* wmat, int32_t w_stride, float* t_out,
@@ -603,6 +639,7 @@ int glm_stat_tc(const void* y_tiles, const float* y_shift, const float* Y, int64
   a.pt = static_cast<const __nv_bfloat16*>(p_tiles);
   a.xt = x_rows;
   a.Y = Y;
+  a.Yc = Y_centred;
   a.shift = y_shift;
   a.u = u_rows;
   a.invdiag = invdiag;
@@ -640,8 +677,8 @@ int glm_tstat_tc(const void* y_tiles, const float* y_shift, const float* Y, int6
                  int32_t n_pad, int64_t V, const void* p_tiles, const float* u_rows, const float* x_rows,
                  int32_t n_sc, const float* invdiag, const float* dof, int32_t G, int32_t kmax,
                  const int32_t* coef, int32_t n_coef, float* t_out, int64_t ldt, int32_t* err, void* stream) {
-  return glm_stat_tc(y_tiles, y_shift, Y, ldy, n, n_pad, V, p_tiles, u_rows, x_rows, n_sc, invdiag, dof, G, kmax, 0,
-                     coef, n_coef, nullptr, 0, t_out, ldt, err, stream);
+  return glm_stat_tc(y_tiles, y_shift, Y, nullptr, ldy, n, n_pad, V, p_tiles, u_rows, x_rows, n_sc, invdiag, dof, G,
+                     kmax, 0, coef, n_coef, nullptr, 0, t_out, ldt, err, stream);
 }
 
 }  // extern "C"

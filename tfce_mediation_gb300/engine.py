@@ -116,6 +116,10 @@ class PermutationEngine:
         self._coef = dev(np.asarray(self.contrasts if self.f_groups is None else self.f_groups,
                                     np.int32).reshape(-1))
         self._tc = TensorCoreOperands(self.Yd) if precision == "bf16x3" else None
+        # the designs [1, pred_x] have an intercept: the tensor-core residuals
+        # use the centred form unless an output needs coefficient 0
+        uses0 = (0 in self.contrasts) if self.f_groups is None else min(s0 for s0, _ in self.f_groups) < 1
+        self._centred = self._tc is not None and self._tc.Yc is not None and not uses0
         if batch == "auto":
             from .autotune import choose_batch
             batch = choose_batch(self)
@@ -141,14 +145,15 @@ class PermutationEngine:
         if (precision or self.precision) == "bf16x3":
             tc = self._tc if self._tc is not None else TensorCoreOperands(self.Yd)
             self._tc = tc
-            P8, U, Xt = tc.host_operands(designs)
+            centred = self._centred and tc.centred_ok(designs)
+            P8, U, Xt = tc.host_operands(designs, centred=centred)
             pt = tc.tile_designs(dev(P8), G, designs.kmax)
             mode, wmat = 0, None
             if self.f_groups is not None:
                 mode, wmat = 2, dev(designs.group_blocks(self.f_groups))
             tc.stat(mode, pt, dev(U), dev(Xt), dev(designs.invdiag64.astype(np.float32)),
                     dev(designs.dof.astype(np.float32)), G, designs.kmax, self._coef, self.C, out, self.V,
-                    wmat=wmat)
+                    wmat=wmat, centred=centred)
             return out
         pinv, Xp, invd, dof = designs.to_device()
         _lib.check(self.lib.glm_tstat(ptr(self.Yd), self.V, self.n, self.V, ptr(pinv), ptr(Xp),
@@ -250,7 +255,7 @@ class PermutationEngine:
                 tc.tile_designs(slot["d_P8"], P, kmax, out=slot["d_pt"])
                 tc.stat(2 if self.f_groups is not None else 0, slot["d_pt"], slot["d_U"], slot["d_Xt"],
                         slot["d_invd"], slot["d_dof"], P, kmax, self._coef, self.C, slot["d_t"], self.V,
-                        wmat=slot.get("d_W"))
+                        wmat=slot.get("d_W"), centred=self._centred)
             else:
                 _lib.check(self.lib.glm_tstat(ptr(self.Yd), self.V, n, self.V, ptr(slot["d_pinv"]),
                                               ptr(slot["d_X"]), ptr(slot["d_invd"]), ptr(slot["d_dof"]), P,
@@ -279,7 +284,8 @@ class PermutationEngine:
         db = DesignBatch(self.X[perms])
         P = perms.shape[0]
         if self._tc is not None:
-            self._tc.host_operands(db, P8=slot["h_P8"].numpy(), U=slot["h_U"].numpy(), Xt=slot["h_Xt"].numpy())
+            self._tc.host_operands(db, P8=slot["h_P8"].numpy(), U=slot["h_U"].numpy(), Xt=slot["h_Xt"].numpy(),
+                                   centred=self._centred)
             if self.f_groups is not None:
                 slot["h_W"].numpy()[:P] = db.group_blocks(self.f_groups)
         else:

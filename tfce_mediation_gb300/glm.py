@@ -152,6 +152,8 @@ class TensorCoreOperands:
         nbytes = int(self.lib.glm_tile_bytes(self.V, self.ROW_BLOCK, self.n_pad))
         self.yt = t.empty(nbytes, dtype=t.uint8, device="cuda")
         self.shift = t.empty(self.V, dtype=t.float32, device="cuda") if centre else None
+        # the data minus its centre: residuals of intercept designs skip the intercept term
+        self.Yc = t.empty_like(Yd) if centre else None
         self.err = t.zeros(1, dtype=t.int32, device="cuda")
         self.retile()
 
@@ -160,6 +162,8 @@ class TensorCoreOperands:
         if self.shift is not None:
             _lib.check(self.lib.glm_col_mean(ptr(self.Yd), self.V, self.n, self.V, ptr(self.shift),
                                              stream_handle()))
+            _lib.check(self.lib.glm_col_center(ptr(self.Yd), self.V, self.n, self.V, ptr(self.shift),
+                                               ptr(self.Yc), stream_handle()))
         _lib.check(self.lib.glm_tile_split(ptr(self.Yd), self.V, 1, self.V, self.n, ptr(self.shift),
                                            self.ROW_BLOCK, self.n_pad, ptr(self.yt), stream_handle()))
 
@@ -170,11 +174,18 @@ class TensorCoreOperands:
         DB = self.block(kmax)
         return (G + DB - 1) // DB * DB
 
-    def host_operands(self, db: DesignBatch, P8=None, U=None, Xt=None):
+    def centred_ok(self, db: DesignBatch, first_column_used=False):
+        """Whether the centred residual form applies: a centred data copy
+        exists, every design's first column is all ones, and no requested
+        output uses coefficient 0."""
+        return self.Yc is not None and not first_column_used and bool(np.all(db.X64[:, :, 0] == 1.0))
+
+    def host_operands(self, db: DesignBatch, P8=None, U=None, Xt=None, centred=False):
         """Host float32 operands of a DesignBatch: stacked pseudoinverse rows
         (G_pad*8, n_pad), u = pinv.1 (G_pad, kmax) and negated design rows
-        (G_pad/DB, n_sc, kmax, DB); written into P8 / U / Xt when given (e.g.
-        pinned buffers of exactly those sizes)."""
+        (G_pad/DB, n_sc, kmax, DB) -- with `centred`, the columns after the
+        first minus their means and the first column zero; written into P8 /
+        U / Xt when given (e.g. pinned buffers of exactly those sizes)."""
         G, kmax, n = db.G, db.kmax, db.n
         DB = self.block(kmax)
         Gp = self.padded(G, kmax)
@@ -188,7 +199,11 @@ class TensorCoreOperands:
         x = np.zeros((Gp // DB, self.n_sc, kmax, DB), np.float32) if Xt is None else \
             Xt.reshape(Gp // DB, self.n_sc, kmax, DB)
         xg = np.zeros((Gp, self.n_sc, kmax), np.float32)
-        xg[:G, :n] = -db.X64
+        if centred:
+            xc = db.X64[:, :, 1:] - db.X64[:, :, 1:].mean(axis=1, keepdims=True)
+            xg[:G, :n, 1:] = -xc
+        else:
+            xg[:G, :n] = -db.X64
         x[...] = xg.reshape(Gp // DB, DB, self.n_sc, kmax).transpose(0, 2, 3, 1)
         return p.reshape(Gp * 8, self.n_pad), u, x
 
@@ -206,11 +221,14 @@ class TensorCoreOperands:
     def tstat(self, p_tiles, u_rows, x_rows, invd, dof, G, kmax, coef_d, n_coef, out, ldt):
         self.stat(0, p_tiles, u_rows, x_rows, invd, dof, G, kmax, coef_d, n_coef, out, ldt)
 
-    def stat(self, mode, p_tiles, u_rows, x_rows, invd, dof, G, kmax, coef_d, n_coef, out, ldt, wmat=None):
+    def stat(self, mode, p_tiles, u_rows, x_rows, invd, dof, G, kmax, coef_d, n_coef, out, ldt, wmat=None,
+             centred=False):
         """mode 0: t of coefficients coef_d; 1: RSS; 2: partial F of the column
-        groups coef_d = (start, width) pairs, wmat from DesignBatch.group_blocks."""
+        groups coef_d = (start, width) pairs, wmat from DesignBatch.group_blocks.
+        centred: x_rows came from host_operands(..., centred=True)."""
         w_stride = 0 if wmat is None else int(wmat.shape[-1])
-        _lib.check(self.lib.glm_stat_tc(ptr(self.yt), ptr(self.shift), ptr(self.Yd), self.V, self.n, self.n_pad,
+        _lib.check(self.lib.glm_stat_tc(ptr(self.yt), ptr(self.shift), ptr(self.Yd),
+                                        ptr(self.Yc) if centred else None, self.V, self.n, self.n_pad,
                                         self.V, ptr(p_tiles), ptr(u_rows), ptr(x_rows), self.n_sc, ptr(invd),
                                         ptr(dof), G, kmax, mode, ptr(coef_d), n_coef, ptr(wmat), w_stride,
                                         ptr(out), ldt, ptr(self.err), stream_handle()))
@@ -227,14 +245,15 @@ def glm_tstat_tc(Y, designs, coef, ops=None, centre=True):
     t = require_cuda()
     db = designs if isinstance(designs, DesignBatch) else DesignBatch(designs)
     ops = ops or TensorCoreOperands(dev(Y, t.float32), centre=centre)
-    P8, U, Xt = ops.host_operands(db)
+    centred = ops.centred_ok(db, first_column_used=0 in list(coef))
+    P8, U, Xt = ops.host_operands(db, centred=centred)
     pt = ops.tile_designs(dev(P8), db.G, db.kmax)
     u, xt = dev(U), dev(Xt)
     invd = dev(db.invdiag64.astype(np.float32))
     dof = dev(db.dof.astype(np.float32))
     coef_d = dev(np.asarray(coef, np.int32))
     out = t.empty((db.G, len(coef), ops.V), device="cuda", dtype=t.float32)
-    ops.tstat(pt, u, xt, invd, dof, db.G, db.kmax, coef_d, len(coef), out, ops.V)
+    ops.stat(0, pt, u, xt, invd, dof, db.G, db.kmax, coef_d, len(coef), out, ops.V, centred=centred)
     t.cuda.synchronize()
     ops.status()
     return out
@@ -248,7 +267,9 @@ def glm_stat_tc(Y, designs, mode, coef=None, groups=None, ops=None):
     t = require_cuda()
     db = designs if isinstance(designs, DesignBatch) else DesignBatch(designs)
     ops = ops or TensorCoreOperands(dev(Y, t.float32))
-    P8, U, Xt = ops.host_operands(db)
+    uses0 = (mode == "t" and 0 in list(coef)) or (mode == "f" and min(s0 for s0, _ in groups) < 1)
+    centred = ops.centred_ok(db, first_column_used=uses0)
+    P8, U, Xt = ops.host_operands(db, centred=centred)
     pt = ops.tile_designs(dev(P8), db.G, db.kmax)
     u, xt = dev(U), dev(Xt)
     invd = dev(db.invdiag64.astype(np.float32))
@@ -265,7 +286,7 @@ def glm_stat_tc(Y, designs, mode, coef=None, groups=None, ops=None):
     else:
         raise ValueError("mode must be 't', 'rss' or 'f'")
     out = t.empty((db.G, rows, ops.V), device="cuda", dtype=t.float32)
-    ops.stat(m, pt, u, xt, invd, dof, db.G, db.kmax, coef_d, rows, out, ops.V, wmat=wmat)
+    ops.stat(m, pt, u, xt, invd, dof, db.G, db.kmax, coef_d, rows, out, ops.V, wmat=wmat, centred=centred)
     t.cuda.synchronize()
     ops.status()
     return out[:, 0] if mode == "rss" else out
