@@ -206,7 +206,8 @@ int glm_fstat(const float* Y, int64_t ldy, int32_t n, int64_t V, const float* pi
  *     minus row_shift[row] when row_shift is not NULL, in row blocks of
  *     row_block (128 for the data, DB*8 for the stacked pseudoinverse rows
  *     [G_pad*8][n_pad], rows >= k_g of a design zero) and 16-deep K steps,
- *     n_pad a multiple of 16 >= cols, zero fill;
+ *     n_pad a multiple of 16 >= cols, zero fill; shifted (optional) receives
+ *     src minus row_shift as FP32 in src's layout (the centred data);
  *   glm_tstat_tc: y_tiles (row block 128, centred on y_shift when that is not
  *     NULL) and p_tiles (row block DB*8) from glm_tile_split; u_rows
  *     [G_pad][kmax] = pinv(X_d).1 (needed with y_shift: beta = beta_c +
@@ -220,7 +221,8 @@ int glm_tc_design_block(int32_t kmax);
 int64_t glm_tile_bytes(int64_t rows, int32_t row_block, int32_t n_pad);
 int glm_col_mean(const float* Y, int64_t ldy, int32_t n, int64_t V, float* mean, void* stream);
 int glm_tile_split(const float* src, int64_t ld_src, int32_t transpose, int64_t rows, int32_t cols,
-                   const float* row_shift, int32_t row_block, int32_t n_pad, void* dst, void* stream);
+                   const float* row_shift, int32_t row_block, int32_t n_pad, void* dst, float* shifted,
+                   void* stream);
 int glm_tstat_tc(const void* y_tiles, const float* y_shift, const float* Y, int64_t ldy, int32_t n,
                  int32_t n_pad, int64_t V, const void* p_tiles, const float* u_rows, const float* x_rows,
                  int32_t n_sc, const float* invdiag, const float* dof, int32_t G, int32_t kmax,

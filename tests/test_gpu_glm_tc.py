@@ -42,7 +42,11 @@ def test_tile_layout_matches_definition():
         sh = torch.from_numpy(shift).cuda() if with_shift else None
         ld = rows if transpose else cols
         dst = torch.zeros(nbytes, dtype=torch.uint8, device="cuda")
-        _lib.check(lib.glm_tile_split(ptr(src), ld, transpose, rows, cols, ptr(sh), rb, n_pad, ptr(dst), None))
+        shifted = torch.zeros_like(src)
+        _lib.check(lib.glm_tile_split(ptr(src), ld, transpose, rows, cols, ptr(sh), rb, n_pad, ptr(dst),
+                                      ptr(shifted), None))
+        exp_shift = (A - shift[:, None]) if with_shift else A
+        np.testing.assert_array_equal(shifted.cpu().numpy(), exp_shift.T if transpose else exp_shift)
         got = dst.cpu().view(torch.int16).numpy()
         Ap = np.zeros(((rows + rb - 1) // rb * rb, n_pad), np.float32)
         Ap[:rows, :cols] = (A - shift[:, None]) if with_shift else A

@@ -69,7 +69,7 @@ SIGNATURES = {
     "glm_tile_bytes": (ctypes.c_int64, [ctypes.c_int64, ctypes.c_int32, ctypes.c_int32]),
     "glm_col_mean": (ctypes.c_int, [c_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int64, c_vp, c_vp]),
     "glm_tile_split": (ctypes.c_int, [c_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32,
-                                      c_vp, ctypes.c_int32, ctypes.c_int32, c_vp, c_vp]),
+                                      c_vp, ctypes.c_int32, ctypes.c_int32, c_vp, c_vp, c_vp]),
     "glm_tstat_tc": (ctypes.c_int, [c_vp, c_vp, c_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
                                     ctypes.c_int64, c_vp, c_vp, c_vp, ctypes.c_int32, c_vp, c_vp, ctypes.c_int32,
                                     ctypes.c_int32, c_vp, ctypes.c_int32, c_vp, ctypes.c_int64, c_vp, c_vp]),

@@ -191,11 +191,12 @@ __device__ inline void tmem_ld8(uint32_t taddr, float* out) {
 //   byte offset of (row R, col c) = ((R/RB * KS + c/16) * 2 + part) * RB*32
 //                                   + ((c%16)/8) * RB*16 + (R%RB) * 16 + (c%8) * 2
 // with KS = n_pad/16 and zero fill past rows / cols; row_shift (optional)
-// is subtracted from every element of its row first.  One thread writes the
+// is subtracted from every element of its row first, and `shifted`
+// (optional) receives the shifted FP32 matrix in src's own layout.  One thread writes the
 // 8 columns of one (row, k-block): 16 bytes hi and 16 bytes lo.
 __global__ void tile_split_kernel(const float* __restrict__ src, int64_t ld_src, int transpose, int64_t rows,
                                   int cols, const float* __restrict__ row_shift, int rb, int ks_count,
-                                  int64_t n_blk, __nv_bfloat16* __restrict__ dst) {
+                                  int64_t n_blk, __nv_bfloat16* __restrict__ dst, float* __restrict__ shifted) {
   const int64_t total = n_blk * ks_count * 2 * rb;
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
@@ -214,7 +215,11 @@ __global__ void tile_split_kernel(const float* __restrict__ src, int64_t ld_src,
     for (int e = 0; e < 8; ++e) {
       const int c = c0 + e;
       float x = 0.0f;
-      if (R < rows && c < cols) x = (transpose ? src[(int64_t)c * ld_src + R] : src[R * ld_src + c]) - sh;
+      if (R < rows && c < cols) {
+        const int64_t at = transpose ? (int64_t)c * ld_src + R : R * ld_src + c;
+        x = src[at] - sh;
+        if (shifted != nullptr) shifted[at] = x;  // the shifted FP32 matrix, same layout as src
+      }
       h[e] = __float2bfloat16_rn(x);
       l[e] = __float2bfloat16_rn(x - __bfloat162float(h[e]));
     }
@@ -595,7 +600,7 @@ int glm_col_center(const float* Y, int64_t ldy, int32_t n, int64_t V, const floa
 }
 
 int glm_tile_split(const float* src, int64_t ld_src, int32_t transpose, int64_t rows, int32_t cols,
-                   const float* row_shift, int32_t row_block, int32_t n_pad, void* dst, void* stream) {
+                   const float* row_shift, int32_t row_block, int32_t n_pad, void* dst, float* shifted, void* stream) {
   tfgb::clear_error();
   TFGB_CHECK_ARG(src && dst, "NULL pointer");
   TFGB_CHECK_ARG(rows >= 0 && cols >= 0 && n_pad >= cols && n_pad % tfgb::kTcK == 0,
@@ -608,7 +613,7 @@ int glm_tile_split(const float* src, int64_t ld_src, int32_t transpose, int64_t 
   const int64_t total = n_blk * ks * 2 * row_block;
   const unsigned blocks = static_cast<unsigned>(std::min<int64_t>((total + 255) / 256, 152 * 16));
   tfgb::tile_split_kernel<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
-      src, ld_src, transpose, rows, cols, row_shift, row_block, ks, n_blk, static_cast<__nv_bfloat16*>(dst));
+      src, ld_src, transpose, rows, cols, row_shift, row_block, ks, n_blk, static_cast<__nv_bfloat16*>(dst), shifted);
   TFGB_CUDA(cudaGetLastError());
   return TFCE_OK;
 }

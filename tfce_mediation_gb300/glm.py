@@ -162,10 +162,9 @@ class TensorCoreOperands:
         if self.shift is not None:
             _lib.check(self.lib.glm_col_mean(ptr(self.Yd), self.V, self.n, self.V, ptr(self.shift),
                                              stream_handle()))
-            _lib.check(self.lib.glm_col_center(ptr(self.Yd), self.V, self.n, self.V, ptr(self.shift),
-                                               ptr(self.Yc), stream_handle()))
+        # tiles of the centred data, and the centred FP32 copy in the same pass
         _lib.check(self.lib.glm_tile_split(ptr(self.Yd), self.V, 1, self.V, self.n, ptr(self.shift),
-                                           self.ROW_BLOCK, self.n_pad, ptr(self.yt), stream_handle()))
+                                           self.ROW_BLOCK, self.n_pad, ptr(self.yt), ptr(self.Yc), stream_handle()))
 
     def block(self, kmax):
         return int(self.lib.glm_tc_design_block(kmax))
@@ -215,7 +214,7 @@ class TensorCoreOperands:
         nbytes = int(self.lib.glm_tile_bytes(rows, rb, self.n_pad))
         out = t.empty(nbytes, dtype=t.uint8, device="cuda") if out is None else out
         _lib.check(self.lib.glm_tile_split(ptr(P8_dev), self.n_pad, 0, rows, self.n_pad, None, rb, self.n_pad,
-                                           ptr(out), stream_handle()))
+                                           ptr(out), None, stream_handle()))
         return out
 
     def tstat(self, p_tiles, u_rows, x_rows, invd, dof, G, kmax, coef_d, n_coef, out, ldt):
