@@ -237,6 +237,21 @@ int glm_tstat_tc(const void* y_tiles, const float* y_shift, const float* Y, int6
  *     [G][w_stride] holds, per design, the groups' inv(inv(X'X)_SS) blocks
  *     (row-major, concatenated in group order).  A group outside [0, kmax)
  *     yields NaN.
+ *   mode 3: a program of n_coef typed output rows, coef = 4 int32 per row
+ *     (kind, column j, width w, offset o into the design's wmat row):
+ *       kind 0: t of coefficient j;  kind 1: -t of coefficient j (the
+ *         reference sweeps -t as its own map);
+ *       kind 2: partial F of the columns [j, j+w), inv(inv(X'X)_SS) at o (w*w);
+ *       kind 3 / 4: the cosinor amplitude / acrophase t of the pair (j, j+1)
+ *         = (cos, sin) coefficients (glm_cosinor, tm/pyfunc.py:2406-2560),
+ *         inv(X'X) entries (jj, j j+1, j+1 j+1) at o: with A^2 = b_j^2 + b_j+1^2
+ *         and sigma^2 = RSS/dof, A^2 / (sigma sqrt(I11 b_j^2 -/+ 2 I12 |b_j b_j+1|
+ *         + I22 b_j+1^2)) for the amplitude (-) and with b_j, b_j+1 swapped
+ *         (+) for the acrophase -- the reference's error propagation through
+ *         |sin|, |cos| of arctan(|b_j+1 / b_j|).
+ *     A row whose columns or weights fall outside kmax / w_stride yields NaN.
+ *     The model F of glm_cosinor / glm_typeI is kind 2 over every column
+ *     after the intercept.
  *   Y_centred (optional): Y minus its per-vertex centre (glm_col_center with
  *     y_shift); only for designs whose first column is all ones and whose
  *     x_rows hold the other columns minus their means: the residuals are then

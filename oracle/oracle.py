@@ -265,6 +265,99 @@ def partial_f_fp64(X, y, groups):
                        for s0, w in groups])
 
 
+def cosinor_design(time_var, period, exog=None, dmy_covariates=None):
+    """[1, cos(2 pi t / p_i), sin(2 pi t / p_i) per period, exog..., covariates]
+    (tm/pyfunc.py:2428-2457)."""
+    t = np.asarray(time_var, np.float64)
+    n = t.shape[0]
+    cols = [np.ones(n)]
+    for p in period:
+        cols.append(np.cos(np.divide(2.0 * np.pi * t, p)))
+        cols.append(np.sin(np.divide(2.0 * np.pi * t, p)))
+    for var in exog or []:
+        cols.append(np.asarray(var, np.float64).reshape(n, -1))
+    if dmy_covariates is not None:
+        cols.append(np.asarray(dmy_covariates, np.float64).reshape(n, -1))
+    return np.column_stack(cols)
+
+
+def _acrophase_quadrant(acro, b_cos, b_sin):
+    """The sign/quadrant rule of tm/pyfunc.py:2487-2490 (and 2545-2548)."""
+    acro = acro.copy()
+    m = (b_sin > 0) & (b_cos >= 0)
+    acro[m] = -acro[m]
+    m = (b_sin > 0) & (b_cos < 0)
+    acro[m] = -np.pi + acro[m]
+    m = (b_sin < 0) & (b_cos <= 0)
+    acro[m] = -np.pi - acro[m]
+    m = (b_sin <= 0) & (b_cos > 0)
+    acro[m] = -2.0 * np.pi + acro[m]
+    return acro
+
+
+def glm_cosinor(endog, time_var, exog=None, dmy_covariates=None, rand_array=None, period=(24.0,),
+                calc_MESOR=True, output_fit_only=False):
+    """glm_cosinor (tm/pyfunc.py:2406-2560), FP64, for 2-D endog (n, V):
+    design rows permuted by rand_array; betas and RSS of the full fit
+    (cy_lin_lstsqr_mat_residual); SS_Total in the data's own type; model F =
+    ((SS_Total - RSS)/(k-1)) / (RSS/(n-k)); SE of the coefficients rounded to
+    float32 (se_of_slope); per period the amplitude sqrt(b_cos^2 + b_sin^2),
+    the acrophase arctan(|b_sin / b_cos|) with the error-propagation SEs taken
+    before the quadrant rule, which only the unpermuted call applies; t of the
+    amplitude A/SE_A and of the acrophase 1/SE_phi, returned as absolute values.
+    Returns the reference's 12-tuple (3-tuple with output_fit_only)."""
+    y_in = np.asarray(endog)
+    y = np.asarray(endog, np.float64)
+    n = y.shape[0]
+    n_per = len(period)
+    X = cosinor_design(time_var, period, exog, dmy_covariates)
+    if rand_array is not None:
+        X = X[np.asarray(rand_array)]
+    k = X.shape[1]
+    df_between, df_within = k - 1, n - k
+    invXX = np.linalg.inv(X.T @ X)
+    a = invXX @ X.T @ y
+    r = y - X @ a
+    rss = np.sum(r ** 2, axis=0)
+    amp, acro = [], []
+    for i in range(n_per):
+        bc, bs = a[1 + 2 * i], a[2 + 2 * i]
+        amp.append(np.sqrt(bc ** 2 + bs ** 2))
+        with np.errstate(divide="ignore", invalid="ignore"):
+            acro.append(np.arctan(np.abs(np.divide(-bs, bc))))
+    if output_fit_only:
+        acro_q = [_acrophase_quadrant(acro[i], a[1 + 2 * i], a[2 + 2 * i]) for i in range(n_per)]
+        return a[0], np.asarray(amp), np.asarray(acro_q)
+    ss_total = np.sum((y_in - np.mean(y_in, 0)) ** 2, 0).astype(np.float64)
+    ms_res = rss / df_within
+    F_model = ((ss_total - rss) / df_between) / ms_res
+    sigma = np.sqrt(ms_res)
+    MESOR = tMESOR = SE_MESOR = tEXOG = None
+    if calc_MESOR or exog is not None:
+        se = np.sqrt(ms_res[None, :] * np.diag(invXX)[:, None]).astype(np.float32)
+        T = a / se
+        MESOR, tMESOR, SE_MESOR = a[0], T[0], se[0]
+        if exog is not None:
+            tEXOG = T[3 + 2 * (n_per - 1):]
+    se_amp, se_acro, t_amp, t_acro = [], [], [], []
+    for i in range(n_per):
+        c, s = 1 + 2 * i, 2 + 2 * i
+        sn, cs = np.sin(acro[i]), np.cos(acro[i])
+        with np.errstate(divide="ignore", invalid="ignore"):
+            se_acro.append(sigma * np.sqrt(invXX[c, c] * sn ** 2 + 2 * invXX[c, s] * sn * cs
+                                           + invXX[s, s] * cs ** 2) / amp[i])
+            se_amp.append(sigma * np.sqrt(invXX[c, c] * cs ** 2 - 2 * invXX[c, s] * sn * cs
+                                          + invXX[s, s] * sn ** 2))
+            t_amp.append(amp[i] / se_amp[i])
+            t_acro.append(1.0 / se_acro[i])
+        if rand_array is None:
+            acro[i] = _acrophase_quadrant(acro[i], a[c], a[s])
+    R2 = 1 - rss / ss_total if rand_array is None else None
+    return (R2, MESOR, SE_MESOR, np.asarray(amp), np.asarray(se_amp), np.asarray(acro), np.asarray(se_acro),
+            F_model, tMESOR, np.abs(np.asarray(t_amp)), np.abs(np.asarray(t_acro)),
+            None if tEXOG is None else np.asarray(tEXOG))
+
+
 def calc_beta_se(x, y, n):
     """cynumstats.pyx:66-74: design [1, x]; returns (beta[1], se float32 k x V)."""
     X = np.column_stack([np.ones(n), x])

@@ -290,6 +290,28 @@ def main():
     out["typeI_y"], out["typeI_ex0"], out["typeI_ex1"] = yt, ex0, ex1
     out["typeI_cov"], out["typeI_perm"] = cov, permt
 
+    # glm_cosinor (tm-models cosinor): observed and permuted statistics with
+    # two periods, one exogenous variable and a covariate; and the fit-only form
+    nc, Vc = 48, 30
+    tcos = rng.uniform(0.0, 48.0, nc)
+    yc = rng.standard_normal((nc, Vc)).astype(np.float32) + 5.0
+    yc[:, :12] += (1.5 * np.cos(2.0 * np.pi * (tcos - 3.0) / 24.0))[:, None].astype(np.float32)
+    yc[:, 12:18] += (0.9 * np.sin(2.0 * np.pi * tcos / 12.0))[:, None].astype(np.float32)
+    exc = rng.standard_normal(nc)
+    covc = rng.standard_normal((nc, 1))
+    permc = np.random.RandomState(78).permutation(nc)
+    names = ("R2", "MESOR", "SE_MESOR", "AMP", "SE_AMP", "ACRO", "SE_ACRO", "F", "tMESOR", "tAMP", "tACRO",
+             "tEXOG")
+    for tag, ra in (("obs", None), ("perm", permc)):
+        res = pyfunc.glm_cosinor(yc, tcos, exog=[exc], dmy_covariates=covc, rand_array=ra, period=[24.0, 12.0],
+                                 calc_MESOR=ra is None)
+        for name, val in zip(names, res):
+            if val is not None:
+                out[f"cos_{name}_{tag}"] = np.asarray(val)
+    fit = pyfunc.glm_cosinor(yc, tcos, period=[24.0, 12.0], output_fit_only=True)
+    out["cos_fit_MESOR"], out["cos_fit_AMP"], out["cos_fit_ACRO"] = (np.asarray(v) for v in fit)
+    out["cos_y"], out["cos_t"], out["cos_ex"], out["cos_cov"], out["cos_perm"] = yc, tcos, exc, covc, permc
+
     path = os.path.join(HERE, "reference_vectors.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({os.path.getsize(path)} bytes, {len(out)} arrays)")

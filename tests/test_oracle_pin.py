@@ -191,3 +191,62 @@ def test_partial_f_is_glm_typeI_drop_one(golden):
     X = np.column_stack([np.ones(n), golden["typeI_ex0"], golden["typeI_ex1"], golden["typeI_cov"]])
     Fv = oracle.partial_f_fp64(X, y, [(1, 2), (3, 1)])
     np.testing.assert_allclose(Fv, golden["typeI_Fvar_obs"], rtol=1e-8, atol=1e-10)
+
+
+_COS_NAMES = ("R2", "MESOR", "SE_MESOR", "AMP", "SE_AMP", "ACRO", "SE_ACRO", "F", "tMESOR", "tAMP", "tACRO",
+              "tEXOG")
+
+
+@pytest.mark.parametrize("tag", ["obs", "perm"])
+def test_glm_cosinor(golden, tag):
+    """The FP64 restatement of glm_cosinor against the reference's own 12-tuple
+    (two periods, one exogenous variable, one covariate; the permuted call
+    skips the quadrant rule and R2, as the reference does)."""
+    ra = None if tag == "obs" else golden["cos_perm"]
+    res = oracle.glm_cosinor(golden["cos_y"], golden["cos_t"], exog=[golden["cos_ex"]],
+                             dmy_covariates=golden["cos_cov"], rand_array=ra, period=[24.0, 12.0],
+                             calc_MESOR=ra is None)
+    for name, val in zip(_COS_NAMES, res):
+        key = f"cos_{name}_{tag}"
+        if key not in golden:
+            assert val is None, name
+            continue
+        np.testing.assert_allclose(val, golden[key], rtol=1e-9, atol=1e-12, err_msg=name)
+
+
+def test_glm_cosinor_fit_only(golden):
+    mesor, amp, acro = oracle.glm_cosinor(golden["cos_y"], golden["cos_t"], period=[24.0, 12.0],
+                                          output_fit_only=True)
+    np.testing.assert_allclose(mesor, golden["cos_fit_MESOR"], rtol=1e-12)
+    np.testing.assert_allclose(amp, golden["cos_fit_AMP"], rtol=1e-12)
+    np.testing.assert_allclose(acro, golden["cos_fit_ACRO"], rtol=1e-12)
+
+
+def test_cosinor_program_forms(golden):
+    """The closed forms of the tensor-core epilogue's cosinor rows (model F as
+    the Wald partial F of every column after the intercept; amplitude and
+    acrophase t without trigonometry) against the restatement, FP64."""
+    y = np.asarray(golden["cos_y"], np.float64)
+    X = oracle.cosinor_design(golden["cos_t"], [24.0, 12.0], [golden["cos_ex"]], golden["cos_cov"])
+    X = X[golden["cos_perm"]]
+    n, k = X.shape
+    inv = np.linalg.inv(X.T @ X)
+    b = inv @ X.T @ y
+    rss = np.sum((y - X @ b) ** 2, 0)
+    sigma = np.sqrt(rss / (n - k))
+    res = oracle.glm_cosinor(golden["cos_y"], golden["cos_t"], exog=[golden["cos_ex"]],
+                             dmy_covariates=golden["cos_cov"], rand_array=golden["cos_perm"],
+                             period=[24.0, 12.0], calc_MESOR=False)
+    S = slice(1, k)
+    Fw = np.einsum("iv,ij,jv->v", b[S], np.linalg.inv(inv[S, S]), b[S]) / (k - 1) / (rss / (n - k))
+    # the reference's SS_Total is a float32 sum: its rounding, amplified by the
+    # SS_Total - RSS cancellation, moves its F by ~5e-6 relative here
+    np.testing.assert_allclose(Fw, res[7], rtol=3e-5)
+    for i in range(2):
+        c, s = 1 + 2 * i, 2 + 2 * i
+        a2 = b[c] ** 2 + b[s] ** 2
+        cr = 2 * inv[c, s] * np.abs(b[c] * b[s])
+        t_amp = a2 / (sigma * np.sqrt(inv[c, c] * b[c] ** 2 - cr + inv[s, s] * b[s] ** 2))
+        t_acro = a2 / (sigma * np.sqrt(inv[c, c] * b[s] ** 2 + cr + inv[s, s] * b[c] ** 2))
+        np.testing.assert_allclose(t_amp, res[9][i], rtol=1e-10)
+        np.testing.assert_allclose(t_acro, res[10][i], rtol=1e-10)

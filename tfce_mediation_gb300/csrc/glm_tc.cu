@@ -54,6 +54,8 @@ constexpr int kTcK = 16;            // subjects per MMA K step / pipeline stage
 constexpr int kTcStages = 4;
 constexpr int kTcSubjChunk = 32;    // subjects per epilogue X chunk
 constexpr uint64_t kTcWaitNs = 2000000000ull;
+// output kinds of the programmed epilogue (mode 3)
+constexpr int kTcOutT = 0, kTcOutNegT = 1, kTcOutF = 2, kTcOutAmp = 3, kTcOutAcro = 4;
 
 __host__ __device__ constexpr int tc_dpt(int kmax) { return kmax <= 5 ? 16 : 8; }  // designs per thread
 __host__ __device__ constexpr int tc_db(int kmax) { return 2 * tc_dpt(kmax); }     // designs per tile
@@ -268,8 +270,9 @@ struct TcArgs {
   const float* u;           // [G_pad][kmax] pinv(X_d).1 (with shift)
   const float* invdiag;     // [G][kmax]
   const float* dof;         // [G]
-  const int32_t* coef;      // mode 0: coefficient indices; mode 2: (start, width) per column group
-  const float* wmat;        // mode 2: [G][w_stride] inverse blocks of inv(X'X) per group
+  const int32_t* coef;      // mode 0: coefficient indices; mode 2: (start, width) per column group;
+                            // mode 3: (kind, column, width, weight offset) per output row
+  const float* wmat;        // modes 2, 3: [G][w_stride] per-design weights (blocks of inv(X'X))
   float* t_out;             // [G][n_coef][ldt]
   int64_t ldy, ldt, V;
   int32_t n, n_sc, ks_count, G, n_db, n_coef, mode, w_stride;
@@ -504,13 +507,11 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
 #pragma unroll
       for (int vv = 0; vv < VT; ++vv)
         if (v0 + vv < a.V) dst[vv] = (vv & 1) ? rss[vv / 2].y : rss[vv / 2].x;
-    } else if (g < a.G && a.mode == 2) {
-      // partial F of each column group S (the F of dropping S from the
-      // design): (RSS_without_S - RSS) / |S| / (RSS / dof), with the extra sum
-      // of squares in its exact Wald form b_S' inv(inv(X'X)_SS) b_S -- no
-      // difference of two residual sums
+    } else if (g < a.G && a.mode >= 2) {
+      // mode 2: partial F of each column group; mode 3: a program of typed
+      // output rows (t, -t, partial F, cosinor amplitude / acrophase t).
       // this thread's betas and RSS go to its own slice of the (now free)
-      // shared area, so the group loops index them at run time
+      // shared area, so the output loops index them at run time
       float* mine = reinterpret_cast<float*>(sm) + tid * VT * (KMAX + 1);
 #pragma unroll
       for (int vv = 0; vv < VT; ++vv) {
@@ -520,22 +521,69 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
         mine[vv * (KMAX + 1) + KMAX] = (vv & 1) ? rss[vv / 2].y : rss[vv / 2].x;
       }
       const float dof = __ldg(a.dof + g);
+      const float inv_dof = 1.0f / dof;
       const float* wg = a.wmat + (int64_t)g * a.w_stride;
       int woff = 0;
-      for (int gi = 0; gi < a.n_coef; ++gi) {
-        const int s0 = __ldg(a.coef + 2 * gi), kv = __ldg(a.coef + 2 * gi + 1);
-        const bool ok = s0 >= 0 && kv >= 1 && s0 + kv <= KMAX;
-        float* dst = a.t_out + ((int64_t)g * a.n_coef + gi) * a.ldt + v0;
+      for (int oi = 0; oi < a.n_coef; ++oi) {
+        int kind, j, kv, wo;
+        if (a.mode == 2) {
+          kind = kTcOutF;
+          j = __ldg(a.coef + 2 * oi);
+          kv = __ldg(a.coef + 2 * oi + 1);
+          wo = woff;
+          woff += kv * kv;
+        } else {
+          kind = __ldg(a.coef + 4 * oi);
+          j = __ldg(a.coef + 4 * oi + 1);
+          kv = __ldg(a.coef + 4 * oi + 2);
+          wo = __ldg(a.coef + 4 * oi + 3);
+        }
+        bool ok;
+        if (kind == kTcOutT || kind == kTcOutNegT) {
+          ok = j >= 0 && j < KMAX;
+        } else if (kind == kTcOutF) {
+          ok = j >= 0 && kv >= 1 && j + kv <= KMAX && wo >= 0 && wo + kv * kv <= a.w_stride;
+        } else if (kind == kTcOutAmp || kind == kTcOutAcro) {
+          ok = j >= 0 && j + 1 < KMAX && wo >= 0 && wo + 3 <= a.w_stride;
+        } else {
+          ok = false;
+        }
+        const float dj = (ok && kind <= kTcOutNegT) ? __ldg(a.invdiag + g * KMAX + j) : 0.0f;
+        float* dst = a.t_out + ((int64_t)g * a.n_coef + oi) * a.ldt + v0;
         for (int vv = 0; vv < VT; ++vv) {
           if (v0 + vv >= a.V) break;
           const float* bv = mine + vv * (KMAX + 1);
-          float q = 0.0f;
-          for (int ja = 0; ok && ja < kv; ++ja)
-            for (int jc = 0; jc < kv; ++jc)
-              q = fmaf(bv[s0 + ja] * __ldg(wg + woff + ja * kv + jc), bv[s0 + jc], q);
-          dst[vv] = ok ? (q / static_cast<float>(kv)) / (bv[KMAX] / dof) : __int_as_float(0x7fc00000);
+          const float rs = bv[KMAX];
+          float val = __int_as_float(0x7fc00000);
+          if (!ok) {
+          } else if (kind == kTcOutT || kind == kTcOutNegT) {
+            val = bv[j] / sqrtf(rs * inv_dof * dj);
+            if (kind == kTcOutNegT) val = -val;
+          } else if (kind == kTcOutF) {
+            // (RSS_without_S - RSS) / |S| / (RSS / dof) with the extra sum of
+            // squares in its exact Wald form b_S' inv(inv(X'X)_SS) b_S -- no
+            // difference of two residual sums
+            float q = 0.0f;
+            for (int ja = 0; ja < kv; ++ja)
+              for (int jc = 0; jc < kv; ++jc)
+                q = fmaf(bv[j + ja] * __ldg(wg + wo + ja * kv + jc), bv[j + jc], q);
+            val = (q / static_cast<float>(kv)) / (rs / dof);
+          } else {
+            // cosinor pair (b1, b2) = (cos, sin) coefficients, wg = inv(X'X)
+            // entries (11, 12, 22): with A^2 = b1^2 + b2^2 and the acrophase
+            // angle's |sin| = |b2|/A, |cos| = |b1|/A,
+            //   t_amplitude = A^2 / (sigma sqrt(I11 b1^2 - 2 I12 |b1 b2| + I22 b2^2))
+            //   t_acrophase = A^2 / (sigma sqrt(I11 b2^2 + 2 I12 |b1 b2| + I22 b1^2))
+            const float b1 = bv[j], b2 = bv[j + 1];
+            const float i11 = __ldg(wg + wo), i12 = __ldg(wg + wo + 1), i22 = __ldg(wg + wo + 2);
+            const float a2 = fmaf(b1, b1, b2 * b2);
+            const float c = 2.0f * i12 * fabsf(b1 * b2);
+            const float q = (kind == kTcOutAmp) ? fmaf(i11, b1 * b1, fmaf(i22, b2 * b2, -c))
+                                                : fmaf(i11, b2 * b2, fmaf(i22, b1 * b1, c));
+            val = a2 / sqrtf(rs * inv_dof * q);
+          }
+          dst[vv] = val;
         }
-        woff += kv * kv;
       }
     }
   }
@@ -631,9 +679,10 @@ int glm_stat_tc(const void* y_tiles, const float* y_shift, const float* Y, const
   TFGB_CHECK_ARG(n > 0 && n_pad >= n && n_pad % tfgb::kTcK == 0, "n_pad must be >= n and a multiple of 16");
   TFGB_CHECK_ARG(n_sc >= n && n_sc % tfgb::kTcSubjChunk == 0, "n_sc must be >= n and a multiple of 32");
   TFGB_CHECK_ARG(kmax >= 1 && kmax <= tfgb::kTcRowsPerDesign, "kmax must be in [1, 8]");
-  TFGB_CHECK_ARG(mode >= 0 && mode <= 2, "mode must be 0 (t), 1 (RSS) or 2 (partial F)");
+  TFGB_CHECK_ARG(mode >= 0 && mode <= 3, "mode must be 0 (t), 1 (RSS), 2 (partial F) or 3 (program)");
   TFGB_CHECK_ARG(mode == 1 || n_coef >= 1, "n_coef must be >= 1");
   TFGB_CHECK_ARG(mode != 2 || (wmat != nullptr && w_stride >= 1), "partial F needs wmat");
+  TFGB_CHECK_ARG(mode != 3 || wmat != nullptr || w_stride == 0, "w_stride > 0 needs wmat");
   TFGB_CHECK_ARG(V >= 0 && G >= 0 && ldt >= V && ldy >= V, "bad sizes");
   TFGB_CHECK_ARG(reinterpret_cast<uintptr_t>(y_tiles) % 16 == 0 && reinterpret_cast<uintptr_t>(p_tiles) % 16 == 0 &&
                      reinterpret_cast<uintptr_t>(x_rows) % 16 == 0,

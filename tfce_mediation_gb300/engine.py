@@ -24,7 +24,7 @@ import numpy as np
 from . import _lib
 from .adjacency import AdjacencySet, is_symmetric, locality_order, relabel_csr, to_csr
 from .device import dev, ptr, require_cuda, stream_handle
-from .glm import DesignBatch, TensorCoreOperands
+from .glm import OUT_NEG_T, OUT_T, DesignBatch, TensorCoreOperands, output_columns, output_program
 
 
 def permutations(n, seed, start, stop):
@@ -51,7 +51,13 @@ class PermutationEngine:
     f_groups: [(start, width), ...] column groups of the design: the maps are
     then the drop-one F of each group (glm_typeI's F per variable,
     tm/pyfunc.py:2282-2400, as tm_models_randomise.py:205-210 permutes it),
-    swept with one sign; needs precision 'bf16x3'.
+    swept with one sign; needs precision 'bf16x3'.  Shorthand for
+    outputs=[("f", start, width), ...].
+    outputs: typed output maps of the tensor-core GLM's programmed epilogue
+    (glm.output_program: ("t", j), ("-t", j), ("f", j, w), ("amp", j),
+    ("acro", j)), each swept with one sign -- e.g. the cosinor path's model F,
+    amplitude and acrophase t and +/- t of the other regressors
+    (tm_models_randomise.py:274-372); needs precision 'bf16x3'.
     precision: GLM arithmetic of the permutation t maps: 'bf16x3' (default;
     tensor cores, split BF16 with FP32 accumulation, t within ~3e-5 relative
     of FP64) or 'fp32' (CUDA cores, ~1e-6).  The observed (unpermuted) t map
@@ -64,15 +70,20 @@ class PermutationEngine:
 
     def __init__(self, Y, pred_x, adjacency, segments=None, H=2.0, E=1.0, vdensity=None,
                  contrasts=None, floor_zero=False, batch=64, signs=2, reorder=False,
-                 accumulation="component", precision="bf16x3", f_groups=None):
+                 accumulation="component", precision="bf16x3", f_groups=None, outputs=None):
         t = require_cuda()
         if precision not in ("bf16x3", "fp32"):
             raise ValueError("precision must be 'bf16x3' (tensor cores) or 'fp32' (CUDA cores)")
         self.precision = precision
         self.f_groups = None if f_groups is None else [(int(a), int(b)) for a, b in f_groups]
         if self.f_groups is not None:
+            if outputs is not None:
+                raise ValueError("give f_groups or outputs, not both")
+            outputs = [("f", s0, w) for s0, w in self.f_groups]
+        self.outputs = None if outputs is None else [tuple(o) for o in outputs]
+        if self.outputs is not None:
             if precision != "bf16x3":
-                raise ValueError("partial-F maps run on the tensor-core GLM (precision='bf16x3')")
+                raise ValueError("programmed output maps run on the tensor-core GLM (precision='bf16x3')")
             signs = 1
         self.t = t
         Yh = Y if isinstance(Y, t.Tensor) else np.asarray(Y, np.float32)
@@ -103,22 +114,30 @@ class PermutationEngine:
         self.adj.set_accumulation(accumulation)
         self.n_seg = self.adj.n_seg
         self.contrasts = list(range(1, self.k)) if contrasts is None else list(contrasts)
+        self._w_stride = 0
         if self.f_groups is not None:
             for s0, w in self.f_groups:
                 if s0 < 1 or w < 1 or s0 + w > self.k:
                     raise ValueError(f"column group ({s0}, {w}) outside the design's {self.k} columns")
-            self.contrasts = list(range(len(self.f_groups)))
+        if self.outputs is not None:
+            prog, self._w_stride = output_program(self.outputs)
+            for kind, j, w, _ in prog:
+                last = j + (0 if kind in (OUT_T, OUT_NEG_T) else w - 1)
+                if j < 0 or last >= self.k:
+                    raise ValueError(f"output {tuple(int(x) for x in (kind, j, w))} outside the design's "
+                                     f"{self.k} columns")
+            self.contrasts = list(range(len(self.outputs)))
         self.C = len(self.contrasts)
         self.signs = signs
         self.floor_zero = bool(floor_zero)
         self.vd = None if vdensity is None else dev(np.asarray(vdensity, np.float32))
         self.lib = _lib.load()
-        self._coef = dev(np.asarray(self.contrasts if self.f_groups is None else self.f_groups,
-                                    np.int32).reshape(-1))
+        self._coef = dev(np.asarray(self.contrasts, np.int32) if self.outputs is None
+                         else output_program(self.outputs)[0].reshape(-1))
         self._tc = TensorCoreOperands(self.Yd) if precision == "bf16x3" else None
         # the designs [1, pred_x] have an intercept: the tensor-core residuals
         # use the centred form unless an output needs coefficient 0
-        uses0 = (0 in self.contrasts) if self.f_groups is None else min(s0 for s0, _ in self.f_groups) < 1
+        uses0 = (0 in self.contrasts) if self.outputs is None else 0 in output_columns(self.outputs)
         self._centred = self._tc is not None and self._tc.Yc is not None and not uses0
         if batch == "auto":
             from .autotune import choose_batch
@@ -149,8 +168,9 @@ class PermutationEngine:
             P8, U, Xt = tc.host_operands(designs, centred=centred)
             pt = tc.tile_designs(dev(P8), G, designs.kmax)
             mode, wmat = 0, None
-            if self.f_groups is not None:
-                mode, wmat = 2, dev(designs.group_blocks(self.f_groups))
+            if self.outputs is not None:
+                mode = 3
+                wmat = dev(designs.program_weights(self.outputs)) if self._w_stride else None
             tc.stat(mode, pt, dev(U), dev(Xt), dev(designs.invdiag64.astype(np.float32)),
                     dev(designs.dof.astype(np.float32)), G, designs.kmax, self._coef, self.C, out, self.V,
                     wmat=wmat, centred=centred)
@@ -226,10 +246,9 @@ class PermutationEngine:
         slot = {"P": P}
         if tc is not None:
             Gp, DB = tc.padded(P, kmax), tc.block(kmax)
-            keys = ("P8", "U", "Xt", "invd", "dof") + (("W",) if self.f_groups is not None else ())
-            if self.f_groups is not None:
-                slot["h_W"] = t.zeros((P, sum(w * w for _, w in self.f_groups)), dtype=t.float32,
-                                      pin_memory=True)
+            keys = ("P8", "U", "Xt", "invd", "dof") + (("W",) if self._w_stride else ())
+            if self._w_stride:
+                slot["h_W"] = t.zeros((P, self._w_stride), dtype=t.float32, pin_memory=True)
             slot["h_P8"] = t.zeros((Gp * 8, tc.n_pad), dtype=t.float32, pin_memory=True)
             slot["h_U"] = t.zeros((Gp, kmax), dtype=t.float32, pin_memory=True)
             slot["h_Xt"] = t.zeros((Gp // DB, tc.n_sc, kmax, DB), dtype=t.float32, pin_memory=True)
@@ -253,7 +272,7 @@ class PermutationEngine:
                 slot["d_" + key].copy_(slot["h_" + key], non_blocking=True)
             if tc is not None:
                 tc.tile_designs(slot["d_P8"], P, kmax, out=slot["d_pt"])
-                tc.stat(2 if self.f_groups is not None else 0, slot["d_pt"], slot["d_U"], slot["d_Xt"],
+                tc.stat(3 if self.outputs is not None else 0, slot["d_pt"], slot["d_U"], slot["d_Xt"],
                         slot["d_invd"], slot["d_dof"], P, kmax, self._coef, self.C, slot["d_t"], self.V,
                         wmat=slot.get("d_W"), centred=self._centred)
             else:
@@ -286,8 +305,8 @@ class PermutationEngine:
         if self._tc is not None:
             self._tc.host_operands(db, P8=slot["h_P8"].numpy(), U=slot["h_U"].numpy(), Xt=slot["h_Xt"].numpy(),
                                    centred=self._centred)
-            if self.f_groups is not None:
-                slot["h_W"].numpy()[:P] = db.group_blocks(self.f_groups)
+            if self._w_stride:
+                db.program_weights(self.outputs, out=slot["h_W"].numpy()[:P])
         else:
             slot["h_pinv"].numpy()[:P] = db.pinv64
             slot["h_X"].numpy()[:P] = db.X64
@@ -361,8 +380,8 @@ class PermutationEngine:
         t = self.t
         db = DesignBatch(self.X[None])
         tm = t.empty((1, self.C, self.V), device="cuda", dtype=t.float32)
-        # the observed map: FP32 CUDA-core t (partial F exists on the tensor-core GLM only)
-        self.tmaps(db, out=tm, precision="fp32" if self.f_groups is None else None)
+        # the observed map: FP32 CUDA-core t (programmed outputs exist on the tensor-core GLM only)
+        self.tmaps(db, out=tm, precision="fp32" if self.outputs is None else None)
         maps = t.empty((self.C, self.signs, self.V), device="cuda", dtype=t.float32)
         mx = t.empty((self.C, self.signs, self.n_seg), device="cuda", dtype=t.float32)
         # the observed image is swept once: use the reference's exact arithmetic

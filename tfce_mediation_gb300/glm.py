@@ -14,6 +14,45 @@ from . import _lib
 from .device import dev, ptr, require_cuda, stream_handle
 
 WHAT_T, WHAT_BETA, WHAT_SE, WHAT_RESID, WHAT_F, WHAT_RSS = range(6)
+# typed output rows of the tensor-core GLM's programmed epilogue (glm_stat_tc mode 3)
+OUT_T, OUT_NEG_T, OUT_F, OUT_AMP, OUT_ACRO = range(5)
+_OUT_KIND = {"t": OUT_T, "-t": OUT_NEG_T, "f": OUT_F, "amp": OUT_AMP, "acro": OUT_ACRO}
+
+
+def output_program(outputs):
+    """Rows (kind, column, width, weight offset) int32 (C, 4) and the weight
+    stride of a list of typed outputs:
+      ("t", j) / ("-t", j): t (negated t) of coefficient j;
+      ("f", j, w): partial F of the columns [j, j+w) (Wald form);
+      ("amp", j) / ("acro", j): cosinor amplitude / acrophase t of the
+        (cos, sin) coefficient pair (j, j+1) (glm_cosinor, pyfunc.py:2406-2560).
+    The model F of an intercept design with k columns is ("f", 1, k-1)."""
+    rows, o = [], 0
+    for spec in outputs:
+        kind = _OUT_KIND.get(spec[0])
+        if kind is None:
+            raise ValueError(f"unknown output kind {spec[0]!r}")
+        j = int(spec[1])
+        if kind in (OUT_T, OUT_NEG_T):
+            rows.append((kind, j, 1, 0))
+        elif kind == OUT_F:
+            w = int(spec[2])
+            if w < 1:
+                raise ValueError("an 'f' row needs a width >= 1")
+            rows.append((kind, j, w, o))
+            o += w * w
+        else:
+            rows.append((kind, j, 2, o))
+            o += 3
+    return np.asarray(rows, np.int32).reshape(-1, 4), o
+
+
+def output_columns(outputs):
+    """The design columns an output program reads."""
+    cols = set()
+    for kind, j, w, _ in output_program(outputs)[0]:
+        cols.update(range(j, j + (1 if kind in (OUT_T, OUT_NEG_T) else w)))
+    return cols
 
 
 class DesignBatch:
@@ -72,14 +111,27 @@ class DesignBatch:
         """(G, sum w^2) float32: per design, inv(inv(X'X)_SS) of every column
         group S = (start, width), row-major, concatenated -- the Wald form of
         the extra sum of squares of dropping S."""
+        return self.program_weights([("f", s0, w) for s0, w in groups])
+
+    def program_weights(self, outputs, out=None):
+        """(G, w_stride) float32 per-design weights of an output program
+        (output_program): inv(inv(X'X)_SS) for an 'f' row, the inv(X'X)
+        entries (jj, j j+1, j+1 j+1) for an 'amp' / 'acro' row; written into
+        `out` (G, w_stride) when given."""
+        rows, stride = output_program(outputs)
         inv = self.inverse()
-        out = np.zeros((self.G, sum(w * w for _, w in groups)), np.float64)
-        for g in range(self.G):
-            o = 0
-            for s0, w in groups:
-                out[g, o:o + w * w] = np.linalg.inv(inv[g, s0:s0 + w, s0:s0 + w]).ravel()
-                o += w * w
-        return out.astype(np.float32)
+        w64 = np.zeros((self.G, stride), np.float64)
+        for kind, j, w, o in rows:
+            if j < 0 or j + w > self.kmax:
+                continue  # outside the designs: the kernel returns NaN for the row
+            if kind == OUT_F:
+                w64[:, o:o + w * w] = np.linalg.inv(inv[:, j:j + w, j:j + w]).reshape(self.G, w * w)
+            elif kind in (OUT_AMP, OUT_ACRO):
+                w64[:, o], w64[:, o + 1], w64[:, o + 2] = inv[:, j, j], inv[:, j, j + 1], inv[:, j + 1, j + 1]
+        if out is None:
+            return w64.astype(np.float32)
+        out[...] = w64
+        return out
 
     def to_device(self):
         return (dev(self.pinv64.astype(np.float32)), dev(self.X64.astype(np.float32)),
@@ -223,7 +275,9 @@ class TensorCoreOperands:
     def stat(self, mode, p_tiles, u_rows, x_rows, invd, dof, G, kmax, coef_d, n_coef, out, ldt, wmat=None,
              centred=False):
         """mode 0: t of coefficients coef_d; 1: RSS; 2: partial F of the column
-        groups coef_d = (start, width) pairs, wmat from DesignBatch.group_blocks.
+        groups coef_d = (start, width) pairs, wmat from DesignBatch.group_blocks;
+        3: output program rows coef_d (output_program), wmat from
+        DesignBatch.program_weights.
         centred: x_rows came from host_operands(..., centred=True)."""
         w_stride = 0 if wmat is None else int(wmat.shape[-1])
         _lib.check(self.lib.glm_stat_tc(ptr(self.yt), ptr(self.shift), ptr(self.Yd),
@@ -258,15 +312,17 @@ def glm_tstat_tc(Y, designs, coef, ops=None, centre=True):
     return out
 
 
-def glm_stat_tc(Y, designs, mode, coef=None, groups=None, ops=None):
+def glm_stat_tc(Y, designs, mode, coef=None, groups=None, ops=None, outputs=None):
     """Tensor-core GLM outputs for a DesignBatch: mode 't' -> (G, len(coef), V)
     t maps; 'rss' -> (G, V) residual sums of squares; 'f' -> (G, len(groups), V)
     partial F of the column groups [(start, width), ...] (glm_typeI's drop-one
-    F, tm/pyfunc.py:2282-2400)."""
+    F, tm/pyfunc.py:2282-2400); 'program' -> (G, len(outputs), V) typed output
+    rows (output_program)."""
     t = require_cuda()
     db = designs if isinstance(designs, DesignBatch) else DesignBatch(designs)
     ops = ops or TensorCoreOperands(dev(Y, t.float32))
-    uses0 = (mode == "t" and 0 in list(coef)) or (mode == "f" and min(s0 for s0, _ in groups) < 1)
+    uses0 = ((mode == "t" and 0 in list(coef)) or (mode == "f" and min(s0 for s0, _ in groups) < 1)
+             or (mode == "program" and 0 in output_columns(outputs)))
     centred = ops.centred_ok(db, first_column_used=uses0)
     P8, U, Xt = ops.host_operands(db, centred=centred)
     pt = ops.tile_designs(dev(P8), db.G, db.kmax)
@@ -282,8 +338,12 @@ def glm_stat_tc(Y, designs, mode, coef=None, groups=None, ops=None):
         m, rows = 2, len(groups)
         coef_d = dev(np.asarray(groups, np.int32).reshape(-1))
         wmat = dev(db.group_blocks(groups))
+    elif mode == "program":
+        rows_i, stride = output_program(outputs)
+        m, rows, coef_d = 3, len(outputs), dev(rows_i.reshape(-1))
+        wmat = dev(db.program_weights(outputs)) if stride else None
     else:
-        raise ValueError("mode must be 't', 'rss' or 'f'")
+        raise ValueError("mode must be 't', 'rss', 'f' or 'program'")
     out = t.empty((db.G, rows, ops.V), device="cuda", dtype=t.float32)
     ops.stat(m, pt, u, xt, invd, dof, db.G, db.kmax, coef_d, rows, out, ops.V, wmat=wmat, centred=centred)
     t.cuda.synchronize()

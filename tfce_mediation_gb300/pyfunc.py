@@ -9,6 +9,8 @@ sweeps, regressions and indirect-effect maps run on the GPU:
 * calc_sobelz                                    (pyfunc.py:130-162)
 * find_nearest                                   (pyfunc.py:254-261)
 * calc_indirect, check_blocks, rand_blocks       (pyfunc.py:2678-2757)
+* glm_typeI                                      (pyfunc.py:2282-2400)
+* glm_cosinor (+ its design, cosinor_design)     (pyfunc.py:2406-2560)
 """
 from __future__ import annotations
 
@@ -286,3 +288,113 @@ def glm_typeI(endog, exog, dmy_covariates=None, output_fvalues=True, output_tval
         return (Fvalues, np.array(Fvar))
     print("No output has been selected")
     return None
+
+
+def cosinor_design(time_var, period, exog=None, dmy_covariates=None):
+    """The cosinor design [1, cos(2 pi t / p), sin(2 pi t / p) per period,
+    exog..., covariates] (pyfunc.py:2428-2457), float64."""
+    t = np.asarray(time_var, np.float64)
+    n = t.shape[0]
+    cols = [np.ones((n, 1))]
+    for p in period:
+        cols.append(np.cos(np.divide(2.0 * np.pi * t, p)).reshape(n, 1))
+        cols.append(np.sin(np.divide(2.0 * np.pi * t, p)).reshape(n, 1))
+    for var in exog or []:
+        cols.append(np.asarray(var, np.float64).reshape(n, -1))
+    if dmy_covariates is not None:
+        cols.append(np.asarray(dmy_covariates, np.float64).reshape(n, -1))
+    return np.column_stack(cols)
+
+
+def _acrophase(b_cos, b_sin, quadrant):
+    """arctan(|b_sin / b_cos|), with the reference's sign/quadrant rule when
+    `quadrant` (pyfunc.py:2475-2490)."""
+    with np.errstate(divide="ignore", invalid="ignore"):
+        acro = np.arctan(np.abs(np.divide(-b_sin, b_cos)))
+    if quadrant:
+        acro = acro.copy()
+        m = (b_sin > 0) & (b_cos >= 0)
+        acro[m] = -acro[m]
+        m = (b_sin > 0) & (b_cos < 0)
+        acro[m] = -np.pi + acro[m]
+        m = (b_sin < 0) & (b_cos <= 0)
+        acro[m] = -np.pi - acro[m]
+        m = (b_sin <= 0) & (b_cos > 0)
+        acro[m] = -2.0 * np.pi + acro[m]
+    return acro
+
+
+def glm_cosinor(endog, time_var, exog=None, dmy_covariates=None, rand_array=None, interaction_var=None,
+                period=[24.0], calc_MESOR=True, output_fit_only=False):
+    """Cosinor GLM of the tm-models path, pyfunc.py:2406-2560, on the GPU.
+
+    Design [1, (cos, sin) per period, exog..., dmy_covariates], rows permuted
+    by rand_array.  Returns the reference's tuple (R2, MESOR, SE_MESOR,
+    AMPLITUDE, SE_AMPLITUDE, ACROPHASE, SE_ACROPHASE, Fmodel, tMESOR,
+    |tAMPLITUDE|, |tACROPHASE|, tEXOG), or (MESOR, AMPLITUDE, ACROPHASE) with
+    output_fit_only.  Betas, RSS, t and the model F (TSS around each column's
+    mean) come from the FP32 CUDA-core GLM; the amplitude/acrophase error
+    propagation is the reference's elementwise FP64 arithmetic on those.  The
+    permutation loop does not call this: its maps come from the tensor-core
+    GLM's programmed epilogue (randomise.tm_models_cosinor_run).
+    interaction_var: the reference multiplies a design ROW by it
+    (exog_vars[i+1] * interaction_var), which only broadcasts for degenerate
+    sizes; it is refused here."""
+    from .glm import WHAT_BETA, WHAT_RSS, glm_fstat
+    if interaction_var is not None:
+        raise ValueError("interaction_var is not supported (the reference's interaction term indexes a design row)")
+    y = np.asarray(endog)
+    one = y.ndim == 1
+    Y = np.ascontiguousarray(y.reshape(y.shape[0], -1), np.float32)
+    n = Y.shape[0]
+    n_per = len(period)
+    X = cosinor_design(time_var, period, exog, dmy_covariates)
+    if rand_array is not None:
+        X = X[np.asarray(rand_array)]
+    k = X.shape[1]
+    db = DesignBatch([X])
+    a = glm_stat(Y, db, WHAT_BETA)[0].cpu().numpy().astype(np.float64)  # (k, V)
+
+    def out(v):
+        return v[..., 0] if one else v
+
+    if output_fit_only:
+        amp = np.asarray([np.sqrt(a[1 + 2 * i] ** 2 + a[2 + 2 * i] ** 2) for i in range(n_per)])
+        acro = np.asarray([_acrophase(a[1 + 2 * i], a[2 + 2 * i], True) for i in range(n_per)])
+        return out(a[0]), out(amp), out(acro)
+    rss = glm_stat(Y, db, WHAT_RSS)[0].cpu().numpy().astype(np.float64)
+    F = glm_fstat(Y, db)[0].cpu().numpy().astype(np.float64)
+    df_between, df_within = k - 1, n - k
+    sigma = np.sqrt(rss / df_within)
+    invXX = db.inverse()[0]
+    MESOR = tMESOR = SE_MESOR = tEXOG = None
+    if calc_MESOR or exog is not None:
+        if one:
+            se = np.sqrt(sigma[None, :] ** 2 * np.diag(invXX)[:, None])
+        else:
+            se = np.sqrt((rss / df_within)[None, :] * np.diag(invXX)[:, None]).astype(np.float32)
+        T = a / se
+        MESOR, tMESOR, SE_MESOR = out(a[0]), out(T[0]), out(se[0])
+        if exog is not None:
+            tEXOG = out(T[3 + 2 * (n_per - 1):])
+    amp, acro, se_amp, se_acro, t_amp, t_acro = [], [], [], [], [], []
+    for i in range(n_per):
+        c, s = 1 + 2 * i, 2 + 2 * i
+        A = np.sqrt(a[c] ** 2 + a[s] ** 2)
+        ph = _acrophase(a[c], a[s], False)
+        sn, cs = np.sin(ph), np.cos(ph)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            sp = sigma * np.sqrt(invXX[c, c] * sn ** 2 + 2 * invXX[c, s] * sn * cs + invXX[s, s] * cs ** 2) / A
+            sa = sigma * np.sqrt(invXX[c, c] * cs ** 2 - 2 * invXX[c, s] * sn * cs + invXX[s, s] * sn ** 2)
+            t_amp.append(np.abs(A / sa))
+            t_acro.append(np.abs(1.0 / sp))
+        amp.append(A)
+        acro.append(_acrophase(a[c], a[s], True) if rand_array is None else ph)
+        se_amp.append(sa)
+        se_acro.append(sp)
+    R2 = None
+    if rand_array is None:
+        ssb = F * rss * df_between / df_within
+        R2 = out(ssb / (ssb + rss))
+    arr = [out(np.asarray(v)) for v in (amp, se_amp, acro, se_acro, t_amp, t_acro)]
+    return (R2, MESOR, SE_MESOR, arr[0], arr[1], arr[2], arr[3], out(F), tMESOR, arr[4], arr[5], tEXOG)

@@ -39,6 +39,16 @@ def _load(path):
     return np.load(path, allow_pickle=True)
 
 
+def _saved_none(a):
+    """Whether a loaded .npy holds a saved None (the reference tests
+    `np.all(x) is None`, which numpy >= 2 no longer answers with None for a
+    0-d object array)."""
+    if a is None:
+        return True
+    a = np.asarray(a)
+    return a.dtype == object and a.ndim == 0 and a.item() is None
+
+
 def _perm_rows(n, start, stop, seed):
     rows = []
     for it in range(start, stop):
@@ -84,15 +94,20 @@ def vertex_regress_parser(ap=None):
     return ap
 
 
-def _designs_for(X, n, start, stop, opts, seed):
+def _designs_for(X, n, start, stop, opts, seed, equal_blocks_only=False):
     """Permuted designs of the reference loop (randomise :90-105), including the
-    in-place cumulative -v column permutation and exchange blocks."""
+    in-place cumulative -v column permutation and exchange blocks.  The
+    vertex/voxel loops always shuffle the blocks' order; the tm-models loops
+    (rand_blocks, pyfunc.py:2733-2757, with check_blocks) shuffle it only when
+    every block has the same size: pass equal_blocks_only=True for those."""
     out = []
     X = X.copy()
     block_list = None
     if getattr(opts, "exchangeblock", None):
         block_list = np.genfromtxt(opts.exchangeblock[0], dtype=str)
         indexer = np.array(range(len(block_list)))
+        sizes = [int(np.sum(block_list == b)) for b in np.unique(block_list)]
+        shuffle_blocks = not equal_blocks_only or all(z == sizes[0] for z in sizes)
     for it in range(start, stop):
         if seed is None:
             np.random.seed(int(it * 1000 + time()))
@@ -104,8 +119,8 @@ def _designs_for(X, n, start, stop, opts, seed):
             X[:, a:b] = X[:, a:b][rng.permutation(list(range(n)))]
             out.append(X.copy())
         elif block_list is not None:
-            randindex = [rng.permutation(indexer[block_list == blk])
-                         for blk in rng.permutation(list(np.unique(block_list)))]
+            order = rng.permutation(list(np.unique(block_list))) if shuffle_blocks else np.unique(block_list)
+            randindex = [rng.permutation(indexer[block_list == blk]) for blk in order]
             out.append(X[np.concatenate(randindex)])
         else:
             out.append(X[rng.permutation(list(range(n)))])
@@ -301,6 +316,22 @@ def mmr_lr_run(surf_num, perm_range, seed, path, H, E_, pred_x=None, mediation=N
     return maxima
 
 
+def _tm_models_space(tempdir, surface):
+    """Adjacency and sweep settings of a tm-models temp directory
+    (tm_models_randomise.py:155-170): surface -> both masked hemispheres as two
+    segments with density weights and the zero-fill floor of
+    write_perm_maxTFCE_vertex; volume -> one voxel adjacency."""
+    if surface:
+        mask_lh, mask_rh = _load(f"{tempdir}/mask_lh.npy"), _load(f"{tempdir}/mask_rh.npy")
+        adj_lh, adj_rh = _load(f"{tempdir}/adjac_lh.npy"), _load(f"{tempdir}/adjac_rh.npy")
+        vd_lh, vd_rh = _load(f"{tempdir}/vdensity_lh.npy"), _load(f"{tempdir}/vdensity_rh.npy")
+        off, idx, seg = _hemispheres(adj_lh, adj_rh, mask_lh, mask_rh)
+        vd = np.concatenate([_vd(vd_lh, mask_lh), _vd(vd_rh, mask_rh)])
+        return off, idx, dict(segments=seg, vdensity=vd, floor_zero=True), "%.4f", "maxVertex"
+    off, idx = to_csr(_load(f"{tempdir}/adjac.npy"))
+    return off, idx, dict(segments=None), "%1.4f", "maxVoxel"
+
+
 def tm_models_glm_parser(ap=None):
     ap = ap or argparse.ArgumentParser(description="tm-models GLM permutations (GPU)")
     ap.add_argument("-r", "--range", nargs=2, type=int, required=True, metavar=("INT", "INT"))
@@ -330,7 +361,7 @@ def tm_models_glm_run(opts):
     data = _load(f"{tempdir}/data.npy")
     optstfce = _load(f"{tempdir}/optstfce.npy")
     cov = _load(f"{tempdir}/dmy_covariates.npy")
-    cov = None if np.all(cov) is None else np.asarray(cov, np.float64)
+    cov = None if _saved_none(cov) else np.asarray(cov, np.float64)
     n = data.shape[0]
     pred_x = exog_flat if cov is None else np.column_stack([exog_flat, cov])
     X = np.column_stack([np.ones(n), pred_x])
@@ -340,23 +371,10 @@ def tm_models_glm_run(opts):
         s0 += w
     numcon = sum(exog_shape)
     H, E_ = float(optstfce[0]), float(optstfce[1])
-    if surface:
-        num_vertex_lh = int(_load(f"{tempdir}/num_vertex_lh.npy"))
-        mask_lh, mask_rh = _load(f"{tempdir}/mask_lh.npy"), _load(f"{tempdir}/mask_rh.npy")
-        adj_lh, adj_rh = _load(f"{tempdir}/adjac_lh.npy"), _load(f"{tempdir}/adjac_rh.npy")
-        vd_lh, vd_rh = _load(f"{tempdir}/vdensity_lh.npy"), _load(f"{tempdir}/vdensity_rh.npy")
-        off, idx, seg = _hemispheres(adj_lh, adj_rh, mask_lh, mask_rh)
-        vd = np.concatenate([_vd(vd_lh, mask_lh), _vd(vd_rh, mask_rh)])
-        kw = dict(segments=seg, vdensity=vd, floor_zero=True)
-        fmt, suffix = "%.4f", "maxVertex"
-        del num_vertex_lh
-    else:
-        off, idx = to_csr(_load(f"{tempdir}/adjac.npy"))
-        kw = dict(segments=None)
-        fmt, suffix = "%1.4f", "maxVoxel"
+    off, idx, kw, fmt, suffix = _tm_models_space(tempdir, surface)
     Y = np.ascontiguousarray(data, np.float32)
     batch = getattr(opts, "batch", 64)
-    designs = _designs_for(X, n, start, stop, opts, seed)
+    designs = _designs_for(X, n, start, stop, opts, seed, equal_blocks_only=True)
     os.makedirs(outdir, exist_ok=True)
     out = {}
 
@@ -381,3 +399,82 @@ def tm_models_glm_run(opts):
                     [fmt % mf[p, j, 0] for p in range(mf.shape[0])])
         out["f"] = mf
     return out
+
+
+def tm_models_cosinor_parser(ap=None):
+    return tm_models_glm_parser(ap or argparse.ArgumentParser(description="tm-models cosinor permutations (GPU)"))
+
+
+def cosinor_outputs(n_period, n_exog, n_cov=0):
+    """Output program of the cosinor permutation statistics
+    (tm_models_randomise.py:274-372, glm_cosinor with calc_MESOR=False): model F
+    (the partial F of every column after the intercept), per period the
+    amplitude and acrophase t, then t and -t of every exogenous column; the
+    design is [1, (cos, sin) per period, exog columns, covariates]."""
+    k = 1 + 2 * n_period + n_exog + n_cov
+    outs = [("f", 1, k - 1)]
+    for i in range(n_period):
+        outs += [("amp", 1 + 2 * i), ("acro", 1 + 2 * i)]
+    c0 = 1 + 2 * n_period
+    for j in range(n_exog):
+        outs += [("t", c0 + j), ("-t", c0 + j)]
+    return outs
+
+
+def tm_models_cosinor_run(opts):
+    """The cosinor branch of tm_models_randomise.py (:102-118, :274-372): per
+    permutation of the design rows (exchange blocks as rand_blocks), the model
+    F, the amplitude and acrophase t of every period and +/- t of every
+    exogenous column, each TFCE'd with one sign (the reference sweeps -t as its
+    own map into the same CSV); maxima appended to the reference's CSVs
+    (perm_Fstat_model, perm_Tstat_amplitude_%2.2f, perm_Tstat_acrophase_%2.2f,
+    perm_Tstat_<name> or perm_Tstat_con%d)."""
+    from .pyfunc import cosinor_design
+    start, stop = int(opts.range[0]), int(opts.range[1]) + 1
+    seed = opts.seed[0] if getattr(opts, "seed", None) else None
+    surface = str(opts.surface[0]) if getattr(opts, "surface", None) else None
+    tempdir = "tmtemp_cosinor_%s" % surface if surface else "tmtemp_cosinor_volume"
+    outdir = "output_cosinor_%s/perm_cosinor" % surface if surface else "output_cosinor_volume/perm_cosinor"
+    time_var = np.asarray(_load(f"{tempdir}/time_var.npy"), np.float64)
+    period = [float(p) for p in np.atleast_1d(_load(f"{tempdir}/period.npy"))]
+    exog_flat = _load(f"{tempdir}/exog_flat.npy")
+    if _saved_none(exog_flat):
+        exog, varnames, numcon = None, [], 0
+    else:
+        exog_flat = np.asarray(exog_flat, np.float64)
+        exog_flat = exog_flat.reshape(exog_flat.shape[0], -1)
+        exog = [exog_flat]
+        numcon = exog_flat.shape[1]
+        varnames = list(_load(f"{tempdir}/varnames.npy"))
+    data = _load(f"{tempdir}/data.npy")
+    optstfce = _load(f"{tempdir}/optstfce.npy")
+    cov = _load(f"{tempdir}/dmy_covariates.npy")
+    cov = None if _saved_none(cov) else np.asarray(cov, np.float64).reshape(data.shape[0], -1)
+    n = data.shape[0]
+    X = cosinor_design(time_var, period, exog, cov)
+    outs = cosinor_outputs(len(period), numcon, 0 if cov is None else cov.shape[1])
+    H, E_ = float(optstfce[0]), float(optstfce[1])
+    off, idx, kw, fmt, suffix = _tm_models_space(tempdir, surface)
+    Y = np.ascontiguousarray(data, np.float32)
+    batch = getattr(opts, "batch", 64)
+    designs = _designs_for(X, n, start, stop, opts, seed, equal_blocks_only=True)
+    os.makedirs(outdir, exist_ok=True)
+    eng = E.PermutationEngine(Y, X[:, 1:], (off, idx), H=H, E=E_, outputs=outs, batch=batch, **kw)
+    m = _run_designs(eng, designs, eng.batch)  # (P, C, 1, S)
+    m = (m.max(axis=-1) if surface else m[..., 0])[:, :, 0]  # (P, C)
+
+    def csv(name):
+        return os.path.join(outdir, "perm_%s_TFCE_%s.csv" % (name, suffix))
+
+    _append(csv("Fstat_model"), [fmt % v for v in m[:, 0]])
+    for i, per in enumerate(period):
+        _append(csv("Tstat_amplitude_%2.2f" % per), [fmt % v for v in m[:, 1 + 2 * i]])
+        _append(csv("Tstat_acrophase_%2.2f" % per), [fmt % v for v in m[:, 2 + 2 * i]])
+    c0 = 1 + 2 * len(period)
+    for j in range(numcon):
+        name = "Tstat_%s" % varnames[j] if len(varnames) == numcon else "Tstat_con%d" % (j + 1)
+        lines = []
+        for p in range(m.shape[0]):
+            lines += [fmt % m[p, c0 + 2 * j], fmt % m[p, c0 + 2 * j + 1]]
+        _append(csv(name), lines)
+    return m
