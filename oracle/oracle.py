@@ -526,3 +526,162 @@ def apply_mfwer(pos_images, neg_images, perm_max, position_array, weight=None, m
         if not mediation:
             negative_data[:, c] = [find_nearest(srt, k, p_array) for k in negative_data[:, c]]
     return positive_data, (None if mediation else negative_data)
+
+
+# -- tm-models repeated-measures ANCOVA (reg_rm_ancova_*_bs_factor) ----------
+def _dummy_code(variable, demean=True):
+    """dummy_code(iscontinous=False) (tm/pyfunc.py:2564-2600): one column per
+    level after the first, squeezed, optionally demeaned."""
+    variable = np.asarray(variable)
+    cols = [(variable == v).astype(np.float64) for v in np.unique(variable)]
+    d = np.squeeze(np.array(cols)[1:]).astype(int).T
+    return d - np.mean(d, 0) if demean else d
+
+
+def _column_product(a1, a2):
+    """column_product (tm/pyfunc.py:2622-2660): every column of a1 times every
+    column of a2, a1-major."""
+    a1, a2 = np.asarray(a1), np.asarray(a2)
+    if a1.ndim == 1:
+        return (a1 * a2.T).T
+    if a2.ndim == 1:
+        return (a2 * a1.T).T
+    return np.concatenate([(a1[:, i] * a2.T).T.reshape(len(a1), -1) for i in range(a1.shape[1])], axis=1)
+
+
+def _ones(a):
+    return np.column_stack([np.ones(len(a)), a])
+
+
+def _rss(X, y):
+    a = np.linalg.inv(X.T @ X) @ X.T @ y
+    return np.sum((y - X @ a) ** 2, axis=0)
+
+
+def _rm_long(data, data_format, n_short):
+    if data_format == "short":
+        data = np.asarray(data)
+        if data.ndim == 2:
+            data = data[:, :, None]
+        s, n = data.shape[0], data.shape[1]
+        return data.reshape(s * n, data.shape[2]), n, s
+    n = n_short
+    return np.asarray(data), n, len(data) // n
+
+
+def _tile(a, s):
+    return None if a is None else np.concatenate([a] * s, 0)
+
+
+def rm_ancova_one(data, dmy_factor1, dmy_subjects, dmy_covariates=None, data_format="short", rand_array=None,
+                  shuffle=None):
+    """reg_rm_ancova_one_bs_factor (tm/pyfunc.py:2067-2280) without p values:
+    (F_a, F_s, F_sa).  Every SS is the reference's SS_Total - RSS difference
+    (FP64 fits; SS_Total in the data's own type).  With rand_array the data's
+    long rows are shuffled by the index array `shuffle` (what the reference's
+    np.random.shuffle draws next from the global RNG) and the factor and
+    covariate rows permuted by rand_array."""
+    endog, n, s = _rm_long(data, data_format, len(dmy_factor1))
+    f1 = np.asarray(dmy_factor1, np.float64)
+    cov = None if dmy_covariates is None else np.asarray(dmy_covariates, np.float64)
+    fa = 2 if f1.ndim == 1 else f1.shape[1] + 1
+    if rand_array is not None:
+        endog = endog[np.asarray(shuffle)]
+        f1 = f1[rand_array]
+        cov = None if cov is None else cov[rand_array]
+    y_in = np.squeeze(endog)
+    y = np.asarray(y_in, np.float64)
+    interval = np.concatenate([np.full(n, float(i)) for i in range(s)])
+    iv = _dummy_code(interval, demean=False)
+    f1l, subl, covl = _tile(f1, s), _tile(np.asarray(dmy_subjects, np.float64), s), _tile(cov, s)
+    sst = np.sum((y_in - np.mean(y_in, axis=0)) ** 2, axis=0).astype(np.float64)
+    ss_ws = _rss(_ones(subl), y)
+    ss_bs = sst - ss_ws
+    X = _ones(f1l) if covl is None else np.column_stack([_ones(f1l), covl])
+    ss_cells_a = sst - _rss(X, y)
+    ss_cov = 0.0 if covl is None else sst - _rss(_ones(covl), y)
+    ss_a = ss_cells_a - ss_cov
+    ss_wf = ss_bs - ss_a - ss_cov
+    ss_s = sst - _rss(_ones(iv), y)
+    ss_scov = 0.0
+    if covl is not None:
+        cells = sst - _rss(np.column_stack([_ones(covl), _column_product(covl, iv), iv]), y)
+        ss_scov = cells - (sst - _rss(np.column_stack([_ones(covl), iv]), y))
+    X = np.column_stack([_ones(f1l), iv, _column_product(f1l, iv)])
+    X2 = np.column_stack([_ones(f1l), iv])
+    if covl is not None:
+        X = np.column_stack([X, covl, _column_product(covl, iv)])
+        X2 = np.column_stack([X2, covl, _column_product(covl, iv)])
+    ss_sa = (sst - _rss(X, y)) - (sst - _rss(X2, y))
+    ss_swf = ss_ws - ss_s - ss_sa - ss_scov
+    df_a = fa - 1
+    df_cov = 0 if cov is None else (1 if cov.ndim == 1 else cov.shape[1])
+    df_wf = n - 1 - df_a - df_cov
+    df_s = s - 1
+    df_sa, df_swf = df_a * df_s, df_wf * df_s
+    ms_wf, ms_swf = ss_wf / df_wf, ss_swf / df_swf
+    return (ss_a / df_a) / ms_wf, (ss_s / df_s) / ms_swf, (ss_sa / df_sa) / ms_swf
+
+
+def rm_ancova_two(data, dmy_factor1, dmy_factor2, dmy_subjects, dmy_covariates=None, data_format="short",
+                  rand_array=None, shuffle=None):
+    """reg_rm_ancova_two_bs_factor (tm/pyfunc.py:1712-2060) without p values:
+    (F_a, F_b, F_ab, F_s, F_sa, F_sb, F_sab), type I sums of squares as the
+    reference forms them (see rm_ancova_one for the permutation arguments)."""
+    endog, n, s = _rm_long(data, data_format, len(dmy_factor1))
+    f1 = np.asarray(dmy_factor1, np.float64)
+    f2 = np.asarray(dmy_factor2, np.float64)
+    cov = None if dmy_covariates is None else np.asarray(dmy_covariates, np.float64)
+    fa = 2 if f1.ndim == 1 else f1.shape[1] + 1
+    fb = 2 if f2.ndim == 1 else f2.shape[1] + 1
+    if rand_array is not None:
+        endog = endog[np.asarray(shuffle)]
+        f1, f2 = f1[rand_array], f2[rand_array]
+        cov = None if cov is None else cov[rand_array]
+    y_in = endog
+    y = np.asarray(y_in, np.float64)
+    f12 = _column_product(f1, f2)
+    interval = np.concatenate([np.full(n, float(i)) for i in range(s)])
+    iv = _dummy_code(interval, demean=False)
+    f1l, f2l, f12l = _tile(f1, s), _tile(f2, s), _tile(f12, s)
+    subl, covl = _tile(np.asarray(dmy_subjects, np.float64), s), _tile(cov, s)
+
+    def with_cov(X, cross=False):
+        if covl is None:
+            return X
+        X = np.column_stack([X, covl])
+        return np.column_stack([X, _column_product(covl, iv)]) if cross else X
+
+    sst = np.sum((y_in - np.mean(y_in, axis=0)) ** 2, axis=0).astype(np.float64)
+    ss_ws = _rss(_ones(subl), y)
+    ss_bs = sst - ss_ws
+    ss_cells_ab = sst - _rss(with_cov(np.column_stack([_ones(f1l), f2l, f12l])), y)
+    ss_ab = ss_cells_ab - (sst - _rss(with_cov(_ones(np.column_stack([f1l, f2l]))), y))
+    ss_cov = 0.0 if covl is None else sst - _rss(_ones(covl), y)
+    ss_a = (sst - _rss(with_cov(_ones(f1l)), y)) - ss_cov
+    ss_b = ss_cells_ab - ss_cov - ss_ab - ss_a
+    ss_wf = ss_bs - ss_a - ss_b - ss_ab - ss_cov
+    ss_s = sst - _rss(_ones(iv), y)
+    base = np.column_stack([_ones(f1l), f2l, f12l, iv, _column_product(f1l, iv), _column_product(f2l, iv)])
+    ss_sab = (sst - _rss(with_cov(np.column_stack([base, _column_product(f12l, iv)]), True), y)) \
+        - (sst - _rss(with_cov(base, True), y))
+    ss_scov = 0.0
+    if covl is not None:
+        cells = sst - _rss(np.column_stack([_ones(covl), _column_product(covl, iv), iv]), y)
+        ss_scov = cells - (sst - _rss(np.column_stack([_ones(covl), iv]), y))
+    ss_sa = (sst - _rss(with_cov(np.column_stack([_ones(f1l), iv, _column_product(f1l, iv)]), True), y)) \
+        - (sst - _rss(with_cov(np.column_stack([_ones(f1l), iv]), True), y))
+    Xb = np.column_stack([_ones(f1l), f2l, iv, _column_product(f1l, iv)])
+    ss_sb = (sst - _rss(with_cov(np.column_stack([Xb, _column_product(f2l, iv)]), True), y)) \
+        - (sst - _rss(with_cov(Xb, True), y))
+    ss_swf = ss_ws - ss_s - ss_sa - ss_sb - ss_sab - ss_scov
+    df_a, df_b = fa - 1, fb - 1
+    df_ab = df_a * df_b
+    df_cov = 0 if cov is None else (1 if cov.ndim == 1 else cov.shape[1])
+    df_wf = n - 1 - df_a - df_b - df_ab - df_cov
+    df_s = s - 1
+    df_swf = df_wf * df_s
+    ms_wf, ms_swf = ss_wf / df_wf, ss_swf / df_swf
+    return ((ss_a / df_a) / ms_wf, (ss_b / df_b) / ms_wf, (ss_ab / df_ab) / ms_wf, (ss_s / df_s) / ms_swf,
+            (ss_sa / (df_a * df_s)) / ms_swf, (ss_sb / (df_b * df_s)) / ms_swf,
+            (ss_sab / (df_ab * df_s)) / ms_swf)

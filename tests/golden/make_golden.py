@@ -312,6 +312,62 @@ def main():
     out["cos_fit_MESOR"], out["cos_fit_AMP"], out["cos_fit_ACRO"] = (np.asarray(v) for v in fit)
     out["cos_y"], out["cos_t"], out["cos_ex"], out["cos_cov"], out["cos_perm"] = yc, tcos, exc, covc, permc
 
+    # reg_rm_ancova_one_bs_factor / _two_bs_factor (tm-models RM-ANCOVA), short
+    # data format, observed and permuted.  A permuted call draws its row
+    # shuffle from the global RNG after rand_array; the same draws are
+    # replayed here and stored ("rm*_shuffle").  The reference shuffles the
+    # caller's array in place (its long form is a view), so every call gets
+    # its own copy of the data.
+    def seeded_call(fn, seed, n_subj, n_long, *args, **kw):
+        np.random.seed(seed)
+        ra = np.random.permutation(n_subj)
+        res = fn(*args, rand_array=ra, **kw)
+        np.random.seed(seed)
+        np.random.permutation(n_subj)
+        return res, ra, np.random.permutation(n_long)
+
+    n1, s1, V1 = 24, 3, 20
+    g1 = rng.integers(0, 2, n1)
+    f1 = pyfunc.dummy_code(g1)
+    subj1 = pyfunc.dummy_code(np.arange(n1), demean=False)
+    cov1 = rng.standard_normal((n1, 1))
+    d1 = rng.standard_normal((s1, n1, V1)).astype(np.float32) + 3.0
+    d1 += (0.7 * rng.standard_normal(n1))[None, :, None].astype(np.float32)  # subject effects
+    d1[2, :, :6] += (0.9 * g1)[:, None].astype(np.float32)  # group x time
+    d1[1:, :, 6:10] += np.float32(0.6)  # time
+    for tag, cv in (("nocov", None), ("cov", cov1)):
+        res = pyfunc.reg_rm_ancova_one_bs_factor(d1.copy(), f1, subj1, dmy_covariates=cv, verbose=False)
+        out[f"rm1_obs_{tag}"] = np.asarray(res)
+        res, ra, sh = seeded_call(pyfunc.reg_rm_ancova_one_bs_factor, 91, n1, n1 * s1, d1.copy(), f1, subj1,
+                                  dmy_covariates=cv, verbose=False)
+        out[f"rm1_perm_{tag}"], out[f"rm1_ra_{tag}"], out[f"rm1_shuffle_{tag}"] = np.asarray(res), ra, sh
+    out["rm1_data"], out["rm1_f1"], out["rm1_subj"], out["rm1_cov"] = d1, f1, subj1, cov1
+    # the caller's array after one permuted call (shuffled in place)
+    d_after = d1.copy()
+    seeded_call(pyfunc.reg_rm_ancova_one_bs_factor, 93, n1, n1 * s1, d_after, f1, subj1, verbose=False)
+    out["rm1_after_perm"] = d_after
+    np.random.seed(93)
+    np.random.permutation(n1)
+    out["rm1_after_shuffle"] = np.random.permutation(n1 * s1)
+
+    n2, s2, V2 = 30, 3, 16
+    ga, gb = rng.integers(0, 2, n2), rng.integers(0, 3, n2)
+    fa2, fb2 = pyfunc.dummy_code(ga), pyfunc.dummy_code(gb)
+    subj2 = pyfunc.dummy_code(np.arange(n2), demean=False)
+    cov2 = rng.standard_normal((n2, 1))
+    d2 = rng.standard_normal((s2, n2, V2)).astype(np.float32) + 2.0
+    d2 += (0.5 * rng.standard_normal(n2))[None, :, None].astype(np.float32)
+    d2[:, :, :5] += (0.8 * (gb == 2))[None, :, None].astype(np.float32)
+    d2[2, :, 5:9] += (0.9 * ga)[:, None].astype(np.float32)
+    for tag, cv in (("nocov", None), ("cov", cov2)):
+        res = pyfunc.reg_rm_ancova_two_bs_factor(d2.copy(), fa2, fb2, subj2, dmy_covariates=cv, verbose=False)
+        out[f"rm2_obs_{tag}"] = np.asarray(res)
+        res, ra, sh = seeded_call(pyfunc.reg_rm_ancova_two_bs_factor, 92, n2, n2 * s2, d2.copy(), fa2, fb2,
+                                  subj2,
+                                  dmy_covariates=cv, verbose=False)
+        out[f"rm2_perm_{tag}"], out[f"rm2_ra_{tag}"], out[f"rm2_shuffle_{tag}"] = np.asarray(res), ra, sh
+    out["rm2_data"], out["rm2_fa"], out["rm2_fb"], out["rm2_subj"], out["rm2_cov"] = d2, fa2, fb2, subj2, cov2
+
     path = os.path.join(HERE, "reference_vectors.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({os.path.getsize(path)} bytes, {len(out)} arrays)")

@@ -250,3 +250,34 @@ def test_cosinor_program_forms(golden):
         t_acro = a2 / (sigma * np.sqrt(inv[c, c] * b[s] ** 2 + cr + inv[s, s] * b[c] ** 2))
         np.testing.assert_allclose(t_amp, res[9][i], rtol=1e-10)
         np.testing.assert_allclose(t_acro, res[10][i], rtol=1e-10)
+
+
+@pytest.mark.parametrize("tag", ["nocov", "cov"])
+@pytest.mark.parametrize("kind", ["obs", "perm"])
+def test_rm_ancova_one(golden, tag, kind):
+    """The FP64 restatement of reg_rm_ancova_one_bs_factor against the
+    reference's (F_a, F_s, F_sa); the permuted call replays the reference's
+    global-RNG row shuffle."""
+    cov = golden["rm1_cov"] if tag == "cov" else None
+    kw = {} if kind == "obs" else dict(rand_array=golden[f"rm1_ra_{tag}"], shuffle=golden[f"rm1_shuffle_{tag}"])
+    got = oracle.rm_ancova_one(golden["rm1_data"], golden["rm1_f1"], golden["rm1_subj"], dmy_covariates=cov, **kw)
+    np.testing.assert_allclose(np.asarray(got), golden[f"rm1_{kind}_{tag}"], rtol=1e-9)
+
+
+@pytest.mark.parametrize("tag", ["nocov", "cov"])
+@pytest.mark.parametrize("kind", ["obs", "perm"])
+def test_rm_ancova_two(golden, tag, kind):
+    cov = golden["rm2_cov"] if tag == "cov" else None
+    kw = {} if kind == "obs" else dict(rand_array=golden[f"rm2_ra_{tag}"], shuffle=golden[f"rm2_shuffle_{tag}"])
+    got = oracle.rm_ancova_two(golden["rm2_data"], golden["rm2_fa"], golden["rm2_fb"], golden["rm2_subj"],
+                               dmy_covariates=cov, **kw)
+    np.testing.assert_allclose(np.asarray(got), golden[f"rm2_{kind}_{tag}"], rtol=1e-9)
+
+
+def test_rm_ancova_shuffles_caller_data_in_place(golden):
+    """A permuted reg_rm_ancova_* call leaves the caller's short-format array
+    shuffled: its long form is a view, and np.random.shuffle acts on it."""
+    d = golden["rm1_data"]
+    s, n, V = d.shape
+    want = d.reshape(s * n, V)[golden["rm1_after_shuffle"]].reshape(s, n, V)
+    np.testing.assert_array_equal(golden["rm1_after_perm"], want)
