@@ -23,6 +23,9 @@
  *   calculate_fweP_voxel.find_nearest   tfce_mediation/tmanalysis/calculate_fweP_voxel.py:23-49,
  *   tm_func.find_nearest                tfce_mediation/tm_func.py:566-573
  *                                                     -> fwer_sort, fwer_lookup
+ *   glm_typeI / glm_cosinor  tfce_mediation/pyfunc.py:2282-2560  -> glm_stat_tc (modes 1-3)
+ *   reg_rm_ancova_one_bs_factor / _two_bs_factor  tfce_mediation/pyfunc.py:1712-2280
+ *                                                     -> glm_stat_tc (mode 4), rm_anova_combine
  */
 #ifndef TFCE_GB300_H_
 #define TFCE_GB300_H_
@@ -249,7 +252,14 @@ int glm_tstat_tc(const void* y_tiles, const float* y_shift, const float* Y, int6
  *         + I22 b_j+1^2)) for the amplitude (-) and with b_j, b_j+1 swapped
  *         (+) for the acrophase -- the reference's error propagation through
  *         |sin|, |cos| of arctan(|b_j+1 / b_j|).
+ *       kind 5: the extra sum of squares of dropping the columns [j, j+w),
+ *         b_S' inv(inv(X'X)_SS) b_S with the block at o (w*w) (kind 2 without
+ *         its division by w and RSS/dof);
  *     A row whose columns or weights fall outside kmax / w_stride yields NaN.
+ *   mode 4: a program of kind-5 rows only, without the residual pass: x_rows,
+ *     invdiag, dof and Y_centred may be NULL (the "designs" may then be any
+ *     stacks of up to kmax pseudoinverse rows, e.g. the column blocks of
+ *     several designs); rows of other kinds yield NaN.
  *     The model F of glm_cosinor / glm_typeI is kind 2 over every column
  *     after the intercept.
  *   Y_centred (optional): Y minus its per-vertex centre (glm_col_center with
@@ -273,6 +283,35 @@ int glm_stat_tc(const void* y_tiles, const float* y_shift, const float* Y, const
 int sobel_combine(const float* ta, int64_t lda, const float* ta_scalar, const float* tb,
                   int64_t ldb, int32_t P, int64_t V, int32_t alg, float* z, int64_t ldz,
                   void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Repeated-measures ANCOVA (reg_rm_ancova_one_bs_factor /
+ * reg_rm_ancova_two_bs_factor, tm/pyfunc.py:2067-2280 and 1712-2060, as
+ * tm_models_randomise.py:522-684 permutes them).  The effect sums of squares
+ * come from glm_stat_tc mode 4 (kind 5 rows: extra sums of squares in Wald
+ * form); rm_anova_combine forms, per permutation p and vertex v, the sums of
+ * squares between and within subject means of the permuted data and the F maps:
+ *   Y       [N][ldy] data (device; centring per vertex is recommended);
+ *   rows    [P][N] int32 (device): data rows of permutation p grouped by
+ *           subject, group g = rows[p][goff[g] .. goff[g+1]);
+ *   goff    [n_groups+1] int32 (device);
+ *   ess     device base of the sums-of-squares rows: row r of permutation p
+ *           at ess[row_off[r] + p * row_pstride[r] + v] (row_off, row_pstride:
+ *           host arrays of n_rows <= 16);
+ *   error terms: between = SS_between - sum of rows eb_rows[0..n_eb),
+ *                within  = SS_within  - sum of rows ew_rows[0..n_ew)  (host arrays);
+ *   F map f (n_f <= 8; host arrays): (ess row f_num[f] / f_df[f]) /
+ *           (error f_err[f] (0 between, 1 within) / df_b or df_w);
+ *   out     [P][n_f][ldo]; ss_out (optional) [P][2][ldo]: SS_between, SS_within.
+ * N <= rm_anova_max_rows() (the kernel stages all N rows of a 32-vertex tile).
+ * A row index or group bound out of range sets *err (device) to 1 and is clamped. */
+int rm_anova_max_rows(void);
+int rm_anova_combine(const float* Y, int64_t ldy, int32_t N, int64_t V, const int32_t* rows, int32_t P,
+                     const int32_t* goff, int32_t n_groups, const float* ess, const int64_t* row_off,
+                     const int64_t* row_pstride, int32_t n_rows, const int32_t* eb_rows, int32_t n_eb,
+                     const int32_t* ew_rows, int32_t n_ew, float df_b, float df_w, const int32_t* f_num,
+                     const int32_t* f_err, const float* f_df, int32_t n_f, float* out, int64_t ldo, float* ss_out,
+                     int32_t* err, void* stream);
 
 /* ---------------------------------------------------------------------------
  * FWER.  fwer_sort sorts n doubles ascending in place (device).  fwer_lookup

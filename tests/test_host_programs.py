@@ -95,3 +95,110 @@ def test_saved_none(tmp_path):
     assert randomise._saved_none(np.load(tmp_path / "a.npy", allow_pickle=True))
     assert not randomise._saved_none(np.load(tmp_path / "b.npy"))
     assert randomise._saved_none(None)
+
+
+def _rm_pipeline_fp64(model, Y, ras, cums):
+    """The RM-ANCOVA device pipeline restated in FP64 numpy: the effect sums of
+    squares from the packed pseudoinverse rows (Wald form), SS between/within
+    subjects from the grouped data rows, the F maps."""
+    P = len(ras)
+    ess = {}
+    for si, (rows, W) in enumerate(model.slot_operands(ras, cums)):
+        b = np.einsum("pin,nv->piv", rows, Y)
+        prog, _ = output_program(model.slot_outputs[si])
+        for q, (kind, j, w, o) in enumerate(prog):
+            nm = [k for k, v in model.ess_at.items() if v == (si, q)][0]
+            Wb = W[:, o:o + w * w].reshape(P, w, w)
+            ess[nm] = np.einsum("piv,pij,pjv->pv", b[:, j:j + w], Wb, b[:, j:j + w])
+    g = model.grouped_rows(cums)
+    out = np.zeros((P, len(model.f_maps), Y.shape[1]))
+    for p in range(P):
+        yg = Y[g[p]]
+        bs = np.zeros(Y.shape[1])
+        ws = np.zeros(Y.shape[1])
+        mu = Y.mean(0)
+        for k in range(model.n_groups):
+            blk = yg[model.goff[k]:model.goff[k + 1]]
+            m = blk.mean(0)
+            ws += ((blk - m) ** 2).sum(0)
+            bs += len(blk) * (m - mu) ** 2
+        eb = bs - sum(ess[x][p] for x in model.between)
+        ew = ws - sum(ess[x][p] for x in model.within)
+        for f, (nm, df, err) in enumerate(model.f_maps):
+            out[p, f] = (ess[nm][p] / df) / ((ew / model.df_w) if err else (eb / model.df_b))
+    return out
+
+
+@pytest.mark.parametrize("two", [False, True])
+@pytest.mark.parametrize("tag", ["nocov", "cov"])
+@pytest.mark.parametrize("kind", ["obs", "perm"])
+def test_rm_anova_decomposition_fp64(golden, two, tag, kind):
+    """Wald-form effect sums of squares + subject split reproduce the
+    reference's RM-ANCOVA F maps (golden vectors) in FP64: the algebra the
+    tensor-core GLM and rm_anova_combine run."""
+    from tfce_mediation_gb300 import rm_anova as R
+    pre = "rm2" if two else "rm1"
+    d = golden[f"{pre}_data"]
+    s, n, V = d.shape
+    cov = golden[f"{pre}_cov"] if tag == "cov" else None
+    if two:
+        model = R.RMModel(n, s, golden["rm2_fa"], golden["rm2_subj"], dmy_factor2=golden["rm2_fb"],
+                          dmy_covariates=cov)
+    else:
+        model = R.RMModel(n, s, golden["rm1_f1"], golden["rm1_subj"], dmy_covariates=cov)
+    Y = d.reshape(s * n, V).astype(np.float64)
+    if kind == "obs":
+        ras, cums = [None], np.arange(s * n)[None]
+    else:
+        ras, cums = [golden[f"{pre}_ra_{tag}"]], golden[f"{pre}_shuffle_{tag}"][None]
+    got = _rm_pipeline_fp64(model, Y, ras, cums)[0]
+    # exact algebra: the oracle with every sum of squares in FP64
+    kw = {} if kind == "obs" else dict(rand_array=ras[0], shuffle=cums[0])
+    if two:
+        ref64 = oracle.rm_ancova_two(d.astype(np.float64), golden["rm2_fa"], golden["rm2_fb"], golden["rm2_subj"],
+                                     dmy_covariates=cov, **kw)
+    else:
+        ref64 = oracle.rm_ancova_one(d.astype(np.float64), golden["rm1_f1"], golden["rm1_subj"], dmy_covariates=cov,
+                                     **kw)
+    np.testing.assert_allclose(got, np.asarray(ref64), rtol=1e-9, atol=1e-12)
+    # the reference itself forms SS_Total as a float32 sum, which enters the
+    # differences of sums of squares: ~1e-5 of max(1, F)
+    ref = golden[f"{pre}_{kind}_{tag}"]
+    assert np.max(np.abs(got - ref) / np.maximum(1.0, np.abs(ref))) <= 5e-5
+
+
+def test_rm_model_packing():
+    from tfce_mediation_gb300 import rm_anova as R
+    rng = np.random.default_rng(1)
+    n, s = 30, 3
+    fa = R.dummy_code(rng.integers(0, 2, n))
+    fb = R.dummy_code(rng.integers(0, 3, n))
+    subj = R.dummy_code(np.arange(n), demean=False)
+    m = R.RMModel(n, s, fa, subj, dmy_factor2=fb, dmy_covariates=rng.standard_normal((n, 1)))
+    assert all(sum(m.blocks[i][2] for i in sl) <= R.SLOT_ROWS for sl in m.slots)
+    assert sorted(i for sl in m.slots for i in sl) == list(range(len(m.blocks)))
+    assert set(m.ess_at) == {"cells", "ab", "a", "b", "s", "scov", "sab", "sa", "sb"}
+    assert m.df_b == n - 1 - 1 - 2 - 2 - 1 and m.df_w == m.df_b * 2
+    np.testing.assert_array_equal(m.goff, np.arange(n + 1) * s)
+    with pytest.raises(ValueError):
+        R.RMModel(n, s, fa, rng.standard_normal((n, 2)))  # not a subject coding
+    empty = R.dummy_code(np.r_[np.zeros(n // 2), np.ones(n - n // 2)])
+    with pytest.raises(ValueError, match="rank deficient"):
+        R.RMModel(n, s, empty, subj, dmy_factor2=empty.copy())  # f1 x f2 cells (0,1), (1,0) empty
+
+
+def test_rm_permutations_replay_the_reference_loop():
+    """rand_array then an in-place shuffle of the one data array per
+    iteration (tm_models_randomise.py:522-530 with pyfunc.py:2139): the
+    cumulative row orders equal what successive shuffles leave in the array."""
+    n, s = 6, 3
+    N = n * s
+    data = np.arange(N * 2, dtype=np.float64).reshape(N, 2)
+    ras, cums = randomise.rm_permutations(n, N, 3, 8, 40)
+    arr = data.copy()
+    for i, it in enumerate(range(3, 8)):
+        rng = np.random.RandomState(40 + it)
+        ra = rng.permutation(list(range(n)))
+        rng.shuffle(arr)
+        np.testing.assert_array_equal(ras[i], ra)
+        np.testing.assert_array_equal(arr, data[cums[i]])

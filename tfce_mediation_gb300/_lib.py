@@ -81,6 +81,12 @@ SIGNATURES = {
     "sobel_combine": (ctypes.c_int, [c_vp, ctypes.c_int64, c_vp, c_vp, ctypes.c_int64,
                                      ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, c_vp,
                                      ctypes.c_int64, c_vp]),
+    "rm_anova_max_rows": (ctypes.c_int, []),
+    "rm_anova_combine": (ctypes.c_int, [c_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int64, c_vp, ctypes.c_int32,
+                                        c_vp, ctypes.c_int32, c_vp, c_vp, c_vp, ctypes.c_int32, c_vp,
+                                        ctypes.c_int32, c_vp, ctypes.c_int32, ctypes.c_float, ctypes.c_float,
+                                        c_vp, c_vp, c_vp, ctypes.c_int32, c_vp, ctypes.c_int64, c_vp, c_vp,
+                                        c_vp]),
     "fwer_sort": (ctypes.c_int, [c_vp, ctypes.c_int64, c_vp]),
     "fwer_lookup": (ctypes.c_int, [c_vp, ctypes.c_int64, c_vp, ctypes.c_int64, ctypes.c_int32,
                                    c_vp, c_vp]),

@@ -55,7 +55,7 @@ constexpr int kTcStages = 4;
 constexpr int kTcSubjChunk = 32;    // subjects per epilogue X chunk
 constexpr uint64_t kTcWaitNs = 2000000000ull;
 // output kinds of the programmed epilogue (mode 3)
-constexpr int kTcOutT = 0, kTcOutNegT = 1, kTcOutF = 2, kTcOutAmp = 3, kTcOutAcro = 4;
+constexpr int kTcOutT = 0, kTcOutNegT = 1, kTcOutF = 2, kTcOutAmp = 3, kTcOutAcro = 4, kTcOutEss = 5;
 
 __host__ __device__ constexpr int tc_dpt(int kmax) { return kmax <= 5 ? 16 : 8; }  // designs per thread
 __host__ __device__ constexpr int tc_db(int kmax) { return 2 * tc_dpt(kmax); }     // designs per tile
@@ -430,7 +430,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
   __syncthreads();  // the beta area becomes the chunk buffers
 
   const int n_chunks = a.n_sc / kTcSubjChunk;
-  const float* xsrc = a.xt + (int64_t)db * a.n_sc * KMAX * DB;
+  const float* xsrc = a.xt != nullptr ? a.xt + (int64_t)db * a.n_sc * KMAX * DB : nullptr;
   const int64_t vt0 = vb * kTcM;
   auto load_chunk = [&](int c) {
     const uint32_t dst = sbase + (c & 1) * (XC + YC);
@@ -446,8 +446,9 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
     cp_async_commit();
   };
   if (!failed) {
-    load_chunk(0);
-    for (int c = 0; c < n_chunks; ++c) {
+    // mode 4 needs no residuals: its rows are quadratic forms of the betas
+    for (int c = 0; a.mode != 4 && c < n_chunks; ++c) {
+      if (c == 0) load_chunk(0);
       // chunk c+1 streams into the other buffer while chunk c is used
       if (c + 1 < n_chunks) {
         load_chunk(c + 1);
@@ -509,7 +510,9 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
         if (v0 + vv < a.V) dst[vv] = (vv & 1) ? rss[vv / 2].y : rss[vv / 2].x;
     } else if (g < a.G && a.mode >= 2) {
       // mode 2: partial F of each column group; mode 3: a program of typed
-      // output rows (t, -t, partial F, cosinor amplitude / acrophase t).
+      // output rows (t, -t, partial F, cosinor amplitude / acrophase t, extra
+      // sum of squares); mode 4: a program of extra-sum-of-squares rows only,
+      // without the residual pass.
       // this thread's betas and RSS go to its own slice of the (now free)
       // shared area, so the output loops index them at run time
       float* mine = reinterpret_cast<float*>(sm) + tid * VT * (KMAX + 1);
@@ -520,7 +523,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
           mine[vv * (KMAX + 1) + jj] = (jj < J0) ? 0.0f : ((vv & 1) ? bp[vv / 2][jj].y : bp[vv / 2][jj].x);
         mine[vv * (KMAX + 1) + KMAX] = (vv & 1) ? rss[vv / 2].y : rss[vv / 2].x;
       }
-      const float dof = __ldg(a.dof + g);
+      const float dof = a.dof != nullptr ? __ldg(a.dof + g) : 1.0f;
       const float inv_dof = 1.0f / dof;
       const float* wg = a.wmat + (int64_t)g * a.w_stride;
       int woff = 0;
@@ -539,9 +542,11 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
           wo = __ldg(a.coef + 4 * oi + 3);
         }
         bool ok;
-        if (kind == kTcOutT || kind == kTcOutNegT) {
+        if (a.mode == 4 && kind != kTcOutEss) {
+          ok = false;  // no residual sum of squares in this mode
+        } else if (kind == kTcOutT || kind == kTcOutNegT) {
           ok = j >= 0 && j < KMAX;
-        } else if (kind == kTcOutF) {
+        } else if (kind == kTcOutF || kind == kTcOutEss) {
           ok = j >= 0 && kv >= 1 && j + kv <= KMAX && wo >= 0 && wo + kv * kv <= a.w_stride;
         } else if (kind == kTcOutAmp || kind == kTcOutAcro) {
           ok = j >= 0 && j + 1 < KMAX && wo >= 0 && wo + 3 <= a.w_stride;
@@ -559,15 +564,15 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
           } else if (kind == kTcOutT || kind == kTcOutNegT) {
             val = bv[j] / sqrtf(rs * inv_dof * dj);
             if (kind == kTcOutNegT) val = -val;
-          } else if (kind == kTcOutF) {
-            // (RSS_without_S - RSS) / |S| / (RSS / dof) with the extra sum of
-            // squares in its exact Wald form b_S' inv(inv(X'X)_SS) b_S -- no
-            // difference of two residual sums
+          } else if (kind == kTcOutF || kind == kTcOutEss) {
+            // the extra sum of squares of dropping S, RSS_without_S - RSS, in
+            // its exact Wald form b_S' inv(inv(X'X)_SS) b_S -- no difference of
+            // two residual sums; F: divided by |S| and RSS / dof
             float q = 0.0f;
             for (int ja = 0; ja < kv; ++ja)
               for (int jc = 0; jc < kv; ++jc)
                 q = fmaf(bv[j + ja] * __ldg(wg + wo + ja * kv + jc), bv[j + jc], q);
-            val = (q / static_cast<float>(kv)) / (rs / dof);
+            val = (kind == kTcOutEss) ? q : (q / static_cast<float>(kv)) / (rs / dof);
           } else {
             // cosinor pair (b1, b2) = (cos, sin) coefficients, wg = inv(X'X)
             // entries (11, 12, 22): with A^2 = b1^2 + b2^2 and the acrophase
@@ -673,16 +678,19 @@ int glm_stat_tc(const void* y_tiles, const float* y_shift, const float* Y, const
                 const int32_t* coef, int32_t n_coef, const float* wmat, int32_t w_stride, float* t_out,
                 int64_t ldt, int32_t* err, void* stream) {
   tfgb::clear_error();
-  TFGB_CHECK_ARG(y_tiles && Y && p_tiles && x_rows && invdiag && dof && t_out && err, "NULL pointer");
+  TFGB_CHECK_ARG(y_tiles && Y && p_tiles && t_out && err, "NULL pointer");
+  TFGB_CHECK_ARG(mode == 4 || (x_rows && invdiag && dof), "x_rows / invdiag / dof are NULL");
   TFGB_CHECK_ARG(mode == 1 || coef != nullptr, "coef is NULL");
   TFGB_CHECK_ARG(!y_shift || u_rows, "a centred data operand needs u_rows");
   TFGB_CHECK_ARG(n > 0 && n_pad >= n && n_pad % tfgb::kTcK == 0, "n_pad must be >= n and a multiple of 16");
   TFGB_CHECK_ARG(n_sc >= n && n_sc % tfgb::kTcSubjChunk == 0, "n_sc must be >= n and a multiple of 32");
   TFGB_CHECK_ARG(kmax >= 1 && kmax <= tfgb::kTcRowsPerDesign, "kmax must be in [1, 8]");
-  TFGB_CHECK_ARG(mode >= 0 && mode <= 3, "mode must be 0 (t), 1 (RSS), 2 (partial F) or 3 (program)");
+  TFGB_CHECK_ARG(mode >= 0 && mode <= 4,
+                 "mode must be 0 (t), 1 (RSS), 2 (partial F), 3 (program) or 4 (sums-of-squares program)");
   TFGB_CHECK_ARG(mode == 1 || n_coef >= 1, "n_coef must be >= 1");
   TFGB_CHECK_ARG(mode != 2 || (wmat != nullptr && w_stride >= 1), "partial F needs wmat");
-  TFGB_CHECK_ARG(mode != 3 || wmat != nullptr || w_stride == 0, "w_stride > 0 needs wmat");
+  TFGB_CHECK_ARG(mode < 3 || wmat != nullptr || w_stride == 0, "w_stride > 0 needs wmat");
+  TFGB_CHECK_ARG(mode != 4 || Y_centred == nullptr, "mode 4 forms no residuals (Y_centred must be NULL)");
   TFGB_CHECK_ARG(V >= 0 && G >= 0 && ldt >= V && ldy >= V, "bad sizes");
   TFGB_CHECK_ARG(reinterpret_cast<uintptr_t>(y_tiles) % 16 == 0 && reinterpret_cast<uintptr_t>(p_tiles) % 16 == 0 &&
                      reinterpret_cast<uintptr_t>(x_rows) % 16 == 0,

@@ -15,8 +15,8 @@ from .device import dev, ptr, require_cuda, stream_handle
 
 WHAT_T, WHAT_BETA, WHAT_SE, WHAT_RESID, WHAT_F, WHAT_RSS = range(6)
 # typed output rows of the tensor-core GLM's programmed epilogue (glm_stat_tc mode 3)
-OUT_T, OUT_NEG_T, OUT_F, OUT_AMP, OUT_ACRO = range(5)
-_OUT_KIND = {"t": OUT_T, "-t": OUT_NEG_T, "f": OUT_F, "amp": OUT_AMP, "acro": OUT_ACRO}
+OUT_T, OUT_NEG_T, OUT_F, OUT_AMP, OUT_ACRO, OUT_ESS = range(6)
+_OUT_KIND = {"t": OUT_T, "-t": OUT_NEG_T, "f": OUT_F, "amp": OUT_AMP, "acro": OUT_ACRO, "ess": OUT_ESS}
 
 
 def output_program(outputs):
@@ -24,6 +24,8 @@ def output_program(outputs):
     stride of a list of typed outputs:
       ("t", j) / ("-t", j): t (negated t) of coefficient j;
       ("f", j, w): partial F of the columns [j, j+w) (Wald form);
+      ("ess", j, w): the extra sum of squares of the columns [j, j+w) (the
+        Wald form alone: glm_stat_tc mode 4 needs no residuals for it);
       ("amp", j) / ("acro", j): cosinor amplitude / acrophase t of the
         (cos, sin) coefficient pair (j, j+1) (glm_cosinor, pyfunc.py:2406-2560).
     The model F of an intercept design with k columns is ("f", 1, k-1)."""
@@ -35,10 +37,10 @@ def output_program(outputs):
         j = int(spec[1])
         if kind in (OUT_T, OUT_NEG_T):
             rows.append((kind, j, 1, 0))
-        elif kind == OUT_F:
+        elif kind in (OUT_F, OUT_ESS):
             w = int(spec[2])
             if w < 1:
-                raise ValueError("an 'f' row needs a width >= 1")
+                raise ValueError("an 'f' / 'ess' row needs a width >= 1")
             rows.append((kind, j, w, o))
             o += w * w
         else:
@@ -124,7 +126,7 @@ class DesignBatch:
         for kind, j, w, o in rows:
             if j < 0 or j + w > self.kmax:
                 continue  # outside the designs: the kernel returns NaN for the row
-            if kind == OUT_F:
+            if kind in (OUT_F, OUT_ESS):
                 w64[:, o:o + w * w] = np.linalg.inv(inv[:, j:j + w, j:j + w]).reshape(self.G, w * w)
             elif kind in (OUT_AMP, OUT_ACRO):
                 w64[:, o], w64[:, o + 1], w64[:, o + 2] = inv[:, j, j], inv[:, j, j + 1], inv[:, j + 1, j + 1]

@@ -11,6 +11,8 @@ sweeps, regressions and indirect-effect maps run on the GPU:
 * calc_indirect, check_blocks, rand_blocks       (pyfunc.py:2678-2757)
 * glm_typeI                                      (pyfunc.py:2282-2400)
 * glm_cosinor (+ its design, cosinor_design)     (pyfunc.py:2406-2560)
+* reg_rm_ancova_one_bs_factor / _two_bs_factor   (pyfunc.py:2067-2280, 1712-2060)
+* dummy_code, column_product, stack_ones         (pyfunc.py:2564-2676)
 """
 from __future__ import annotations
 
@@ -398,3 +400,87 @@ def glm_cosinor(endog, time_var, exog=None, dmy_covariates=None, rand_array=None
         R2 = out(ssb / (ssb + rss))
     arr = [out(np.asarray(v)) for v in (amp, se_amp, acro, se_acro, t_amp, t_acro)]
     return (R2, MESOR, SE_MESOR, arr[0], arr[1], arr[2], arr[3], out(F), tMESOR, arr[4], arr[5], tEXOG)
+
+
+# -- tm-models repeated-measures ANCOVA ----------------------------------------
+from .rm_anova import column_product, dummy_code, stack_ones  # noqa: E402,F401  (pyfunc.py:2564-2676)
+
+
+def _rm_anova(data, factors, dmy_subjects, dmy_covariates, data_format, output_sig, verbose, rand_array,
+              use_reduced_residuals, output_reduced_residuals, labels):
+    """Shared body of the two reg_rm_ancova_* drop-ins (see there)."""
+    from .glm import WHAT_RESID
+    from .rm_anova import RMAncovaEngine, RMModel, long_data
+    endog, n, s = long_data(data, data_format, len(factors[0]))
+    squeeze = endog.shape[1] == 1
+    N = n * s
+    facs = [np.asarray(f) for f in factors]
+    cov = None if dmy_covariates is None else np.asarray(dmy_covariates)
+
+    def long_exog(fs, cv):
+        cols = [np.tile(np.asarray(f, np.float64).reshape(n, -1), (s, 1)) for f in fs]
+        if len(fs) == 2:
+            cols.append(np.tile(column_product(fs[0], fs[1]).reshape(n, -1), (s, 1)))
+        if cv is not None:
+            cols.append(np.tile(np.asarray(cv, np.float64).reshape(n, -1), (s, 1)))
+        return stack_ones(np.column_stack(cols))
+
+    if rand_array is not None:
+        if use_reduced_residuals:
+            X = long_exog(facs, cov)
+            endog = glm_stat(np.ascontiguousarray(endog, np.float32), DesignBatch([X]), WHAT_RESID)[0].cpu().numpy()
+        # the reference shuffles the long rows in place: the caller's array
+        # when the long form is a view of it
+        np.random.shuffle(endog)
+        facs = [f[rand_array] for f in facs]
+        cov = None if cov is None else cov[rand_array]
+    model = RMModel(n, s, facs[0], dmy_subjects, dmy_factor2=facs[1] if len(facs) == 2 else None,
+                    dmy_covariates=cov)
+    eng = RMAncovaEngine(np.ascontiguousarray(endog, np.float32), model)
+    F = eng.fmaps([None], np.arange(N)[None])[0].cpu().numpy().astype(np.float64)
+    eng.status()
+    if verbose:
+        print("Source\t\tDF\tF(Max)")
+        for (nm, df, err), lab, Fi in zip(model.f_maps, labels, F):
+            tab = "\t" if len(lab) >= 8 else "\t\t"
+            print("%s%s(%d,%d)\t%.2f" % (lab, tab, df, model.df_w if err else model.df_b, Fi.max()))
+    Fs = [Fi[0] if squeeze else Fi for Fi in F]
+    if output_sig:
+        from scipy.stats import f as fdist
+        Ps = [1 - fdist.cdf(Fi, df, model.df_w if err else model.df_b) for Fi, (_, df, err) in zip(Fs, model.f_maps)]
+        return tuple(Fs) + tuple(Ps)
+    if output_reduced_residuals:
+        X = long_exog(facs if len(facs) == 2 else facs[:1], cov)
+        reduced = glm_stat(np.ascontiguousarray(endog, np.float32), DesignBatch([X]), WHAT_RESID)[0].cpu().numpy()
+        return tuple(Fs) + (reduced,)
+    return tuple(Fs)
+
+
+def reg_rm_ancova_one_bs_factor(data, dmy_factor1, dmy_subjects, data_format="short", dmy_covariates=None,
+                                output_sig=False, verbose=True, rand_array=None, use_reduced_residuals=False,
+                                output_reduced_residuals=False):
+    """One between-subject factor repeated-measures ANCOVA, pyfunc.py:2067-2280,
+    on the GPU: (F_a, F_s, F_sa) [+ (P_a, P_s, P_sa) with output_sig, or the
+    reduced residuals].  data: (s intervals, n subjects[, V]) ('short') or
+    (n*s[, V]) ('long', interval-major rows).  Effect sums of squares in exact
+    Wald form on the tensor-core GLM, subject split and F on the device
+    (tfce_mediation_gb300.rm_anova).  With rand_array the long data rows are
+    shuffled in place with np.random.shuffle (the caller's array when the long
+    form is a view of it) and the factor / covariate rows permuted, as the
+    reference does.  'long' data is accepted with an integer interval count
+    (the reference's own long path divides with / and fails on Python 3)."""
+    return _rm_anova(data, [dmy_factor1], dmy_subjects, dmy_covariates, data_format, output_sig, verbose,
+                     rand_array, use_reduced_residuals, output_reduced_residuals,
+                     ["Factor", "Time", "Factor*Time"])
+
+
+def reg_rm_ancova_two_bs_factor(data, dmy_factor1, dmy_factor2, dmy_subjects, dmy_covariates=None,
+                                data_format="short", output_sig=False, verbose=True, rand_array=None,
+                                use_reduced_residuals=False, output_reduced_residuals=False):
+    """Two between-subject factor repeated-measures ANCOVA (type I sums of
+    squares), pyfunc.py:1712-2060, on the GPU: (F_a, F_b, F_ab, F_s, F_sa, F_sb,
+    F_sab) [+ P values or the reduced residuals]; see
+    reg_rm_ancova_one_bs_factor."""
+    return _rm_anova(data, [dmy_factor1, dmy_factor2], dmy_subjects, dmy_covariates, data_format, output_sig,
+                     verbose, rand_array, use_reduced_residuals, output_reduced_residuals,
+                     ["Factor1", "Factor2", "F1*F2", "Time", "F1*Time", "F2*Time", "F1*F2*Time"])

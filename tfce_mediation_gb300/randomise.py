@@ -478,3 +478,92 @@ def tm_models_cosinor_run(opts):
             lines += [fmt % m[p, c0 + 2 * j], fmt % m[p, c0 + 2 * j + 1]]
         _append(csv(name), lines)
     return m
+
+
+def tm_models_rmancova_parser(ap=None):
+    ap = tm_models_glm_parser(ap or argparse.ArgumentParser(description="tm-models RM-ANCOVA permutations (GPU)"))
+    ap.add_argument("-tfa", "--twobetweenssubjectfactor", action="store_true",
+                    help="two between-subject factors (default: one)")
+    return ap
+
+
+def rm_permutations(n, N, start, stop, seed, block_list=None):
+    """Subject permutations and cumulative long-row shuffles of the reference's
+    RM-ANCOVA loop (tm_models_randomise.py:522-530, 577-585 with
+    pyfunc.py:2139 / 1833): per iteration rand_array (np.random.permutation(n),
+    or rand_blocks when exchange blocks are given: blocks shuffled only when of
+    equal size), then np.random.shuffle of the n*s data rows -- which the
+    reference applies to its one data array, so the shuffles compose.
+    Returns (ras (P, n), cums (P, N)), cums[i] the long-row order of the data
+    seen by iteration i."""
+    ras, cums = [], []
+    c = np.arange(N)
+    if block_list is not None:
+        block_list = np.asarray(block_list)
+        uniq = np.unique(block_list)
+        sizes = [int(np.sum(block_list == b)) for b in uniq]
+        equal = all(z == sizes[0] for z in sizes)
+        indexer = np.arange(len(block_list))
+    for it in range(start, stop):
+        if seed is None:
+            np.random.seed(int(it * 1000 + time()))
+            rng = np.random
+        else:
+            rng = np.random.RandomState(seed + it)
+        if block_list is None:
+            ra = rng.permutation(list(range(n)))
+        else:
+            order = rng.permutation(list(uniq)) if equal else uniq
+            ra = np.concatenate([rng.permutation(indexer[block_list == b]) for b in order])
+        c = c[rng.permutation(N)]
+        ras.append(np.asarray(ra))
+        cums.append(c.copy())
+    return np.asarray(ras), np.asarray(cums)
+
+
+def tm_models_rmancova_run(opts):
+    """The RM-ANCOVA branches of tm_models_randomise.py (-ofa :135-145, :522-571;
+    -tfa :146-156, :574-684): per permutation the F maps of
+    reg_rm_ancova_one_bs_factor (F_a, F_s, F_sa) or reg_rm_ancova_two_bs_factor
+    (F_a, F_b, F_ab, F_s, F_sa, F_sb, F_sab), each TFCE'd with one sign, maxima
+    appended to the reference's CSVs (perm_Fstat_<factor>, perm_Fstat_time,
+    perm_Fstat_<factor>.X.time, ...)."""
+    from .rm_anova import RMAncovaEngine, RMModel, long_data
+    two = bool(getattr(opts, "twobetweenssubjectfactor", False))
+    start, stop = int(opts.range[0]), int(opts.range[1]) + 1
+    seed = opts.seed[0] if getattr(opts, "seed", None) else None
+    surface = str(opts.surface[0]) if getattr(opts, "surface", None) else None
+    tag = "rmANCOVA2BS" if two else "rmANCOVA1BS"
+    tempdir = "tmtemp_%s_%s" % (tag, surface if surface else "volume")
+    outdir = "output_%s_%s/perm_%s" % (tag, surface if surface else "volume", tag)
+    f1 = _load(f"{tempdir}/dmy_factor1.npy")
+    f2 = _load(f"{tempdir}/dmy_factor2.npy") if two else None
+    factors = [str(x) for x in np.atleast_1d(_load(f"{tempdir}/factors.npy"))]
+    subj = _load(f"{tempdir}/dmy_subjects.npy")
+    dformat = str(np.atleast_1d(_load(f"{tempdir}/dformat.npy"))[0])
+    data = _load(f"{tempdir}/data.npy")
+    optstfce = _load(f"{tempdir}/optstfce.npy")
+    cov = _load(f"{tempdir}/dmy_covariates.npy")
+    cov = None if _saved_none(cov) else np.asarray(cov, np.float64)
+    n = len(f1)
+    endog, n, s = long_data(data, dformat, n)
+    model = RMModel(n, s, f1, subj, dmy_factor2=f2, dmy_covariates=cov)
+    H, E_ = float(optstfce[0]), float(optstfce[1])
+    off, idx, kw, fmt, suffix = _tm_models_space(tempdir, surface)
+    block_list = None
+    if getattr(opts, "exchangeblock", None):
+        block_list = np.genfromtxt(opts.exchangeblock[0], dtype=str)
+    ras, cums = rm_permutations(n, n * s, start, stop, seed, block_list)
+    os.makedirs(outdir, exist_ok=True)
+    eng = RMAncovaEngine(np.ascontiguousarray(endog, np.float32), model, (off, idx), H=H, E=E_,
+                         batch=getattr(opts, "batch", 64), **kw)
+    m = eng.maxima(list(ras), cums)  # (P, n_f, S)
+    m = m.max(axis=-1) if surface else m[..., 0]
+    if two:
+        names = [factors[0], factors[2], "%s.X.%s" % (factors[0], factors[2]), "time", "%s.X.time" % factors[0],
+                 "%s.X.time" % factors[2], "%s.X.%s.X.time" % (factors[0], factors[2])]
+    else:
+        names = [factors[0], "time", "%s.X.time" % factors[0]]
+    for j, nm in enumerate(names):
+        _append(os.path.join(outdir, "perm_Fstat_%s_TFCE_%s.csv" % (nm, suffix)), [fmt % v for v in m[:, j]])
+    return m
