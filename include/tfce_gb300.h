@@ -26,6 +26,7 @@
  *   glm_typeI / glm_cosinor  tfce_mediation/pyfunc.py:2282-2560  -> glm_stat_tc (modes 1-3)
  *   reg_rm_ancova_one_bs_factor / _two_bs_factor  tfce_mediation/pyfunc.py:1712-2280
  *                                                     -> glm_stat_tc (mode 4), rm_anova_combine
+ *   calc_gd_fwhm  tfce_mediation/cynumstats.pyx:76-107  -> gd_fwhm_weights, gd_fwhm_smooth
  */
 #ifndef TFCE_GB300_H_
 #define TFCE_GB300_H_
@@ -312,6 +313,25 @@ int rm_anova_combine(const float* Y, int64_t ldy, int32_t N, int64_t V, const in
                      const int32_t* ew_rows, int32_t n_ew, float df_b, float df_w, const int32_t* f_num,
                      const int32_t* f_err, const float* f_df, int32_t n_f, float* out, int64_t ldo, float* ss_out,
                      int32_t* err, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Geodesic FWHM smoothing (calc_gd_fwhm, tm/cynumstats.pyx:76-107, as
+ * tools/tm_gd_fwhm_smoothing.py:96 calls it per subject image).
+ * gd_fwhm_weights: w[x] = pdf_compute(dist[x], 0, scale) for x < M and the
+ *   self weight pdf_compute(0, 0, scale) at w[M] (device arrays; w has M+1).
+ * gd_fwhm_smooth: B images data [B][ld] over V vertices -> out [B][ldo]:
+ *   out[v] = (sum_k w[pidx[k]] * data[src[k]] + w[M] * data[v]) /
+ *            (sum_k w[pidx[k]] + w[M]) over k in [off[v], off[v+1]),
+ *   float32 with one rounding per product and per sum, in k order.  The gather
+ *   list (device: off [V+1] int64, src / pidx [off[V]] int32) holds, for every
+ *   pair x = (i, j) of the reference's list, the entry (i, x) under vertex j
+ *   and (j, x) under vertex i, each vertex's entries in pair order (the order
+ *   of the reference's scatter).  An entry outside [0, V) / [0, M) sets *err
+ *   (device) to 1 and is skipped. */
+int gd_fwhm_weights(const float* dist, int64_t M, float scale, float* w, void* stream);
+int gd_fwhm_smooth(const int64_t* off, const int32_t* src, const int32_t* pidx, const float* w, int64_t M,
+                   const float* data, int64_t ld, int32_t B, int32_t V, float* out, int64_t ldo, int32_t* err,
+                   void* stream);
 
 /* ---------------------------------------------------------------------------
  * FWER.  fwer_sort sorts n doubles ascending in place (device).  fwer_lookup

@@ -13,6 +13,7 @@ from a reference checkout -- against the reference sweep directly.
 from __future__ import annotations
 
 import ctypes
+import ctypes.util
 import math
 import os
 import subprocess
@@ -685,3 +686,61 @@ def rm_ancova_two(data, dmy_factor1, dmy_factor2, dmy_subjects, dmy_covariates=N
     return ((ss_a / df_a) / ms_wf, (ss_b / df_b) / ms_wf, (ss_ab / df_ab) / ms_wf, (ss_s / df_s) / ms_swf,
             (ss_sa / (df_a * df_s)) / ms_swf, (ss_sb / (df_b * df_s)) / ms_swf,
             (ss_sab / (df_ab * df_s)) / ms_swf)
+
+
+# -- geodesic FWHM smoothing (cynumstats.calc_gd_fwhm) -------------------------
+_LIBM = None
+
+
+def _libm():
+    """The host C math library: the reference's compiled pdf_compute calls
+    powf and, being C++, the float overload of exp (expf)."""
+    global _LIBM
+    if _LIBM is None:
+        m = ctypes.CDLL(ctypes.util.find_library("m") or "libm.so.6")
+        m.powf.restype, m.powf.argtypes = ctypes.c_float, [ctypes.c_float, ctypes.c_float]
+        m.expf.restype, m.expf.argtypes = ctypes.c_float, [ctypes.c_float]
+        _LIBM = m
+    return _LIBM
+
+
+def gd_weight(x, scale):
+    """pdf_compute(x, 0, scale) as the reference's compiled Cython evaluates it
+    (tm/cynumstats.pyx:76-81, C float arguments, result stored to a C float):
+      norm     = float(sqrt((2.0 * M_PI) * scale))            double sqrt
+      exponent = float((-1.0 * powf(x - 0, 2)) / (2.0 * scale)) double division
+      weight   = float((1.0 / norm) * expf(exponent))          float exp (C++ overload)
+    The reference's 'scale' acts as a variance."""
+    m = _libm()
+    s32 = np.float32(scale)
+    norm = np.float32(math.sqrt((2.0 * math.pi) * float(s32)))
+    p = np.float32(m.powf(float(np.float32(np.float32(x) - np.float32(0.0))), 2.0))
+    ex = np.float32((-1.0 * float(p)) / (2.0 * float(s32)))
+    return np.float32((1.0 / float(norm)) * float(m.expf(float(ex))))
+
+
+def calc_gd_fwhm(indices, dist, data, sigma):
+    """calc_gd_fwhm (tm/cynumstats.pyx:83-107), a pure-Python loop for small
+    cases: every pair (i, j) adds weight*data[i] to j and weight*data[j] to i
+    and the weight to both, then the self weight, then sumval / sum_weight.
+    The product is a C float product; the accumulators are float32 arrays
+    updated through numpy scalars, and with numpy >= 2 (NEP 50) a float32
+    scalar plus a Python float stays float32: every update is one float32
+    rounding of the product and one of the sum."""
+    indices = np.asarray(indices)
+    data = np.asarray(data, np.float32)
+    V = data.shape[0]
+    sumval = [np.float32(0.0)] * V
+    sumw = [np.float32(0.0)] * V
+    for x in range(len(dist)):
+        i, j = int(indices[x, 0]), int(indices[x, 1])
+        w = gd_weight(dist[x], sigma)
+        sumval[j] = np.float32(sumval[j] + np.float32(w * data[i]))
+        sumval[i] = np.float32(sumval[i] + np.float32(w * data[j]))
+        sumw[i] = np.float32(sumw[i] + w)
+        sumw[j] = np.float32(sumw[j] + w)
+    w0 = gd_weight(0.0, sigma)
+    for i in range(V):
+        sumval[i] = np.float32(sumval[i] + np.float32(w0 * data[i]))
+        sumw[i] = np.float32(sumw[i] + w0)
+    return np.asarray(sumval, np.float32) / np.asarray(sumw, np.float32)

@@ -368,6 +368,24 @@ def main():
         out[f"rm2_perm_{tag}"], out[f"rm2_ra_{tag}"], out[f"rm2_shuffle_{tag}"] = np.asarray(res), ra, sh
     out["rm2_data"], out["rm2_fa"], out["rm2_fb"], out["rm2_subj"], out["rm2_cov"] = d2, fa2, fb2, subj2, cov2
 
+    # calc_gd_fwhm (geodesic FWHM smoothing): vertex pairs of a level-3
+    # icosphere within a radius (chord lengths standing in for geodesic
+    # distances), plus a repeated pair and a self pair
+    rg = np.random.default_rng(77)
+    vg, _ = synth.icosphere(3)
+    dd = np.linalg.norm(vg[:, None, :] - vg[None, :, :], axis=2)
+    ii, jj = np.nonzero((dd < 0.35) & (np.arange(len(vg))[:, None] < np.arange(len(vg))[None, :]))
+    order = rg.permutation(len(ii))
+    pairs = np.column_stack([ii[order], jj[order]])
+    pairs = np.concatenate([pairs, pairs[:3], [[5, 5]]]).astype(np.int32)
+    dist = np.linalg.norm(vg[pairs[:, 0]] - vg[pairs[:, 1]], axis=1).astype(np.float32)
+    dist[-1] = np.float32(0.0)
+    out["gd_pairs"], out["gd_dist"] = pairs, dist
+    for k, sg in enumerate((0.02, 0.005)):
+        img = (rg.standard_normal(len(vg)) * 2.0 + 1.0).astype(np.float32)
+        out[f"gd_data{k}"], out[f"gd_sigma{k}"] = img, np.float64(sg)
+        out[f"gd_out{k}"] = cyn.calc_gd_fwhm(np.ascontiguousarray(pairs), np.ascontiguousarray(dist), img.copy(), sg)
+
     path = os.path.join(HERE, "reference_vectors.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({os.path.getsize(path)} bytes, {len(out)} arrays)")

@@ -202,3 +202,27 @@ def test_rm_permutations_replay_the_reference_loop():
         rng.shuffle(arr)
         np.testing.assert_array_equal(ras[i], ra)
         np.testing.assert_array_equal(arr, data[cums[i]])
+
+
+def test_gd_gather_list_keeps_the_scatter_order(golden):
+    """The per-vertex gather list, accumulated in float32 in list order with
+    the oracle's weights, equals the reference's scatter bit for bit."""
+    from tfce_mediation_gb300.gd_fwhm import gather_list
+    pairs, dist = golden["gd_pairs"], golden["gd_dist"]
+    data = golden["gd_data0"]
+    sg = float(golden["gd_sigma0"])
+    V = data.shape[0]
+    off, src, pidx = gather_list(pairs, V)
+    assert off[-1] == 2 * len(pairs)
+    w = np.array([oracle.gd_weight(d, sg) for d in dist], np.float32)
+    w0 = oracle.gd_weight(0.0, sg)
+    out = np.zeros(V, np.float32)
+    for v in range(V):
+        s = sw = np.float32(0.0)
+        for k in range(off[v], off[v + 1]):
+            s = np.float32(s + np.float32(w[pidx[k]] * data[src[k]]))
+            sw = np.float32(sw + w[pidx[k]])
+        out[v] = np.float32(s + np.float32(w0 * data[v])) / np.float32(sw + w0)
+    np.testing.assert_array_equal(out, golden["gd_out0"])
+    with pytest.raises(ValueError):
+        gather_list([[0, V]], V)

@@ -281,3 +281,12 @@ def test_rm_ancova_shuffles_caller_data_in_place(golden):
     s, n, V = d.shape
     want = d.reshape(s * n, V)[golden["rm1_after_shuffle"]].reshape(s, n, V)
     np.testing.assert_array_equal(golden["rm1_after_perm"], want)
+
+
+@pytest.mark.parametrize("k", [0, 1])
+def test_calc_gd_fwhm(golden, k):
+    """The restatement of calc_gd_fwhm (float32 accumulation in pair order,
+    powf / expf weights) against the reference's own output, bit for bit."""
+    got = oracle.calc_gd_fwhm(golden["gd_pairs"], golden["gd_dist"], golden[f"gd_data{k}"],
+                              float(golden[f"gd_sigma{k}"]))
+    np.testing.assert_array_equal(got, golden[f"gd_out{k}"])

@@ -87,6 +87,9 @@ SIGNATURES = {
                                         ctypes.c_int32, c_vp, ctypes.c_int32, ctypes.c_float, ctypes.c_float,
                                         c_vp, c_vp, c_vp, ctypes.c_int32, c_vp, ctypes.c_int64, c_vp, c_vp,
                                         c_vp]),
+    "gd_fwhm_weights": (ctypes.c_int, [c_vp, ctypes.c_int64, ctypes.c_float, c_vp, c_vp]),
+    "gd_fwhm_smooth": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, ctypes.c_int64, c_vp, ctypes.c_int64,
+                                      ctypes.c_int32, ctypes.c_int32, c_vp, ctypes.c_int64, c_vp, c_vp]),
     "fwer_sort": (ctypes.c_int, [c_vp, ctypes.c_int64, c_vp]),
     "fwer_lookup": (ctypes.c_int, [c_vp, ctypes.c_int64, c_vp, ctypes.c_int64, ctypes.c_int32,
                                    c_vp, c_vp]),

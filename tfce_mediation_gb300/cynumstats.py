@@ -103,3 +103,6 @@ def cython_lstsqr(x, y):
     x_avg, y_avg = x.mean(), y.mean()
     slope = np.sum((x - x_avg) * (y - y_avg)) / np.sum((x - x_avg) ** 2)
     return (y_avg - slope * x_avg, slope)
+
+
+from .gd_fwhm import calc_gd_fwhm  # noqa: E402,F401  (cynumstats.pyx:76-107, on the GPU)
