@@ -428,10 +428,13 @@ class MediationEngine:
     one glm_tstat launch (2P designs, kmax 3), sobel_combine forms z, and one
     sweep launch gives the maxima (one sign: z >= 0 for Aroian/Sobel).  For
     medtype 'Y' path a is a host regression of depend_y on pred_x (scipy
-    linregress), as in the reference."""
+    linregress), as in the reference.  covariates: unpermuted columns appended
+    to both designs (the tm-models mediation branch,
+    tm_models_randomise.py:430-503, where path a of 'Y' is glm_typeI's t)."""
 
     def __init__(self, Y, pred_x, depend_y, medtype, adjacency, segments=None, H=2.0, E=1.0, vdensity=None,
-                 floor_zero=False, batch=64, alg="aroian", accumulation="component", precision="bf16x3"):
+                 floor_zero=False, batch=64, alg="aroian", accumulation="component", precision="bf16x3",
+                 covariates=None):
         from .pyfunc import ALG
         if medtype not in ("I", "M", "Y"):
             raise ValueError("Invalid mediation type")
@@ -444,7 +447,13 @@ class MediationEngine:
         self.medtype, self.alg_code, self.batch = medtype, ALG[alg], int(batch)
         self.pred_x = np.asarray(pred_x, np.float64)
         self.depend_y = np.asarray(depend_y, np.float64)
+        self.cov = None if covariates is None else np.asarray(covariates, np.float64)
         self.n, self.V, self.n_seg = self.inner.n, self.inner.V, self.inner.n_seg
+        n_cov = 0 if self.cov is None else self.cov.reshape(self.n, -1).shape[1]
+        width = self.pred_x.reshape(self.n, -1).shape[1] + self.depend_y.reshape(self.n, -1).shape[1]
+        self.kmax = 1 + width + n_cov
+        if self.kmax > 8:
+            raise ValueError("at most 8 design columns (intercept, pred_x, depend_y, covariates)")
         self._z = self.t.empty((self.batch, self.V), device="cuda", dtype=self.t.float32)
         self._max = self.t.empty((self.batch, 1, self.inner.n_seg), device="cuda", dtype=self.t.float32)
 
@@ -454,7 +463,7 @@ class MediationEngine:
         for p in perms:
             x = self.pred_x[p]
             dy = self.depend_y if self.medtype in ("M", "I") else self.depend_y[p]
-            Xa, Xb, tas = mediation_designs(self.medtype, x, dy, self.n)
+            Xa, Xb, tas = mediation_designs(self.medtype, x, dy, self.n, covariates=self.cov)
             A.append(Xa)
             B.append(Xb)
             ta.append(tas)
@@ -468,13 +477,13 @@ class MediationEngine:
         z = self._z[:P] if out is None else out
         lib = inner.lib
         if self.medtype == "Y":
-            tm = inner.tmaps(DesignBatch(B, kmax=3))  # (P, 1, V)
+            tm = inner.tmaps(DesignBatch(B, kmax=self.kmax))  # (P, 1, V)
             tas = dev(np.asarray(ta, np.float32))
             _lib.check(lib.sobel_combine(None, self.V, ptr(tas), ptr(tm), self.V, P, self.V, self.alg_code,
                                          ptr(z), self.V, stream_handle()))
         else:
             designs = [m for pair in zip(A, B) for m in pair]
-            tm = inner.tmaps(DesignBatch(designs, kmax=3))  # (2P, 1, V): a, b, a, b ...
+            tm = inner.tmaps(DesignBatch(designs, kmax=self.kmax))  # (2P, 1, V): a, b, a, b ...
             _lib.check(lib.sobel_combine(ptr(tm), 2 * self.V, None, ptr(tm) + 4 * self.V, 2 * self.V, P,
                                          self.V, self.alg_code, ptr(z), self.V, stream_handle()))
         return z

@@ -107,21 +107,32 @@ def write_voxelStat_img(statname, voxelStat, out_path, data_index, affine, TFCEf
 # ---------------------------------------------------------------------------
 # mediation
 # ---------------------------------------------------------------------------
-def mediation_designs(medtype, pred_x, depend_y, n):
+def mediation_designs(medtype, pred_x, depend_y, n, covariates=None):
     """Path-a and path-b designs of calc_sobelz (pyfunc.py:131-145); the tested
     coefficient is column 1 of each.  For medtype 'Y' path a is a scalar
-    regression of depend_y on pred_x (scipy linregress), returned as ta."""
+    regression of depend_y on pred_x (scipy linregress), returned as ta.
+    covariates: appended to both designs, as the tm-models mediation branch
+    passes dmy_covariates to glm_typeI (tm_models_randomise.py:430-503); path a
+    of 'Y' is then the FP64 OLS t of pred_x in [1, pred_x, covariates]."""
     x = np.asarray(pred_x, np.float64).reshape(n, -1)
     dy = np.asarray(depend_y, np.float64).reshape(n, -1)
     one = np.ones((n, 1))
+    cov = [] if covariates is None else [np.asarray(covariates, np.float64).reshape(n, -1)]
     if medtype == "I":
-        return np.hstack([one, x]), np.hstack([one, x, dy]), None
+        return np.hstack([one, x] + cov), np.hstack([one, x, dy] + cov), None
     if medtype == "M":
-        return np.hstack([one, x]), np.hstack([one, dy, x]), None
+        return np.hstack([one, x] + cov), np.hstack([one, dy, x] + cov), None
     if medtype == "Y":
-        from scipy.stats import linregress
-        lr = linregress(np.asarray(pred_x, np.float64).ravel(), np.asarray(depend_y, np.float64).ravel())
-        return None, np.hstack([one, dy, x]), lr.slope / lr.stderr
+        if covariates is None:
+            from scipy.stats import linregress
+            lr = linregress(np.asarray(pred_x, np.float64).ravel(), np.asarray(depend_y, np.float64).ravel())
+            return None, np.hstack([one, dy, x]), lr.slope / lr.stderr
+        Xa = np.hstack([one, x] + cov)
+        inv = np.linalg.inv(Xa.T @ Xa)
+        y = dy[:, 0]
+        a = inv @ Xa.T @ y
+        sigma2 = np.sum((y - Xa @ a) ** 2) / (n - Xa.shape[1])
+        return None, np.hstack([one, dy, x] + cov), a[1] / np.sqrt(sigma2 * inv[1, 1])
     raise ValueError("Invalid mediation type")
 
 

@@ -567,3 +567,101 @@ def tm_models_rmancova_run(opts):
     for j, nm in enumerate(names):
         _append(os.path.join(outdir, "perm_Fstat_%s_TFCE_%s.csv" % (nm, suffix)), [fmt % v for v in m[:, j]])
     return m
+
+
+def _subject_perms(n, start, stop, seed, opts):
+    """Index rows of the tm-models loops' rand_array: np.random.permutation(n)
+    per iteration, or rand_blocks with the equal-size rule when exchange blocks
+    are given (seeded RandomState(seed + i), or clock seeding)."""
+    ident = np.arange(n, dtype=np.float64)[:, None]
+    return _designs_for(ident, n, start, stop, opts, seed, equal_blocks_only=True)[:, :, 0].astype(np.int64)
+
+
+def tm_models_mediation_run(opts):
+    """The mediation branch of tm_models_randomise.py (:93-101, :430-520): per
+    permutation dmy_leftvar (and for medtype 'Y' also dmy_rightvar) is
+    permuted, path a = t of column 1 of glm_typeI on [1, left, covariates]
+    (for 'Y': of dmy_rightvar on it, a scalar), path b = t of column 1 of
+    [1, left, right, covariates] ('I') or [1, right, left, covariates] ('M',
+    'Y'); Aroian z, TFCE'd with one sign, appended to perm_Zstat_<medtype>.
+    The reference reassigns dmy_leftvar = dmy_leftvar[rand_array] inside its
+    loop, so the permutations compose: iteration i sees the rows c_i =
+    c_{i-1}[rand_array_i]."""
+    start, stop = int(opts.range[0]), int(opts.range[1]) + 1
+    seed = opts.seed[0] if getattr(opts, "seed", None) else None
+    surface = str(opts.surface[0]) if getattr(opts, "surface", None) else None
+    tempdir = "tmtemp_mediation_%s" % surface if surface else "tmtemp_mediation_volume"
+    outdir = "output_mediation_%s/perm_mediation" % surface if surface else "output_mediation_volume/perm_mediation"
+    left = np.asarray(_load(f"{tempdir}/dmy_leftvar.npy"), np.float64)
+    right = np.asarray(_load(f"{tempdir}/dmy_rightvar.npy"), np.float64)
+    medtype = str(np.atleast_1d(_load(f"{tempdir}/medtype.npy"))[0])
+    data = _load(f"{tempdir}/data.npy")
+    optstfce = _load(f"{tempdir}/optstfce.npy")
+    cov = _load(f"{tempdir}/dmy_covariates.npy")
+    cov = None if _saved_none(cov) else np.asarray(cov, np.float64)
+    n = left.shape[0]
+    H, E_ = float(optstfce[0]), float(optstfce[1])
+    off, idx, kw, fmt, suffix = _tm_models_space(tempdir, surface)
+    perms = _subject_perms(n, start, stop, seed, opts)
+    c = np.arange(n)
+    for i in range(perms.shape[0]):
+        c = c[perms[i]]
+        perms[i] = c
+    os.makedirs(outdir, exist_ok=True)
+    eng = E.MediationEngine(np.ascontiguousarray(data, np.float32), left, right, medtype, (off, idx), H=H, E=E_,
+                            batch=getattr(opts, "batch", 64), covariates=cov, **kw)
+    m = eng.run(perms=perms)[:, 0, 0, :]
+    m = m.max(axis=-1) if surface else m[:, 0]
+    _append(os.path.join(outdir, "perm_Zstat_%s_TFCE_%s.csv" % (medtype, suffix)), [fmt % v for v in m])
+    return m
+
+
+def tm_models_cosinor_mediation_run(opts):
+    """The cosinor-mediation branch of tm_models_randomise.py (:119-133,
+    :374-428): path a = the unpermuted amplitude t of the mediator's own
+    cosinor fit (glm_cosinor of dmy_mediator, first period), path b = t of the
+    mediator column in the permuted cosinor design [1, (cos, sin) per period,
+    mediator] (the tensor-core GLM's programmed epilogue); Aroian z, TFCE'd with
+    one sign, appended to perm_Zstat_<medtype>."""
+    from .glm import DesignBatch
+    from .pyfunc import ALG, cosinor_design, glm_cosinor
+    start, stop = int(opts.range[0]), int(opts.range[1]) + 1
+    seed = opts.seed[0] if getattr(opts, "seed", None) else None
+    surface = str(opts.surface[0]) if getattr(opts, "surface", None) else None
+    tempdir = "tmtemp_medcosinor_%s" % surface if surface else "tmtemp_medcosinor_volume"
+    outdir = "output_medcosinor_%s/perm_cosinor" % surface if surface else "output_medcosinor_volume/perm_cosinor"
+    time_var = np.asarray(_load(f"{tempdir}/time_var.npy"), np.float64)
+    period = [float(p) for p in np.atleast_1d(_load(f"{tempdir}/period.npy"))]
+    mediator = np.asarray(_load(f"{tempdir}/dmy_mediator.npy"), np.float64)
+    medtype = str(np.atleast_1d(_load(f"{tempdir}/medtype.npy"))[0])
+    data = _load(f"{tempdir}/data.npy")
+    optstfce = _load(f"{tempdir}/optstfce.npy")
+    n = data.shape[0]
+    H, E_ = float(optstfce[0]), float(optstfce[1])
+    off, idx, kw, fmt, suffix = _tm_models_space(tempdir, surface)
+    t_amp_a = float(np.ravel(glm_cosinor(mediator, time_var, period=period)[9][0])[0])
+    X = cosinor_design(time_var, period, [mediator])
+    c0 = 1 + 2 * len(period)
+    perms = _subject_perms(n, start, stop, seed, opts)
+    os.makedirs(outdir, exist_ok=True)
+    eng = E.PermutationEngine(np.ascontiguousarray(data, np.float32), X[:, 1:], (off, idx), H=H, E=E_,
+                              outputs=[("t", c0)], batch=getattr(opts, "batch", 64), **kw)
+    from . import _lib
+    from .device import dev, ptr, stream_handle
+    t = eng.t
+    res = []
+    for b in range(0, perms.shape[0], eng.batch):
+        rows = perms[b:b + eng.batch]
+        P = rows.shape[0]
+        tb = eng.tmaps(DesignBatch(X[rows]))  # (P, 1, V)
+        z = t.empty((P, eng.V), device="cuda", dtype=t.float32)
+        tas = dev(np.full(P, t_amp_a, np.float32))
+        _lib.check(eng.lib.sobel_combine(None, eng.V, ptr(tas), ptr(tb), eng.V, P, eng.V, ALG["aroian"], ptr(z),
+                                         eng.V, stream_handle()))
+        mx = eng.sweep_max(z, P)
+        res.append(mx.cpu().numpy().reshape(P, 1, eng.n_seg))
+        eng.status()
+    m = np.concatenate(res)[:, 0, :]
+    m = m.max(axis=-1) if surface else m[:, 0]
+    _append(os.path.join(outdir, "perm_Zstat_%s_TFCE_%s.csv" % (medtype, suffix)), [fmt % v for v in m])
+    return m
