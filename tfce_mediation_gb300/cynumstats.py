@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import numpy as np
 
+from .gd_fwhm import calc_gd_fwhm  # noqa: F401  (cynumstats.pyx:76-107, on the GPU)
 from .glm import WHAT_BETA, WHAT_RESID, WHAT_RSS, WHAT_SE, WHAT_T, DesignBatch, glm_fstat, glm_stat
 
 
@@ -104,5 +105,3 @@ def cython_lstsqr(x, y):
     slope = np.sum((x - x_avg) * (y - y_avg)) / np.sum((x - x_avg) ** 2)
     return (y_avg - slope * x_avg, slope)
 
-
-from .gd_fwhm import calc_gd_fwhm  # noqa: E402,F401  (cynumstats.pyx:76-107, on the GPU)

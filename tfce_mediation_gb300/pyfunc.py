@@ -26,6 +26,7 @@ from .adjacency import create_adjac_vertex, create_adjac_voxel  # noqa: F401
 from .device import dev, ptr, require_cuda, stream_handle
 from .glm import WHAT_T, DesignBatch, glm_stat
 from .io import save_mgh, save_nifti
+from .rm_anova import column_product, dummy_code, stack_ones  # noqa: F401  (pyfunc.py:2564-2676)
 
 ALG = {"aroian": 0, "sobel": 1, "goodman": 2}
 
@@ -414,7 +415,6 @@ def glm_cosinor(endog, time_var, exog=None, dmy_covariates=None, rand_array=None
 
 
 # -- tm-models repeated-measures ANCOVA ----------------------------------------
-from .rm_anova import column_product, dummy_code, stack_ones  # noqa: E402,F401  (pyfunc.py:2564-2676)
 
 
 def _rm_anova(data, factors, dmy_subjects, dmy_covariates, data_format, output_sig, verbose, rand_array,

@@ -332,7 +332,6 @@ class RMAncovaEngine:
             row_off.ctypes.data, row_ps.ctypes.data, len(row_off), eb.ctypes.data, len(eb), ew.ctypes.data,
             len(ew), m.df_b, m.df_w, f_num.ctypes.data, f_err.ctypes.data, f_df.ctypes.data, len(f_num), ptr(out),
             self.V, ptr(ss_out), ptr(self.err), stream_handle()))
-        self._keep = (ess, rows_d)  # alive until the stream has used them
         return out
 
     def status(self):
