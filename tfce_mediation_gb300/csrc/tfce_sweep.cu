@@ -66,6 +66,11 @@ constexpr int kMaxSteps = 128;
 #ifndef TFGB_SWEEP_THREADS
 #define TFGB_SWEEP_THREADS 512
 #endif
+#ifndef TFGB_ACTIVE_BITMAP
+#define TFGB_ACTIVE_BITMAP 1
+#endif
+// largest activity bitmap kept in shared memory (segments up to 393,216 vertices)
+constexpr int kBitmapMaxBytes = 48 * 1024;
 #ifndef TFGB_SWEEP_MINBLOCKS
 #define TFGB_SWEEP_MINBLOCKS 2
 #endif
@@ -120,6 +125,8 @@ struct SweepArgs {
   // the kernel validates segment ranges and list extents against.
   int32_t n_vertices;
   int64_t n_entries;
+  // words of the shared-memory activity bitmap (dynamic shared memory), 0 = none
+  int32_t bm_words;
 };
 
 // Per-component mode: the increments so far (root) or the potential to the
@@ -172,6 +179,13 @@ __device__ inline Slot make_slot(char* base, int32_t vcap) {
 }
 
 __device__ inline void set_err(int32_t* err, int32_t code) { atomicCAS(err, 0, code); }
+
+// dynamic shared memory of the activity bitmap for segments of up to vmax
+// vertices (0 when it would not fit: the union phase then loads every key)
+inline int bitmap_bytes(int64_t vmax) {
+  const int64_t b = (vmax + 31) / 32 * 4;
+  return (TFGB_ACTIVE_BITMAP && b <= kBitmapMaxBytes) ? static_cast<int>(b) : 0;
+}
 
 // Union-find state of an item is private to the one CTA (one SM) sweeping it,
 // so loads and stores of it are relaxed at CTA scope: coherent with the
@@ -306,6 +320,10 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
   __shared__ int32_t sStart[kMaxSteps + 1];
   __shared__ float sRed[32];
   __shared__ int32_t sItem, sL, sNDead, sNRoots, sNext, sGrab, sGrabS, sGrabA;
+  // bit v set once vertex v is active (its activation step <= the current
+  // step): the union phase loads a neighbour's key only when it is set
+  extern __shared__ uint32_t sAct[];
+  const bool use_bm = TFGB_ACTIVE_BITMAP && a.bm_words > 0;
 
   Slot sl = make_slot(a.ws + (int64_t)blockIdx.x * a.ws_slot_bytes, a.vcap);
   const int tid = threadIdx.x, nth = blockDim.x;
@@ -377,6 +395,8 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
       if (a.n_steps_out) *a.n_steps_out = L;
     }
     for (int i = tid; i <= kMaxSteps; i += nth) sCnt[i] = 0;
+    if (use_bm)
+      for (int32_t w = tid; w < (Vs + 31) / 32; w += nth) sAct[w] = 0u;
     __syncthreads();
     TFGB_PHASE_MARK(0);
     const int L = sL;
@@ -433,6 +453,7 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
         base = __shfl_sync(peers, base, leader);
         const int32_t p = sStart[lv] + base + __popc(peers & ((1u << lane) - 1u));
         key = (static_cast<uint32_t>(lv) << kPosBits) | static_cast<uint32_t>(p);
+        if (use_bm && lv == 0) atomicOr(&sAct[v >> 5], 1u << (v & 31));
         sl.order[p] = v;
         sl.parent[p] = p;
         if constexpr (kLazy) {
@@ -502,7 +523,7 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
             ka[k] = kInactiveKey;
             if (eb + k < e1) {
               if (ag < 0 || ag >= Vs) set_err(a.err, kDevBadIndex);
-              else ka[k] = sl.key[an[k]];
+              else if (!use_bm || ((sAct[an[k] >> 5] >> (an[k] & 31)) & 1u)) ka[k] = sl.key[an[k]];
             }
           }
           // Batched union: the roots of all effective neighbours in this
@@ -591,6 +612,14 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
       }
       __syncthreads();
       if (tid == 0) sGrab = s1;  // the next step's first position
+      if (use_bm && i + 1 < L) {
+        // the next step's vertices become active (read after two more barriers)
+        const int32_t s2 = sStart[i + 2];
+        for (int32_t q = s1 + tid; q < s2; q += nth) {
+          const int32_t vq = sl.order[q];
+          atomicOr(&sAct[vq >> 5], 1u << (vq & 31));
+        }
+      }
       TFGB_PHASE_MARK(2);
       // (S) linked roots hand their extent to their final root: the listed
       // older roots and the positions of this step that are no longer roots.
@@ -877,7 +906,7 @@ int resident_slots(tfce_adjset* h) {
   int sms = 0, per_sm = 0;
   TFGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
   TFGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tfgb::tfce_sweep_kernel<false, false>,
-                                                          tfgb::kSweepThreads, 0));
+                                                          tfgb::kSweepThreads, tfgb::bitmap_bytes(h->vmax_seg)));
   h->max_slots = std::max(1, sms * std::max(1, per_sm));
   // tuning knob: fewer CTAs in flight (smaller L2 working set)
   if (const char* env = std::getenv("TFCE_SWEEP_MAX_CTAS")) {
@@ -940,8 +969,10 @@ int launch_sweep(tfce_adjset* h, const float* stats, int64_t map_stride, int32_t
   a.err = h->d_ctrl + 1;
   a.n_items = items;
   a.item_order = nullptr;
-  if (lazy) tfgb::tfce_sweep_kernel<false, true><<<slots, tfgb::kSweepThreads, 0, st>>>(a);
-  else tfgb::tfce_sweep_kernel<false, false><<<slots, tfgb::kSweepThreads, 0, st>>>(a);
+  const int bm = tfgb::bitmap_bytes(h->vmax_seg);
+  a.bm_words = bm / 4;
+  if (lazy) tfgb::tfce_sweep_kernel<false, true><<<slots, tfgb::kSweepThreads, bm, st>>>(a);
+  else tfgb::tfce_sweep_kernel<false, false><<<slots, tfgb::kSweepThreads, bm, st>>>(a);
   TFGB_CUDA(cudaGetLastError());
   return TFCE_OK;
 }
