@@ -267,7 +267,7 @@ class PermutationEngine:
         slot["d_t"] = t.empty((P, self.C, self.V), device="cuda", dtype=t.float32)
         slot["d_max"] = t.empty((P, self.C, self.signs, self.n_seg), device="cuda", dtype=t.float32)
 
-        def body():
+        def body_glm():
             for key in keys:
                 slot["d_" + key].copy_(slot["h_" + key], non_blocking=True)
             if tc is not None:
@@ -280,23 +280,31 @@ class PermutationEngine:
                                               ptr(slot["d_X"]), ptr(slot["d_invd"]), ptr(slot["d_dof"]), P,
                                               kmax, ptr(self._coef), self.C, ptr(slot["d_t"]), self.V,
                                               stream_handle()))
+
+        def body_sweep():
             self.adj.sweep_batch(ptr(slot["d_t"]), self.V, P * self.C, self.signs, ptr(self.vd),
                                  int(self.floor_zero), ptr(slot["d_max"]), None, 0, stream_handle())
             slot["h_max"].copy_(slot["d_max"], non_blocking=True)
 
         # warm-up outside capture (allocates the sweep workspace), then capture
+        # two graphs: the GLM part (the last reader of the resident data) and
+        # the sweep part, so new data can be uploaded while a sweep runs
         side = t.cuda.Stream()
         side.wait_stream(t.cuda.current_stream())
         with t.cuda.stream(side):
-            body()
+            body_glm()
+            body_sweep()
         t.cuda.current_stream().wait_stream(side)
         t.cuda.synchronize()
         self.status()
-        g = t.cuda.CUDAGraph()
-        with t.cuda.graph(g):
-            body()
-        slot["graph"] = g
+        g1, g2 = t.cuda.CUDAGraph(), t.cuda.CUDAGraph()
+        with t.cuda.graph(g1):
+            body_glm()
+        with t.cuda.graph(g2):
+            body_sweep()
+        slot["graph_glm"], slot["graph_sweep"] = g1, g2
         slot["event"] = t.cuda.Event()
+        slot["glm_done"] = t.cuda.Event()
         return slot
 
     def _fill(self, slot, perms):
@@ -329,17 +337,25 @@ class PermutationEngine:
         pair (data, perms) -- data: new (n, V) host data in the caller's
         vertex order (pinned memory keeps the copy asynchronous) or None to
         keep the resident data; perms: at most `batch` permutation index rows.
-        Two captured batch graphs are replayed in turn.  The host forms a
-        batch's design operators while the GPU runs the previous batch; new
-        data is copied and re-tiled in stream order, after the previous
-        batch's kernels and before this batch's; each batch's maxima come back
-        when its slot is reused or at the end.  A short batch is padded with
-        its last row inside the captured graph and the padding discarded.
+        Two captured batch slots are replayed in turn, each as a GLM graph and
+        a sweep graph.  The host forms a batch's design operators while the
+        GPU runs the previous batch; new data is copied and re-tiled on a side
+        stream once the previous batch's GLM (the last reader of the resident
+        data) is done, so the upload overlaps that batch's sweep, and this
+        batch's GLM waits for it; each batch's maxima come back when its slot
+        is reused or at the end.  A short batch is padded with its last row
+        inside the captured graph and the padding discarded.
         Returns the per-batch maxima, (rows, C, signs, n_seg) each."""
+        t = self.t
         P = self.batch
         if not hasattr(self, "_slots") or self._slots[0]["P"] != P:
             self._slots = [self._graph_slot(P), self._graph_slot(P)]
+        if not hasattr(self, "_up_stream"):
+            self._up_stream = t.cuda.Stream()
+            self._up_done = t.cuda.Event()
+        main = t.cuda.current_stream()
         results = {}
+        prev = None
 
         def collect(slot):
             slot["event"].synchronize()
@@ -363,10 +379,18 @@ class PermutationEngine:
                 collect(slot)
             self._fill(slot, perms)
             if data is not None:
-                self.upload(data)
-            slot["graph"].replay()
-            slot["event"].record()
+                up = self._up_stream
+                up.wait_stream(main) if prev is None else up.wait_event(prev["glm_done"])
+                with t.cuda.stream(up):
+                    self.upload(data)
+                self._up_done.record(up)
+                main.wait_event(self._up_done)
+            slot["graph_glm"].replay()
+            slot["glm_done"].record(main)
+            slot["graph_sweep"].replay()
+            slot["event"].record(main)
             slot["busy"], slot["order"], slot["rows"] = True, s_, rows
+            prev = slot
             n_steps = s_ + 1
         for slot in self._slots:
             if slot.get("busy"):
