@@ -262,3 +262,32 @@ def test_component_accumulation_segments_and_asymmetric(golden):
     adj2.set_accumulation("component")
     e_c, _ = _batch(adj2, m2)
     np.testing.assert_allclose(e_c, e_e, rtol=COMPONENT_RTOL)
+
+
+def test_large_segment_without_activity_bitmap():
+    """A segment above the shared-memory activity bitmap's capacity (393,216
+    vertices) sweeps without it: exact mode bit-identical to the oracle,
+    per-component mode within its bar."""
+    import torch
+    rng = np.random.default_rng(71)
+    mask = np.ones((80, 80, 66), bool)  # 422,400 voxels
+    off, idx = A.voxel_csr(mask, 6, "pyfunc")
+    V = int(mask.sum())
+    maps = rng.standard_normal((2, V)).astype(np.float32)
+    vol = maps.reshape(2, 80, 80, 66)
+    for _ in range(2):  # light smoothing so clusters form
+        vol = (vol + np.roll(vol, 1, 1) + np.roll(vol, -1, 1) + np.roll(vol, 1, 2) + np.roll(vol, -1, 2)) / 5.0
+    maps = np.ascontiguousarray(vol.reshape(2, V) * 3.0, np.float32)
+    adj = A.AdjacencySet((off, idx), 2.0, 0.5)
+    d = torch.from_numpy(maps).cuda()
+    out = torch.empty((2, 2, 1), device="cuda")
+    adj.sweep_batch(d.data_ptr(), V, 2, 2, None, 0, out.data_ptr())
+    adj.status()
+    got = out.cpu().numpy()
+    for sgn, s in enumerate((1.0, -1.0)):
+        ref = oracle.tfce_max_batch(off, idx, maps, 2.0, 0.5, sign=s, hh_exact=True)
+        np.testing.assert_array_equal(got[:, sgn, 0], ref)
+    adj.set_accumulation("component")
+    adj.sweep_batch(d.data_ptr(), V, 2, 2, None, 0, out.data_ptr())
+    adj.status()
+    np.testing.assert_allclose(out.cpu().numpy(), got, rtol=COMPONENT_RTOL)
