@@ -223,7 +223,7 @@ def run_gpu(args):
     import torch.distributed as dist
 
     from tfce_mediation_gb300 import engine as E
-    from tfce_mediation_gb300 import synth
+    from tfce_mediation_gb300 import shard, synth
     from tfce_mediation_gb300.glm import DesignBatch
 
     ws, rank, local = dist_env()
@@ -240,7 +240,7 @@ def run_gpu(args):
     C, S, V, n = eng.C, eng.n_seg, eng.V, eng.n
     total_steps = args.warmup + args.steps
     # disjoint permutation ranges per rank
-    base = rank * total_steps * P
+    base = shard.shard_range(ws * total_steps * P, ws, rank)[0]
     perms = [E.permutations(n, SEED, base + s * P, base + (s + 1) * P) for s in range(total_steps)]
     # device-resident design operators (inputs resident before the timed region)
     tc = eng._tc
@@ -298,10 +298,7 @@ def run_gpu(args):
     ms = start.elapsed_time(stop)
     glm_ms = [e[0].elapsed_time(e[1]) for e in evs]
     sweep_ms = [e[1].elapsed_time(e[2]) for e in evs]
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = shard.max_over_ranks(ms)  # the slowest rank's time
     perms_total = args.steps * P * ws
     value = perms_total / (ms / 1000.0)
 

@@ -29,6 +29,8 @@ from .glm import OUT_NEG_T, OUT_T, DesignBatch, TensorCoreOperands, output_colum
 
 def permutations(n, seed, start, stop):
     """Index streams of the mmr-lr convention (tm_func.py:147-151)."""
+    if stop <= start:
+        return np.zeros((0, n), np.int64)
     return np.stack([np.random.RandomState(seed + p).permutation(n) for p in range(start, stop)])
 
 
