@@ -180,3 +180,15 @@ def test_tm_models_rmancova_driver_volume(tmp_path, monkeypatch):
         for j in range(7):
             ref = oracle.tfce_max_batch(off, idx, np.asarray(F[j], np.float32), 2.0, 0.5)[0]
             assert abs(csv[j][p] - ref) <= 1e-3 * abs(ref) + 1e-3, (names[j], p, csv[j][p], ref)
+
+
+def test_long_format_equals_short(golden):
+    """'long' data (n*s rows, interval-major) gives the short-format F maps."""
+    d = golden["rm2_data"]
+    s, n, V = d.shape
+    short = pyfunc.reg_rm_ancova_two_bs_factor(d.copy(), golden["rm2_fa"], golden["rm2_fb"], golden["rm2_subj"],
+                                               dmy_covariates=golden["rm2_cov"], verbose=False)
+    long_ = pyfunc.reg_rm_ancova_two_bs_factor(d.reshape(s * n, V).copy(), golden["rm2_fa"], golden["rm2_fb"],
+                                               golden["rm2_subj"], dmy_covariates=golden["rm2_cov"],
+                                               data_format="long", verbose=False)
+    np.testing.assert_array_equal(np.asarray(short), np.asarray(long_))
