@@ -841,15 +841,6 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
   }
 }
 
-// Per-component accumulation with the union-find indexed by VERTEX: a
-// neighbour's activity is its 1-byte activation step and its union-find
-// entry is parent[neighbour] itself, so the union phase touches the level
-// array (V bytes per item) and the vertex-indexed parent array, whose entries
-// for mesh neighbours share cache sectors.  Links put the larger vertex index
-// under the smaller (parent[x] <= x, walks end).  The component partition,
-// extents and increments are those of the position-indexed kernel; only the
-// representative of a component differs, which the per-component potentials
-// do not depend on.
 }  // namespace tfgb
 
 // ---------------------------------------------------------------------------
