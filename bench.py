@@ -162,6 +162,196 @@ def _cpu_perm(p):
     return out
 
 
+# ---------------------------------------------------------------------------
+# The next rows' workloads (--workload cosinor | rmancova | gd_fwhm): the
+# tm-models cosinor and RM-ANCOVA permutation statistics on the config-2
+# surfaces, and geodesic FWHM smoothing of subject images on one L7 hemisphere
+# ---------------------------------------------------------------------------
+NEXT = {
+    "cosinor": "tm-models cosinor on config-2 surfaces (327,684 vertices), n=350, period 24 h, 1 exog + 1 "
+               "covariate: model F, amplitude t, acrophase t, +/-t exog = 5 maps x 2 hemispheres",
+    "rmancova": "tm-models RM-ANCOVA (one between-subject factor + covariate) on config-2 surfaces (327,684 "
+                "vertices), 120 subjects x 3 intervals: F_a, F_s, F_sa = 3 maps x 2 hemispheres",
+    "gd_fwhm": "geodesic FWHM smoothing, one icosphere-L7 hemisphere (163,842 vertices), vertex pairs within "
+               "chord 0.038 (~60 per vertex), batches of 64 images",
+}
+
+
+def _next_study(kind):
+    """Seeded inputs of a next-row workload (deterministic, rebuilt in every process)."""
+    from tfce_mediation_gb300 import synth
+    rng = np.random.default_rng(7)
+    if kind == "cosinor":
+        st = synth.config2()
+        tv = rng.uniform(0.0, 24.0, st.n)
+        from tfce_mediation_gb300.pyfunc import cosinor_design
+        X = cosinor_design(tv, [24.0], [st.pred_x[:, 1]], st.pred_x[:, 2])
+        return dict(st=st, X=X, tv=tv)
+    if kind == "rmancova":
+        n, s = 120, 3
+        st = synth.config2(n=n * s)
+        g = rng.integers(0, 2, n)
+        from tfce_mediation_gb300.rm_anova import dummy_code
+        Y = st.Y.reshape(s, n, -1) + (0.6 * rng.standard_normal(n))[None, :, None].astype(np.float32)
+        return dict(st=st, Y=np.ascontiguousarray(Y.reshape(s * n, -1), np.float32), n=n, s=s,
+                    f1=dummy_code(g), subj=dummy_code(np.arange(n), demean=False),
+                    cov=rng.standard_normal((n, 1)))
+    if kind == "gd_fwhm":
+        from scipy.spatial import cKDTree
+        v, _ = synth.icosphere(7)
+        qp = cKDTree(v).query_pairs(0.038, output_type="ndarray")
+        pairs = np.ascontiguousarray(qp[np.lexsort((qp[:, 1], qp[:, 0]))], np.int32)
+        dist = np.linalg.norm(v[pairs[:, 0]] - v[pairs[:, 1]], axis=1).astype(np.float32)
+        imgs = rng.standard_normal((64, v.shape[0])).astype(np.float32)
+        return dict(pairs=pairs, dist=dist, imgs=imgs, V=v.shape[0], sigma=4e-4)
+    raise ValueError(kind)
+
+
+def _next_cpu_init(kind):
+    _W["next"] = (kind, _next_study(kind))
+    from oracle import oracle
+    oracle.lib()
+
+
+def _segment_max(st, img, s=1.0):
+    from oracle import oracle
+    best = -np.inf
+    for h in range(2):
+        a, b = st.segments[h], st.segments[h + 1]
+        off = st.offsets[a:b + 1] - st.offsets[a]
+        idx = st.indices[st.offsets[a]:st.offsets[b]] - a
+        best = max(best, oracle.tfce_max_batch(off, idx, img[a:b], 2.0, 1.0, sign=s, floor_zero=True)[0])
+    return best
+
+
+def _next_cpu_perm(p):
+    """One permutation (or, for gd_fwhm, a bounded slice of one image's pair
+    scatter) as the reference computes it, with the oracle."""
+    from oracle import oracle
+    kind, d = _W["next"]
+    if kind == "cosinor":
+        st = d["st"]
+        perm = np.random.RandomState(SEED + p).permutation(st.n)
+        r = oracle.glm_cosinor(st.Y, d["tv"], exog=[st.pred_x[:, 1]], dmy_covariates=st.pred_x[:, 2],
+                               rand_array=perm, period=[24.0], calc_MESOR=False)
+        maps = [r[7], r[9][0], r[10][0], r[11][0], -r[11][0]]
+        return [_segment_max(st, np.asarray(m, np.float32)) for m in maps]
+    if kind == "rmancova":
+        st, n, s = d["st"], d["n"], d["s"]
+        rng = np.random.RandomState(SEED + p)
+        ra, sh = rng.permutation(n), rng.permutation(n * s)
+        F = oracle.rm_ancova_one(d["Y"].reshape(s, n, -1), d["f1"], d["subj"], dmy_covariates=d["cov"],
+                                 rand_array=ra, shuffle=sh)
+        return [_segment_max(st, np.asarray(m, np.float32)) for m in F]
+    sl = slice(p * 20_000, (p + 1) * 20_000)
+    oracle.calc_gd_fwhm(d["pairs"][sl], d["dist"][sl], d["imgs"][0], d["sigma"])
+    return []
+
+
+def run_next(args):
+    """One JSON line for a next-row workload: whole-job rate through the public
+    API with the data resident (the engines' own batched loops), the device
+    kernels timed with CUDA events, and the oracle on one core for a bounded
+    sample."""
+    import multiprocessing as mp
+    kind = args.workload
+    cpu = None
+    if not args.no_cpu_baseline:  # before the first GPU call (spawned pool)
+        _one_thread_per_process()
+        ctx = mp.get_context("spawn")
+        n_cpu = 3 if kind == "gd_fwhm" else 2
+        with ctx.Pool(1, initializer=_next_cpu_init, initargs=(kind,)) as pool:
+            t0 = time.perf_counter()
+            pool.map(_next_cpu_perm, range(n_cpu))
+            dt = time.perf_counter() - t0
+        if kind == "gd_fwhm":
+            M = len(_next_study(kind)["pairs"])
+            per_img = dt / (n_cpu * 20_000) * M
+            cpu = {"value": 1.0 / per_img, "unit": "images/s", "cores": 1, "kind": "port",
+                   "sample": f"{n_cpu} x 20,000 of {M:,} pairs of one image, extrapolated per pair"}
+        else:
+            cpu = {"value": n_cpu / dt, "unit": "perm/s", "cores": 1, "kind": "port",
+                   "sample": f"{n_cpu} permutations of the same workload, {dt:.1f} s"}
+    import torch
+    from tfce_mediation_gb300 import engine as E
+    d = _next_study(kind)
+    torch.cuda.set_device(0)
+    K = args.steps
+    if kind == "gd_fwhm":
+        from tfce_mediation_gb300.gd_fwhm import GeodesicSmoother
+        from tfce_mediation_gb300.device import ptr
+        sm = GeodesicSmoother(d["pairs"], d["dist"], d["sigma"], d["V"])
+        x = torch.from_numpy(d["imgs"]).cuda()
+        out = torch.empty_like(x)
+        B, V, M = x.shape[0], d["V"], sm.M
+        st_ = torch.cuda.current_stream().cuda_stream
+
+        def launch():
+            sm.lib.gd_fwhm_smooth(ptr(sm.off), ptr(sm.src), ptr(sm.pidx), ptr(sm.w), M, ptr(x), V, B, V,
+                                  ptr(out), V, ptr(sm.err), st_)
+        for _ in range(args.warmup):
+            launch()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(K):
+            launch()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / K
+        assert int(sm.err.item()) == 0
+        # per image: the gather list (src + pidx, 8 B per entry, 2M entries) and the weights it
+        # indexes (4 B per entry), the image gather (4 B per entry) and the output (4V)
+        alg_bytes = B * (2 * M * 16 + 4 * V)
+        hbm, _, peak_kind = measured_peaks()
+        achieved = alg_bytes / (ms / 1e3) / 1e9
+        line = {"metric": "images/s", "value": B / (ms / 1e3), "unit": "images/s", "workload": kind,
+                "config": {"workload": NEXT[kind], "pairs": int(M), "images_per_launch": B},
+                "ms_per_launch": ms, "steps": K, "warmup": args.warmup, "higher_is_better": True,
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                             "frac": achieved / hbm, "peak_source": peak_kind + " hbm_gbs",
+                             "note": "16 B per gather entry (index, pair, weight, value; every image re-reads "
+                                     "the list)"},
+                "cpu_baseline": cpu, "gpu_launches": K, "data": "synthetic"}
+        print(json.dumps(line), flush=True)
+        return
+    st = d["st"]
+    if kind == "cosinor":
+        from tfce_mediation_gb300.randomise import cosinor_outputs
+        eng = E.PermutationEngine(st.Y, d["X"][:, 1:], (st.offsets, st.indices), st.segments, 2.0, 1.0,
+                                  batch=args.batch or 256, floor_zero=True, outputs=cosinor_outputs(1, 1, 1))
+        P = eng.batch
+        eng.run_graph(perms=E.permutations(st.n, SEED, 0, P))  # capture
+        torch.cuda.synchronize()
+        perms = E.permutations(st.n, SEED, P, P + K * P)
+        t0 = time.perf_counter()
+        eng.run_graph(perms=perms)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        maps = 5 * 2
+    else:
+        from tfce_mediation_gb300 import randomise
+        from tfce_mediation_gb300.rm_anova import RMAncovaEngine, RMModel
+        model = RMModel(d["n"], d["s"], d["f1"], d["subj"], dmy_covariates=d["cov"])
+        P = args.batch or 128
+        eng = RMAncovaEngine(d["Y"], model, (st.offsets, st.indices), st.segments, 2.0, 1.0, floor_zero=True,
+                             batch=P)
+        ras, cums = randomise.rm_permutations(d["n"], d["n"] * d["s"], 0, P + K * P, SEED)
+        eng.maxima(list(ras[:P]), cums[:P])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        eng.maxima(list(ras[P:]), cums[P:])
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        maps = 3 * 2
+    line = {"metric": "perm/s", "value": K * P / dt, "unit": "perm/s", "workload": kind,
+            "config": {"workload": NEXT[kind], "perms_per_step": P, "sweeps_per_perm": maps},
+            "ms_per_step": dt / K * 1e3, "steps": K, "warmup": 1, "higher_is_better": True,
+            "note": "whole job through the engine's public loop, data resident, host design work included",
+            "cpu_baseline": cpu, "data": "synthetic"}
+    print(json.dumps(line), flush=True)
+
+
 def _one_thread_per_process():
     """BLAS / OpenMP thread counts of 1 for the worker processes (spawned
     children read these when their numpy loads), so `cores` processes use
@@ -451,8 +641,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", default="bf16x3", choices=["bf16x3", "fp32"],
                     help="GLM arithmetic: tensor-core split BF16 or FP32 CUDA cores")
+    ap.add_argument("--workload", default="config2", choices=["config2"] + sorted(NEXT),
+                    help="config2: the headline; others: the next rows' workloads (one JSON line each)")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.workload != "config2":
+        if args.steps == 60:
+            args.steps = 8
+        run_next(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

@@ -212,10 +212,12 @@ class RMModel:
         for bi, (name, build, w, ess) in enumerate(self.blocks):
             parts = [np.ones((P, self.N, 1))] + [x for x in build(L) if x is not None]
             D = np.concatenate(parts, axis=2)
-            D = np.take_along_axis(D, inv_order[:, :, None], axis=1)  # row i <- built row argsort(c)[i]
-            inv = np.linalg.inv(np.einsum("pni,pnj->pij", D, D))
+            Dt = D.transpose(0, 2, 1)
+            inv = np.linalg.inv(Dt @ D)  # the row shuffle leaves D'D unchanged
             k = D.shape[2]
-            rows = np.einsum("pij,pnj->pin", inv[:, k - w:, :], D)  # (P, w, N)
+            # pseudoinverse rows of the block on the built rows, then columns in
+            # the shuffled order: column i <- built row argsort(c)[i]
+            rows = np.take_along_axis(inv[:, k - w:, :] @ Dt, inv_order[:, None, :], axis=2)  # (P, w, N)
             blocks_w = []
             for _, off, width in ess:
                 a = k - w + off
@@ -344,18 +346,29 @@ class RMAncovaEngine:
             self.adj.status()
 
     def maxima(self, ras, cums):
-        """TFCE null maxima (P, n_f, n_seg), one sign per map."""
+        """TFCE null maxima (P, n_f, n_seg), one sign per map.  A batch's
+        maxima are read back after the next batch is launched, so the host
+        forms the next batch's designs while the GPU runs the current one."""
         t = self.t
         P = len(ras)
-        res = []
+        res, prev = [], None
+
+        def collect(item):
+            mx, nb = item
+            res.append(mx.cpu().numpy().reshape(nb, self.n_f, self.n_seg))
+            self.status()
+
         for b in range(0, P, self.batch):
             Fm = self.fmaps(ras[b:b + self.batch], cums[b:b + self.batch])
             nb = Fm.shape[0]
             mx = t.empty(nb * self.n_f * self.n_seg, device="cuda", dtype=t.float32)
             self.adj.sweep_batch(ptr(Fm), self.V, nb * self.n_f, 1, ptr(self.vd), int(self.floor_zero), ptr(mx),
                                  None, 0, stream_handle())
-            res.append(mx.cpu().numpy().reshape(nb, self.n_f, self.n_seg))
-            self.status()
+            if prev is not None:
+                collect(prev)
+            prev = (mx, nb)
+        if prev is not None:
+            collect(prev)
         return np.concatenate(res) if res else np.zeros((0, self.n_f, self.n_seg), np.float32)
 
 
