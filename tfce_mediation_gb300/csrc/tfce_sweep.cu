@@ -72,7 +72,7 @@ constexpr int kMaxSteps = 128;
 // largest activity bitmap kept in shared memory (segments up to 393,216 vertices)
 constexpr int kBitmapMaxBytes = 48 * 1024;
 #ifndef TFGB_SWEEP_MINBLOCKS
-#define TFGB_SWEEP_MINBLOCKS 2
+#define TFGB_SWEEP_MINBLOCKS 3  // 3 x 512 threads per SM (40 registers; a few spills)
 #endif
 #ifndef TFGB_UBATCH
 #define TFGB_UBATCH 6
