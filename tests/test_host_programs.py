@@ -226,3 +226,26 @@ def test_gd_gather_list_keeps_the_scatter_order(golden):
     np.testing.assert_array_equal(out, golden["gd_out0"])
     with pytest.raises(ValueError):
         gather_list([[0, V]], V)
+
+
+def test_tm_models_randomise_cli_dispatch(monkeypatch):
+    """The tm_models_randomise flags select the same branch as the reference."""
+    calls = []
+    for name in ("tm_models_glm_run", "tm_models_mediation_run", "tm_models_rmancova_run", "tm_models_cosinor_run",
+                 "tm_models_cosinor_mediation_run"):
+        monkeypatch.setattr(randomise, name, lambda opts, _n=name: calls.append((_n, opts.surface)))
+    p = randomise.tm_models_randomise_parser()
+    cases = [(["-r", "0", "9", "-s", "area", "-glm"], "tm_models_glm_run", ["area"]),
+             (["-r", "0", "9", "-v", "-med"], "tm_models_mediation_run", None),
+             (["-r", "0", "9", "-v", "-ofa"], "tm_models_rmancova_run", None),
+             (["-r", "0", "9", "-s", "thickness", "-tfa"], "tm_models_rmancova_run", ["thickness"]),
+             (["-r", "0", "9", "-v", "-cos"], "tm_models_cosinor_run", None),
+             (["-r", "0", "9", "-v", "-mcos"], "tm_models_cosinor_mediation_run", None)]
+    for argv, want, surf in cases:
+        calls.clear()
+        randomise.tm_models_randomise_run(p.parse_args(argv))
+        assert calls == [(want, surf)], argv
+    with pytest.raises(ValueError):
+        randomise.tm_models_randomise_run(p.parse_args(["-r", "0", "9", "-t", "-glm"]))
+    with pytest.raises(SystemExit):
+        p.parse_args(["-r", "0", "9", "-v", "-glm", "-cos"])  # one statistic at a time

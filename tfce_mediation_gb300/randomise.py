@@ -16,6 +16,10 @@ appends the same CSV lines in the same order and format:
 * tm_models_glm_run    -- tmanalysis/tm_models_randomise.py:76-92,193-274 (the GLM branch:
   tmtemp_GLM_<surface|volume>/, output_GLM_<..>/perm_GLM/perm_Fstat_<var>_TFCE_max*.csv
   and perm_Tstat_con<c>_TFCE_max*.csv)
+* tm_models_cosinor_run, tm_models_rmancova_run, tm_models_mediation_run,
+  tm_models_cosinor_mediation_run -- the other tm_models_randomise.py branches;
+  tm_models_randomise_run dispatches on the reference's own flags
+  (python -m tfce_mediation_gb300.randomise -r 0 99 -s area -glm)
 
 Permutations: the reference seeds each iteration from the clock
 (``np.random.seed(int(iter_perm*1000+time()))``); that stays the default.
@@ -665,3 +669,50 @@ def tm_models_cosinor_mediation_run(opts):
     m = m.max(axis=-1) if surface else m[:, 0]
     _append(os.path.join(outdir, "perm_Zstat_%s_TFCE_%s.csv" % (medtype, suffix)), [fmt % v for v in m])
     return m
+
+
+def tm_models_randomise_parser(ap=None):
+    """The argument parser of tmanalysis/tm_models_randomise.py:30-68 (same
+    flags), plus --seed (host-seeded stream) and --batch (permutations per
+    launch)."""
+    ap = ap or argparse.ArgumentParser(description="tm-models permutations on the GPU")
+    ap.add_argument("-r", "--range", nargs=2, type=int, required=True, metavar=("INT", "INT"))
+    modality = ap.add_mutually_exclusive_group(required=True)
+    modality.add_argument("-s", "--surface", nargs=1, metavar=("STR",))
+    modality.add_argument("-v", "--voxel", action="store_true")
+    modality.add_argument("-t", "--tmi", action="store_true")
+    stat = ap.add_mutually_exclusive_group(required=False)
+    for short, long_ in (("-glm", "--generalizedlinearmodel"), ("-med", "--mediation"),
+                         ("-ofa", "--onebetweenssubjectfactor"), ("-tfa", "--twobetweenssubjectfactor"),
+                         ("-cos", "--cosinor"), ("-mcos", "--cosinormediation")):
+        stat.add_argument(short, long_, action="store_true")
+    ap.add_argument("-e", "--exchangeblock", nargs=1, metavar=("*.csv",))
+    ap.add_argument("--seed", nargs=1, type=int, default=None,
+                    help="host-seeded permutation stream RandomState(seed + i) (default: clock seeding)")
+    ap.add_argument("--batch", type=int, default=64)
+    return ap
+
+
+def tm_models_randomise_run(opts):
+    """tm_models_randomise.run (tmanalysis/tm_models_randomise.py:70-684): the
+    branch its statistic flag selects, on the GPU.  The reference has no
+    branch for -t (TMI) input; it is refused here."""
+    if getattr(opts, "tmi", False):
+        raise ValueError("tm_models_randomise has no TMI (-t) branch; use -s SURFACE or -v")
+    if getattr(opts, "voxel", False):
+        opts.surface = None
+    if getattr(opts, "generalizedlinearmodel", False):
+        return tm_models_glm_run(opts)
+    if getattr(opts, "mediation", False):
+        return tm_models_mediation_run(opts)
+    if getattr(opts, "onebetweenssubjectfactor", False) or getattr(opts, "twobetweenssubjectfactor", False):
+        return tm_models_rmancova_run(opts)
+    if getattr(opts, "cosinor", False):
+        return tm_models_cosinor_run(opts)
+    if getattr(opts, "cosinormediation", False):
+        return tm_models_cosinor_mediation_run(opts)
+    return None  # no statistic flag: the reference's loop does nothing either
+
+
+if __name__ == "__main__":  # python -m tfce_mediation_gb300.randomise -r 0 99 -s area -glm
+    tm_models_randomise_run(tm_models_randomise_parser().parse_args())
