@@ -249,3 +249,43 @@ def test_tm_models_randomise_cli_dispatch(monkeypatch):
         randomise.tm_models_randomise_run(p.parse_args(["-r", "0", "9", "-t", "-glm"]))
     with pytest.raises(SystemExit):
         p.parse_args(["-r", "0", "9", "-v", "-glm", "-cos"])  # one statistic at a time
+
+
+def test_tm_models_surface_space(tmp_path):
+    """Surface tm-models inputs: both masked hemispheres as two segments of one
+    CSR (the masked subgraphs), density weights of the masked vertices, the
+    zero-fill floor and the vertex CSV format; a volume: one voxel CSR."""
+    from tfce_mediation_gb300 import adjacency as A
+    from tfce_mediation_gb300 import synth
+    v, f = synth.icosphere(2)
+    off, idx = A.mesh_csr(f, v.shape[0])
+    adj = np.empty(v.shape[0], dtype=object)
+    for i in range(v.shape[0]):
+        adj[i] = np.asarray(idx[off[i]:off[i + 1]], np.int64)
+    rng = np.random.default_rng(2)
+    m_lh = rng.random(v.shape[0]) > 0.2
+    m_rh = rng.random(v.shape[0]) > 0.3
+    vd_rh = rng.random(v.shape[0]).astype(np.float32)
+    d = tmp_path / "tmtemp_GLM_area"
+    d.mkdir()
+    np.save(d / "mask_lh.npy", m_lh)
+    np.save(d / "mask_rh.npy", m_rh)
+    np.save(d / "adjac_lh.npy", adj, allow_pickle=True)
+    np.save(d / "adjac_rh.npy", adj, allow_pickle=True)
+    np.save(d / "vdensity_lh.npy", np.array(1))
+    np.save(d / "vdensity_rh.npy", vd_rh)
+    o, i, kw, fmt, suffix = randomise._tm_models_space(str(d), "area")
+    o1, i1 = A.induced_csr(adj, m_lh)
+    o2, i2 = A.induced_csr(adj, m_rh)
+    oc, ic, seg = A.concat_csr([(o1, i1), (o2, i2)])
+    np.testing.assert_array_equal(o, oc)
+    np.testing.assert_array_equal(i, ic)
+    np.testing.assert_array_equal(kw["segments"], [0, m_lh.sum(), m_lh.sum() + m_rh.sum()])
+    np.testing.assert_array_equal(kw["vdensity"], np.concatenate([np.ones(m_lh.sum(), np.float32), vd_rh[m_rh]]))
+    assert kw["floor_zero"] and (fmt, suffix) == ("%.4f", "maxVertex")
+    dv = tmp_path / "tmtemp_GLM_volume"
+    dv.mkdir()
+    np.save(dv / "adjac.npy", adj, allow_pickle=True)
+    o, i, kw, fmt, suffix = randomise._tm_models_space(str(dv), None)
+    np.testing.assert_array_equal(o, off)
+    assert kw == {"segments": None} and (fmt, suffix) == ("%1.4f", "maxVoxel")
