@@ -9,7 +9,9 @@ Per launch, P permutations:
      float64, each permuted design's inv(X'X) X' and diag(inv(X'X));
   2. device: one GLM launch -> t maps [P][C][V] (float32, resident): the
      tcgen05 split-BF16 GEMM with the fused residual epilogue (precision
-     'bf16x3', default) or the FP32 CUDA-core kernel ('fp32');
+     'bf16x3', default) or the FP32 CUDA-core kernel ('fp32'); with
+     `outputs` / `f_groups` the epilogue's programmed rows instead (partial F,
+     cosinor amplitude / acrophase t, +/- t), swept with one sign;
   3. device: one tfce_sweep_batch launch over P x C maps x (+,-) x segments
      -> the scaled per-segment maximum of every sweep;
   4. host: max over segments (hemispheres) gives the reference's per-permutation
