@@ -534,7 +534,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
           j = __ldg(a.coef + 2 * oi);
           kv = __ldg(a.coef + 2 * oi + 1);
           wo = woff;
-          woff += kv * kv;
+          woff += (kv >= 1 && kv <= KMAX) ? kv * kv : 0;
         } else {
           kind = __ldg(a.coef + 4 * oi);
           j = __ldg(a.coef + 4 * oi + 1);
@@ -547,9 +547,10 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
         } else if (kind == kTcOutT || kind == kTcOutNegT) {
           ok = j >= 0 && j < KMAX;
         } else if (kind == kTcOutF || kind == kTcOutEss) {
-          ok = j >= 0 && kv >= 1 && j + kv <= KMAX && wo >= 0 && wo + kv * kv <= a.w_stride;
+          // written without sums that could overflow on a corrupt program row
+          ok = j >= 0 && j < KMAX && kv >= 1 && kv <= KMAX - j && wo >= 0 && wo <= a.w_stride - kv * kv;
         } else if (kind == kTcOutAmp || kind == kTcOutAcro) {
-          ok = j >= 0 && j + 1 < KMAX && wo >= 0 && wo + 3 <= a.w_stride;
+          ok = j >= 0 && j < KMAX - 1 && wo >= 0 && wo <= a.w_stride - 3;
         } else {
           ok = false;
         }
