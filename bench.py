@@ -256,7 +256,7 @@ def run_next(args):
     import multiprocessing as mp
     kind = args.workload
     cpu = None
-    if not args.no_cpu_baseline:  # before the first GPU call (spawned pool)
+    if not args.no_cpu_baseline or args.impl == "reference":  # before the first GPU call (spawned pool)
         _one_thread_per_process()
         ctx = mp.get_context("spawn")
         n_cpu = 3 if kind == "gd_fwhm" else 2
@@ -272,6 +272,13 @@ def run_next(args):
         else:
             cpu = {"value": n_cpu / dt, "unit": "perm/s", "cores": 1, "kind": "port",
                    "sample": f"{n_cpu} permutations of the same workload, {dt:.1f} s"}
+    if args.impl == "reference":  # the oracle port alone, on the line's own metric
+        print(json.dumps({"impl": "reference", "metric": cpu["unit"], "value": cpu["value"], "unit": cpu["unit"],
+                          "workload": kind, "config": {"workload": NEXT[kind]}, "higher_is_better": True,
+                          "cpu_baseline": cpu, "data": "synthetic",
+                          "e2e": {"value": cpu["value"], "unit": cpu["unit"], "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}), flush=True)
+        return
     import torch
     from tfce_mediation_gb300 import engine as E
     d = _next_study(kind)
