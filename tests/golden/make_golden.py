@@ -368,6 +368,36 @@ def main():
         out[f"rm2_perm_{tag}"], out[f"rm2_ra_{tag}"], out[f"rm2_shuffle_{tag}"] = np.asarray(res), ra, sh
     out["rm2_data"], out["rm2_fa"], out["rm2_fb"], out["rm2_subj"], out["rm2_cov"] = d2, fa2, fb2, subj2, cov2
 
+    # wider RM-ANCOVA and cosinor shapes: a three-level factor, two covariates,
+    # four intervals; cosinor with two exogenous variables (one of two columns)
+    rw = np.random.default_rng(79)
+    n3, s3, V3 = 30, 4, 12
+    g3 = rw.integers(0, 3, n3)
+    f3 = pyfunc.dummy_code(g3)
+    subj3 = pyfunc.dummy_code(np.arange(n3), demean=False)
+    cov3 = rw.standard_normal((n3, 2))
+    d3 = rw.standard_normal((s3, n3, V3)).astype(np.float32) + 1.0
+    d3 += (0.5 * rw.standard_normal(n3))[None, :, None].astype(np.float32)
+    d3[3, :, :4] += (0.8 * (g3 == 2))[:, None].astype(np.float32)
+    out["rm3_obs"] = np.asarray(pyfunc.reg_rm_ancova_one_bs_factor(d3.copy(), f3, subj3, dmy_covariates=cov3,
+                                                                  verbose=False))
+    res, ra, sh = seeded_call(pyfunc.reg_rm_ancova_one_bs_factor, 94, n3, n3 * s3, d3.copy(), f3, subj3,
+                              dmy_covariates=cov3, verbose=False)
+    out["rm3_perm"], out["rm3_ra"], out["rm3_shuffle"] = np.asarray(res), ra, sh
+    out["rm3_data"], out["rm3_f1"], out["rm3_subj"], out["rm3_cov"] = d3, f3, subj3, cov3
+    nw, Vw = 40, 15
+    tw = rw.uniform(0.0, 24.0, nw)
+    yw = rw.standard_normal((nw, Vw)).astype(np.float32) + 3.0
+    yw[:, :5] += (np.cos(2.0 * np.pi * tw / 24.0))[:, None].astype(np.float32)
+    exw = [rw.standard_normal((nw, 2)), rw.standard_normal(nw)]
+    permw = np.random.RandomState(80).permutation(nw)
+    for tag, ra_ in (("obs", None), ("perm", permw)):
+        r = pyfunc.glm_cosinor(yw, tw, exog=exw, rand_array=ra_, period=[24.0, 8.0])
+        for name, val in zip(names, r):
+            if val is not None:
+                out[f"cosw_{name}_{tag}"] = np.asarray(val)
+    out["cosw_y"], out["cosw_t"], out["cosw_ex0"], out["cosw_ex1"], out["cosw_perm"] = yw, tw, exw[0], exw[1], permw
+
     # calc_gd_fwhm (geodesic FWHM smoothing): vertex pairs of a level-3
     # icosphere within a radius (chord lengths standing in for geodesic
     # distances), plus a repeated pair and a self pair

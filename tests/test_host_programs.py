@@ -129,6 +129,27 @@ def _rm_pipeline_fp64(model, Y, ras, cums):
     return out
 
 
+@pytest.mark.parametrize("kind", ["obs", "perm"])
+def test_rm_anova_decomposition_fp64_wider(golden, kind):
+    """Three-level factor, two covariates, four intervals: the Wald-form
+    decomposition equals the FP64 restatement."""
+    from tfce_mediation_gb300 import rm_anova as R
+    d = golden["rm3_data"]
+    s, n, V = d.shape
+    model = R.RMModel(n, s, golden["rm3_f1"], golden["rm3_subj"], dmy_covariates=golden["rm3_cov"])
+    assert all(sum(model.blocks[i][2] for i in sl) <= R.SLOT_ROWS for sl in model.slots)
+    Y = d.reshape(s * n, V).astype(np.float64)
+    if kind == "obs":
+        ras, cums, kw = [None], np.arange(s * n)[None], {}
+    else:
+        ras, cums = [golden["rm3_ra"]], golden["rm3_shuffle"][None]
+        kw = dict(rand_array=ras[0], shuffle=cums[0])
+    got = _rm_pipeline_fp64(model, Y, ras, cums)[0]
+    ref64 = oracle.rm_ancova_one(d.astype(np.float64), golden["rm3_f1"], golden["rm3_subj"],
+                                 dmy_covariates=golden["rm3_cov"], **kw)
+    np.testing.assert_allclose(got, np.asarray(ref64), rtol=1e-9, atol=1e-12)
+
+
 @pytest.mark.parametrize("two", [False, True])
 @pytest.mark.parametrize("tag", ["nocov", "cov"])
 @pytest.mark.parametrize("kind", ["obs", "perm"])

@@ -290,3 +290,27 @@ def test_calc_gd_fwhm(golden, k):
     got = oracle.calc_gd_fwhm(golden["gd_pairs"], golden["gd_dist"], golden[f"gd_data{k}"],
                               float(golden[f"gd_sigma{k}"]))
     np.testing.assert_array_equal(got, golden[f"gd_out{k}"])
+
+
+@pytest.mark.parametrize("kind", ["obs", "perm"])
+def test_rm_ancova_one_wider(golden, kind):
+    """Three-level factor, two covariates, four intervals."""
+    kw = {} if kind == "obs" else dict(rand_array=golden["rm3_ra"], shuffle=golden["rm3_shuffle"])
+    got = oracle.rm_ancova_one(golden["rm3_data"], golden["rm3_f1"], golden["rm3_subj"],
+                               dmy_covariates=golden["rm3_cov"], **kw)
+    np.testing.assert_allclose(np.asarray(got), golden[f"rm3_{kind}"], rtol=1e-9)
+
+
+@pytest.mark.parametrize("tag", ["obs", "perm"])
+def test_glm_cosinor_two_exog(golden, tag):
+    """Two periods, two exogenous variables (one of two columns), no covariate,
+    calc_MESOR default."""
+    ra = None if tag == "obs" else golden["cosw_perm"]
+    res = oracle.glm_cosinor(golden["cosw_y"], golden["cosw_t"], exog=[golden["cosw_ex0"], golden["cosw_ex1"]],
+                             rand_array=ra, period=[24.0, 8.0])
+    for name, val in zip(_COS_NAMES, res):
+        key = f"cosw_{name}_{tag}"
+        if key not in golden:
+            assert val is None, name
+            continue
+        np.testing.assert_allclose(val, golden[key], rtol=1e-9, atol=1e-12, err_msg=name)
