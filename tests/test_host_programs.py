@@ -310,3 +310,27 @@ def test_tm_models_surface_space(tmp_path):
     o, i, kw, fmt, suffix = randomise._tm_models_space(str(dv), None)
     np.testing.assert_array_equal(o, off)
     assert kw == {"segments": None} and (fmt, suffix) == ("%1.4f", "maxVoxel")
+
+
+@pytest.mark.parametrize("s,la,lb,c", [(2, 2, 0, 0), (2, 3, 0, 1), (3, 2, 2, 1), (2, 2, 3, 0), (5, 2, 0, 2)])
+def test_rm_anova_decomposition_shapes(s, la, lb, c):
+    """Random studies over interval counts, factor levels and covariates: the
+    Wald-form decomposition equals the FP64 restatement (permuted call)."""
+    from tfce_mediation_gb300 import rm_anova as R
+    rng = np.random.default_rng(s * 100 + la * 10 + lb + c)
+    n, V = 36, 7
+    ga = rng.permutation(np.arange(n) % la)
+    gb = rng.permutation(np.arange(n) % lb) if lb else None
+    fa = R.dummy_code(ga)
+    fb = None if gb is None else R.dummy_code(gb)
+    cov = rng.standard_normal((n, c)) if c else None
+    subj = R.dummy_code(np.arange(n), demean=False)
+    d = rng.standard_normal((s, n, V)) + rng.standard_normal(n)[None, :, None]
+    model = R.RMModel(n, s, fa, subj, dmy_factor2=fb, dmy_covariates=cov)
+    ra, sh = rng.permutation(n), rng.permutation(n * s)
+    got = _rm_pipeline_fp64(model, d.reshape(s * n, V), [ra], sh[None])[0]
+    if fb is None:
+        ref = oracle.rm_ancova_one(d, fa, subj, dmy_covariates=cov, rand_array=ra, shuffle=sh)
+    else:
+        ref = oracle.rm_ancova_two(d, fa, fb, subj, dmy_covariates=cov, rand_array=ra, shuffle=sh)
+    np.testing.assert_allclose(got, np.asarray(ref), rtol=1e-8, atol=1e-12)
