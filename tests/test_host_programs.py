@@ -334,3 +334,50 @@ def test_rm_anova_decomposition_shapes(s, la, lb, c):
     else:
         ref = oracle.rm_ancova_two(d, fa, fb, subj, dmy_covariates=cov, rand_array=ra, shuffle=sh)
     np.testing.assert_allclose(got, np.asarray(ref), rtol=1e-8, atol=1e-12)
+
+
+@pytest.mark.parametrize("sizes", [(5, 5, 5), (4, 6, 5)])
+def test_rm_permutations_exchange_blocks(sizes):
+    """rand_blocks semantics inside the RM-ANCOVA loop: blocks shuffled only
+    when of equal size, rows permuted within every block, then the long-row
+    shuffle drawn from the same stream."""
+    labels = np.concatenate([np.full(z, "b%d" % i) for i, z in enumerate(sizes)])
+    n = labels.shape[0]
+    s = 2
+    ras, cums = randomise.rm_permutations(n, n * s, 0, 4, 3, block_list=labels)
+    equal = len(set(sizes)) == 1
+    c = np.arange(n * s)
+    for i in range(4):
+        rng = np.random.RandomState(3 + i)
+        uniq = np.unique(labels)
+        order = rng.permutation(list(uniq)) if equal else uniq
+        idx = np.arange(n)
+        want = np.concatenate([rng.permutation(idx[labels == b]) for b in order])
+        c = c[rng.permutation(n * s)]
+        np.testing.assert_array_equal(ras[i], want)
+        np.testing.assert_array_equal(cums[i], c)
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_cosinor_closed_forms_random(seed):
+    """The epilogue's trigonometry-free amplitude / acrophase t equal the
+    reference's arctan / sin / cos error propagation on random fits (both
+    coefficient signs, two periods)."""
+    rng = np.random.default_rng(seed)
+    n, V = 50, 40
+    tv = rng.uniform(0, 48, n)
+    y = rng.standard_normal((n, V)) + rng.choice([-1.0, 1.0], V) * np.cos(2 * np.pi * (tv[:, None] - 7) / 24)
+    perm = rng.permutation(n)
+    X = oracle.cosinor_design(tv, [24.0, 12.0])[perm]
+    inv = np.linalg.inv(X.T @ X)
+    b = inv @ X.T @ y
+    sigma = np.sqrt(np.sum((y - X @ b) ** 2, 0) / (n - X.shape[1]))
+    res = oracle.glm_cosinor(y.astype(np.float32), tv, rand_array=perm, period=[24.0, 12.0], calc_MESOR=False)
+    for i in range(2):
+        c_, s_ = 1 + 2 * i, 2 + 2 * i
+        a2 = b[c_] ** 2 + b[s_] ** 2
+        cr = 2 * inv[c_, s_] * np.abs(b[c_] * b[s_])
+        t_amp = a2 / (sigma * np.sqrt(inv[c_, c_] * b[c_] ** 2 - cr + inv[s_, s_] * b[s_] ** 2))
+        t_acro = a2 / (sigma * np.sqrt(inv[c_, c_] * b[s_] ** 2 + cr + inv[s_, s_] * b[c_] ** 2))
+        np.testing.assert_allclose(t_amp, res[9][i], rtol=1e-6)
+        np.testing.assert_allclose(t_acro, res[10][i], rtol=1e-6)
