@@ -122,6 +122,10 @@ int tfce_sweep_batch(tfce_adjset* h, const float* stats, int64_t map_stride, int
  * TFCE_EINVAL (entry outside its segment), TFCE_ETIMEOUT (iteration limit),
  * TFCE_ERANGE (threshold table overflow). */
 int tfce_sweep_status(tfce_adjset* h, void* stream);
+/* Sweep items the batched sweep runs at once on the handle's device: its
+ * persistent grid (resident CTAs per SM x SMs; TFCE_SWEEP_MAX_CTAS caps it).
+ * A launch of n items runs in ceil(n / slots) waves. */
+int tfce_sweep_resident_slots(tfce_adjset* h, int32_t* slots);
 
 /* Allocation-free form of tfce_sweep_batch.  No counterpart in the reference.
  *

@@ -52,6 +52,7 @@ SIGNATURES = {
     "tfce_sweep_batch": (ctypes.c_int, [c_vp, c_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
                                         c_vp, ctypes.c_int32, c_vp, c_vp, ctypes.c_int32, c_vp]),
     "tfce_sweep_status": (ctypes.c_int, [c_vp, c_vp]),
+    "tfce_sweep_resident_slots": (ctypes.c_int, [c_vp, c_vp]),
     "tfce_sweep_batch_noalloc": (ctypes.c_int, [c_vp, c_vp, ctypes.c_int32, ctypes.c_int64, c_vp,
                                                 ctypes.c_int32, ctypes.c_int32, c_vp, c_vp, c_vp,
                                                 ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, c_vp,

@@ -357,6 +357,12 @@ class AdjacencySet:
                                               int(signs), vdensity_ptr, int(floor_zero),
                                               out_max_ptr, out_maps_ptr, int(out_mode), stream))
 
+    def resident_slots(self):
+        """Sweep items run at once (the persistent grid's CTAs)."""
+        n = ctypes.c_int32(0)
+        _lib.check(self._lib.tfce_sweep_resident_slots(self._h, ctypes.byref(n)))
+        return int(n.value)
+
     def status(self, stream=None):
         """Synchronise and raise if a queued sweep set the device error word."""
         _lib.check(self._lib.tfce_sweep_status(self._h, stream))

@@ -4,9 +4,10 @@ Each candidate P is timed on the device (CUDA events, after a warm-up launch)
 for the GLM + sweep of one batch; the one with the highest permutations per
 second wins.  Good values fill the persistent sweep grid evenly: one launch
 has P x contrasts x signs x segments sweep items spread over the resident
-CTAs (2 per SM), so P where that count is a multiple of the CTA count avoids
-a ragged last wave.  Results are cached per (GPU, n, k, V, entries, segments,
-contrasts, signs) in ~/.cache/tfce_mediation_gb300/autotune.json.
+CTAs (tfce_sweep_resident_slots), so P where that count is a multiple of the
+CTA count avoids a ragged last wave.  Results are cached per (GPU, n, k, V,
+entries, segments, contrasts, signs, precision) in
+~/.cache/tfce_mediation_gb300/autotune.json.
 """
 from __future__ import annotations
 
@@ -47,9 +48,11 @@ def _save(d):
 def candidates(eng, max_p=256):
     """Batch sizes whose sweep items fill whole waves of the resident CTAs,
     plus the powers of two."""
-    import torch
-    sms = torch.cuda.get_device_properties(0).multi_processor_count
-    ctas = 2 * sms
+    try:
+        ctas = eng.adj.resident_slots()
+    except Exception:  # a tuning hint only: fall back to two CTAs per SM
+        import torch
+        ctas = 2 * torch.cuda.get_device_properties(0).multi_processor_count
     per_perm = eng.C * eng.signs * eng.n_seg
     out = {16, 32, 64, 128, 256}
     for waves in range(1, 64):

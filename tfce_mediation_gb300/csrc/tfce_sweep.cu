@@ -1249,6 +1249,16 @@ int tfce_debug_phase_cycles(unsigned long long* out16) {
 #endif
 
 // Error word of the last batched sweep on this handle (synchronises `stream`).
+int tfce_sweep_resident_slots(tfce_adjset* h, int32_t* slots) {
+  tfgb::clear_error();
+  TFGB_CHECK_ARG(h != nullptr && slots != nullptr, "NULL pointer");
+  std::lock_guard<std::mutex> lk(h->mu);
+  const int rc = resident_slots(h);
+  if (rc) return rc;
+  *slots = h->max_slots;
+  return TFCE_OK;
+}
+
 int tfce_sweep_status(tfce_adjset* h, void* stream) {
   tfgb::clear_error();
   TFGB_CHECK_ARG(h != nullptr, "handle is NULL");
