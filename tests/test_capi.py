@@ -59,3 +59,27 @@ def test_invalid_arguments_are_rejected_on_host():
     assert lib.tfce_sweep_batch(None, None, 0, 0, 2, None, 0, None, None, 0, None) == _lib.TFCE_EINVAL
     assert lib.glm_tstat(None, 1, 1, 1, None, None, None, None, 1, 1, None, 1, None, 1, None) == _lib.TFCE_EINVAL
     assert lib.fwer_lookup(None, 0, None, 1, 0, None, None) == _lib.TFCE_EINVAL
+
+
+def test_new_entries_reject_invalid_arguments_on_host():
+    """The tm-models, smoothing and slot-query entries validate before any
+    device work."""
+    lib = _lib.load()
+    E = _lib.TFCE_EINVAL
+    assert lib.tfce_sweep_resident_slots(None, None) == E
+    # rm_anova_combine: NULL data, then N out of range
+    assert lib.rm_anova_combine(None, 1, 2, 1, None, 1, None, 1, None, None, None, 0, None, 0, None, 0,
+                                ctypes.c_float(1.0), ctypes.c_float(1.0), None, None, None, 0, None, 1, None,
+                                None, None) == E
+    one = ctypes.c_void_p(16)  # never dereferenced: the size checks fail first
+    assert lib.rm_anova_combine(one, 1, 100000, 1, one, 1, one, 1, None, None, None, 0, None, 0, None, 0,
+                                ctypes.c_float(1.0), ctypes.c_float(1.0), None, None, None, 0, one, 1, None,
+                                one, None) == E
+    assert b"N (data rows)" in lib.tfce_last_error()
+    assert lib.gd_fwhm_weights(None, 1, ctypes.c_float(0.5), None, None) == E
+    assert lib.gd_fwhm_weights(one, 1, ctypes.c_float(-1.0), one, None) == E
+    assert lib.gd_fwhm_smooth(None, None, None, None, 0, None, 1, 1, 1, None, 1, None, None) == E
+    # glm_stat_tc: mode out of range
+    assert lib.glm_stat_tc(one, None, one, None, 16, 16, 16, 16, one, None, one, 32, one, one, 1, 5, 9, one, 1,
+                           None, 0, one, 16, one, None) == E
+    assert b"mode" in lib.tfce_last_error()
