@@ -75,6 +75,17 @@ int tfce_adjset_set_params(tfce_adjset* h, const float* H, const float* E);
 /* 1 if every entry has its reverse (the usual triangle-mesh / 26-neighbour
  * case), 0 otherwise. */
 int tfce_adjset_is_symmetric(const tfce_adjset* h);
+/* Threshold groups of tfce_sweep_batch: group [n_seg] (host; ids in
+ * [0, n_seg)), or NULL to give every segment its own table again.  Segments
+ * of one group share one threshold table per (map, sign), built from the
+ * largest maximum among them -- the sweep of tm_func.calculate_tfce
+ * (tfce_mediation/tm_func.py:68-78) over one merged adjacency of several
+ * surfaces (merge_adjacency_array, tm_func.py:521-540), whose dT is the
+ * merged image's max / 100, while each surface is still scaled by its own
+ * max / 100 (tm_func.py:84-91).  calc_mixed_tfce (tm_func.py:327-378) is one
+ * group per TFCE setting.  A grouped launch adds one segment-maximum pass
+ * over the maps. */
+int tfce_adjset_set_threshold_groups(tfce_adjset* h, const int32_t* group);
 
 /* How tfce_sweep_batch accumulates (the other entry points always use 0):
  *   0  the reference's arithmetic: every active vertex adds its float
@@ -147,12 +158,17 @@ int tfce_sweep_resident_slots(tfce_adjset* h, int32_t* slots);
  *     found larger on the device returns TFCE_EINVAL;
  *   stats, map_stride, n_maps, signs, vdensity, floor_zero, out_max: as
  *     tfce_sweep_batch (device pointers; only the maxima are written).
- * The first call on each device looks up the array's device address with
- * that device current; make that first call before any stream capture.  The
- * call returns when the sweeps have finished (it synchronises `stream`) with
- * the device status.  All calls share the one array, which keeps the last
- * call's contents (the queue and error words are cleared on entry): calls
- * that overlap on the GPU -- from two threads, or on two streams -- race. */
+ * Every call looks up the array's device address in the current context
+ * (cudaGetSymbolAddress) with the caller's device current.  The call is
+ * synchronous: it returns when the sweeps have finished (it copies the error
+ * word back and synchronises `stream`) with the device status, so it cannot
+ * be called while `stream` is being captured into a CUDA graph.  All calls
+ * share the one array, which keeps the last call's contents (the queue and
+ * error words are cleared on entry): calls that overlap on the GPU -- from
+ * two threads, or on two streams -- race.  A negative list entry, an entry
+ * outside its segment or a segment longer than max_segment_vertices makes
+ * the call return TFCE_EINVAL; the item it belongs to then reports 0 (a
+ * segment too long) or is swept without that entry. */
 int tfce_sweep_batch_noalloc(const int64_t* offsets, const int32_t* indices, int32_t n_vertices,
                              int64_t n_entries, const int64_t* seg_offsets, int32_t n_seg,
                              int32_t max_segment_vertices, const float* H, const float* E,

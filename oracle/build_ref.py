@@ -1,8 +1,9 @@
 """ORACLE build recipe -- test infrastructure, not product code.
 
 Compiles the reference's own code for the TFCE/GLM path from the sources where
-they lie in a reference checkout (default ``/root/reference``), writing only
-into ``oracle/_ref/``:
+they lie in a reference checkout, writing only into ``oracle/_ref/``.  The
+checkout is ``$TFCE_REFERENCE_ROOT`` when that is set, else a directory named
+``reference`` beside the repository's own directory:
 
 * ``oracle/_ref/libref_tfce.so`` -- ``tfce_mediation/lib/fast_tfce.hpp``
   (the reference sweep) behind the C-ABI shim ``oracle/ref_tfce_shim.cpp``;
@@ -24,11 +25,14 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-DEFAULT_REF = "/root/reference"
+REPO = os.path.dirname(HERE)
 
 
 def ref_root() -> str:
-    return os.environ.get("TFCE_REFERENCE_ROOT", DEFAULT_REF)
+    """The reference checkout: $TFCE_REFERENCE_ROOT, else ``reference`` next
+    to the repository directory (absent on machines without a checkout)."""
+    env = os.environ.get("TFCE_REFERENCE_ROOT")
+    return env if env else os.path.join(os.path.dirname(REPO), "reference")
 
 
 def build_shim(ref: str) -> str | None:

@@ -446,6 +446,130 @@ def perm_max_vertex(stat, segments, H, E, vdensity=None):
     return np.float32(best)
 
 
+def merge_adjacency(adjacency_array):
+    """tm_func.merge_adjacency_array (tm_func.py:521-540) for the common call,
+    adjacent_range = range(len(adjacency_array)): the surfaces' lists
+    concatenated, each offset by the vertex count before it.  Returns a CSR."""
+    offs, idxs, base = [np.zeros(1, np.int64)], [], 0
+    e = 0
+    for adj in adjacency_array:
+        lens = np.array([len(list(a)) for a in adj], np.int64)
+        offs.append(np.cumsum(lens) + e)
+        e += int(lens.sum())
+        idxs.append(np.concatenate([np.asarray(list(a), np.int64) for a in adj]) + base if len(adj) else
+                    np.zeros(0, np.int64))
+        base += len(adj)
+    return np.concatenate(offs), np.concatenate(idxs).astype(np.int32)
+
+
+def _full_mask(masking_array):
+    """tm_func.create_full_mask (tm_func.py:502-510): surfaces ([V,1,1]
+    masks) contribute their whole mask, volumes their in-mask voxels."""
+    parts = []
+    for m in masking_array:
+        m = np.asarray(m)
+        parts.append(m[:, 0, 0].astype(np.float64) if m.shape[2] == 1 else np.ones(int(m.sum())))
+    return np.concatenate(parts)
+
+
+def _positions(masking_array):
+    """tm_func.create_position_array (tm_func.py:556-562)."""
+    pos = [0]
+    for m in masking_array:
+        pos.append(pos[-1] + int(np.asarray(m).sum()))
+    return pos
+
+
+def _scaled(enh, tv, pos, vdensity):
+    out = np.zeros_like(enh)
+    for s in range(len(pos) - 1):
+        a, b = pos[s], pos[s + 1]
+        vd = vdensity if np.isscalar(vdensity) else np.asarray(vdensity)[a:b]
+        out[a:b] = enh[a:b] * (tv[a:b].max() / 100) * vd
+    return out
+
+
+def calculate_tfce(merge_y, masking_array, pred_x, adjacency_array, H, E, vdensity=1, perm=None):
+    """tm_func.calculate_tfce (tm_func.py:54-123), observed form: t of every
+    non-intercept column (tval_int precision), each contrast scattered into the
+    zero-filled merged image of all surfaces and swept once over the merged
+    adjacency (one threshold table: dT = the merged image's max / 100, Q6),
+    then every surface scaled by its own max / 100 and vdensity.
+    perm: row permutation of the design (the randomised call's X[perm]).
+    Returns (tvals, tfce_tvals, neg_tfce_tvals) float32 [C][V_masked]."""
+    merge_y = np.asarray(merge_y)
+    n = merge_y.shape[0]
+    X = np.column_stack([np.ones(n), pred_x])
+    if perm is not None:
+        X = X[perm]
+    k = X.shape[1]
+    tv = tval_int_ref(X, np.linalg.inv(X.T @ X), merge_y, n, k)[1:].astype(np.float32)
+    off, idx = merge_adjacency(adjacency_array)
+    full = _full_mask(masking_array) == 1
+    pos = _positions(masking_array)
+    tp, tn = np.zeros_like(tv), np.zeros_like(tv)
+    for c in range(tv.shape[0]):
+        img = np.zeros(full.shape[0], np.float32)
+        img[full] = tv[c]
+        ep = tfce(off, idx, img, H, E)[full]
+        en = tfce(off, idx, img * -1, H, E)[full]
+        tp[c] = _scaled(ep, img[full], pos, vdensity)
+        tn[c] = _scaled(en, (img * -1)[full], pos, vdensity)
+    return tv, tp, tn
+
+
+def surface_maxima(tfce_maps, position_array):
+    """np.nanmax of a scaled map over each surface: the value the randomised
+    call appends to perm_maxTFCE_surf<s>_* (tm_func.py:93-97)."""
+    return np.array([np.nanmax(tfce_maps[..., a:b], axis=-1)
+                     for a, b in zip(position_array[:-1], position_array[1:])]).T
+
+
+def calc_mixed_tfce(assign, merge_y, masking_array, adjacency_array, settings, pred_x, vdensity=1, perm=None):
+    """tm_func.calc_mixed_tfce (tm_func.py:327-378), observed form: the
+    surfaces of each TFCE setting i (assign == i) are one calculate_tfce over
+    their own merged adjacency with settings[i] = (H, E).  Returns the
+    per-group (tvals, tfce, neg_tfce) placed in the full column range, plus
+    the per-surface maxima of both signs [C][n_surf]."""
+    assign = np.asarray(assign)
+    pos = _positions(masking_array)
+    merge_y = np.asarray(merge_y)
+    C = np.asarray(pred_x).reshape(merge_y.shape[0], -1).shape[1]
+    tv_all = np.zeros((C, merge_y.shape[1]), np.float32)
+    tp_all, tn_all = np.zeros_like(tv_all), np.zeros_like(tv_all)
+    for g in np.unique(assign):
+        surf = np.flatnonzero(assign == g)
+        cols = np.concatenate([np.arange(pos[s], pos[s + 1]) for s in surf])
+        vd = vdensity if np.isscalar(vdensity) else np.asarray(vdensity)[cols]
+        H, E = settings[int(g)]
+        tv, tp, tn = calculate_tfce(merge_y[:, cols], [masking_array[s] for s in surf], pred_x,
+                                    [adjacency_array[s] for s in surf], H, E, vd, perm=perm)
+        tv_all[:, cols], tp_all[:, cols], tn_all[:, cols] = tv, tp, tn
+    return tv_all, tp_all, tn_all
+
+
+def calculate_mediation_tfce(medtype, merge_y, masking_array, pred_x, depend_y, adjacency_array, H, E,
+                             vdensity=1, perm=None):
+    """tm_func.calculate_mediation_tfce (tm_func.py:207-249), observed form:
+    the Aroian z map (calc_sobelz) swept once over the merged adjacency and
+    scaled per surface.  perm permutes pred_x (and depend_y for 'Y'), as the
+    randomised call does.  Returns (SobelZ, tfce_SobelZ) float32."""
+    merge_y = np.asarray(merge_y)
+    n = merge_y.shape[0]
+    x, dy = np.asarray(pred_x), np.asarray(depend_y)
+    if perm is not None:
+        x = x[perm]
+        if medtype == "Y":
+            dy = dy[perm]
+    z = calc_sobelz(medtype, x, dy, merge_y, n).astype(np.float32)
+    off, idx = merge_adjacency(adjacency_array)
+    full = _full_mask(masking_array) == 1
+    img = np.zeros(full.shape[0], np.float32)
+    img[full] = z
+    e = tfce(off, idx, img, H, E)[full]
+    return z, _scaled(e, img[full], _positions(masking_array), vdensity)
+
+
 def fwep_vertex(tfce_values, null):
     """1-p(FWER) as tfce_mediation/tmanalysis/calculate_fweP_vertex.py:37-69:
     sorted null, p_array[j] = j/N, idx = searchsorted(left),

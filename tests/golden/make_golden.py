@@ -1,7 +1,8 @@
 """Generate the golden vectors in tests/golden/ by running the reference itself.
 
-Run in a container that holds a reference checkout (default /root/reference,
-override with TFCE_REFERENCE_ROOT) after ``python oracle/build_ref.py``:
+Run on a machine that holds a reference checkout (``$TFCE_REFERENCE_ROOT``,
+else ``reference`` beside the repository directory) after
+``python oracle/build_ref.py``:
 
     python tests/golden/make_golden.py
 
@@ -24,8 +25,10 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("TFCE_REFERENCE_ROOT", "/root/reference")
 sys.path.insert(0, ROOT)
+from oracle.build_ref import ref_root  # noqa: E402
+
+REF = ref_root()
 
 
 def _stub(name):
@@ -71,6 +74,13 @@ class _OldNumpyArray(types.ModuleType):
 
     def __getattr__(self, name):
         return getattr(np, name)
+
+    @staticmethod
+    def argwhere(a):
+        # int() of a one-element array row (tm_func.calc_mixed_tfce) worked on
+        # older numpy; rows of a 1-D argument come back as plain indices
+        r = np.argwhere(a)
+        return r.ravel() if np.ndim(a) == 1 else r
 
     @staticmethod
     def array(obj, *a, **k):
@@ -415,6 +425,113 @@ def main():
         img = (rg.standard_normal(len(vg)) * 2.0 + 1.0).astype(np.float32)
         out[f"gd_data{k}"], out[f"gd_sigma{k}"] = img, np.float64(sg)
         out[f"gd_out{k}"] = cyn.calc_gd_fwhm(np.ascontiguousarray(pairs), np.ascontiguousarray(dist), img.copy(), sg)
+
+    # in-memory multisurface (mmr) bodies of tm_func: calculate_tfce (one sweep
+    # over the merged adjacency of all surfaces, each surface scaled by its own
+    # max), calc_mixed_tfce (one merged sweep per TFCE setting) and
+    # calculate_mediation_tfce, observed and randomised.  Three surfaces: an
+    # icosphere-3 mesh (full mask), an icosphere-2 mesh with masked-out
+    # vertices and a small voxel volume (26-neighbour mmr lists).  The
+    # randomised calls seed from the clock (tm_func.py:57); the module's
+    # `time` is replaced by a constant so the seeds, and the CSV lines they
+    # give, are reproducible.
+    if "tm_func" in R:
+        tmf = R["tm_func"]
+        rm = np.random.default_rng(81)
+        va, fa = synth.icosphere(3)
+        vb, fb = synth.icosphere(2)
+        oa, ia = A.mesh_csr(fa, va.shape[0])
+        ob, ib = A.mesh_csr(fb, vb.shape[0])
+        vol = np.zeros((7, 6, 5), bool)
+        vol[1:6, 1:5, 1:4] = True
+        vol[0, 0, 0] = True
+        vol[3, 3, 4] = True
+        adj_vol = A.create_adjac_voxel_mmr(vol, 26)
+        mask_b = np.ones(vb.shape[0], bool)
+        mask_b[rm.choice(vb.shape[0], 30, replace=False)] = False
+        masks = np.empty(3, dtype=object)
+        masks[0] = np.ones((va.shape[0], 1, 1), bool)
+        masks[1] = mask_b[:, None, None]
+        masks[2] = vol
+        def obj_lists(lists):  # adjacency sets as the TMI reader returns them: object arrays of lists
+            o = np.empty(len(lists), dtype=object)
+            for i_, a_ in enumerate(lists):
+                o[i_] = list(a_)
+            return o
+
+        adjs = np.empty(3, dtype=object)
+        adjs[0] = obj_lists(A.from_csr(oa, ia))
+        adjs[1] = obj_lists(A.from_csr(ob, ib))
+        adjs[2] = obj_lists([sorted(a) for a in adj_vol])
+        nm = 36
+        Sa, Sb = synth.smoothing_matrix(oa, ia), synth.smoothing_matrix(ob, ib)
+        ya = rm.standard_normal((va.shape[0], nm)).astype(np.float32)
+        yb = rm.standard_normal((vb.shape[0], nm)).astype(np.float32)
+        for _ in range(3):
+            ya, yb = (Sa @ ya).astype(np.float32), (Sb @ yb).astype(np.float32)
+        yv = rm.standard_normal((int(vol.sum()), nm)).astype(np.float32)
+        xm = np.column_stack([np.repeat([0.0, 1.0], nm // 2), rm.standard_normal(nm)])
+        ym = np.concatenate([ya, yb[mask_b], yv]).T.astype(np.float32)
+        ym[:, :120] += (0.9 * xm[:, 0])[:, None].astype(np.float32)
+        ym[:, 650:690] -= (0.7 * xm[:, 1])[:, None].astype(np.float32)
+        pos = tmf.create_position_array(masks)
+        full = tmf.create_full_mask(masks)
+        vd = []
+        for i in range(3):
+            deg = np.array([len(a) for a in adjs[i]], np.float64)
+            if masks[i].shape[2] == 1:
+                deg = deg[masks[i][:, 0, 0]]
+            vd = np.hstack((vd, np.array(1 - deg / deg.max() + deg.mean() / deg.max(), np.float32)))
+        out["mmr_y"], out["mmr_x"], out["mmr_pos"], out["mmr_full"], out["mmr_vd"] = ym, xm, np.array(pos), full, vd
+        out["mmr_mask_b"], out["mmr_vol"] = mask_b, vol
+        out["mmr_adj_vol_off"], out["mmr_adj_vol_idx"] = A.to_csr(adjs[2])
+        op = tfce.CreateAdjSet(2.0, 1.0, tmf.merge_adjacency_array(range(3), adjs))
+        permm = np.random.RandomState(83).permutation(nm)
+        out["mmr_perm"] = permm
+        for tag, vdx, px in (("obs", 1, xm), ("vd", vd, xm), ("perm", 1, xm[permm])):
+            tv, tp, tn = tmf.calculate_tfce(ym, masks, px, op, vdx, pos, full)
+            out[f"mmr_calc_t_{tag}"], out[f"mmr_calc_pos_{tag}"], out[f"mmr_calc_neg_{tag}"] = tv, tp, tn
+        tmf.np = _OldNumpyArray()
+        assign = np.array([0, 0, 1])
+        settings = [(2.0, 1.0), (2.0, 0.5)]
+        ops = []
+        for i in range(2):
+            sel = assign == i
+            ops.append(tfce.CreateAdjSet(settings[i][0], settings[i][1],
+                                         tmf.merge_adjacency_array(np.arange(3)[sel], adjs[sel])))
+        out["mmr_mixed_assign"], out["mmr_mixed_settings"] = assign, np.array(settings)
+        res = tmf.calc_mixed_tfce(assign, ym, masks, pos, 1, xm, ops)
+        out["mmr_mixed_obs"] = np.asarray(res[2])  # the reference returns one array three times
+        xb, dyb = xm[:, 0], (0.5 * xm[:, 0] + rm.standard_normal(nm))
+        out["mmr_med_x"], out["mmr_med_dy"] = xb, dyb
+        with np.errstate(all="ignore"):
+            z, tz = tmf.calculate_mediation_tfce("M", ym, masks, xb, dyb, op, 1, pos, full)
+        out["mmr_med_z"], out["mmr_med_tfce"] = z, tz
+        tmf.time = lambda: 1700000000.25  # str(...)[-6:] = '000.25' -> seed = perm_number + 25
+        out["mmr_time_seed_offset"] = np.int64(25)
+        with tempfile.TemporaryDirectory() as td:
+            cwd = os.getcwd()
+            os.chdir(td)
+            try:
+                for pn in (0, 1):
+                    tmf.calculate_tfce(ym, masks, xm, op, 1, pos, full, perm_number=pn, randomise=True)
+                for s_ in range(3):
+                    for c in (1, 2):
+                        out[f"mmr_csv_calc_s{s_}_c{c}"] = np.array(open(f"perm_maxTFCE_surf{s_}_tcon{c}.csv").read())
+                        os.remove(f"perm_maxTFCE_surf{s_}_tcon{c}.csv")
+                for pn in (0, 1):
+                    tmf.calc_mixed_tfce(assign, ym, masks, pos, 1, xm, ops, perm_number=pn, randomise=True)
+                for s_ in range(3):
+                    for c in (1, 2):
+                        out[f"mmr_csv_mixed_s{s_}_c{c}"] = np.array(open(f"perm_maxTFCE_surf{s_}_tcon{c}.csv").read())
+                with np.errstate(all="ignore"):
+                    for pn in (0, 1):
+                        tmf.calculate_mediation_tfce("M", ym, masks, xb, dyb, op, 1, pos, full, perm_number=pn,
+                                                     randomise=True)
+                for s_ in range(3):
+                    out[f"mmr_csv_med_s{s_}"] = np.array(open(f"perm_maxTFCE_surf{s_}_M_zstat.csv").read())
+            finally:
+                os.chdir(cwd)
 
     path = os.path.join(HERE, "reference_vectors.npz")
     np.savez_compressed(path, **out)

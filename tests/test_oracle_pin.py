@@ -314,3 +314,93 @@ def test_glm_cosinor_two_exog(golden, tag):
             assert val is None, name
             continue
         np.testing.assert_allclose(val, golden[key], rtol=1e-9, atol=1e-12, err_msg=name)
+
+
+# --- in-memory multisurface bodies (tm_func.calculate_tfce & co.) ----------
+def _mmr():
+    from tests.mmr_case import mmr_case
+    return mmr_case
+
+
+@pytest.mark.parametrize("tag", ["obs", "vd", "perm"])
+def test_mmr_calculate_tfce(golden, tag):
+    case = _mmr()(golden)
+    vd = case["vd"] if tag == "vd" else 1
+    perm = case["perm"] if tag == "perm" else None
+    tv, tp, tn = oracle.calculate_tfce(case["y"], case["masks"], case["x"], case["adjs"], 2.0, 1.0, vd, perm=perm)
+    np.testing.assert_allclose(tv, golden[f"mmr_calc_t_{tag}"], rtol=1e-6, atol=1e-6)
+    # the same float32 t -> the sweep and scaling are the reference's arithmetic
+    t_ref = golden[f"mmr_calc_t_{tag}"]
+    np.testing.assert_array_equal(tv, t_ref)
+    np.testing.assert_array_equal(tp, golden[f"mmr_calc_pos_{tag}"])
+    np.testing.assert_array_equal(tn, golden[f"mmr_calc_neg_{tag}"])
+
+
+def test_mmr_global_thresholds_differ_from_per_surface(golden):
+    """One merged sweep (global dT) differs from sweeping each surface on its
+    own, so the restatement must not be the per-surface one."""
+    case = _mmr()(golden)
+    _, tp, _ = oracle.calculate_tfce(case["y"], case["masks"], case["x"], case["adjs"], 2.0, 1.0, 1)
+    pos = case["pos"]
+    # surface 1 swept alone on its induced lists
+    off, idx = A.induced_csr(A.to_csr(list(case["adjs"][1])), case["masks"][1][:, 0, 0])
+    t1 = oracle.calculate_tfce(case["y"], case["masks"], case["x"], case["adjs"], 2.0, 1.0, 1)[0][0, pos[1]:pos[2]]
+    alone = oracle.tfce(off, idx, t1, 2.0, 1.0) * (t1.max() / np.float32(100))
+    assert not np.array_equal(alone, tp[0, pos[1]:pos[2]])
+
+
+def test_mmr_calc_mixed_tfce(golden):
+    case = _mmr()(golden)
+    settings = [tuple(s) for s in golden["mmr_mixed_settings"]]
+    _, _, tn = oracle.calc_mixed_tfce(golden["mmr_mixed_assign"], case["y"], case["masks"], case["adjs"], settings,
+                                      case["x"], 1)
+    # the reference hands back one array three times, holding the negative maps
+    np.testing.assert_array_equal(tn.astype(np.float64), golden["mmr_mixed_obs"])
+
+
+def test_mmr_calculate_mediation_tfce(golden):
+    case = _mmr()(golden)
+    z, tz = oracle.calculate_mediation_tfce("M", case["y"], case["masks"], golden["mmr_med_x"], golden["mmr_med_dy"],
+                                            case["adjs"], 2.0, 1.0, 1)
+    np.testing.assert_allclose(z, golden["mmr_med_z"], rtol=2e-6, atol=2e-6)
+    np.testing.assert_allclose(tz, golden["mmr_med_tfce"], rtol=2e-5, atol=1e-6)
+
+
+def _replayed_perm(n, pn, offset):
+    np.random.seed(pn + offset)
+    return np.random.permutation(list(range(n)))
+
+
+def test_mmr_randomised_csv_lines(golden):
+    """The randomised calls (clock seed replaced by a constant): per surface
+    and contrast, + then - maxima of every permutation, '%f'."""
+    from tests.mmr_case import csv_values
+    case = _mmr()(golden)
+    off = int(golden["mmr_time_seed_offset"])
+    n = case["y"].shape[0]
+    got = {(s, c): [] for s in range(3) for c in (1, 2)}
+    mixed = {(s, c): [] for s in range(3) for c in (1, 2)}
+    settings = [tuple(s) for s in golden["mmr_mixed_settings"]]
+    for pn in (0, 1):
+        perm = _replayed_perm(n, pn, off)
+        _, tp, tn = oracle.calculate_tfce(case["y"], case["masks"], case["x"], case["adjs"], 2.0, 1.0, 1, perm=perm)
+        mp, mn = oracle.surface_maxima(tp, case["pos"]), oracle.surface_maxima(tn, case["pos"])
+        _, tp2, tn2 = oracle.calc_mixed_tfce(golden["mmr_mixed_assign"], case["y"], case["masks"], case["adjs"],
+                                             settings, case["x"], 1, perm=perm)
+        mp2, mn2 = oracle.surface_maxima(tp2, case["pos"]), oracle.surface_maxima(tn2, case["pos"])
+        for s in range(3):
+            for c in (1, 2):
+                got[(s, c)] += ["%f" % mp[c - 1, s], "%f" % mn[c - 1, s]]
+                mixed[(s, c)] += ["%f" % mp2[c - 1, s], "%f" % mn2[c - 1, s]]
+    for s in range(3):
+        for c in (1, 2):
+            assert got[(s, c)] == str(golden[f"mmr_csv_calc_s{s}_c{c}"]).split(), (s, c)
+            assert mixed[(s, c)] == str(golden[f"mmr_csv_mixed_s{s}_c{c}"]).split(), (s, c)
+    for s in range(3):
+        vals = []
+        for pn in (0, 1):
+            perm = _replayed_perm(n, pn, off)
+            _, tz = oracle.calculate_mediation_tfce("M", case["y"], case["masks"], golden["mmr_med_x"],
+                                                    golden["mmr_med_dy"], case["adjs"], 2.0, 1.0, 1, perm=perm)
+            vals.append(oracle.surface_maxima(tz, case["pos"])[s])
+        np.testing.assert_allclose(vals, csv_values(golden[f"mmr_csv_med_s{s}"]), rtol=2e-5, atol=2e-6)

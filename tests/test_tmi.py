@@ -11,7 +11,9 @@ import pytest
 
 from tfce_mediation_gb300 import tmi
 
-REF = os.environ.get("TFCE_REFERENCE_ROOT", "/root/reference")
+from oracle.build_ref import ref_root
+
+REF = ref_root()
 
 
 def _sample(rng):

@@ -102,3 +102,71 @@ def test_noalloc_refuses_segments_beyond_scratch():
     rc = lib.tfce_sweep_batch_noalloc(1, 1, 10, 0, 1, 1, 3_000_000, 1, 1, 1, 10, 1, 2, None, 0, 1, None)
     assert rc == _lib.TFCE_ERANGE
     assert b"static scratch" in lib.tfce_last_error()
+
+
+def _two_segment_case():
+    v, f = synth.icosphere(3)
+    o1, i1 = A.mesh_csr(f, v.shape[0])
+    off, idx, seg = A.concat_csr([(o1, i1), (o1, i1)])
+    V, D = off.shape[0] - 1, int(off[-1])
+    H = np.array([2.0, 2.0], np.float32)
+    E = np.array([1.0, 1.0], np.float32)
+    stats = _maps(off, idx, V, 4, 21)
+    return off, idx, seg, V, D, H, E, stats
+
+
+def test_noalloc_rejects_a_segment_longer_than_declared():
+    """max_segment_vertices below a segment's real length: the call returns
+    TFCE_EINVAL and the items of that segment report 0; the kernel skips
+    them without touching the workspace beyond the declared size."""
+    import torch
+    off, idx, seg, V, D, H, E, stats = _two_segment_case()
+    seg = np.array([0, 100, V], np.int64)  # segment 1 is longer than declared
+    lib = _lib.load()
+    out = torch.full((4, 2, 2), float("nan"), device="cuda")
+    # segment 0 = vertices [0, 100) of the first mesh: drop the entries that
+    # cross between [0, 100) and the rest, then rebuild the CSR
+    rows = np.repeat(np.arange(V), np.diff(off))
+    ok = (rows < 100) == (idx < 100)
+    o2 = np.zeros(V + 1, np.int64)
+    np.add.at(o2, rows[ok] + 1, 1)
+    o2 = np.cumsum(o2)
+    i2 = idx[ok].astype(np.int32)
+    dev = {k: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+           for k, a in (("off", o2), ("idx", i2), ("seg", seg), ("H", H), ("E", E))}
+    rc = lib.tfce_sweep_batch_noalloc(dev["off"].data_ptr(), dev["idx"].data_ptr(), V, int(o2[-1]),
+                                      dev["seg"].data_ptr(), 2, 200, dev["H"].data_ptr(), dev["E"].data_ptr(),
+                                      torch.from_numpy(stats).cuda().data_ptr(), V, 4, 2, None, 1,
+                                      out.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    assert rc == _lib.TFCE_EINVAL
+    got = out.cpu().numpy()
+    assert (got[:, :, 1] == 0).all()
+    ref = _reference_path(torch, o2, i2, seg, H, E, stats, 2)
+    np.testing.assert_array_equal(got[:, :, 0], ref[:, :, 0])
+
+
+def test_noalloc_rejects_entries_outside_their_segment():
+    """A negative list entry and an entry pointing into the other segment:
+    TFCE_EINVAL, the entries are skipped (never read through), and the items
+    of the segment without bad entries still equal the allocating sweep."""
+    import torch
+    off, idx, seg, V, D, H, E, stats = _two_segment_case()
+    bad = idx.copy()
+    Vh = V // 2
+    e_neg = int(off[Vh + 3])          # first entry of vertex Vh+3 (segment 1)
+    e_cross = int(off[Vh + 10]) + 1   # second entry of vertex Vh+10 (segment 1)
+    bad[e_neg] = np.int32(-2147483643)  # bit 31 set; masked it would read as vertex 5
+    bad[e_cross] = 7                    # a vertex of segment 0
+    dev = {k: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+           for k, a in (("off", off), ("idx", bad), ("seg", seg), ("H", H), ("E", E))}
+    lib = _lib.load()
+    for _ in range(2):
+        out = torch.full((4, 2, 2), float("nan"), device="cuda")
+        rc = lib.tfce_sweep_batch_noalloc(dev["off"].data_ptr(), dev["idx"].data_ptr(), V, D,
+                                          dev["seg"].data_ptr(), 2, int(np.diff(seg).max()), dev["H"].data_ptr(),
+                                          dev["E"].data_ptr(), torch.from_numpy(stats).cuda().data_ptr(), V, 4, 2,
+                                          None, 1, out.data_ptr(), torch.cuda.current_stream().cuda_stream)
+        assert rc == _lib.TFCE_EINVAL
+        assert b"outside" in lib.tfce_last_error()
+        ref = _reference_path(torch, off, idx, seg, H, E, stats, 2)
+        np.testing.assert_array_equal(out.cpu().numpy()[:, :, 0], ref[:, :, 0])

@@ -301,6 +301,7 @@ class AdjacencySet:
             _lib.ptr(segments, _lib.c_i64p), n_seg, _lib.ptr(Hs, _lib.c_f32p),
             _lib.ptr(Es, _lib.c_f32p), ctypes.byref(h)))
         self._h = h
+        self.csr = (off, idx)  # host copy: the in-memory multisurface bodies re-cut it into segments
         self.n_vertices = V
         self.n_entries = int(off[-1])
         self.segments = segments
@@ -322,6 +323,20 @@ class AdjacencySet:
         _lib.check(self._lib.tfce_adjset_set_params(self._h, _lib.ptr(Hs, _lib.c_f32p),
                                                     _lib.ptr(Es, _lib.c_f32p)))
         self.H, self.E = Hs.copy(), Es.copy()
+
+    def set_threshold_groups(self, groups):
+        """Segments sharing a group id share one threshold table per map and
+        sign, built from the largest of their maxima (one merged adjacency
+        over several surfaces, tm_func.py:68-91); None: one table per segment."""
+        if groups is None:
+            _lib.check(self._lib.tfce_adjset_set_threshold_groups(self._h, None))
+            self.threshold_groups = None
+            return
+        g = np.ascontiguousarray(np.asarray(groups, np.int32))
+        if g.shape != (self.n_seg,):
+            raise ValueError(f"threshold groups: {self.n_seg} ids expected, got shape {g.shape}")
+        _lib.check(self._lib.tfce_adjset_set_threshold_groups(self._h, _lib.ptr(g, _lib.c_i32p)))
+        self.threshold_groups = g.copy()
 
     def set_accumulation(self, mode: str):
         """'exact' (the reference's float arithmetic, bit-identical) or

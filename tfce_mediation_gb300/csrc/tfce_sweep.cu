@@ -127,6 +127,14 @@ struct SweepArgs {
   int64_t n_entries;
   // words of the shared-memory activity bitmap (dynamic shared memory), 0 = none
   int32_t bm_words;
+  // Threshold groups (nullable): segments with the same thr_group[seg] share
+  // one threshold table, built from the largest of their maxima -- the sweep
+  // of one merged adjacency over several surfaces (tm_func.py:68-78), whose
+  // dT is the merged image's max / 100.  seg_max [n_maps][n_signs][n_seg]
+  // holds every segment's maximum (segment_max_kernel); the scale stays each
+  // segment's own max / 100 (tm_func.py:84-91).
+  const int32_t* thr_group;
+  const float* seg_max;
 };
 
 // Per-component mode: the increments so far (root) or the potential to the
@@ -375,10 +383,19 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
     mx = block_max(mx, sRed);
     if (a.floor_zero) mx = fmaxf(mx, 0.0f);
     if (tid == 0) {
+      // the threshold table's maximum: this segment's, or its group's
+      float tmx = mx;
+      if (a.thr_group) {
+        const int32_t g = a.thr_group[seg];
+        const float* gm = a.seg_max + (int64_t)ms * a.n_seg;
+        tmx = -INFINITY;
+        for (int32_t s2 = 0; s2 < a.n_seg; ++s2)
+          if (a.thr_group[s2] == g) tmx = fmaxf(tmx, gm[s2]);
+      }
       int L = 0;
-      if (mx > 0.0f && isfinite(mx)) {
-        const float dT = __fdiv_rn(mx, 100.0f);
-        float T = mx;
+      if (tmx > 0.0f && isfinite(tmx)) {
+        const float dT = __fdiv_rn(tmx, 100.0f);
+        float T = tmx;
         while (T >= 0.0f) {
           if (L >= kMaxSteps) {
             set_err(a.err, kDevTooManySteps);
@@ -522,7 +539,8 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
             an[k] = static_cast<int32_t>(ag);
             ka[k] = kInactiveKey;
             if (eb + k < e1) {
-              if (ag < 0 || ag >= Vs) set_err(a.err, kDevBadIndex);
+              // a caller's negative int32 entry has bit 31 set: rejected, not masked
+              if (ag < 0 || ag >= Vs || (kChecked && (raw[k] & kOneWay))) set_err(a.err, kDevBadIndex);
               else if (!use_bm || ((sAct[an[k] >> 5] >> (an[k] & 31)) & 1u)) ka[k] = sl.key[an[k]];
             }
           }
@@ -841,6 +859,44 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
   }
 }
 
+// Maximum of +x and of -x over every (map, segment), finite values only:
+// seg_max[(map * signs + sign) * n_seg + seg].  One block per (map, segment).
+__global__ void __launch_bounds__(256) segment_max_kernel(const float* __restrict__ stats, int64_t map_stride,
+                                                          int32_t signs, const int64_t* __restrict__ seg_off,
+                                                          int32_t n_seg, float* __restrict__ seg_max) {
+  __shared__ float red[2][8];
+  const int64_t b = blockIdx.x;
+  const int32_t seg = static_cast<int32_t>(b % n_seg);
+  const int64_t map = b / n_seg;
+  const float* x = stats + map * map_stride;
+  float mp = -INFINITY, mn = -INFINITY;
+  for (int64_t v = seg_off[seg] + threadIdx.x; v < seg_off[seg + 1]; v += blockDim.x) {
+    const float xv = x[v];
+    if (isfinite(xv)) {
+      mp = fmaxf(mp, xv);
+      mn = fmaxf(mn, -xv);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mp = fmaxf(mp, __shfl_xor_sync(0xffffffffu, mp, o));
+    mn = fmaxf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    red[0][w] = mp;
+    red[1][w] = mn;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 1; i < (int)(blockDim.x >> 5); ++i) {
+      mp = fmaxf(mp, red[0][i]);
+      mn = fmaxf(mn, red[1][i]);
+    }
+    seg_max[(map * signs) * n_seg + seg] = mp;
+    if (signs == 2) seg_max[(map * signs + 1) * n_seg + seg] = mn;
+  }
+}
+
 }  // namespace tfgb
 
 // ---------------------------------------------------------------------------
@@ -869,6 +925,9 @@ struct tfce_adjset {
   float* d_enh = nullptr;
   int32_t run_cap = 0;
   int32_t accumulation = 0;  // 0: reference arithmetic, 1: per-component
+  int32_t* d_group = nullptr;  // threshold group of every segment, or NULL
+  float* d_segmax = nullptr;   // segment maxima of the last grouped launch
+  int64_t segmax_cap = 0;
   std::mutex mu;
 };
 
@@ -888,6 +947,8 @@ int release(tfce_adjset* h) {
   cudaFree(h->d_ws);
   cudaFree(h->d_img);
   cudaFree(h->d_enh);
+  cudaFree(h->d_group);
+  cudaFree(h->d_segmax);
   cudaSetDevice(dev);
   return TFCE_OK;
 }
@@ -962,6 +1023,23 @@ int launch_sweep(tfce_adjset* h, const float* stats, int64_t map_stride, int32_t
   a.item_order = nullptr;
   const int bm = tfgb::bitmap_bytes(h->vmax_seg);
   a.bm_words = bm / 4;
+  if (h->d_group) {
+    const int64_t need = (int64_t)n_maps * signs * h->n_seg;
+    if (h->segmax_cap < need) {
+      cudaFree(h->d_segmax);
+      h->d_segmax = nullptr;
+      h->segmax_cap = 0;
+      TFGB_CUDA(cudaMalloc(&h->d_segmax, sizeof(float) * need));
+      h->segmax_cap = need;
+    }
+    const int64_t blocks = (int64_t)n_maps * h->n_seg;
+    TFGB_CHECK_ARG(blocks < (1LL << 31), "too many segment-max blocks");
+    tfgb::segment_max_kernel<<<static_cast<unsigned>(blocks), 256, 0, st>>>(stats, map_stride, signs,
+                                                                          h->d_seg_off, h->n_seg, h->d_segmax);
+    TFGB_CUDA(cudaGetLastError());
+    a.thr_group = h->d_group;
+    a.seg_max = h->d_segmax;
+  }
   if (lazy) tfgb::tfce_sweep_kernel<false, true><<<slots, tfgb::kSweepThreads, bm, st>>>(a);
   else tfgb::tfce_sweep_kernel<false, false><<<slots, tfgb::kSweepThreads, bm, st>>>(a);
   TFGB_CUDA(cudaGetLastError());
@@ -1126,6 +1204,21 @@ int tfce_adjset_set_params(tfce_adjset* h, const float* H, const float* E) {
 
 int tfce_adjset_is_symmetric(const tfce_adjset* h) { return (h && h->symmetric) ? 1 : 0; }
 
+int tfce_adjset_set_threshold_groups(tfce_adjset* h, const int32_t* group) {
+  tfgb::clear_error();
+  TFGB_CHECK_ARG(h != nullptr, "handle is NULL");
+  std::lock_guard<std::mutex> lk(h->mu);
+  if (!group) {
+    cudaFree(h->d_group);
+    h->d_group = nullptr;
+    return TFCE_OK;
+  }
+  for (int s = 0; s < h->n_seg; ++s) TFGB_CHECK_ARG(group[s] >= 0 && group[s] < h->n_seg, "group id outside [0, n_seg)");
+  if (!h->d_group) TFGB_CUDA(cudaMalloc(&h->d_group, sizeof(int32_t) * h->n_seg));
+  TFGB_CUDA(cudaMemcpy(h->d_group, group, sizeof(int32_t) * h->n_seg, cudaMemcpyHostToDevice));
+  return TFCE_OK;
+}
+
 int tfce_adjset_set_accumulation(tfce_adjset* h, int32_t mode) {
   tfgb::clear_error();
   TFGB_CHECK_ARG(h != nullptr, "handle is NULL");
@@ -1287,12 +1380,12 @@ constexpr int64_t kNoAllocCtrlBytes = 256;              // queue counter, error 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 struct NoAllocDevice {
-  void* scratch = nullptr;  // device address of g_noalloc_scratch on that device
+  void* scratch = nullptr;  // device address of g_noalloc_scratch in the current context
   int max_slots = 0;        // resident CTAs of the checked kernel
 };
 
 std::mutex g_noalloc_mu;
-NoAllocDevice g_noalloc_dev[128];
+int g_noalloc_slots[128];  // resident CTAs per device ordinal (0 = not yet queried)
 
 // Largest segment one workspace slot of the static scratch can hold.
 int32_t noalloc_max_segment() {
@@ -1305,31 +1398,32 @@ int32_t noalloc_max_segment() {
   return static_cast<int32_t>(lo);
 }
 
-// Per-device set-up, done by the first call on each device with that device
-// current: the host-side name of the array is not a device address, so its
-// device address is looked up once with cudaGetSymbolAddress.
+// Set-up of every call, with the caller's device current: the host-side name
+// of the array is not a device address, so its device address in the current
+// context is looked up with cudaGetSymbolAddress (cheap; looked up on every
+// call, so a context re-created after cudaDeviceReset is served correctly).
+// The resident-CTA count is queried once per device ordinal.
 int noalloc_setup(int dev, NoAllocDevice* out) {
-  std::lock_guard<std::mutex> lk(g_noalloc_mu);
   if (dev < 0 || dev >= 128) {
     set_error("device ordinal %d out of range", dev);
     return TFCE_EINVAL;
   }
-  NoAllocDevice& d = g_noalloc_dev[dev];
-  if (!d.scratch) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || p == nullptr) {
-      set_error("cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
-      return TFCE_EDEVICE;
-    }
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || p == nullptr) {
+    set_error("cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
+    return TFCE_EDEVICE;
+  }
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_slots[dev]) {
     int sms = 0, per_sm = 0;
     TFGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     TFGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tfce_sweep_kernel<true, false>,
                                                             kSweepThreads, 0));
-    d.max_slots = std::max(1, sms * std::max(1, per_sm));
-    d.scratch = p;
+    g_noalloc_slots[dev] = std::max(1, sms * std::max(1, per_sm));
   }
-  *out = d;
+  out->scratch = p;
+  out->max_slots = g_noalloc_slots[dev];
   return TFCE_OK;
 }
 

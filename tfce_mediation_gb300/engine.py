@@ -66,6 +66,14 @@ class PermutationEngine:
     tensor cores, split BF16 with FP32 accumulation, t within ~3e-5 relative
     of FP64) or 'fp32' (CUDA cores, ~1e-6).  The observed (unpermuted) t map
     always uses 'fp32'.
+    threshold_groups: one group id per segment, or None.  Segments of one
+    group share one threshold table per map and sign, from the largest of
+    their maxima: the sweep of one merged adjacency over several surfaces
+    (tm_func.calculate_tfce, tm_func.py:54-123: dT = the merged image's
+    max / 100) or of one TFCE setting's surfaces (calc_mixed_tfce,
+    tm_func.py:327-378); each segment is still scaled by its own max / 100.
+    None: every segment its own table (the hemispheres of the vertex path,
+    the surfaces of mmr-lr).
     reorder: renumber vertices inside every segment for memory locality
     (reverse Cuthill-McKee); Y's columns are permuted once here and every map
     handed back is in the caller's order.  Only symmetric adjacency is
@@ -74,7 +82,8 @@ class PermutationEngine:
 
     def __init__(self, Y, pred_x, adjacency, segments=None, H=2.0, E=1.0, vdensity=None,
                  contrasts=None, floor_zero=False, batch=64, signs=2, reorder=False,
-                 accumulation="component", precision="bf16x3", f_groups=None, outputs=None):
+                 accumulation="component", precision="bf16x3", f_groups=None, outputs=None,
+                 threshold_groups=None):
         t = require_cuda()
         if precision not in ("bf16x3", "fp32"):
             raise ValueError("precision must be 'bf16x3' (tensor cores) or 'fp32' (CUDA cores)")
@@ -117,6 +126,8 @@ class PermutationEngine:
             raise ValueError(f"adjacency has {self.adj.n_vertices} vertices, data {self.V}")
         self.adj.set_accumulation(accumulation)
         self.n_seg = self.adj.n_seg
+        if threshold_groups is not None:
+            self.adj.set_threshold_groups(threshold_groups)
         self.contrasts = list(range(1, self.k)) if contrasts is None else list(contrasts)
         self._w_stride = 0
         if self.f_groups is not None:
@@ -462,7 +473,7 @@ class MediationEngine:
 
     def __init__(self, Y, pred_x, depend_y, medtype, adjacency, segments=None, H=2.0, E=1.0, vdensity=None,
                  floor_zero=False, batch=64, alg="aroian", accumulation="component", precision="bf16x3",
-                 covariates=None):
+                 covariates=None, threshold_groups=None):
         from .pyfunc import ALG
         if medtype not in ("I", "M", "Y"):
             raise ValueError("Invalid mediation type")
@@ -470,7 +481,8 @@ class MediationEngine:
             raise ValueError("Unknown indirect test algorithm")
         self.inner = PermutationEngine(Y, np.zeros((np.asarray(Y).shape[0], 1)), adjacency, segments, H, E,
                                        vdensity, contrasts=[1], floor_zero=floor_zero, batch=2 * batch, signs=1,
-                                       reorder=False, accumulation=accumulation, precision=precision)
+                                       reorder=False, accumulation=accumulation, precision=precision,
+                                       threshold_groups=threshold_groups)
         self.t = self.inner.t
         self.medtype, self.alg_code, self.batch = medtype, ALG[alg], int(batch)
         self.pred_x = np.asarray(pred_x, np.float64)

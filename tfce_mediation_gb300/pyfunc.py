@@ -148,18 +148,24 @@ def sobel_from_t(ta, tb, alg="aroian", ta_scalar=None):
     return z
 
 
+def sobel_z_device(medtype, pred_x, depend_y, Y, n, alg="aroian"):
+    """Indirect-effect z of the data Y (n, V) as a device tensor (1, V): the
+    path-a and path-b t maps in one GLM launch, then sobel_combine."""
+    if alg not in ALG:
+        raise ValueError("Unknown indirect test algorithm")
+    Xa, Xb, ta_scalar = mediation_designs(medtype, pred_x, depend_y, n)
+    if ta_scalar is None:
+        tab = glm_stat(Y, DesignBatch([Xa, Xb]), WHAT_T, coef=[1])[:, 0]
+        return sobel_from_t(tab[0:1], tab[1:2], alg)
+    tb = glm_stat(Y, DesignBatch([Xb]), WHAT_T, coef=[1])[:, 0]
+    return sobel_from_t(None, tb, alg, ta_scalar=[ta_scalar])
+
+
 def calc_sobelz(medtype, pred_x, depend_y, merge_y, n, num_vertex, alg="aroian"):
     """Sobel/Aroian/Goodman z per vertex (pyfunc.py:130-162), float64 host array."""
     if alg not in ALG:
         raise ValueError("Unknown indirect test algorithm")
-    Xa, Xb, ta_scalar = mediation_designs(medtype, pred_x, depend_y, n)
-    Y = np.asarray(merge_y, np.float32)
-    if ta_scalar is None:
-        tab = glm_stat(Y, DesignBatch([Xa, Xb]), WHAT_T, coef=[1])[:, 0]
-        z = sobel_from_t(tab[0:1], tab[1:2], alg)
-    else:
-        tb = glm_stat(Y, DesignBatch([Xb]), WHAT_T, coef=[1])[:, 0]
-        z = sobel_from_t(None, tb, alg, ta_scalar=[ta_scalar])
+    z = sobel_z_device(medtype, pred_x, depend_y, np.asarray(merge_y, np.float32), n, alg)
     return z[0].cpu().numpy().astype(np.float64)
 
 

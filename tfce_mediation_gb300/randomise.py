@@ -13,6 +13,12 @@ appends the same CSV lines in the same order and format:
 * voxel_mediation_run  -- tmanalysis/voxel_tfce_mediation_randomise.py:42-77
 * mmr_lr_run           -- tm_multisurface/tm_mmr_rand_low_ram_parallel.py:166-207
   (tmi_temp/<s>_*_temp.npy, <path>/perm_maxTFCE_surf<s>_tcon<c>.csv, %f)
+* mmr_run              -- tm_multisurface/tm_multimodality_multisurface_regression.py:404-640
+  (the in-memory multisurface driver: reads the TMI file; with -p the
+  permutation loop of calculate_tfce / calc_mixed_tfce / calculate_mediation_tfce,
+  many permutations per launch, output_<name>/output_[med_]stats_<name>.tmi/
+  perm_maxTFCE_surf<s>_tcon<c>.csv (or _<m>_zstat.csv), %f; without -p the
+  observed maps in stats_<name>.tmi)
 * tm_models_glm_run    -- tmanalysis/tm_models_randomise.py:76-92,193-274 (the GLM branch:
   tmtemp_GLM_<surface|volume>/, output_GLM_<..>/perm_GLM/perm_Fstat_<var>_TFCE_max*.csv
   and perm_Tstat_con<c>_TFCE_max*.csv)
@@ -317,6 +323,153 @@ def mmr_lr_run(surf_num, perm_range, seed, path, H, E_, pred_x=None, mediation=N
                             vdensity=vd, floor_zero=floor, batch=batch)
     maxima = eng.run(perms=perms)[:, 0, 0, 0]
     _append(os.path.join(path, "perm_maxTFCE_surf%d_%s_zstat.csv" % (surf_num, medtype)), ["%f" % v for v in maxima])
+    return maxima
+
+
+def mmr_parser(ap=None):
+    """The arguments of tm_multimodality_multisurface_regression.py:33-130
+    that the statistics use, plus --seed and --batch."""
+    ap = ap or argparse.ArgumentParser(description="Multimodal multisurface regression / mediation (GPU)")
+    ap.add_argument("-i_tmi", "--tmifile", nargs=1, required=True, metavar=("*.tmi",))
+    group = ap.add_mutually_exclusive_group(required=True)
+    group.add_argument("-i", "--input", nargs="+", metavar=("*.csv",))
+    group.add_argument("-im", "--inputmediation", nargs=3, metavar=("{I,M,Y}", "*.csv", "*.csv"))
+    group.add_argument("-r", "--regressors", nargs=1, metavar=("*.csv",))
+    ap.add_argument("-c", "--covariates", nargs=1, metavar=("*.csv",))
+    ap.add_argument("-p", "--randomise", nargs=2, type=int, metavar=("INT", "INT"))
+    ap.add_argument("-i_name", "--analysisname", nargs=1)
+    ap.add_argument("--tfce", nargs="+", default=[2.0, 1.0], type=float)
+    ap.add_argument("-sa", "--setadjacencyobjs", nargs="+", type=int)
+    ap.add_argument("-st", "--assigntfcesettings", nargs="+", type=int)
+    ap.add_argument("--noweight", action="store_true")
+    ap.add_argument("--subset", nargs=1)
+    ap.add_argument("--seed", nargs=1, type=int, default=None,
+                    help="host-seeded permutation stream RandomState(seed + i) (default: clock seeding)")
+    ap.add_argument("--batch", type=int, default=64)
+    return ap
+
+
+def _mmr_layout(masking_array, adjacency_array, adjacent_range, noweight):
+    """Segments of the in-memory multisurface study: per surface the lists of
+    its masked vertices (surfaces: [V,1,1] masks; volumes: the lists are over
+    the mask's voxels already), concatenated in position order, and the
+    vertex-density weights of the driver
+    (tm_multimodality_multisurface_regression.py:449-462)."""
+    parts, vd = [], []
+    for i, m in enumerate(masking_array):
+        m = np.asarray(m)
+        adj = adjacency_array[adjacent_range[i]]
+        if m.shape[2] == 1:
+            parts.append(induced_csr(list(adj), m[:, 0, 0]))
+        else:
+            parts.append(to_csr(list(adj)))
+        if not noweight:
+            deg = np.array([len(a) for a in adj], np.float64)
+            if m.shape[2] == 1:
+                deg = deg[m[:, 0, 0] == True]  # noqa: E712
+            vd.append(np.array(1 - deg / deg.max() + deg.mean() / deg.max(), np.float32))
+    off, idx, seg = concat_csr(parts)
+    return off, idx, seg, (np.concatenate(vd) if vd else None)
+
+
+def mmr_run(opts):
+    """The randomise and observed branches of the in-memory multisurface
+    driver on one GPU.  Each launch covers P permutations x contrasts x signs
+    x surfaces; with -st every TFCE setting is a threshold group with its own
+    (H, E) (calc_mixed_tfce), otherwise all surfaces share one group
+    (calculate_tfce's merged adjacency); mediation sweeps the indirect-effect z
+    (calculate_mediation_tfce).  Returns the maxima (P, C, signs, surfaces)
+    with -p, else the observed maps."""
+    from . import cynumstats
+    from .tmi import read_tm_filetype, write_tm_filetype
+    _, image_array, masking_array, maskname, affine_array, vertex_array, face_array, surfname, adjacency_array, _, _ = \
+        read_tm_filetype(opts.tmifile[0], verbose=False)
+    n_surf = len(masking_array)
+    adjacent_range = (list(opts.setadjacencyobjs) if getattr(opts, "setadjacencyobjs", None)
+                      else list(range(len(adjacency_array))))
+    if len(adjacent_range) < n_surf:
+        raise ValueError("every masking array needs an adjacency set")
+    tfce_opts = [float(v) for v in opts.tfce]
+    if getattr(opts, "assigntfcesettings", None):
+        assign = np.asarray(opts.assigntfcesettings, np.int32)
+        if assign.shape[0] != n_surf:
+            raise ValueError(f"# of masking arrays ({n_surf}) and of tfce setting assignments ({assign.shape[0]}) "
+                             f"must be equal")
+        if len(tfce_opts) % 2:
+            raise ValueError("--tfce needs H E pairs")
+        settings = np.unique(assign)
+        groups = np.searchsorted(settings, assign).astype(np.int32)
+        H = np.array([tfce_opts[2 * int(a)] for a in assign], np.float32)
+        E = np.array([tfce_opts[2 * int(a) + 1] for a in assign], np.float32)
+    else:
+        groups = np.zeros(n_surf, np.int32)
+        H = np.full(n_surf, tfce_opts[0], np.float32)
+        E = np.full(n_surf, tfce_opts[1], np.float32)
+    off, idx, seg, vd = _mmr_layout(masking_array, adjacency_array, adjacent_range, opts.noweight)
+    data = np.asarray(image_array[0])
+    sub = None
+    if getattr(opts, "subset", None):
+        sub = np.isfinite(np.genfromtxt(str(opts.subset[0]), delimiter=","))
+    medtype = None
+    if getattr(opts, "inputmediation", None):
+        medtype = opts.inputmediation[0]
+        pred_x = np.genfromtxt(opts.inputmediation[1], delimiter=",")
+        depend_y = np.genfromtxt(opts.inputmediation[2], delimiter=",")
+    elif getattr(opts, "regressors", None):
+        pred_x = np.genfromtxt(opts.regressors[0], delimiter=",")
+    else:
+        cols = [np.genfromtxt(a, delimiter=",") for a in opts.input]
+        pred_x = cols[0] if len(cols) == 1 else np.column_stack(cols)
+    if sub is not None:
+        data = data[:, sub]
+    if getattr(opts, "covariates", None) and not getattr(opts, "regressors", None):
+        covars = np.genfromtxt(opts.covariates[0], delimiter=",")
+        merge_y = cynumstats.resid_covars(np.column_stack([np.ones(len(covars)), covars]), data)
+    else:
+        merge_y = data.T
+    merge_y = np.ascontiguousarray(merge_y, np.float32)
+    n = merge_y.shape[0]
+    outname = opts.analysisname[0] if getattr(opts, "analysisname", None) else opts.tmifile[0][:-4]
+    base = "output_%s" % outname
+    os.makedirs(base, exist_ok=True)
+    tag = ("med_stats_" if medtype else "stats_") + (outname if outname.endswith("tmi") else outname + ".tmi")
+    kw = dict(vdensity=vd, threshold_groups=groups, batch=getattr(opts, "batch", 64))
+    if medtype:
+        eng = E.MediationEngine(merge_y, pred_x, depend_y, medtype, (off, idx), seg, H, E, **kw)
+    else:
+        eng = E.PermutationEngine(merge_y, pred_x, (off, idx), seg, H, E, **kw)
+    if not getattr(opts, "randomise", None):
+        if medtype:
+            z, tz, _ = eng.observed()
+            outdata = np.column_stack((z, tz))
+            names = ["SobelZ", "SobelZ_tfce"]
+        else:
+            tv, maps, _ = eng.observed()
+            C = tv.shape[0]
+            outdata = np.column_stack((tv.T, maps[:, 0].T, maps[:, 1].T))
+            names = (["tstat_con%d" % (i + 1) for i in range(C)] + ["tstat_tfce_con%d" % (i + 1) for i in range(C)]
+                     + ["negtstat_tfce_con%d" % (i + 1) for i in range(C)])
+        write_tm_filetype(os.path.join(base, tag), image_array=outdata, masking_array=masking_array,
+                          maskname=maskname, affine_array=affine_array, vertex_array=vertex_array,
+                          face_array=face_array, surfname=surfname, checkname=False, columnids=np.array(names),
+                          tmi_history=[])
+        return outdata
+    start, stop = int(opts.randomise[0]), int(opts.randomise[1]) + 1
+    seed = opts.seed[0] if getattr(opts, "seed", None) else None
+    perms = _perm_rows(n, start, stop, seed)
+    maxima = eng.run(perms=perms)  # (P, C, signs, n_surf)
+    out = os.path.join(base, "output_%s" % tag)
+    os.makedirs(out, exist_ok=True)
+    for s_ in range(n_surf):
+        if medtype:
+            _append(os.path.join(out, "perm_maxTFCE_surf%d_%s_zstat.csv" % (s_, medtype)),
+                    ["%f" % v for v in maxima[:, 0, 0, s_]])
+            continue
+        for c in range(maxima.shape[1]):
+            lines = []
+            for p in range(maxima.shape[0]):
+                lines += ["%f" % maxima[p, c, 0, s_], "%f" % maxima[p, c, 1, s_]]
+            _append(os.path.join(out, "perm_maxTFCE_surf%d_tcon%d.csv" % (s_, c + 1)), lines)
     return maxima
 
 

@@ -1,20 +1,28 @@
 """Drop-in for the multimodal multisurface (mmr) bodies of ``tfce_mediation.tm_func``.
 
-Same names, arguments, outputs and CSV files as tfce_mediation/tm_func.py;
-regressions, indirect-effect maps and TFCE sweeps run on the GPU:
+Same names, arguments, outputs and CSV files as tfce_mediation/tm_func.py.
+Every call is one GLM launch (t of all contrasts, or the path-a / path-b t of
+the indirect effect) and one sweep launch over every (contrast, sign, surface)
+of the study on the GPU; surfaces are segments of one device adjacency cut
+from the caller's merged adjacency (the masked vertices of each surface, in
+position_array order), and the threshold tables follow the reference's sweep
+of the merged image:
 
-* calculate_tfce              (tm_func.py:54-123)   one sweep over the merged
-  adjacency of all surfaces (global dT), each surface scaled by its own max
+* calculate_tfce              (tm_func.py:54-123)   one threshold table per
+  map from the max over all surfaces (the merged adjacency's global dT),
+  each surface scaled by its own max / 100
 * low_ram_calculate_tfce      (tm_func.py:144-185)  one surface
 * calculate_mediation_tfce    (tm_func.py:207-249)
 * low_ram_calculate_mediation_tfce (tm_func.py:269-305)
-* calc_mixed_tfce             (tm_func.py:327-378)  per-group H/E settings
+* calc_mixed_tfce             (tm_func.py:327-378)  one threshold group and one
+  (H, E) per TFCE setting, all settings in the same launch
 * apply_mfwer                 (tm_func.py:403-491)  study-wide FWER
 * create_full_mask, merge_adjacency_array, lowest_length,
   create_position_array, find_nearest (tm_func.py:502-573)
 
 Permutation seeding follows the reference: ``perm_number + perm_seed`` when a
-seed is given, the time-based seed otherwise.
+seed is given, the time-based seed otherwise.  The batched permutation loop
+over many permutations per launch is ``randomise.mmr_run``.
 """
 from __future__ import annotations
 
@@ -24,10 +32,12 @@ from time import time
 
 import numpy as np
 
-from . import cynumstats
+from .adjacency import AdjacencySet, concat_csr, induced_csr
 from .adjacency import merge_adjacency_array  # noqa: F401
+from .device import dev, ptr, require_cuda, stream_handle
 from .fwer import apply_mfwer as _apply_mfwer_gpu
-from .pyfunc import calc_sobelz
+from .glm import WHAT_T, DesignBatch, glm_stat
+from .pyfunc import sobel_z_device
 
 
 def _append(path, line):
@@ -42,97 +52,184 @@ def _seed(perm_number, perm_seed=None):
         np.random.seed(perm_number + int(float(str(time())[-6:]) * 100))
 
 
-def _tvals(X, y):
-    k = X.shape[1]
-    invXX = np.linalg.inv(np.dot(X.T, X))
-    return cynumstats.tval_int(X, invXX, y, y.shape[0], k, y.shape[1])
+_DATA = {}
 
 
-def _sweep(calcTFCE, img):
-    out = np.zeros_like(img)
-    calcTFCE.run(np.ascontiguousarray(img, np.float32), out)
-    return out
+def _data_dev(y):
+    """The data on the device, kept between the calls of a permutation loop
+    (the same array is passed to every call)."""
+    y = np.asarray(y)
+    key = (id(y), y.__array_interface__["data"][0], y.shape, y.dtype.str)
+    if _DATA.get("key") != key:
+        _DATA.clear()
+        _DATA["dev"] = dev(np.ascontiguousarray(y, np.float32))
+        _DATA["key"] = key
+    return _DATA["dev"]
+
+
+def _surface_lengths(masking_array):
+    """Length of every surface in the merged (zero-filled) image: the whole
+    surface for [V,1,1] masks, the in-mask voxels for volumes
+    (create_full_mask, tm_func.py:502-510)."""
+    return [int(np.asarray(m).shape[0]) if np.asarray(m).shape[2] == 1 else int(np.asarray(m).sum())
+            for m in masking_array]
+
+
+def _surface_parts(adjset, masking_array, fullmask):
+    """Per-surface CSRs (local indices) of the masked vertices, cut from the
+    merged adjacency of a CreateAdjSet; surfaces are disconnected in a merged
+    adjacency, so each cut keeps every entry."""
+    off, idx = adjset.csr
+    full = np.asarray(fullmask) == 1
+    lens = _surface_lengths(masking_array)
+    if sum(lens) != full.shape[0] or off.shape[0] - 1 != full.shape[0]:
+        raise ValueError(f"merged adjacency has {off.shape[0] - 1} vertices, the masks {sum(lens)}, "
+                         f"fullmask {full.shape[0]}")
+    parts, base = [], 0
+    for n_s in lens:
+        o = off[base:base + n_s + 1] - off[base]
+        x = idx[off[base]:off[base + n_s]].astype(np.int64) - base
+        parts.append(induced_csr((o, x), full[base:base + n_s]))
+        base += n_s
+    return parts
+
+
+class _Study:
+    """One device adjacency of a multisurface study: the surfaces as
+    segments, per-segment H/E and threshold groups, reference arithmetic."""
+
+    def __init__(self, parts, H, E, groups):
+        off, idx, seg = concat_csr(parts)
+        self.adj = AdjacencySet((off, idx), H, E, seg)
+        self.adj.set_accumulation("exact")
+        self.adj.set_threshold_groups(groups)
+        self.seg = seg
+        self.V = int(seg[-1])
+        self.n_seg = seg.shape[0] - 1
+
+    def sweep(self, maps, n_maps, signs, vdensity=1, floor_zero=False, want_maps=False):
+        """Per-surface maxima (n_maps, signs, n_seg) and, with want_maps, the
+        scaled maps (n_maps, signs, V), host float32."""
+        t = require_cuda()
+        vd = None
+        if not (np.isscalar(vdensity) and float(vdensity) == 1.0):
+            vd = dev(np.ascontiguousarray(np.broadcast_to(np.asarray(vdensity, np.float32), (self.V,))))
+        out_max = t.empty((n_maps, signs, self.n_seg), device="cuda", dtype=t.float32)
+        out_maps = t.empty((n_maps, signs, self.V), device="cuda", dtype=t.float32) if want_maps else None
+        self.adj.sweep_batch(ptr(maps), self.V, n_maps, signs, ptr(vd), int(bool(floor_zero)), ptr(out_max),
+                             ptr(out_maps), 1 if want_maps else 0, stream_handle())
+        self.adj.status()
+        return out_max.cpu().numpy(), (out_maps.cpu().numpy() if want_maps else None)
+
+
+def _study_for(ops, groups_of_ops, masking_array, fullmask_of):
+    """The _Study of a list of CreateAdjSets (one per threshold group),
+    cached on the first operator."""
+    masks = list(masking_array)
+    key = (tuple(id(o) for o in ops), tuple(int(g) for g in groups_of_ops),
+           tuple(_surface_lengths(masks)), tuple(int(np.asarray(m).sum()) for m in masks))
+    cache = getattr(ops[0], "_tfgb_studies", None)
+    if cache is None:
+        cache = {}
+        try:
+            ops[0]._tfgb_studies = cache
+        except AttributeError:
+            pass
+    if key in cache:
+        return cache[key]
+    groups_of_ops = np.asarray(groups_of_ops)
+    parts = [None] * len(masks)
+    H = np.zeros(len(masks), np.float32)
+    E = np.zeros(len(masks), np.float32)
+    grp = np.zeros(len(masks), np.int32)
+    for gi, op in enumerate(ops):
+        surf = np.flatnonzero(groups_of_ops == gi)
+        sub = [masks[s] for s in surf]
+        for s, part in zip(surf, _surface_parts(op.adjacency, sub, fullmask_of(sub))):
+            parts[s] = part
+            H[s], E[s], grp[s] = op.H, op.E, gi
+    study = _Study(parts, H, E, grp)
+    cache[key] = study
+    return study
+
+
+def _tmaps(merge_y, X, coefs):
+    return glm_stat(_data_dev(merge_y), DesignBatch([X]), WHAT_T, coef=coefs)  # (1, C, V)
+
+
+def _perm_design(X, perm_number, randomise, perm_seed=None, clock=True):
+    if not randomise:
+        return X
+    if clock:
+        np.random.seed(perm_number + int(float(str(time())[-6:]) * 100))
+    else:
+        _seed(perm_number, perm_seed)
+    return X[np.random.permutation(list(range(X.shape[0])))]
+
+
+def _write_surface_maxima(mx, labels, path_of):
+    for tc in range(mx.shape[0]):
+        for sc, label in enumerate(labels):
+            _append(path_of(label, tc), "%f" % mx[tc, 0, sc])
+            _append(path_of(label, tc), "%f" % mx[tc, 1, sc])
 
 
 def calculate_tfce(merge_y, masking_array, pred_x, calcTFCE, vdensity, position_array, fullmask,
                    perm_number=None, randomise=False, verbose=False, no_intercept=True,
                    set_surf_count=None, print_interation=False):
-    """tm_func.py:54-123."""
-    X = np.column_stack([np.ones(merge_y.shape[0]), pred_x])
+    """tm_func.py:54-123: t of every contrast, each swept as + and - over all
+    surfaces in one launch with the merged image's threshold table."""
+    n = np.asarray(merge_y).shape[0]
+    X = _perm_design(np.column_stack([np.ones(n), pred_x]), perm_number, randomise)
+    k = X.shape[1]
+    coefs = list(range(1 if no_intercept else 0, k))
+    study = _study_for([calcTFCE], np.zeros(len(masking_array), np.int32), masking_array, create_full_mask)
+    if np.asarray(position_array)[-1] != study.V:
+        raise ValueError("position_array does not match the masks")
+    tm = _tmaps(merge_y, X, coefs)
+    C = len(coefs)
+    mx, maps = study.sweep(tm, C, 2, vdensity, want_maps=not randomise)
+    labels = ([int(np.ravel(set_surf_count[sc])[0]) for sc in range(len(masking_array))]
+              if set_surf_count is not None else list(range(len(masking_array))))
     if randomise:
-        np.random.seed(perm_number + int(float(str(time())[-6:]) * 100))
-        X = X[np.random.permutation(list(range(merge_y.shape[0])))]
-    tvals = _tvals(X, merge_y)
-    if no_intercept:
-        tvals = tvals[1:, :]
-    tvals = tvals.astype(np.float32, order="C")
-    tfce_tvals = np.zeros_like(tvals).astype(np.float32, order="C")
-    neg_tfce_tvals = np.zeros_like(tvals).astype(np.float32, order="C")
-    for tc in range(tvals.shape[0]):
-        tval_temp = np.zeros_like(fullmask).astype(np.float32, order="C")
-        tval_temp[fullmask == 1] = tvals[0] if tvals.shape[0] == 1 else tvals[tc]
-        tfce_temp = _sweep(calcTFCE, tval_temp)
-        neg_tfce_temp = _sweep(calcTFCE, tval_temp * -1)
-        tval_temp = tval_temp[fullmask == 1]
-        tfce_temp = tfce_temp[fullmask == 1]
-        neg_tfce_temp = neg_tfce_temp[fullmask == 1]
-        for sc in range(len(masking_array)):
-            start, end = position_array[sc], position_array[sc + 1]
-            vd = vdensity if isinstance(vdensity, int) else vdensity[start:end]
-            tfce_tvals[tc, start:end] = tfce_temp[start:end] * (tval_temp[start:end].max() / 100) * vd
-            neg_tfce_tvals[tc, start:end] = (neg_tfce_temp[start:end] * ((tval_temp * -1)[start:end].max() / 100)
-                                             * vd)
-            label = int(set_surf_count[sc]) if set_surf_count is not None else sc
-            if randomise:
-                _append("perm_maxTFCE_surf%d_tcon%d.csv" % (label, tc + 1),
-                        "%f" % np.nanmax(tfce_tvals[tc, start:end]))
-                _append("perm_maxTFCE_surf%d_tcon%d.csv" % (label, tc + 1),
-                        "%f" % np.nanmax(neg_tfce_tvals[tc, start:end]))
-            else:
-                print("Maximum (untransformed) postive tfce value for surface %s, tcon %d: %f"
-                      % (label, tc + 1, np.nanmax(tfce_tvals[tc, start:end])))
-                print("Maximum (untransformed) negative tfce value for surface %s, tcon %d: %f"
-                      % (label, tc + 1, np.nanmax(neg_tfce_tvals[tc, start:end])))
-        if verbose:
-            print("T-contrast: %d" % tc)
-            print("Max tfce from all surfaces = %f" % tfce_tvals[tc].max())
-            print("Max negative tfce from all surfaces = %f" % neg_tfce_tvals[tc].max())
-    if randomise:
+        _write_surface_maxima(mx, labels, lambda lab, tc: "perm_maxTFCE_surf%d_tcon%d.csv" % (lab, tc + 1))
         if print_interation:
             print("Interation number: %d" % perm_number)
         return None
-    return (tvals.astype(np.float32, order="C"), tfce_tvals.astype(np.float32, order="C"),
-            neg_tfce_tvals.astype(np.float32, order="C"))
+    tvals = tm[0].cpu().numpy()
+    for tc in range(C):
+        for sc, label in enumerate(labels):
+            print("Maximum (untransformed) postive tfce value for surface %s, tcon %d: %f" % (label, tc + 1, mx[tc, 0, sc]))
+            print("Maximum (untransformed) negative tfce value for surface %s, tcon %d: %f" % (label, tc + 1, mx[tc, 1, sc]))
+        if verbose:
+            print("T-contrast: %d" % tc)
+            print("Max tfce from all surfaces = %f" % maps[tc, 0].max())
+            print("Max negative tfce from all surfaces = %f" % maps[tc, 1].max())
+    return (np.ascontiguousarray(tvals, np.float32), np.ascontiguousarray(maps[:, 0], np.float32),
+            np.ascontiguousarray(maps[:, 1], np.float32))
 
 
 def low_ram_calculate_tfce(data, mask, pred_x, calcTFCE, vdensity, set_surf_count=0, perm_number=None,
                            randomise=False, no_intercept=True, output_dir=None, perm_seed=None):
-    """tm_func.py:144-185."""
-    X = np.column_stack([np.ones(data.shape[0]), pred_x])
+    """tm_func.py:144-185: one surface; the scale is the max over the
+    zero-filled surface (masked-out vertices count as 0)."""
+    n = np.asarray(data).shape[0]
+    X = _perm_design(np.column_stack([np.ones(n), pred_x]), perm_number, randomise, perm_seed, clock=False)
+    k = X.shape[1]
+    coefs = list(range(1 if no_intercept else 0, k))
+    m = np.asarray(mask).ravel() == 1
+    masks = [m[:, None, None]]
+    study = _study_for([calcTFCE], [0], masks, lambda ms: np.asarray(ms[0])[:, 0, 0].astype(np.float64))
+    tm = _tmaps(data, X, coefs)
+    C = len(coefs)
+    mx, maps = study.sweep(tm, C, 2, vdensity, floor_zero=not m.all(), want_maps=not randomise)
     if randomise:
-        _seed(perm_number, perm_seed)
-        X = X[np.random.permutation(list(range(data.shape[0])))]
-    tvals = _tvals(X, data)
-    if no_intercept:
-        tvals = tvals[1:, :]
-    tvals = tvals.astype(np.float32, order="C")
-    tfce_tvals = np.zeros_like(tvals).astype(np.float32, order="C")
-    neg_tfce_tvals = np.zeros_like(tvals).astype(np.float32, order="C")
-    for tc in range(tvals.shape[0]):
-        tval_temp = np.zeros_like(mask).astype(np.float32, order="C")
-        tval_temp[mask == 1] = tvals[0] if tvals.shape[0] == 1 else tvals[tc]
-        tfce_temp = _sweep(calcTFCE, tval_temp)
-        neg_tfce_temp = _sweep(calcTFCE, -tval_temp)
-        tfce_tvals[tc, :] = tfce_temp[mask == 1] * (tval_temp.max() / 100) * vdensity
-        neg_tfce_tvals[tc, :] = neg_tfce_temp[mask == 1] * ((tval_temp * -1).max() / 100) * vdensity
-        if randomise:
-            name = "perm_maxTFCE_surf%d_tcon%d.csv" % (int(set_surf_count), tc + 1)
-            permfile = os.path.join(output_dir, name) if output_dir is not None else name
-            _append(permfile, "%f" % np.nanmax(tfce_tvals[tc, :]))
-            _append(permfile, "%f" % np.nanmax(neg_tfce_tvals[tc, :]))
-    if not randomise:
-        return (tvals.astype(np.float32, order="C"), tfce_tvals.astype(np.float32, order="C"),
-                neg_tfce_tvals.astype(np.float32, order="C"))
+        name = lambda lab, tc: "perm_maxTFCE_surf%d_tcon%d.csv" % (lab, tc + 1)  # noqa: E731
+        path_of = (lambda lab, tc: os.path.join(output_dir, name(lab, tc))) if output_dir is not None else name
+        _write_surface_maxima(mx, [int(set_surf_count)], path_of)
+        return None
+    return (np.ascontiguousarray(tm[0].cpu().numpy(), np.float32), np.ascontiguousarray(maps[:, 0], np.float32),
+            np.ascontiguousarray(maps[:, 1], np.float32))
 
 
 def _mediation_perm(medtype, pred_x, depend_y, n):
@@ -145,89 +242,76 @@ def _mediation_perm(medtype, pred_x, depend_y, n):
 def calculate_mediation_tfce(medtype, merge_y, masking_array, pred_x, depend_y, calcTFCE, vdensity,
                              position_array, fullmask, perm_number=None, randomise=False, verbose=False,
                              no_intercept=True, print_interation=False):
-    """tm_func.py:207-249."""
+    """tm_func.py:207-249: the indirect-effect z map, swept (one sign) over all
+    surfaces in one launch with the merged image's threshold table."""
+    n = np.asarray(merge_y).shape[0]
     if randomise:
         np.random.seed(perm_number + int(float(str(time())[-6:]) * 100))
-        pred_x, depend_y = _mediation_perm(medtype, pred_x, depend_y, merge_y.shape[0])
-    SobelZ = calc_sobelz(medtype, pred_x, depend_y, merge_y, merge_y.shape[0], merge_y.shape[1])
-    SobelZ = SobelZ.astype(np.float32, order="C")
-    tfce_SobelZ = np.zeros_like(SobelZ).astype(np.float32, order="C")
-    zval_temp = np.zeros_like(fullmask).astype(np.float32, order="C")
-    zval_temp[fullmask == 1] = SobelZ
-    tfce_temp = _sweep(calcTFCE, zval_temp)
-    zval_temp = zval_temp[fullmask == 1]
-    tfce_temp = tfce_temp[fullmask == 1]
+        pred_x, depend_y = _mediation_perm(medtype, pred_x, depend_y, n)
+    study = _study_for([calcTFCE], np.zeros(len(masking_array), np.int32), masking_array, create_full_mask)
+    z = sobel_z_device(medtype, pred_x, depend_y, _data_dev(merge_y), n)
+    mx, maps = study.sweep(z, 1, 1, vdensity, want_maps=not randomise)
     for sc in range(len(masking_array)):
-        start, end = position_array[sc], position_array[sc + 1]
-        vd = vdensity if isinstance(vdensity, int) else vdensity[start:end]
-        tfce_SobelZ[start:end] = tfce_temp[start:end] * (zval_temp[start:end].max() / 100) * vd
         if randomise:
-            _append("perm_maxTFCE_surf%d_%s_zstat.csv" % (sc, medtype), "%f" % np.nanmax(tfce_SobelZ[start:end]))
+            _append("perm_maxTFCE_surf%d_%s_zstat.csv" % (sc, medtype), "%f" % mx[0, 0, sc])
         else:
-            print("Max Sobel Z tfce value for surface %s:\t %1.5f" % (sc, np.nanmax(tfce_SobelZ[start:end])))
-    if verbose:
-        print("Max Zstat tfce from all surfaces = %f" % tfce_SobelZ.max())
+            print("Max Sobel Z tfce value for surface %s:\t %1.5f" % (sc, mx[0, 0, sc]))
+    if verbose and maps is not None:
+        print("Max Zstat tfce from all surfaces = %f" % maps[0, 0].max())
     if randomise:
         print("Interation number: %d" % perm_number)
         return None
-    return SobelZ.astype(np.float32, order="C"), tfce_SobelZ.astype(np.float32, order="C")
+    return (np.ascontiguousarray(z[0].cpu().numpy(), np.float32), np.ascontiguousarray(maps[0, 0], np.float32))
 
 
 def low_ram_calculate_mediation_tfce(medtype, data, mask, pred_x, depend_y, calcTFCE, vdensity, set_surf_count=0,
                                      perm_number=None, randomise=False, no_intercept=True, output_dir=None,
                                      perm_seed=None):
     """tm_func.py:269-305."""
+    n = np.asarray(data).shape[0]
     if randomise:
         _seed(perm_number, perm_seed)
-        pred_x, depend_y = _mediation_perm(medtype, pred_x, depend_y, data.shape[0])
-    SobelZ = calc_sobelz(medtype, pred_x, depend_y, data, data.shape[0], data.shape[1])
-    SobelZ = SobelZ.astype(np.float32, order="C")
-    zval = np.zeros_like(mask).astype(np.float32, order="C")
-    zval[mask == 1] = SobelZ
-    tfce_zval = _sweep(calcTFCE, zval)
-    zval = zval[mask == 1]
-    tfce_zval = tfce_zval[mask == 1]
-    tfce_zval = tfce_zval * (zval.max() / 100) * vdensity
+        pred_x, depend_y = _mediation_perm(medtype, pred_x, depend_y, n)
+    m = np.asarray(mask).ravel() == 1
+    study = _study_for([calcTFCE], [0], [m[:, None, None]], lambda ms: np.asarray(ms[0])[:, 0, 0].astype(np.float64))
+    z = sobel_z_device(medtype, pred_x, depend_y, _data_dev(data), n)
+    mx, maps = study.sweep(z, 1, 1, vdensity, floor_zero=not m.all(), want_maps=not randomise)
     if randomise:
         name = "perm_maxTFCE_surf%d_%s_zstat.csv" % (set_surf_count, medtype)
         permfile = os.path.join(output_dir, name) if output_dir is not None else name
-        _append(permfile, "%f" % np.nanmax(tfce_zval))
-    else:
-        return zval.astype(np.float32, order="C"), tfce_zval.astype(np.float32, order="C")
+        _append(permfile, "%f" % mx[0, 0, 0])
+        return None
+    return np.ascontiguousarray(z[0].cpu().numpy(), np.float32), np.ascontiguousarray(maps[0, 0], np.float32)
 
 
 def calc_mixed_tfce(assigntfcesettings, merge_y, masking_array, position_array, vdensity, pred_x, calcTFCE,
                     perm_number=None, randomise=False, medtype=None, depend_y=None):
-    """tm_func.py:327-378: surfaces grouped by TFCE setting, each group swept
-    with its own operator."""
-    tvals = tfce_tvals = neg_tfce_tvals = None
-    for i in np.unique(assigntfcesettings):
-        data_mask = np.zeros(merge_y.shape[1], dtype=bool)
-        extract_range = np.argwhere(assigntfcesettings == i)
-        for surface in extract_range:
-            data_mask[position_array[int(surface)]:position_array[int(surface) + 1]] = True
-        sub = merge_y[:, data_mask]
-        try:
-            temp_vdensity = vdensity[data_mask]
-        except Exception:
-            temp_vdensity = 1
-        group = np.array(masking_array)[assigntfcesettings == i]
-        if randomise:
-            calculate_tfce(sub, group, pred_x, calcTFCE[i], temp_vdensity, create_position_array(group),
-                           create_full_mask(group), set_surf_count=extract_range, perm_number=perm_number,
-                           randomise=True, print_interation=(i == 0))
-        else:
-            tv, tp, tn = calculate_tfce(sub, group, pred_x, calcTFCE[i], temp_vdensity,
-                                        create_position_array(group), create_full_mask(group),
-                                        set_surf_count=extract_range)
-            if tvals is None:
-                # the reference binds the three names to one array here
-                tvals = tfce_tvals = neg_tfce_tvals = np.zeros((tv.shape[0], merge_y.shape[1]))
-            tvals[:, data_mask] = tv
-            tfce_tvals[:, data_mask] = tp
-            neg_tfce_tvals[:, data_mask] = tn
-    if not randomise:
-        return tvals, tfce_tvals, neg_tfce_tvals
+    """tm_func.py:327-378: the surfaces of each TFCE setting i swept with
+    calcTFCE[i]'s H and E and their own merged threshold table, every
+    setting in one launch.  One permutation serves all settings (the
+    reference re-seeds from the clock for each setting)."""
+    assign = np.asarray(assigntfcesettings)
+    settings = np.unique(assign)
+    ops = [calcTFCE[int(i)] for i in settings]
+    group_of = np.searchsorted(settings, assign)
+    study = _study_for(ops, group_of, masking_array, create_full_mask)
+    n = np.asarray(merge_y).shape[0]
+    X = _perm_design(np.column_stack([np.ones(n), pred_x]), perm_number, randomise)
+    coefs = list(range(1, X.shape[1]))
+    if np.asarray(position_array)[-1] != study.V:
+        raise ValueError("position_array does not match the masks")
+    tm = _tmaps(merge_y, X, coefs)
+    C = len(coefs)
+    mx, maps = study.sweep(tm, C, 2, vdensity, want_maps=not randomise)
+    if randomise:
+        _write_surface_maxima(mx, list(range(len(assign))),
+                              lambda lab, tc: "perm_maxTFCE_surf%d_tcon%d.csv" % (lab, tc + 1))
+        print("Interation number: %d" % perm_number)
+        return None
+    # the reference binds tvals, tfce_tvals and neg_tfce_tvals to one array,
+    # which ends up holding the negative maps
+    out = np.asarray(maps[:, 1], np.float64)
+    return out, out, out
 
 
 def apply_mfwer(image_array, num_contrasts, surface_range, num_perm, num_surf, tminame, position_array, pos_range,

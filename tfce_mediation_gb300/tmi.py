@@ -54,6 +54,8 @@ def check_outname(outname):
 def _count(arr, one_ndim, many_ndim):
     """Number of objects in an element argument: a single array of
     `one_ndim` dimensions, or a stack / object array of them."""
+    if isinstance(arr, (list, tuple)) and arr and all(isinstance(x, np.ndarray) for x in arr):
+        return len(arr)  # a list of arrays (their shapes may differ)
     a = np.asarray(arr) if not isinstance(arr, np.ndarray) else arr
     if a.dtype.kind == "O" or a.ndim == many_ndim:
         return int(a.shape[0])
@@ -63,6 +65,8 @@ def _count(arr, one_ndim, many_ndim):
 
 
 def _items(arr, n, one_ndim):
+    if isinstance(arr, (list, tuple)) and arr and all(isinstance(x, np.ndarray) for x in arr):
+        return list(arr)
     a = np.asarray(arr) if not isinstance(arr, np.ndarray) else arr
     if n == 1 and a.dtype.kind != "O" and a.ndim == one_ndim:
         return [a]
