@@ -359,6 +359,241 @@ def run_next(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# The other synthetic configurations (sub-lines of the default run): the
+# small vertex study, the voxel study, mediation and the multimodal study
+# ---------------------------------------------------------------------------
+CONFIGS = {
+    "config1": "icosphere-L5 (10,242 vertices), n=100, k=3, 2 contrasts x +/-, H=2 E=1",
+    "config3": "91x109x91 ellipsoid mask (~230k voxels, 26-neighbour), n=200, k=4, 3 contrasts x +/-, H=2 E=0.5",
+    "config4a": "mediation 'M' (Aroian z) on 2 x icosphere-L7 (327,684 vertices), n=350, one sign x 2 hemispheres",
+    "config4b": "multimodal: 20 icospheres (levels 5-7) + ~120k-voxel skeleton (~1.4M elements), n=350, k=3, "
+                "2 contrasts x +/- x 21 surfaces; icospheres one threshold group (H=2 E=1), skeleton (H=2 E=0.5)",
+}
+CONFIG_BATCH = {"config1": 512, "config3": 128, "config4a": 128, "config4b": 32}
+CONFIG_CPU_PERMS = {"config1": 10, "config3": 2, "config4a": 2, "config4b": 1}
+
+
+def _config_study(kind):
+    from tfce_mediation_gb300 import synth
+    if kind == "config1":
+        return synth.config1()
+    if kind == "config3":
+        return synth.config3()
+    if kind == "config4a":
+        return synth.config4_mediation()
+    return synth.config4_mmr()
+
+
+def _config_groups(st):
+    S = len(st.segments) - 1
+    return np.array([0] * (S - 1) + [1], np.int32)
+
+
+def _config_cpu_init(kind):
+    _W["cfg"] = (kind, _config_study(kind))
+    from oracle import oracle
+    oracle.lib()
+
+
+def _config_cpu_perm(p):
+    """One permutation of a configuration as the reference's CPU path
+    computes it (the oracle port: FP64 t or Sobel z, C sweeps)."""
+    from oracle import oracle
+    kind, st = _W["cfg"]
+    perm = np.random.RandomState(SEED + p).permutation(st.n)
+    segs = [(int(st.segments[h]), int(st.segments[h + 1])) for h in range(len(st.segments) - 1)]
+
+    def sub(a, b):
+        return st.offsets[a:b + 1] - st.offsets[a], st.indices[st.offsets[a]:st.offsets[b]] - a
+
+    if kind == "config4a":
+        with np.errstate(all="ignore"):
+            z = oracle.calc_sobelz("M", st.pred_x[perm, 0], st.depend_y, st.Y.astype(np.float64), st.n)
+        z = z.astype(np.float32)
+        return [max(oracle.tfce_max_batch(*sub(a, b), z[a:b], 2.0, 1.0, floor_zero=True)[0] for a, b in segs)]
+    X = st.design()[perm]
+    n, k = X.shape
+    invXX = np.linalg.inv(X.T @ X)
+    t = np.empty((k, st.V), np.float32)
+    for v0 in range(0, st.V, 32768):
+        t[:, v0:v0 + 32768] = oracle.tval_int_ref(X, invXX, st.Y[:, v0:v0 + 32768], n, k)
+    out = []
+    if kind == "config4b":
+        groups = _config_groups(st)
+        for c in range(1, k):
+            for sgn in (1.0, -1.0):
+                for g in (0, 1):
+                    ss = np.flatnonzero(groups == g)
+                    a, b = st.segments[ss[0]], st.segments[ss[-1] + 1]
+                    im = (t[c, a:b] * np.float32(sgn)).astype(np.float32)
+                    e = oracle.tfce(*sub(a, b), im, float(st.H[ss[0]]), float(st.E[ss[0]]))
+                    for s_ in ss:
+                        lo, hi = st.segments[s_] - a, st.segments[s_ + 1] - a
+                        out.append(float(np.max(e[lo:hi] * (im[lo:hi].max() / np.float32(100)))))
+        return out
+    E_ = 0.5 if kind == "config3" else 1.0
+    for c in range(1, k):
+        for sgn in (1.0, -1.0):
+            out.append(max(oracle.tfce_max_batch(*sub(a, b), t[c, a:b], 2.0, E_, sign=sgn,
+                                                 floor_zero=(kind != "config3"))[0] for a, b in segs))
+    return out
+
+
+def config_cpu_baseline(kind):
+    import multiprocessing as mp
+    _one_thread_per_process()
+    ctx = mp.get_context("spawn")
+    n_cpu = CONFIG_CPU_PERMS[kind]
+    with ctx.Pool(1, initializer=_config_cpu_init, initargs=(kind,)) as pool:
+        pool.map(_config_cpu_perm, [10_000])  # warm: libraries loaded, caches filled
+        t0 = time.perf_counter()
+        pool.map(_config_cpu_perm, range(n_cpu))
+        dt = time.perf_counter() - t0
+    return {"value": n_cpu / dt, "unit": "perm/s", "cores": 1, "kind": "port",
+            "sample": f"{n_cpu} permutation(s) of the same workload, {dt:.1f} s, single process"}
+
+
+def _sweep_bytes(st):
+    """Algorithmic bytes of one sweep of every segment: statistic 4V +
+    offsets 4(V+1) + entries 4D per segment, summed over the segments."""
+    tot = 0
+    for h in range(len(st.segments) - 1):
+        a, b = int(st.segments[h]), int(st.segments[h + 1])
+        tot += 4 * (b - a) + 4 * (b - a + 1) + 4 * int(st.offsets[b] - st.offsets[a])
+    return tot
+
+
+def run_config(kind, args):
+    """Sub-line of one configuration: whole-job rate through the engine's
+    public loop with the data resident, the same through the pipelined entry
+    with the data copied from pinned host memory every step (e2e), and the
+    sweep kernel's CUDA-event time against its algorithmic bytes."""
+    import torch
+    from tfce_mediation_gb300 import engine as E
+    from tfce_mediation_gb300.device import ptr
+    from tfce_mediation_gb300.glm import DesignBatch
+    st = _config_study(kind)
+    P = CONFIG_BATCH[kind]
+    K = max(2, min(args.steps, 6))
+    signs = 1 if kind == "config4a" else 2
+    if kind == "config4a":
+        eng = E.MediationEngine(st.Y, st.pred_x[:, 0], st.depend_y, "M", (st.offsets, st.indices), st.segments,
+                                2.0, 1.0, floor_zero=True, batch=P)
+        C, adj = 1, eng.inner.adj
+    else:
+        kw = dict(threshold_groups=_config_groups(st)) if kind == "config4b" else {}
+        seg = None if kind == "config3" else st.segments
+        eng = E.PermutationEngine(st.Y, st.pred_x, (st.offsets, st.indices), seg, st.H, st.E,
+                                  floor_zero=(kind != "config3"), batch=P, **kw)
+        C, adj = eng.C, eng.adj
+    S = adj.n_seg
+    perms = E.permutations(st.n, SEED, 0, (2 * K + 2) * P)
+    run = eng.run if kind == "config4a" else eng.run_graph
+    run(perms=perms[:P])  # warm (graph capture)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    run(perms=perms[P:(K + 1) * P])
+    torch.cuda.synchronize()
+    job_s = time.perf_counter() - t0
+    # e2e: new data from pinned host memory every step
+    Yh = torch.from_numpy(st.Y).pin_memory()
+    if kind == "config4a":
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for s_ in range(K):
+            eng.inner.upload(Yh)
+            eng.run(perms=perms[(K + 1 + s_) * P:(K + 2 + s_) * P])
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+        h2d = st.Y.nbytes
+    else:
+        eng.run_stream([(Yh, perms[:P])])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        eng.run_stream((Yh, perms[(K + 1 + s_) * P:(K + 2 + s_) * P]) for s_ in range(K))
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+        h2d = st.Y.nbytes
+    # the sweep kernel alone: P x C maps (x signs x segments items)
+    if kind == "config4a":
+        maps = eng.zmaps(perms[:P])
+    else:
+        maps = eng.tmaps(DesignBatch(eng.X[perms[:P]]))
+    out = torch.empty((P * C, signs, S), device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def sweep():
+        adj.sweep_batch(ptr(maps), eng.V, P * C, signs, None, int(kind != "config3"), ptr(out), None, 0,
+                        stream.cuda_stream)
+    for _ in range(2):
+        sweep()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(3):
+        sweep()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    adj.status()
+    ms = e0.elapsed_time(e1) / 3
+    hbm, _, peak_kind = measured_peaks()
+    alg = _sweep_bytes(st) * P * C * signs
+    achieved = alg / (ms / 1e3) / 1e9
+    line = {"workload": CONFIGS[kind], "metric": "perm/s", "value": K * P / job_s, "unit": "perm/s",
+            "perms_per_step": P, "steps": K, "ms_per_step": job_s / K * 1e3,
+            "note": "whole job through the engine's public loop (%s), data resident" %
+                    ("MediationEngine.run" if kind == "config4a" else "PermutationEngine.run_graph"),
+            "e2e": {"value": K * P / e2e_s, "unit": "perm/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(P * C * signs * S * 4),
+                    "note": "new data from pinned host memory every step" +
+                            ("" if kind == "config4a" else " (PermutationEngine.run_stream)")},
+            "roofline": {"bound": "hbm", "kernel": "tfce_sweep_kernel", "achieved": achieved, "peak": hbm,
+                         "unit": "GB/s", "frac": achieved / hbm, "peak_source": f"{peak_kind} hbm_gbs",
+                         "traffic": None, "algorithmic_bytes_per_launch": alg, "ms_per_launch": ms,
+                         "sweeps_per_launch": P * C * signs * S}}
+    del eng, maps, out
+    torch.cuda.empty_cache()
+    return line
+
+
+def time_to_fwer(eng, st, n_perm=10_000, seed=99):
+    """Wall time from the resident data to the 1-p(FWER) maps of every
+    contrast and sign: the plain path (n_perm permutations) and the learned
+    tail (300 permutations + the margin fallback), and how far apart the
+    two maps are where the plain p <= 0.05."""
+    import torch
+    from tfce_mediation_gb300.tail import data, gpd
+    from tfce_mediation_gb300.tail.surrogate import TailSurrogate, learned_fwer_maps
+    _, maps, _ = eng.observed()
+    V1 = int(st.segments[1])
+    rho = data.neighbour_correlation(torch.from_numpy(st.Y[:, :V1]).cuda(), st.offsets[:V1 + 1],
+                                     st.indices[:st.offsets[V1]])
+    sur = TailSurrogate()
+    images = {c: [maps[c, 0], maps[c, 1]] for c in range(eng.C)}
+    learned_fwer_maps(eng, images, rho, 1.0, seed=seed, surrogate=sur)  # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    mx = eng.run_graph(n_perm=n_perm, seed=seed).max(axis=-1)
+    plain = {c: [gpd.one_minus_p(maps[c, s_], mx[:, c, :].reshape(-1)) for s_ in range(2)] for c in range(eng.C)}
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    m, info = learned_fwer_maps(eng, images, rho, 1.0, seed=seed, surrogate=sur)
+    worst, nsig = 0.0, 0
+    for c in range(eng.C):
+        for s_ in range(2):
+            sig = (1.0 - plain[c][s_]) <= 0.05
+            nsig += int(sig.sum())
+            if sig.any():
+                worst = max(worst, float(np.abs(m[c][s_] - plain[c][s_])[sig].max()))
+    return {"plain": {"perms": n_perm, "seconds": plain_s, "maps": 2 * eng.C},
+            "learned_tail": {"perms": info["perms"], "seconds": info["seconds"],
+                             "fraction_of_plain": info["seconds"] / plain_s, "near_alpha_vertices": info["near_alpha"],
+                             "max_abs_dp_where_p_le_0.05": worst, "vertices_p_le_0.05": nsig},
+            "note": "1-p(FWER) maps of 4 contrasts x (+,-) of the observed study (calculate_fweP formula); "
+                    "learned tail: MLP GPD tail from 300 permutations, margin 0.01 fallback"}
+
+
 def _one_thread_per_process():
     """BLAS / OpenMP thread counts of 1 for the worker processes (spawned
     children read these when their numpy loads), so `cores` processes use
@@ -434,6 +669,13 @@ def run_gpu(args):
                               batch="auto" if args.batch == 0 else args.batch, floor_zero=True,
                               precision=args.precision)
     P = eng.batch
+    if ws > 1:
+        # every rank runs rank 0's batch, so the whole-job count is P x steps x ranks
+        pt = torch.tensor([P], device="cuda", dtype=torch.int64)
+        dist.broadcast(pt, 0)
+        if int(pt.item()) != P:
+            P = eng.batch = int(pt.item())
+            eng._alloc_buffers()
     C, S, V, n = eng.C, eng.n_seg, eng.V, eng.n
     total_steps = args.warmup + args.steps
     # disjoint permutation ranges per rank
@@ -624,12 +866,21 @@ def run_gpu(args):
         "glm": glm_info,
         "clocks": clocks,
     }
+    if not args.no_configs:
+        line["time_to_fwer"] = time_to_fwer(eng, st)
+        del eng
+        torch.cuda.empty_cache()
+        line["configs"] = {}
+        for kind in CONFIGS:
+            line["configs"][kind] = run_config(kind, args)
     if not args.no_cpu_baseline:
         cores = 1
         v, dt = cpu_rate(args.cpu_perms, cores, {"n": args.n, "level": args.level})
         line["cpu_baseline"] = {"value": v, "unit": "perm/s", "cores": cores, "kind": "port",
                                 "sample": f"{args.cpu_perms} permutations of the same workload, "
                                           f"{dt:.1f} s, single process"}
+        for kind in line.get("configs", {}):
+            line["configs"][kind]["cpu_baseline"] = config_cpu_baseline(kind)
     print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()
@@ -646,6 +897,8 @@ def main():
     ap.add_argument("--level", type=int, default=7)
     ap.add_argument("--cpu-perms", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the other configurations' sub-lines and the time-to-FWER block")
     ap.add_argument("--precision", default="bf16x3", choices=["bf16x3", "fp32"],
                     help="GLM arithmetic: tensor-core split BF16 or FP32 CUDA cores")
     ap.add_argument("--workload", default="config2", choices=["config2"] + sorted(NEXT),

@@ -570,6 +570,25 @@ def calculate_mediation_tfce(medtype, merge_y, masking_array, pred_x, depend_y, 
     return z, _scaled(e, img[full], _positions(masking_array), vdensity)
 
 
+def vert_stat_tfce_image(vertStat, bin_mask, offsets, indices, H, E, density=1):
+    """The TFCE image of write_vertStat_img (pyfunc.py:80-92): the masked
+    statistic scattered into a zero-filled hemisphere, swept, scaled by the max
+    of its finite masked values / 100 and the density weight."""
+    bin_mask = np.asarray(bin_mask, bool)
+    out = np.zeros(bin_mask.shape[0], np.float32)
+    out[bin_mask] = vertStat
+    e = tfce(offsets, indices, out, H, E)
+    vs = np.asarray(vertStat)
+    return e * (vs[np.isfinite(vs)].max() / 100) * density
+
+
+def voxel_stat_tfce_image(voxelStat, offsets, indices, H, E):
+    """The TFCE values of write_voxelStat_img (pyfunc.py:94-103) over the
+    mask's voxels: swept, scaled by the statistic's max / 100."""
+    v = np.asarray(voxelStat).astype(np.float32)
+    return tfce(offsets, indices, v, H, E) * (v.max() / 100)
+
+
 def fwep_vertex(tfce_values, null):
     """1-p(FWER) as tfce_mediation/tmanalysis/calculate_fweP_vertex.py:37-69:
     sorted null, p_array[j] = j/N, idx = searchsorted(left),

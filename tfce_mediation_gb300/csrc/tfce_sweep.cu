@@ -928,6 +928,12 @@ struct tfce_adjset {
   int32_t* d_group = nullptr;  // threshold group of every segment, or NULL
   float* d_segmax = nullptr;   // segment maxima of the last grouped launch
   int64_t segmax_cap = 0;
+  // Device buffers replaced by larger ones.  A launch captured into a CUDA
+  // graph keeps the workspace pointer it was captured with, so a buffer is
+  // never freed while the handle lives: it is retired here and freed by
+  // tfce_adjset_destroy.  Growth is geometric, so the retired total stays
+  // below the live buffer's size.
+  std::vector<void*> retired;
   std::mutex mu;
 };
 
@@ -949,6 +955,8 @@ int release(tfce_adjset* h) {
   cudaFree(h->d_enh);
   cudaFree(h->d_group);
   cudaFree(h->d_segmax);
+  for (void* p : h->retired) cudaFree(p);
+  h->retired.clear();
   cudaSetDevice(dev);
   return TFCE_OK;
 }
@@ -968,15 +976,21 @@ int resident_slots(tfce_adjset* h) {
   return TFCE_OK;
 }
 
+// One slot layout serves both accumulation modes (the per-component layout
+// is the larger), so switching modes never replaces the workspace; a launch
+// with more items than the workspace has slots replaces it by one at least
+// twice as large (capped at the resident-slot count), retiring the old one.
 int ensure_workspace(tfce_adjset* h, int32_t slots, bool lazy) {
-  const int64_t per = lazy ? tfgb::slot_bytes_lazy(h->vmax_seg) : tfgb::slot_bytes(h->vmax_seg);
-  if (h->d_ws && h->ws_slots >= slots && h->ws_slot == per) return TFCE_OK;
-  cudaFree(h->d_ws);
-  h->d_ws = nullptr;
-  h->ws_slots = 0;
-  TFGB_CUDA(cudaMalloc(&h->d_ws, per * slots));
+  (void)lazy;
+  const int64_t per = std::max(tfgb::slot_bytes_lazy(h->vmax_seg), tfgb::slot_bytes(h->vmax_seg));
+  if (h->d_ws && h->ws_slots >= slots && h->ws_slot >= per) return TFCE_OK;
+  const int32_t want = std::max(slots, std::min(h->max_slots, 2 * h->ws_slots));
+  char* fresh = nullptr;
+  TFGB_CUDA(cudaMalloc(&fresh, per * want));
+  if (h->d_ws) h->retired.push_back(h->d_ws);
+  h->d_ws = fresh;
   h->ws_slot = per;
-  h->ws_slots = slots;
+  h->ws_slots = want;
   return TFCE_OK;
 }
 
@@ -1026,11 +1040,12 @@ int launch_sweep(tfce_adjset* h, const float* stats, int64_t map_stride, int32_t
   if (h->d_group) {
     const int64_t need = (int64_t)n_maps * signs * h->n_seg;
     if (h->segmax_cap < need) {
-      cudaFree(h->d_segmax);
-      h->d_segmax = nullptr;
-      h->segmax_cap = 0;
-      TFGB_CUDA(cudaMalloc(&h->d_segmax, sizeof(float) * need));
-      h->segmax_cap = need;
+      const int64_t cap = std::max(need, 2 * h->segmax_cap);
+      float* fresh = nullptr;
+      TFGB_CUDA(cudaMalloc(&fresh, sizeof(float) * cap));
+      if (h->d_segmax) h->retired.push_back(h->d_segmax);  // a captured launch may still use it
+      h->d_segmax = fresh;
+      h->segmax_cap = cap;
     }
     const int64_t blocks = (int64_t)n_maps * h->n_seg;
     TFGB_CHECK_ARG(blocks < (1LL << 31), "too many segment-max blocks");

@@ -76,15 +76,15 @@ def _tfce_map(op, image):
     return e
 
 
-def write_vertStat_img(statname, vertStat, outdata_mask, affine_mask, surf, hemi, bin_mask, TFCEfunc,
-                       all_vertex, density_corr=1, TFCE=True):
-    """pyfunc.py:80-92: TFCE image scaled by max(masked stat)/100 * density,
-    max appended to max_TFCE_contrast_values.csv, both images saved as MGH."""
+def vert_stat_images(statname, vertStat, tfce_scaled, outdata_mask, affine_mask, surf, hemi, bin_mask,
+                     all_vertex):
+    """The file side of write_vertStat_img (pyfunc.py:80-92) for a TFCE image
+    already scaled (full hemisphere, or None for TFCE=False): the TFCE image
+    and its max line in max_TFCE_contrast_values.csv, then the statistic."""
     vertStat_out = np.zeros(all_vertex).astype(np.float32, order="C")
     vertStat_out[bin_mask] = vertStat
-    if TFCE:
-        vertStat_TFCE = _tfce_map(TFCEfunc, vertStat_out)
-        outdata_mask[:, 0, 0] = vertStat_TFCE * (vertStat[np.isfinite(vertStat)].max() / 100) * density_corr
+    if tfce_scaled is not None:
+        outdata_mask[:, 0, 0] = tfce_scaled
         _append("max_TFCE_contrast_values.csv", "%s_%s_%s,%f" % (
             statname, surf, hemi, outdata_mask[np.isfinite(outdata_mask[:, 0, 0])].max()))
         save_mgh(outdata_mask, affine_mask, "%s_%s_%s_TFCE.mgh" % (statname, surf, hemi))
@@ -92,17 +92,39 @@ def write_vertStat_img(statname, vertStat, outdata_mask, affine_mask, surf, hemi
     save_mgh(outdata_mask, affine_mask, "%s_%s_%s.mgh" % (statname, surf, hemi))
 
 
-def write_voxelStat_img(statname, voxelStat, out_path, data_index, affine, TFCEfunc, imgext=".nii.gz",
-                        TFCE=True):
-    """pyfunc.py:94-103."""
+def write_vertStat_img(statname, vertStat, outdata_mask, affine_mask, surf, hemi, bin_mask, TFCEfunc,
+                       all_vertex, density_corr=1, TFCE=True):
+    """pyfunc.py:80-92: TFCE image scaled by max(masked stat)/100 * density,
+    max appended to max_TFCE_contrast_values.csv, both images saved as MGH."""
+    scaled = None
     if TFCE:
-        voxelStat_out = voxelStat.astype(np.float32, order="C")
-        voxelStat_TFCE = _tfce_map(TFCEfunc, voxelStat_out)
-        out_path[data_index] = voxelStat_TFCE * (voxelStat_out.max() / 100)
+        vertStat_out = np.zeros(all_vertex).astype(np.float32, order="C")
+        vertStat_out[bin_mask] = vertStat
+        vertStat_TFCE = _tfce_map(TFCEfunc, vertStat_out)
+        scaled = vertStat_TFCE * (vertStat[np.isfinite(vertStat)].max() / 100) * density_corr
+    vert_stat_images(statname, vertStat, scaled, outdata_mask, affine_mask, surf, hemi, bin_mask, all_vertex)
+
+
+def voxel_stat_images(statname, voxelStat, tfce_scaled, out_path, data_index, affine, imgext=".nii.gz"):
+    """The file side of write_voxelStat_img (pyfunc.py:94-103) for a TFCE map
+    already scaled (over the mask's voxels, or None for TFCE=False)."""
+    if tfce_scaled is not None:
+        out_path[data_index] = tfce_scaled
         save_nifti(out_path, affine, "%s_TFCE%s" % (statname, imgext))
         _append("max_TFCE_contrast_values.csv", "%s,%f" % (statname, out_path.max()))
     out_path[data_index] = voxelStat
     save_nifti(out_path, affine, "%s%s" % (statname, imgext))
+
+
+def write_voxelStat_img(statname, voxelStat, out_path, data_index, affine, TFCEfunc, imgext=".nii.gz",
+                        TFCE=True):
+    """pyfunc.py:94-103."""
+    scaled = None
+    if TFCE:
+        voxelStat_out = voxelStat.astype(np.float32, order="C")
+        voxelStat_TFCE = _tfce_map(TFCEfunc, voxelStat_out)
+        scaled = voxelStat_TFCE * (voxelStat_out.max() / 100)
+    voxel_stat_images(statname, voxelStat, scaled, out_path, data_index, affine, imgext)
 
 
 # ---------------------------------------------------------------------------

@@ -400,11 +400,11 @@ def mmr_run(opts):
         settings = np.unique(assign)
         groups = np.searchsorted(settings, assign).astype(np.int32)
         H = np.array([tfce_opts[2 * int(a)] for a in assign], np.float32)
-        E = np.array([tfce_opts[2 * int(a) + 1] for a in assign], np.float32)
+        Es = np.array([tfce_opts[2 * int(a) + 1] for a in assign], np.float32)
     else:
         groups = np.zeros(n_surf, np.int32)
         H = np.full(n_surf, tfce_opts[0], np.float32)
-        E = np.full(n_surf, tfce_opts[1], np.float32)
+        Es = np.full(n_surf, tfce_opts[1], np.float32)
     off, idx, seg, vd = _mmr_layout(masking_array, adjacency_array, adjacent_range, opts.noweight)
     data = np.asarray(image_array[0])
     sub = None
@@ -435,9 +435,9 @@ def mmr_run(opts):
     tag = ("med_stats_" if medtype else "stats_") + (outname if outname.endswith("tmi") else outname + ".tmi")
     kw = dict(vdensity=vd, threshold_groups=groups, batch=getattr(opts, "batch", 64))
     if medtype:
-        eng = E.MediationEngine(merge_y, pred_x, depend_y, medtype, (off, idx), seg, H, E, **kw)
+        eng = E.MediationEngine(merge_y, pred_x, depend_y, medtype, (off, idx), seg, H, Es, **kw)
     else:
-        eng = E.PermutationEngine(merge_y, pred_x, (off, idx), seg, H, E, **kw)
+        eng = E.PermutationEngine(merge_y, pred_x, (off, idx), seg, H, Es, **kw)
     if not getattr(opts, "randomise", None):
         if medtype:
             z, tz, _ = eng.observed()

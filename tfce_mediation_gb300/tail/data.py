@@ -88,6 +88,10 @@ def null_for_setting(s, n_perm, batch=128):
     cols = [synth.binary_half(rng, s["n"])] + [rng.standard_normal(s["n"]) for _ in range(s["k"] - 2)]
     pred_x = np.column_stack(cols)
     eng = E.PermutationEngine(Y, pred_x, (off, idx), seg, 2.0, s["E"], contrasts=[1], batch=batch)
-    mx = eng.run(n_perm=n_perm, seed=s["seed"] + 11)  # (P, 1, 2, H)
+    full = n_perm // batch * batch  # whole batches through the captured graphs, the rest as one short batch
+    parts = [eng.run_graph(n_perm=full, seed=s["seed"] + 11)] if full else []
+    if n_perm > full:
+        parts.append(eng.run(start=full, stop=n_perm, seed=s["seed"] + 11))
+    mx = np.concatenate(parts)  # (P, 1, 2, H)
     null = mx[:, 0, :, :].max(axis=-1).reshape(-1).astype(np.float64)
     return null, neighbour_correlation(Ys[0], off1, idx1), off.shape[0] - 1

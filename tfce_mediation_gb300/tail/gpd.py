@@ -74,23 +74,29 @@ def decode(pred, m):
     return float(m * np.exp(pred[2])), xi, float(m * np.exp(pred[1]))
 
 
-def one_minus_p(values, null, u=None, xi=None, sigma=None, quant=QUANT):
+def apply_tail(out, v, u, xi, sigma, quant=QUANT):
+    """Overwrite out[i] with the GPD tail's 1-p where v[i] > u."""
+    tail = v > u
+    if np.any(tail):
+        y = (v[tail] - u) / sigma
+        if abs(xi) < 1e-9:
+            sf = np.exp(-y)
+        else:
+            base = np.maximum(1.0 + xi * y, 0.0)
+            sf = np.where(base > 0, base ** (-1.0 / xi), 0.0)
+        out[tail] = 1.0 - (1.0 - quant) * sf
+    return out
+
+
+def one_minus_p(values, null, u=None, xi=None, sigma=None, quant=QUANT, presorted=False):
     """1-p(FWER) of TFCE values given a null sample and (optionally) a tail.
     Without a tail this is exactly the reference's calculate_fweP formula."""
-    srt = np.sort(np.asarray(null, np.float64))
+    srt = np.asarray(null, np.float64) if presorted else np.sort(np.asarray(null, np.float64))
     N = srt.shape[0]
     v = np.asarray(values, np.float64)
     idx = np.searchsorted(srt, v, side="left")
     out = np.maximum(idx - 1, 0) / N
     if u is not None:
-        tail = v > u
-        if np.any(tail):
-            y = (v[tail] - u) / sigma
-            if abs(xi) < 1e-9:
-                sf = np.exp(-y)
-            else:
-                base = np.maximum(1.0 + xi * y, 0.0)
-                sf = np.where(base > 0, base ** (-1.0 / xi), 0.0)
-            out[tail] = 1.0 - (1.0 - quant) * sf
+        apply_tail(out, v, u, xi, sigma, quant)
     out[v <= 0] = 0.0
     return out
