@@ -97,7 +97,13 @@ int tfce_adjset_set_threshold_groups(tfce_adjset* h, const int32_t* group);
  *      the chain of components it joined; the value is the float rounding of
  *      the exact sum of the same float increments, i.e. it differs from the
  *      reference by the reference's own float summation error (~1e-7 rel).
- *      Work per threshold is O(live components) instead of O(active vertices). */
+ *      Work per threshold is O(live components) instead of O(active vertices).
+ *      A launch that asks only for maxima (out_maps NULL) without vertex
+ *      weights (vdensity NULL) keeps, per component, the largest sum of any
+ *      component merged into it instead of the potentials, and takes the
+ *      map's maximum over the last live components: no per-vertex pass;
+ *   2  as 1, but maxima-only launches keep the potentials and resolve every
+ *      vertex as well (the same values; for comparisons). */
 int tfce_adjset_set_accumulation(tfce_adjset* h, int32_t mode);
 
 /* CreateAdjSet.run(image, enhn) on host float32 arrays of length V (one

@@ -291,3 +291,41 @@ def test_large_segment_without_activity_bitmap():
     adj.sweep_batch(d.data_ptr(), V, 2, 2, None, 0, out.data_ptr())
     adj.status()
     np.testing.assert_allclose(out.cpu().numpy(), got, rtol=COMPONENT_RTOL)
+
+
+@pytest.mark.parametrize("E", [1.0, 0.5])
+def test_maxima_only_form_equals_potential_form(E):
+    """Maxima-only launches keep each component's largest sum instead of the
+    potentials; the maxima equal the potential form's (which resolves every
+    vertex) to the last float bit or two, on smooth maps of both signs and
+    two segments, and the oracle's to the float summation error."""
+    import torch
+    from oracle import oracle
+    from tfce_mediation_gb300 import adjacency as A
+    from tfce_mediation_gb300 import synth
+    v, f = synth.icosphere(5)
+    o1, i1 = A.mesh_csr(f, v.shape[0])
+    off, idx, seg = A.concat_csr([(o1, i1), (o1, i1)])
+    V = off.shape[0] - 1
+    S = synth.smoothing_matrix(off, idx)
+    rng = np.random.default_rng(17)
+    m = rng.standard_normal((V, 24)).astype(np.float32)
+    for _ in range(5):
+        m = (S @ m).astype(np.float32)
+    maps = np.ascontiguousarray((3.5 * m.T / m.std()).astype(np.float32))
+    adj = A.AdjacencySet((off, idx), 2.0, E, seg)
+    d = torch.from_numpy(maps).cuda()
+    res = {}
+    for mode in ("component", "component-chain"):
+        adj.set_accumulation(mode)
+        out = torch.empty((24, 2, 2), device="cuda")
+        adj.sweep_batch(d.data_ptr(), V, 24, 2, None, 1, out.data_ptr())
+        adj.status()
+        res[mode] = out.cpu().numpy()
+    np.testing.assert_allclose(res["component"], res["component-chain"], rtol=2e-7, atol=0)
+    Vh = V // 2
+    for i in range(0, 24, 5):
+        for si, s in enumerate((1.0, -1.0)):
+            for h in range(2):
+                ref = oracle.tfce_max_batch(o1, i1, maps[i, h * Vh:(h + 1) * Vh], 2.0, E, sign=s, floor_zero=True)[0]
+                assert abs(res["component"][i, si, h] - ref) <= 1e-5 * abs(ref) + 1e-12, (i, s, h)

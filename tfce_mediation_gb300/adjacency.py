@@ -339,9 +339,12 @@ class AdjacencySet:
         self.threshold_groups = g.copy()
 
     def set_accumulation(self, mode: str):
-        """'exact' (the reference's float arithmetic, bit-identical) or
-        'component' (per-component double accumulation for batched sweeps)."""
-        code = {"exact": 0, "component": 1}[mode]
+        """'exact' (the reference's float arithmetic, bit-identical),
+        'component' (per-component double accumulation for batched sweeps;
+        maxima-only launches keep each component's largest sum) or
+        'component-chain' (per-component, every vertex resolved along its
+        chain of potentials even when only maxima are asked for)."""
+        code = {"exact": 0, "component": 1, "component-chain": 2}[mode]
         _lib.check(self._lib.tfce_adjset_set_accumulation(self._h, code))
         self.accumulation = mode
 

@@ -80,6 +80,10 @@ constexpr int kBitmapMaxBytes = 48 * 1024;
 #ifndef TFGB_ALANES
 #define TFGB_ALANES 1
 #endif
+// path halving in the maxima-only form (no potential chains to preserve)
+#ifndef TFGB_MAX_HALVE
+#define TFGB_MAX_HALVE 0
+#endif
 constexpr int kSweepThreads = TFGB_SWEEP_THREADS;
 constexpr int kUBatch = TFGB_UBATCH;   // list entries of one vertex looked up together
 constexpr int kALanes = TFGB_ALANES;   // positions per thread per accumulation round
@@ -320,8 +324,18 @@ __device__ inline float block_max(float v, float* red) {
 // components) instead of O(active vertices); the result is the exact sum of
 // the same float increments, so it differs from the reference only by the
 // reference's own float summation error.
-template <bool kChecked, bool kLazy>
+//
+// kMaxOnly (with kLazy): only the scaled maxima are wanted and no vertex
+// weights apply.  Every vertex of a component gets the same increment from
+// the threshold it joins it on, so the largest TFCE in a component is the
+// largest sum accumulated by any of the components merged into it, plus the
+// merged component's own increments since: a root keeps that largest sum
+// (a linked root hands its sum to its final root by atomic max) and the
+// map's maximum is the largest sum among the last live roots.  No potentials
+// are kept, so there is no per-vertex resolve pass.
+template <bool kChecked, bool kLazy, bool kMaxOnly = false>
 __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_sweep_kernel(SweepArgs a) {
+  static_assert(!kMaxOnly || kLazy, "the maxima-only form is a per-component form");
   __shared__ float sT[kMaxSteps];
   __shared__ float sHH[kMaxSteps];
   __shared__ int32_t sCnt[kMaxSteps + 1];
@@ -338,7 +352,7 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
   // Per-component mode keeps every dead root's parent at the root it joined
   // (no path halving), so parent[] is also the chain of the potentials; the
   // exact mode halves paths.
-  constexpr bool kHalve = !kLazy;
+  constexpr bool kHalve = !kLazy || (kMaxOnly && TFGB_MAX_HALVE);
 #ifdef TFGB_PHASE_PROFILE
   long long _pt = clock64();
 #endif
@@ -691,7 +705,7 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
             const Rec rd = sl.rec[d[k]];
             sz[k] = rd.size;
             wd[k] = rd.w;
-            wr[k] = sl.rec[c[k]].w;
+            if constexpr (!kMaxOnly) wr[k] = sl.rec[c[k]].w;
           } else {
             sz[k] = ld_state(sl.size + d[k]);
           }
@@ -702,7 +716,11 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
           if constexpr (kLazy) atomicAdd(&sl.rec[c[k]].size, sz[k]);
           else atomicAdd(sl.size + c[k], sz[k]);
           if (c[k] != pd[k]) st_state(sl.parent + d[k], c[k]);
-          if constexpr (kLazy) {
+          if constexpr (kMaxOnly) {
+            // sums are >= 0, so their bit patterns order as the values do
+            atomicMax(reinterpret_cast<unsigned long long*>(&sl.rec[c[k]].w),
+                      static_cast<unsigned long long>(__double_as_longlong(wd[k])));
+          } else if constexpr (kLazy) {
             sl.rec[d[k]].w = wd[k] - wr[k];
           }
         }
@@ -818,6 +836,17 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
     }
 
     // ---- 4. scale, reduce, write
+    if constexpr (kMaxOnly) {
+      float best = (n_act < Vs) ? __fmul_rn(0.0f, scale) : -INFINITY;
+      const int32_t nr = sNRoots;
+      for (int32_t q = tid; q < nr; q += nth)
+        best = fmaxf(best, __fmul_rn(__double2float_rn(sl.rec[cur_roots[q]].w), scale));
+      best = block_max(best, sRed);
+      if (tid == 0 && a.out_max) a.out_max[item] = (best == -INFINITY) ? 0.0f : best;
+      __syncthreads();
+      TFGB_PHASE_MARK(5);
+      continue;
+    }
     if constexpr (kLazy) {
       // resolve every active vertex: sum of potentials along its parent chain
       for (int32_t p = tid; p < n_act; p += nth) {
@@ -925,6 +954,7 @@ struct tfce_adjset {
   float* d_enh = nullptr;
   int32_t run_cap = 0;
   int32_t accumulation = 0;  // 0: reference arithmetic, 1: per-component
+  bool no_max_only = false;  // accumulation 2: the potential form for maxima-only launches too
   int32_t* d_group = nullptr;  // threshold group of every segment, or NULL
   float* d_segmax = nullptr;   // segment maxima of the last grouped launch
   int64_t segmax_cap = 0;
@@ -1055,7 +1085,10 @@ int launch_sweep(tfce_adjset* h, const float* stats, int64_t map_stride, int32_t
     a.thr_group = h->d_group;
     a.seg_max = h->d_segmax;
   }
-  if (lazy) tfgb::tfce_sweep_kernel<false, true><<<slots, tfgb::kSweepThreads, bm, st>>>(a);
+  // maxima only, no vertex weights: the per-component form without potentials
+  const bool max_only = lazy && !vdensity && !out_maps && !labels && out_max && !h->no_max_only;
+  if (max_only) tfgb::tfce_sweep_kernel<false, true, true><<<slots, tfgb::kSweepThreads, bm, st>>>(a);
+  else if (lazy) tfgb::tfce_sweep_kernel<false, true><<<slots, tfgb::kSweepThreads, bm, st>>>(a);
   else tfgb::tfce_sweep_kernel<false, false><<<slots, tfgb::kSweepThreads, bm, st>>>(a);
   TFGB_CUDA(cudaGetLastError());
   return TFCE_OK;
@@ -1237,9 +1270,11 @@ int tfce_adjset_set_threshold_groups(tfce_adjset* h, const int32_t* group) {
 int tfce_adjset_set_accumulation(tfce_adjset* h, int32_t mode) {
   tfgb::clear_error();
   TFGB_CHECK_ARG(h != nullptr, "handle is NULL");
-  TFGB_CHECK_ARG(mode == 0 || mode == 1, "mode must be 0 (reference) or 1 (per-component)");
+  TFGB_CHECK_ARG(mode >= 0 && mode <= 2, "mode must be 0 (reference), 1 (per-component) or 2 (per-component, "
+                                          "potentials kept)");
   std::lock_guard<std::mutex> lk(h->mu);
-  h->accumulation = mode;
+  h->accumulation = mode == 0 ? 0 : 1;
+  h->no_max_only = (mode == 2);
   return TFCE_OK;
 }
 
