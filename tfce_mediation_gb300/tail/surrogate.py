@@ -68,7 +68,7 @@ def _image_maps(img, srt, tail, alpha, margin):
 
 
 def learned_fwer(eng, tfce_values, contrast, smoothness, E, alpha=0.05, margin=0.01, n_small=300,
-                 n_fallback=1700, seed=0, method="mlp", surrogate=None):
+                 n_fallback=1200, seed=0, method="mlp", surrogate=None):
     """1-p(FWER) of `tfce_values` (observed TFCE image, host) for one contrast
     of a PermutationEngine; returns (map, info)."""
     maps, info = learned_fwer_maps(eng, {contrast: tfce_values}, smoothness, E, alpha, margin, n_small,
@@ -76,7 +76,7 @@ def learned_fwer(eng, tfce_values, contrast, smoothness, E, alpha=0.05, margin=0
     return maps[contrast], info
 
 
-def learned_fwer_maps(eng, images, smoothness, E, alpha=0.05, margin=0.01, n_small=300, n_fallback=1700,
+def learned_fwer_maps(eng, images, smoothness, E, alpha=0.05, margin=0.01, n_small=300, n_fallback=1200,
                       seed=0, method="mlp", surrogate=None):
     """1-p(FWER) maps of several observed TFCE images at once.  images:
     {contrast index: image or list of images (e.g. the + and - images)}; the
