@@ -371,7 +371,7 @@ CONFIGS = {
                 "2 contrasts x +/- x 21 surfaces; icospheres one threshold group (H=2 E=1), skeleton (H=2 E=0.5)",
 }
 CONFIG_BATCH = {"config1": 512, "config3": 128, "config4a": 128, "config4b": 32}
-CONFIG_CPU_PERMS = {"config1": 10, "config3": 2, "config4a": 2, "config4b": 1}
+CONFIG_CPU_PERMS = {"config1": 200, "config3": 4, "config4a": 3, "config4b": 2}
 
 
 def _config_study(kind):

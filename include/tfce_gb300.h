@@ -16,7 +16,8 @@
  *   tm_func.calculate_tfce / low_ram_calculate_tfce  tfce_mediation/tm_func.py:54-185
  *                                                     -> tfce_sweep_batch
  *   tval_int + se_of_slope  tfce_mediation/cynumstats.pyx:47-64,
- *   calc_beta_se            tfce_mediation/cynumstats.pyx:66-74  -> glm_tstat
+ *   calc_beta_se            tfce_mediation/cynumstats.pyx:66-74  -> glm_tstat (FP32, permutations),
+ *                                                                   glm_stat_f64 (observed, helpers)
  *   calc_sobelz / calc_indirect  tfce_mediation/pyfunc.py:130-162,2678-2709
  *                                                     -> sobel_combine
  *   calculate_fweP_vertex.find_nearest  tfce_mediation/tmanalysis/calculate_fweP_vertex.py:37-69,
@@ -211,6 +212,18 @@ int glm_stat(const float* Y, int64_t ldy, int32_t n, int64_t V, const float* pin
              const float* X, const float* invdiag, const float* dof, int32_t G, int32_t kmax,
              const int32_t* coef, int32_t n_coef, int32_t what, float* out, int64_t ldo,
              void* stream);
+
+/* The same fit in FP64 with the reference's precision (the observed
+ * statistic and the one-off helpers): betas and sigma^2 in double from the
+ * float32 data, the SE rounded to float32 as se_of_slope stores it
+ * (tfce_mediation/cynumstats.pyx:47-52), t = double beta / that SE
+ * (tval_int, :59-64).  pinv [G][kmax][n], X [G][n][kmax], invdiag [G][kmax],
+ * dof [G] are double; what 0 = t, 1 = beta, 2 = SE; out [G][n_coef][ldo]
+ * double.  G <= 65535; 2 * kmax * n doubles must fit in 200 KB of shared
+ * memory (n <= 1600 at kmax = 8). */
+int glm_stat_f64(const float* Y, int64_t ldy, int32_t n, int64_t V, const double* pinv, const double* X,
+                 const double* invdiag, const double* dof, int32_t G, int32_t kmax, const int32_t* coef,
+                 int32_t n_coef, int32_t what, double* out, int64_t ldo, void* stream);
 
 /* Model F as calcF computes it (tfce_mediation/cynumstats.pyx:31-36):
  * ((TSS - RSS)/(k_g-1)) / (RSS/dof_g) with TSS taken around *centre (a device

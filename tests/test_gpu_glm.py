@@ -3,7 +3,11 @@ and the FP64 oracle.
 
 Tolerance (FP32 path): |t_gpu - t_ref| <= 1e-4 * max(1, |t_ref|), i.e. the
 relative tolerance of the FP32 path with an absolute floor for t near 0
-(the kernel accumulates n-term dot products in float32).
+(the kernel accumulates n-term dot products in float32).  FP64 path
+(tval_int, calc_beta_se, glm_stat_f64): t within 1e-6 relative of the
+reference's (the SE is rounded to float32 in both; only the order of the
+double sums differs, which can move that rounding by one float ulp), and
+most values exactly equal in float32.
 """
 import numpy as np
 import pytest
@@ -29,16 +33,19 @@ def test_tval_int(golden):
     X = np.column_stack([np.ones(n), x])
     t = cy.tval_int(X, np.linalg.inv(X.T @ X), y, n, X.shape[1], V)
     assert t.shape == golden["glm_tval_int"].shape and t.dtype == np.float64
-    assert_t_close(t, golden["glm_tval_int"])
+    ref = golden["glm_tval_int"]
+    np.testing.assert_allclose(t, ref, rtol=1e-6, atol=1e-12)
+    # cast to float32 as callers do before sweeping: almost every value is the reference's
+    assert np.mean(t.astype(np.float32) == ref.astype(np.float32)) >= 0.99
 
 
 def test_calc_beta_se_and_lstsqr(golden):
     y, x = golden["glm_y"], golden["glm_x"]
     n, V = y.shape
     b, se = cy.calc_beta_se(x[:, 0], y, n, V)
-    np.testing.assert_allclose(b, golden["glm_cbs_beta"], rtol=1e-4, atol=1e-5)
+    np.testing.assert_allclose(b, golden["glm_cbs_beta"], rtol=1e-10, atol=1e-12)
     assert se.dtype == np.float32
-    np.testing.assert_allclose(se, golden["glm_cbs_se"], rtol=1e-4)
+    np.testing.assert_allclose(se, golden["glm_cbs_se"], rtol=2e-7)
     X = np.column_stack([np.ones(n), x])
     np.testing.assert_allclose(cy.cy_lin_lstsqr_mat(X, y), golden["glm_lstsqr"], rtol=1e-4, atol=1e-5)
     a, rss = cy.cy_lin_lstsqr_mat_residual(X, y)

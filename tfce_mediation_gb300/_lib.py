@@ -64,6 +64,9 @@ SIGNATURES = {
     "glm_stat": (ctypes.c_int, [c_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int64, c_vp, c_vp,
                                 c_vp, c_vp, ctypes.c_int32, ctypes.c_int32, c_vp, ctypes.c_int32,
                                 ctypes.c_int32, c_vp, ctypes.c_int64, c_vp]),
+    "glm_stat_f64": (ctypes.c_int, [c_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int64, c_vp, c_vp, c_vp, c_vp,
+                                    ctypes.c_int32, ctypes.c_int32, c_vp, ctypes.c_int32, ctypes.c_int32, c_vp,
+                                    ctypes.c_int64, c_vp]),
     "glm_fstat": (ctypes.c_int, [c_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int64, c_vp, c_vp,
                                  c_vp, ctypes.c_int32, ctypes.c_int32, c_vp, c_vp, ctypes.c_int64,
                                  c_vp]),

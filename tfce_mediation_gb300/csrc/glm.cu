@@ -16,6 +16,8 @@
 // maps (tfce_mediation/pyfunc.py:146-161).
 #include <algorithm>
 
+#include <math_constants.h>
+
 #include "common.cuh"
 
 namespace tfgb {
@@ -181,6 +183,59 @@ int launch_glm_k(int tv, const float* Y, int64_t ldy, int32_t n, int64_t V, cons
   return TFCE_OK;
 }
 
+// FP64 form for the observed (unpermuted) statistic and the one-off helpers,
+// with the reference's precision: betas and sigma^2 in double from the float32
+// data, the SE rounded to float32 (se_of_slope stores it in a float32 array,
+// cynumstats.pyx:47-52) and t = double beta / that SE (tval_int, :59-64).
+// One thread per vertex, the design's pseudoinverse and rows in shared memory.
+template <int KMAX>
+__global__ void __launch_bounds__(256) glm_f64_kernel(
+    const float* __restrict__ Y, int64_t ldy, int32_t n, int64_t V, const double* __restrict__ pinv,
+    const double* __restrict__ X, const double* __restrict__ invdiag, const double* __restrict__ dof,
+    const int32_t* __restrict__ coef, int32_t n_coef, int32_t what, double* __restrict__ out, int64_t ldo) {
+  extern __shared__ double sm64[];
+  double* ps = sm64;              // [KMAX][n]
+  double* xs = sm64 + KMAX * n;   // [n][KMAX]
+  const int64_t g = blockIdx.y;
+  for (int i = threadIdx.x; i < KMAX * n; i += blockDim.x) {
+    ps[i] = pinv[g * KMAX * n + i];
+    xs[i] = X[g * n * KMAX + i];
+  }
+  __syncthreads();
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= V) return;
+  double b[KMAX];
+#pragma unroll
+  for (int j = 0; j < KMAX; ++j) b[j] = 0.0;
+  for (int s = 0; s < n; ++s) {
+    const double y = (double)Y[(int64_t)s * ldy + v];
+#pragma unroll
+    for (int j = 0; j < KMAX; ++j) b[j] = fma(ps[j * n + s], y, b[j]);
+  }
+  double rss = 0.0;
+  for (int s = 0; s < n; ++s) {
+    double r = (double)Y[(int64_t)s * ldy + v];
+#pragma unroll
+    for (int j = 0; j < KMAX; ++j) r = fma(-xs[s * KMAX + j], b[j], r);
+    rss = fma(r, r, rss);
+  }
+  const double sigma2 = rss / dof[g];
+  for (int c = 0; c < n_coef; ++c) {
+    const int j = coef[c];
+    double bj = 0.0;
+#pragma unroll
+    for (int jj = 0; jj < KMAX; ++jj)
+      if (jj == j) bj = b[jj];
+    double* dst = out + (g * n_coef + c) * ldo + v;
+    if (j < 0 || j >= KMAX) {
+      *dst = CUDART_NAN;
+      continue;
+    }
+    const double se = (double)__double2float_rn(sqrt(sigma2 * invdiag[g * KMAX + j]));
+    *dst = (what == kWhatBeta) ? bj : (what == kWhatSE) ? se : bj / se;
+  }
+}
+
 // Aroian (0), Sobel (1), Goodman (2) z from path t values, in double like
 // the reference's numpy expression, stored as float32.
 __global__ void sobel_combine_kernel(const float* __restrict__ ta, int64_t lda,
@@ -253,6 +308,43 @@ int glm_fstat(const float* Y, int64_t ldy, int32_t n, int64_t V, const float* pi
               const float* dof, int32_t G, int32_t kmax, const float* centre, float* f_out,
               int64_t ldf, void* stream) {
   return glm_stat(Y, ldy, n, V, pinv, X, centre, dof, G, kmax, nullptr, 0, 4, f_out, ldf, stream);
+}
+
+int glm_stat_f64(const float* Y, int64_t ldy, int32_t n, int64_t V, const double* pinv, const double* X,
+                 const double* invdiag, const double* dof, int32_t G, int32_t kmax, const int32_t* coef,
+                 int32_t n_coef, int32_t what, double* out, int64_t ldo, void* stream) {
+  tfgb::clear_error();
+  TFGB_CHECK_ARG(Y && pinv && X && dof && out && coef, "NULL pointer");
+  TFGB_CHECK_ARG(what >= 0 && what <= 2, "what must be 0 (t), 1 (beta) or 2 (se)");
+  TFGB_CHECK_ARG(what == 1 || invdiag, "invdiag is NULL");
+  TFGB_CHECK_ARG(n > 0 && V >= 0 && G >= 0 && n_coef >= 1, "bad sizes");
+  TFGB_CHECK_ARG(kmax >= 1 && kmax <= 8, "kmax must be in [1, 8]");
+  TFGB_CHECK_ARG(ldy >= V && ldo >= V, "leading dimension < V");
+  TFGB_CHECK_ARG(G < 65536, "at most 65535 designs per launch");
+  const size_t smem = sizeof(double) * 2 * (size_t)kmax * n;
+  if (smem > 200 * 1024) {
+    tfgb::set_error("n = %d subjects x %d columns exceeds the shared-memory design tile", n, kmax);
+    return TFCE_EINVAL;
+  }
+  if (V == 0 || G == 0) return TFCE_OK;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const dim3 grid(static_cast<unsigned>((V + 255) / 256), static_cast<unsigned>(G));
+  switch (kmax) {
+#define TFGB_K64(KK)                                                                                   \
+    case KK: {                                                                                         \
+      const size_t sm = sizeof(double) * 2 * KK * (size_t)n;                                           \
+      TFGB_CUDA(cudaFuncSetAttribute(tfgb::glm_f64_kernel<KK>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                     static_cast<int>(sm)));                                           \
+      tfgb::glm_f64_kernel<KK><<<grid, 256, sm, st>>>(Y, ldy, n, V, pinv, X, invdiag, dof, coef, n_coef, \
+                                                      what, out, ldo);                                 \
+      break;                                                                                           \
+    }
+    TFGB_K64(1) TFGB_K64(2) TFGB_K64(3) TFGB_K64(4) TFGB_K64(5) TFGB_K64(6) TFGB_K64(7) TFGB_K64(8)
+#undef TFGB_K64
+    default: break;
+  }
+  TFGB_CUDA(cudaGetLastError());
+  return TFCE_OK;
 }
 
 int sobel_combine(const float* ta, int64_t lda, const float* ta_scalar, const float* tb,

@@ -80,12 +80,6 @@ constexpr int kBitmapMaxBytes = 48 * 1024;
 #ifndef TFGB_ALANES
 #define TFGB_ALANES 1
 #endif
-// Per-component forms: each newly bucketed vertex's list (up to 8 entries,
-// 32 bytes) copied to its position, so the union phase reads it in one
-// coalesced load instead of a packed list start and then the list
-#ifndef TFGB_POSLIST
-#define TFGB_POSLIST 0
-#endif
 // path halving in the maxima-only form (no potential chains to preserve)
 #ifndef TFGB_MAX_HALVE
 #define TFGB_MAX_HALVE 0
@@ -100,7 +94,6 @@ constexpr int kSLanes = TFGB_SLANES;   // dead roots per thread per size round
 constexpr uint32_t kOneWay = 0x80000000u;   // entry whose reverse entry is missing
 constexpr uint32_t kIndexMask = 0x7fffffffu;
 constexpr uint32_t kInactiveKey = 0xffffffffu;
-constexpr uint32_t kUseCsr = 0xfffffffeu;   // position list: the vertex has more than 8 entries
 constexpr int kPosBits = 24;                 // key = step << 24 | position
 constexpr int32_t kMaxSegVertices = (1 << kPosBits) - 1;
 constexpr int kWalkLimit = 1 << 26;
@@ -168,7 +161,6 @@ struct Slot {
   int32_t* roots_a;  // live roots after the previous threshold ...
   int32_t* roots_b;  // ... and after this one (swapped every step)
   Rec* rec;          // {W, extent} per position
-  uint32_t* plist;   // 8 list entries per position (TFGB_POSLIST)
 };
 
 __host__ __device__ inline int64_t align_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
@@ -180,8 +172,7 @@ __host__ __device__ inline int64_t slot_bytes(int32_t vcap) {
 // Per-component accumulation adds two root lists and a 16-byte {W, extent}
 // record per vertex to the six int32/float arrays of the exact mode.
 __host__ __device__ inline int64_t slot_bytes_lazy(int32_t vcap) {
-  return 8 * align_up((int64_t)vcap * 4, 256) + align_up((int64_t)vcap * 16, 256) +
-         (TFGB_POSLIST ? align_up((int64_t)vcap * 32, 256) : 0);
+  return 8 * align_up((int64_t)vcap * 4, 256) + align_up((int64_t)vcap * 16, 256);
 }
 
 __device__ inline Slot make_slot(char* base, int32_t vcap) {
@@ -190,7 +181,6 @@ __device__ inline Slot make_slot(char* base, int32_t vcap) {
   sl.roots_a = reinterpret_cast<int32_t*>(base + 6 * s);
   sl.roots_b = reinterpret_cast<int32_t*>(base + 7 * s);
   sl.rec = reinterpret_cast<Rec*>(base + 8 * s);
-  sl.plist = reinterpret_cast<uint32_t*>(base + 8 * s + align_up((int64_t)vcap * 16, 256));
   sl.key = reinterpret_cast<uint32_t*>(base);
   sl.order = reinterpret_cast<int32_t*>(base + s);
   sl.parent = reinterpret_cast<int32_t*>(base + 2 * s);
@@ -503,19 +493,8 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
           // position, so the union phase reads it without a dependent load;
           // -1: out of the packed range, read the offsets
           const int64_t e0 = a.offsets[v0 + v], deg = a.offsets[v0 + v + 1] - e0, rel = e0 - seg_e0;
-#if TFGB_POSLIST
-          uint32_t ent[8];
-#pragma unroll
-          for (int j = 0; j < 8; ++j) ent[j] = (j < deg) ? a.indices[e0 + j] : kIndexMask;
-          if (deg > 8) ent[0] = kUseCsr;
-          uint4* dst = reinterpret_cast<uint4*>(sl.plist + (int64_t)p * 8);
-          dst[0] = make_uint4(ent[0], ent[1], ent[2], ent[3]);
-          dst[1] = make_uint4(ent[4], ent[5], ent[6], ent[7]);
-          (void)rel;
-#else
           reinterpret_cast<int32_t*>(sl.acc)[p] =
               (deg <= 63 && rel >= 0 && rel < (int64_t(1) << 25)) ? static_cast<int32_t>((rel << 6) | deg) : -1;
-#endif
         } else {
           sl.size[p] = 1;
           sl.acc[p] = (a.out_mode == 2 && omap) ? omap[v] : 0.0f;
@@ -545,29 +524,15 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
       // shared cursor, so threads with short walks do not wait for slow ones
       for (int32_t p = atomicAdd(&sGrab, 1); p < s1; p = atomicAdd(&sGrab, 1)) {
         int32_t v = -1;  // the vertex: read when needed
-        int64_t e0 = 0, e1 = 0;
-        const uint32_t* src = a.indices;  // list entries src[e0, e1)
-        bool csr = true;
-#if TFGB_POSLIST
-        if constexpr (kLazy) {
-          const uint32_t* pl = sl.plist + (int64_t)p * 8;
-          if (pl[0] != kUseCsr) {
-            src = pl;
-            e1 = 8;
-            csr = false;
-          }
-        }
-#endif
-        if (csr) {
-          const int32_t pk = (kLazy && !TFGB_POSLIST) ? reinterpret_cast<const int32_t*>(sl.acc)[p] : -1;
-          if (pk >= 0) {
-            e0 = seg_e0 + (pk >> 6);
-            e1 = e0 + (pk & 63);
-          } else {
-            v = sl.order[p];
-            e0 = a.offsets[v0 + v];
-            e1 = a.offsets[v0 + v + 1];
-          }
+        int64_t e0, e1;
+        const int32_t pk = kLazy ? reinterpret_cast<const int32_t*>(sl.acc)[p] : -1;
+        if (pk >= 0) {
+          e0 = seg_e0 + (pk >> 6);
+          e1 = e0 + (pk & 63);
+        } else {
+          v = sl.order[p];
+          e0 = a.offsets[v0 + v];
+          e1 = a.offsets[v0 + v + 1];
         }
         if constexpr (kChecked) {
           if (e0 < 0 || e1 > a.n_entries || e1 < e0) {
@@ -576,21 +541,18 @@ __global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_swee
           }
         }
         int32_t rp = p;
-        bool listed = false;  // the list's last entry has been read
-        for (int64_t eb = e0; eb < e1 && !listed; eb += kUBatch) {
+        for (int64_t eb = e0; eb < e1; eb += kUBatch) {
           uint32_t raw[kUBatch], ka[kUBatch];
           int32_t an[kUBatch];
 #pragma unroll
-          for (int k = 0; k < kUBatch; ++k) raw[k] = (eb + k < e1) ? src[eb + k] : kIndexMask;
-          // a position list ends at its first unused entry (kIndexMask)
-          listed = !csr && raw[kUBatch - 1] == kIndexMask;
+          for (int k = 0; k < kUBatch; ++k) raw[k] = (eb + k < e1) ? a.indices[eb + k] : kIndexMask;
           TFGB_COUNT(5, (e1 - eb < kUBatch) ? (e1 - eb) : kUBatch);
 #pragma unroll
           for (int k = 0; k < kUBatch; ++k) {
             const int64_t ag = static_cast<int64_t>(raw[k] & kIndexMask) - v0;
             an[k] = static_cast<int32_t>(ag);
             ka[k] = kInactiveKey;
-            if (eb + k < e1 && (csr || raw[k] != kIndexMask)) {
+            if (eb + k < e1) {
               // a caller's negative int32 entry has bit 31 set: rejected, not masked
               if (ag < 0 || ag >= Vs || (kChecked && (raw[k] & kOneWay))) set_err(a.err, kDevBadIndex);
               else if (!use_bm || ((sAct[an[k] >> 5] >> (an[k] & 31)) & 1u)) ka[k] = sl.key[an[k]];

@@ -1,17 +1,19 @@
 """Drop-in for ``tfce_mediation.cynumstats`` (tfce_mediation/cynumstats.pyx).
 
-Same names, arguments and return shapes; the n x V work runs in the
-``glm_stat`` kernel on the GPU in float32 (the reference computes betas and
-sigma^2 in float64 and rounds SE to float32, cynumstats.pyx:47-52).  Results
-come back as host float64 arrays like the reference's, except ``se`` outputs,
-which the reference itself returns as float32.
+Same names, arguments and return shapes; the n x V work runs on the GPU.
+``tval_int`` and ``calc_beta_se`` use the FP64 kernel (``glm_stat_f64``)
+with the reference's precision: betas and sigma^2 in float64, SE rounded to
+float32 (cynumstats.pyx:47-52), t = beta / SE.  The other helpers use the
+float32 kernel (``glm_stat``).  Results come back as host float64 arrays like
+the reference's, except ``se`` outputs, which the reference itself returns as
+float32.
 """
 from __future__ import annotations
 
 import numpy as np
 
 from .gd_fwhm import calc_gd_fwhm  # noqa: F401  (cynumstats.pyx:76-107, on the GPU)
-from .glm import WHAT_BETA, WHAT_RESID, WHAT_RSS, WHAT_SE, WHAT_T, DesignBatch, glm_fstat, glm_stat
+from .glm import WHAT_BETA, WHAT_RESID, WHAT_RSS, WHAT_SE, WHAT_T, DesignBatch, glm_fstat, glm_stat, glm_stat_f64
 
 
 def _as_2d(y):
@@ -41,7 +43,7 @@ def tval_int(X, invXX, y, n, k, numvoxel):
     db = DesignBatch([X], invXX=np.asarray(invXX, np.float64)[None])
     if db.dof[0] != n - k:
         db.dof[0] = n - k
-    out = glm_stat(y2.astype(np.float32), db, WHAT_T)[0]
+    out = glm_stat_f64(y2.astype(np.float32), db, WHAT_T)[0]
     return _host(out, sq)
 
 
@@ -52,8 +54,8 @@ def calc_beta_se(x, y, n, num_voxel):
     y2, sq = _as_2d(y)
     Yf = y2.astype(np.float32)
     db = DesignBatch([X])
-    beta = glm_stat(Yf, db, WHAT_BETA, coef=[1])[0, 0]
-    se = glm_stat(Yf, db, WHAT_SE)[0]
+    beta = glm_stat_f64(Yf, db, WHAT_BETA, coef=[1])[0, 0]
+    se = glm_stat_f64(Yf, db, WHAT_SE)[0]
     b = beta.to("cpu").numpy().astype(np.float64)
     s = se.to("cpu").numpy().astype(np.float32)
     return (b[0], s[:, 0]) if sq else (b, s)

@@ -418,9 +418,15 @@ class PermutationEngine:
         (write_vertStat_img's TFCE image, pyfunc.py:80-92)."""
         t = self.t
         db = DesignBatch(self.X[None])
-        tm = t.empty((1, self.C, self.V), device="cuda", dtype=t.float32)
-        # the observed map: FP32 CUDA-core t (programmed outputs exist on the tensor-core GLM only)
-        self.tmaps(db, out=tm, precision="fp32" if self.outputs is None else None)
+        if self.outputs is None:
+            # the observed map in FP64 with the reference's precision (tval_int): it is the
+            # image the reference writes and compares against its null
+            from .glm import WHAT_T, glm_stat_f64
+            tm = glm_stat_f64(self.Yd, db, WHAT_T, coef=self.contrasts).float().contiguous()
+        else:
+            # programmed outputs exist on the tensor-core GLM only
+            tm = t.empty((1, self.C, self.V), device="cuda", dtype=t.float32)
+            self.tmaps(db, out=tm)
         maps = t.empty((self.C, self.signs, self.V), device="cuda", dtype=t.float32)
         mx = t.empty((self.C, self.signs, self.n_seg), device="cuda", dtype=t.float32)
         # the observed image is swept once: use the reference's exact arithmetic
@@ -484,7 +490,7 @@ class MediationEngine:
                                        reorder=False, accumulation=accumulation, precision=precision,
                                        threshold_groups=threshold_groups)
         self.t = self.inner.t
-        self.medtype, self.alg_code, self.batch = medtype, ALG[alg], int(batch)
+        self.medtype, self.alg, self.alg_code, self.batch = medtype, alg, ALG[alg], int(batch)
         self.pred_x = np.asarray(pred_x, np.float64)
         self.depend_y = np.asarray(depend_y, np.float64)
         self.cov = None if covariates is None else np.asarray(covariates, np.float64)
@@ -551,8 +557,10 @@ class MediationEngine:
     def observed(self):
         """Unpermuted z map (V,) and scaled TFCE map (V,) on the host."""
         t = self.t
-        ident = np.arange(self.n)[None]
-        z = self.zmaps(ident)[:1]
+        from .pyfunc import sobel_z_device
+        # the observed z from FP64 path t maps (the reference's precision)
+        z = sobel_z_device(self.medtype, self.pred_x, self.depend_y, self.inner.Yd, self.n,
+                           alg=self.alg, covariates=self.cov)
         maps = t.empty((1, 1, self.V), device="cuda", dtype=t.float32)
         mx = t.empty((1, 1, self.n_seg), device="cuda", dtype=t.float32)
         adj = self.inner.adj

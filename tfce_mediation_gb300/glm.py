@@ -169,6 +169,29 @@ def glm_stat(Y, designs, what=WHAT_T, coef=None, out=None, stream=None):
     return out
 
 
+def glm_stat_f64(Y, designs, what=WHAT_T, coef=None, stream=None):
+    """t (what=WHAT_T), betas or SE of every design in FP64 with the
+    reference's precision (glm_stat_f64: double betas and sigma^2, SE rounded
+    to float32 as se_of_slope stores it, t = beta / SE); a CUDA float64 tensor
+    (G, n_coef, V).  Used for the observed statistic and the one-off helpers,
+    where the map is compared with the reference's own."""
+    t = require_cuda()
+    if what not in (WHAT_T, WHAT_BETA, WHAT_SE):
+        raise ValueError("glm_stat_f64 computes t, betas or SE")
+    Yd = dev(Y, t.float32)
+    n, V = Yd.shape
+    db = designs if isinstance(designs, DesignBatch) else DesignBatch(designs)
+    if db.n != n:
+        raise ValueError(f"design has {db.n} rows, data has {n}")
+    coef = list(range(db.kmax)) if coef is None else list(coef)
+    out = t.empty((db.G, len(coef), V), device="cuda", dtype=t.float64)
+    _lib.check(_lib.load().glm_stat_f64(ptr(Yd), V, n, V, ptr(dev(db.pinv64, t.float64)), ptr(dev(db.X64, t.float64)),
+                                        ptr(dev(db.invdiag64, t.float64)), ptr(dev(db.dof, t.float64)), db.G, db.kmax,
+                                        ptr(dev(np.asarray(coef, np.int32))), len(coef), what, ptr(out), V,
+                                        stream_handle(stream)))
+    return out
+
+
 def glm_fstat(Y, designs, centre=None, stream=None):
     """Model F (G, V) with TSS around `centre` (None: each column's mean)."""
     t = require_cuda()

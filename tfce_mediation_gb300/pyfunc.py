@@ -24,7 +24,7 @@ import numpy as np
 from . import _lib
 from .adjacency import create_adjac_vertex, create_adjac_voxel  # noqa: F401
 from .device import dev, ptr, require_cuda, stream_handle
-from .glm import WHAT_T, DesignBatch, glm_stat
+from .glm import WHAT_T, DesignBatch, glm_stat, glm_stat_f64
 from .io import save_mgh, save_nifti
 from .rm_anova import column_product, dummy_code, stack_ones  # noqa: F401  (pyfunc.py:2564-2676)
 
@@ -170,16 +170,22 @@ def sobel_from_t(ta, tb, alg="aroian", ta_scalar=None):
     return z
 
 
-def sobel_z_device(medtype, pred_x, depend_y, Y, n, alg="aroian"):
+def sobel_z_device(medtype, pred_x, depend_y, Y, n, alg="aroian", precision="fp64", covariates=None):
     """Indirect-effect z of the data Y (n, V) as a device tensor (1, V): the
-    path-a and path-b t maps in one GLM launch, then sobel_combine."""
+    path-a and path-b t maps in one GLM launch (FP64 with the reference's
+    precision by default, or 'fp32'), then sobel_combine."""
     if alg not in ALG:
         raise ValueError("Unknown indirect test algorithm")
-    Xa, Xb, ta_scalar = mediation_designs(medtype, pred_x, depend_y, n)
+    Xa, Xb, ta_scalar = mediation_designs(medtype, pred_x, depend_y, n, covariates=covariates)
+
+    def tmap(designs):
+        if precision == "fp64":
+            return glm_stat_f64(Y, DesignBatch(designs), WHAT_T, coef=[1])[:, 0].float().contiguous()
+        return glm_stat(Y, DesignBatch(designs), WHAT_T, coef=[1])[:, 0]
     if ta_scalar is None:
-        tab = glm_stat(Y, DesignBatch([Xa, Xb]), WHAT_T, coef=[1])[:, 0]
+        tab = tmap([Xa, Xb])
         return sobel_from_t(tab[0:1], tab[1:2], alg)
-    tb = glm_stat(Y, DesignBatch([Xb]), WHAT_T, coef=[1])[:, 0]
+    tb = tmap([Xb])
     return sobel_from_t(None, tb, alg, ta_scalar=[ta_scalar])
 
 

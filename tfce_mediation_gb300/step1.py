@@ -14,8 +14,8 @@ names, formats and max_TFCE_contrast_values.csv lines.
   data_mask, affine_mask), output/{neg,}tstat_con<j>{,_TFCE}.nii.gz, or
   fstat{,_TFCE}.nii.gz for the F-test (write_voxelStat_img, pyfunc.py:94-103).
 
-The statistic maps use the FP32 GLM (~1e-6 of the reference's FP64) and the
-reference's sweep arithmetic (bit-identical sweeps of the same map).  Each
+The statistic maps use the FP64 GLM with the reference's precision
+(glm_stat_f64) and the reference's sweep arithmetic (bit-identical sweeps of the same map).  Each
 TFCE image is scaled by the max of its own statistic / 100 (and the vertex
 density weights), as the reference's writers do.
 """
@@ -27,7 +27,7 @@ import numpy as np
 
 from .adjacency import AdjacencySet, to_csr
 from .device import dev, ptr, require_cuda, stream_handle
-from .glm import WHAT_T, DesignBatch, glm_fstat, glm_stat
+from .glm import WHAT_T, DesignBatch, glm_fstat, glm_stat_f64
 from .pyfunc import vert_stat_images, voxel_stat_images
 from .randomise import _hemispheres, _load, _vd
 
@@ -61,7 +61,7 @@ def vertex_observed_run(surface, outdir=None):
     X = np.column_stack([np.ones(n), pred_x])
     k = X.shape[1]
     coefs = list(range(1, k))
-    tm = glm_stat(merge_y, DesignBatch([X]), WHAT_T, coef=coefs)[0]  # (C, V)
+    tm = glm_stat_f64(merge_y, DesignBatch([X]), WHAT_T, coef=coefs)[0].float().contiguous()  # (C, V)
     adj = AdjacencySet((off, idx), float(optstfce[0]), float(optstfce[1]), seg)
     maps = _sweep_maps(adj, tm, len(coefs), 2, vd)
     tv = tm.cpu().numpy().astype(np.float64)
@@ -117,7 +117,7 @@ def voxel_observed_run(temp="python_temp", outdir="output", imgext=".nii.gz"):
             os.chdir(cwd)
         return fv[None], maps
     coefs = list(range(1, k))
-    tm = glm_stat(ny, DesignBatch([X]), WHAT_T, coef=coefs)[0]
+    tm = glm_stat_f64(ny, DesignBatch([X]), WHAT_T, coef=coefs)[0].float().contiguous()
     tm[tm.isnan()] = 0.0
     maps = _sweep_maps(adj, tm, len(coefs), 2)
     tv = tm.cpu().numpy().astype(np.float64)

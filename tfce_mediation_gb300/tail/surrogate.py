@@ -121,4 +121,5 @@ def learned_fwer_maps(eng, images, smoothness, E, alpha=0.05, margin=0.01, n_sma
         used += n_fallback
     torch.cuda.synchronize()
     res = {c: (m if isinstance(images[c], (list, tuple)) else m[0]) for c, m in out.items()}
-    return res, {"perms": used, "seconds": time.perf_counter() - t0, "near_alpha": n_near, "tail": tails}
+    return res, {"perms": used, "seconds": time.perf_counter() - t0, "near_alpha": n_near, "tail": tails,
+                 "fallback_vertices": near_any}

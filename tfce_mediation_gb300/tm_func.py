@@ -36,7 +36,7 @@ from .adjacency import AdjacencySet, concat_csr, induced_csr
 from .adjacency import merge_adjacency_array  # noqa: F401
 from .device import dev, ptr, require_cuda, stream_handle
 from .fwer import apply_mfwer as _apply_mfwer_gpu
-from .glm import WHAT_T, DesignBatch, glm_stat
+from .glm import WHAT_T, DesignBatch, glm_stat_f64
 from .pyfunc import sobel_z_device
 
 
@@ -154,7 +154,10 @@ def _study_for(ops, groups_of_ops, masking_array, fullmask_of):
 
 
 def _tmaps(merge_y, X, coefs):
-    return glm_stat(_data_dev(merge_y), DesignBatch([X]), WHAT_T, coef=coefs)  # (1, C, V)
+    """t maps (1, C, V) float32 on the device, computed in FP64 with the
+    reference's precision (tval_int) and cast to float32 as the reference
+    casts them before sweeping (tm_func.py:64)."""
+    return glm_stat_f64(_data_dev(merge_y), DesignBatch([X]), WHAT_T, coef=coefs).float().contiguous()
 
 
 def _perm_design(X, perm_number, randomise, perm_seed=None, clock=True):
