@@ -76,6 +76,11 @@ int tfce_adjset_set_params(tfce_adjset* h, const float* H, const float* E);
 /* 1 if every entry has its reverse (the usual triangle-mesh / 26-neighbour
  * case), 0 otherwise. */
 int tfce_adjset_is_symmetric(const tfce_adjset* h);
+/* CTA shape of the per-component sweeps (tfce_sweep_batch with
+ * accumulation 1 or 2): 3 resident CTAs of 512 threads per SM (40 registers,
+ * the most sweeps in flight; the default) or 2 (64 registers, no spills).
+ * The autotuner picks it per study together with the batch size. */
+int tfce_adjset_set_sweep_shape(tfce_adjset* h, int32_t ctas_per_sm);
 /* Threshold groups of tfce_sweep_batch: group [n_seg] (host; ids in
  * [0, n_seg)), or NULL to give every segment its own table again.  Segments
  * of one group share one threshold table per (map, sign), built from the

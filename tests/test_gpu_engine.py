@@ -132,3 +132,20 @@ def test_run_stream_with_new_data_per_step(config1):
     np.testing.assert_allclose(got[1], e2.run(perms=perms[8:16]), rtol=1e-6)
     np.testing.assert_allclose(got[2], e2.run(perms=perms[16:24]), rtol=1e-6)
     np.testing.assert_allclose(got[3], e1.run(perms=perms[24:29]), rtol=1e-6)
+
+
+def test_sweep_shapes_agree(config1):
+    """The two CTA shapes of the per-component sweep (3 x 512 threads per SM,
+    40 registers; 2 x 512, 64 registers) give the same maxima."""
+    import torch
+    st = config1
+    eng = E.PermutationEngine(st.Y, st.pred_x, (st.offsets, st.indices), st.segments, 2.0, 1.0, batch=32,
+                              floor_zero=True)
+    perms = E.permutations(st.n, 3, 0, 32)
+    res = []
+    for shape in (3, 2):
+        eng.adj.set_sweep_shape(shape)
+        res.append(eng.run(perms=perms))
+    np.testing.assert_allclose(res[0], res[1], rtol=1e-6)
+    with pytest.raises(Exception):
+        eng.adj.set_sweep_shape(4)

@@ -46,6 +46,7 @@ SIGNATURES = {
     "tfce_adjset_set_params": (ctypes.c_int, [c_vp, c_f32p, c_f32p]),
     "tfce_adjset_is_symmetric": (ctypes.c_int, [c_vp]),
     "tfce_adjset_set_threshold_groups": (ctypes.c_int, [c_vp, c_i32p]),
+    "tfce_adjset_set_sweep_shape": (ctypes.c_int, [c_vp, ctypes.c_int32]),
     "tfce_adjset_set_accumulation": (ctypes.c_int, [c_vp, ctypes.c_int32]),
     "tfce_adjset_run": (ctypes.c_int, [c_vp, c_f32p, c_f32p, ctypes.c_int32]),
     "tfce_adjset_run_labels": (ctypes.c_int, [c_vp, c_f32p, c_f32p, ctypes.c_int32, c_i32p, c_i32p,

@@ -338,6 +338,12 @@ class AdjacencySet:
         _lib.check(self._lib.tfce_adjset_set_threshold_groups(self._h, _lib.ptr(g, _lib.c_i32p)))
         self.threshold_groups = g.copy()
 
+    def set_sweep_shape(self, ctas_per_sm: int):
+        """Resident CTAs per SM of the per-component sweeps: 3 (40 registers,
+        most items in flight) or 2 (64 registers, no spills)."""
+        _lib.check(self._lib.tfce_adjset_set_sweep_shape(self._h, int(ctas_per_sm)))
+        self.ctas_per_sm = int(ctas_per_sm)
+
     def set_accumulation(self, mode: str):
         """'exact' (the reference's float arithmetic, bit-identical),
         'component' (per-component double accumulation for batched sweeps;

@@ -1,11 +1,15 @@
-"""Choice of P (permutations per launch) for a permutation engine.
+"""Choice of P (permutations per launch) and of the sweep's CTA shape for a
+permutation engine.
 
-Each candidate P is timed on the device (CUDA events, after a warm-up launch)
-for the GLM + sweep of one batch; the one with the highest permutations per
-second wins.  Good values fill the persistent sweep grid evenly: one launch
-has P x contrasts x signs x segments sweep items spread over the resident
-CTAs (tfce_sweep_resident_slots), so P where that count is a multiple of the
-CTA count avoids a ragged last wave.  Results are cached per (GPU, n, k, V,
+Each candidate (P, CTAs per SM) is timed on the device (CUDA events, after a
+warm-up launch) for the GLM + sweep of one batch; the one with the highest
+permutations per second wins.  The sweep runs 3 CTAs of 512 threads per SM
+(40 registers, the most items in flight) or 2 (64 registers, no spills);
+which is faster depends on the segments' sizes and list lengths.  Good
+values of P fill the persistent sweep grid evenly: one launch has P x
+contrasts x signs x segments sweep items spread over the resident CTAs
+(tfce_sweep_resident_slots), so P where that count is a multiple of the CTA
+count avoids a ragged last wave.  Results are cached per (GPU, n, k, V,
 entries, segments, contrasts, signs, precision) in
 ~/.cache/tfce_mediation_gb300/autotune.json.
 """
@@ -85,21 +89,27 @@ def time_batch(eng, P, seed=12345, repeats=3):
     return a.elapsed_time(b) / repeats
 
 
-def choose_batch(eng, max_p=256, use_cache=True):
-    """Best P for this engine's problem (cached)."""
+def choose_batch(eng, max_p=256, use_cache=True, shapes=(3, 2)):
+    """Best P and sweep CTA shape for this engine's problem (cached); the
+    shape is set on the engine's adjacency handle, P is returned."""
     key = _key(eng)
     cache = _load() if use_cache else {}
-    if key in cache:
+    if key in cache and "ctas_per_sm" in cache[key]:
+        eng.adj.set_sweep_shape(int(cache[key]["ctas_per_sm"]))
         return int(cache[key]["P"])
     results = {}
-    for P in candidates(eng, max_p):
-        try:
-            ms = time_batch(eng, P)
-        except RuntimeError:
-            continue
-        results[P] = P / ms * 1000.0
-    best = max(results, key=results.get)
-    cache[key] = {"P": best, "perm_per_s": results}
+    for shape in shapes:
+        eng.adj.set_sweep_shape(shape)
+        for P in candidates(eng, max_p):
+            try:
+                ms = time_batch(eng, P)
+            except RuntimeError:
+                continue
+            results[(shape, P)] = P / ms * 1000.0
+    shape, best = max(results, key=results.get)
+    eng.adj.set_sweep_shape(shape)
+    cache[key] = {"P": best, "ctas_per_sm": shape,
+                  "perm_per_s": {f"{s}x{p}": v for (s, p), v in results.items()}}
     if use_cache:
         _save(cache)
     return best

@@ -333,8 +333,12 @@ __device__ inline float block_max(float v, float* red) {
 // (a linked root hands its sum to its final root by atomic max) and the
 // map's maximum is the largest sum among the last live roots.  No potentials
 // are kept, so there is no per-vertex resolve pass.
-template <bool kChecked, bool kLazy, bool kMaxOnly = false>
-__global__ void __launch_bounds__(kSweepThreads, TFGB_SWEEP_MINBLOCKS) tfce_sweep_kernel(SweepArgs a) {
+//
+// kMinBlocks: resident CTAs per SM the register budget is cut for (3: 40
+// registers with a few spills, the most items in flight; 2: 64 registers, no
+// spills) -- the sweep's CTA shape, chosen per study by the autotuner.
+template <bool kChecked, bool kLazy, bool kMaxOnly = false, int kMinBlocks = TFGB_SWEEP_MINBLOCKS>
+__global__ void __launch_bounds__(kSweepThreads, kMinBlocks) tfce_sweep_kernel(SweepArgs a) {
   static_assert(!kMaxOnly || kLazy, "the maxima-only form is a per-component form");
   __shared__ float sT[kMaxSteps];
   __shared__ float sHH[kMaxSteps];
@@ -955,6 +959,7 @@ struct tfce_adjset {
   int32_t run_cap = 0;
   int32_t accumulation = 0;  // 0: reference arithmetic, 1: per-component
   bool no_max_only = false;  // accumulation 2: the potential form for maxima-only launches too
+  int32_t ctas_per_sm = TFGB_SWEEP_MINBLOCKS;  // sweep CTA shape of the per-component launches (3 or 2)
   int32_t* d_group = nullptr;  // threshold group of every segment, or NULL
   float* d_segmax = nullptr;   // segment maxima of the last grouped launch
   int64_t segmax_cap = 0;
@@ -995,8 +1000,12 @@ int resident_slots(tfce_adjset* h) {
   if (h->max_slots) return TFCE_OK;
   int sms = 0, per_sm = 0;
   TFGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
-  TFGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tfgb::tfce_sweep_kernel<false, false>,
-                                                          tfgb::kSweepThreads, tfgb::bitmap_bytes(h->vmax_seg)));
+  if (h->ctas_per_sm == 2)
+    TFGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tfgb::tfce_sweep_kernel<false, true, true, 2>,
+                                                            tfgb::kSweepThreads, tfgb::bitmap_bytes(h->vmax_seg)));
+  else
+    TFGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tfgb::tfce_sweep_kernel<false, false>,
+                                                            tfgb::kSweepThreads, tfgb::bitmap_bytes(h->vmax_seg)));
   h->max_slots = std::max(1, sms * std::max(1, per_sm));
   // tuning knob: fewer CTAs in flight (smaller L2 working set)
   if (const char* env = std::getenv("TFCE_SWEEP_MAX_CTAS")) {
@@ -1087,7 +1096,10 @@ int launch_sweep(tfce_adjset* h, const float* stats, int64_t map_stride, int32_t
   }
   // maxima only, no vertex weights: the per-component form without potentials
   const bool max_only = lazy && !vdensity && !out_maps && !labels && out_max && !h->no_max_only;
-  if (max_only) tfgb::tfce_sweep_kernel<false, true, true><<<slots, tfgb::kSweepThreads, bm, st>>>(a);
+  const bool two = (h->ctas_per_sm == 2);
+  if (max_only && two) tfgb::tfce_sweep_kernel<false, true, true, 2><<<slots, tfgb::kSweepThreads, bm, st>>>(a);
+  else if (max_only) tfgb::tfce_sweep_kernel<false, true, true><<<slots, tfgb::kSweepThreads, bm, st>>>(a);
+  else if (lazy && two) tfgb::tfce_sweep_kernel<false, true, false, 2><<<slots, tfgb::kSweepThreads, bm, st>>>(a);
   else if (lazy) tfgb::tfce_sweep_kernel<false, true><<<slots, tfgb::kSweepThreads, bm, st>>>(a);
   else tfgb::tfce_sweep_kernel<false, false><<<slots, tfgb::kSweepThreads, bm, st>>>(a);
   TFGB_CUDA(cudaGetLastError());
@@ -1251,6 +1263,18 @@ int tfce_adjset_set_params(tfce_adjset* h, const float* H, const float* E) {
 }
 
 int tfce_adjset_is_symmetric(const tfce_adjset* h) { return (h && h->symmetric) ? 1 : 0; }
+
+int tfce_adjset_set_sweep_shape(tfce_adjset* h, int32_t ctas_per_sm) {
+  tfgb::clear_error();
+  TFGB_CHECK_ARG(h != nullptr, "handle is NULL");
+  TFGB_CHECK_ARG(ctas_per_sm == 2 || ctas_per_sm == 3, "ctas_per_sm must be 2 or 3");
+  std::lock_guard<std::mutex> lk(h->mu);
+  if (h->ctas_per_sm != ctas_per_sm) {
+    h->ctas_per_sm = ctas_per_sm;
+    h->max_slots = 0;  // recomputed for the new shape at the next launch
+  }
+  return TFCE_OK;
+}
 
 int tfce_adjset_set_threshold_groups(tfce_adjset* h, const int32_t* group) {
   tfgb::clear_error();
