@@ -48,8 +48,9 @@ class GeodesicSmoother:
             raise ValueError("one distance per pair")
         self.off, self.src, self.pidx = dev(off), dev(src), dev(pidx)
         self.w = t.empty(self.M + 1, device="cuda", dtype=t.float32)
-        _lib.check(self.lib.gd_fwhm_weights(ptr(dev(dist)) if self.M else None, self.M, float(np.float32(sigma)),
-                                            ptr(self.w), stream_handle()))
+        dist_d = dev(dist) if self.M else None  # referenced until the launch is queued
+        _lib.check(self.lib.gd_fwhm_weights(ptr(dist_d), self.M, float(np.float32(sigma)), ptr(self.w),
+                                            stream_handle()))
         self.err = t.zeros(1, device="cuda", dtype=t.int32)
 
     def smooth(self, images):

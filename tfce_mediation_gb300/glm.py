@@ -185,10 +185,12 @@ def glm_stat_f64(Y, designs, what=WHAT_T, coef=None, stream=None):
         raise ValueError(f"design has {db.n} rows, data has {n}")
     coef = list(range(db.kmax)) if coef is None else list(coef)
     out = t.empty((db.G, len(coef), V), device="cuda", dtype=t.float64)
-    _lib.check(_lib.load().glm_stat_f64(ptr(Yd), V, n, V, ptr(dev(db.pinv64, t.float64)), ptr(dev(db.X64, t.float64)),
-                                        ptr(dev(db.invdiag64, t.float64)), ptr(dev(db.dof, t.float64)), db.G, db.kmax,
-                                        ptr(dev(np.asarray(coef, np.int32))), len(coef), what, ptr(out), V,
-                                        stream_handle(stream)))
+    # the operands stay referenced until the launch is queued (a temporary's
+    # memory goes back to the caching allocator as soon as it is released)
+    pinv, Xd, invd, dof = (dev(a, t.float64) for a in (db.pinv64, db.X64, db.invdiag64, db.dof))
+    coef_d = dev(np.asarray(coef, np.int32))
+    _lib.check(_lib.load().glm_stat_f64(ptr(Yd), V, n, V, ptr(pinv), ptr(Xd), ptr(invd), ptr(dof), db.G, db.kmax,
+                                        ptr(coef_d), len(coef), what, ptr(out), V, stream_handle(stream)))
     return out
 
 
