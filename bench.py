@@ -591,7 +591,8 @@ def time_to_fwer(eng, st, n_perm=10_000, seed=99):
                              "fraction_of_plain": info["seconds"] / plain_s, "near_alpha_vertices": info["near_alpha"],
                              "max_abs_dp_where_p_le_0.05": worst, "vertices_p_le_0.05": nsig},
             "note": "1-p(FWER) maps of 4 contrasts x (+,-) of the observed study (calculate_fweP formula); "
-                    "learned tail: MLP GPD tail from 300 permutations, margin 0.01 fallback"}
+                    "learned tail: MLP GPD tail from 300 permutations; vertices whose surrogate or small-sample p lies within "
+                    "0.02 of alpha get 1,200 more permutations"}
 
 
 def _one_thread_per_process():

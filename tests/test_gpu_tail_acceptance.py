@@ -1,7 +1,8 @@
 """The learned-tail FWER path on the headline study at its full size (two
-icosphere-L7 hemispheres, 327,684 vertices, n = 350, k = 5): for two seeds
+icosphere-L7 hemispheres, 327,684 vertices, n = 350, k = 5): for three seeds
 and all four contrasts x (+, -), the 1-p(FWER) maps from 300 permutations
-plus the margin fallback reproduce the plain 10,000-permutation maps within
+plus the margin fallback (vertices whose surrogate or small-sample p lies
+within 0.02 of alpha get 1,200 more permutations) reproduce the plain 10,000-permutation maps within
 0.01 wherever the plain p <= 0.05, in at most a fifth of the plain path's
 wall time (the bar stated for the learned path)."""
 import time
@@ -29,7 +30,7 @@ def test_learned_tail_reproduces_plain_fwer_maps():
     sur = TailSurrogate()
     images = {c: [maps[c, 0], maps[c, 1]] for c in range(eng.C)}
     learned_fwer_maps(eng, images, rho, 1.0, seed=1, surrogate=sur)  # graph capture, warm caches
-    for seed in (99, 123):
+    for seed in (99, 123, 31):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         mx = eng.run_graph(n_perm=10_000, seed=seed).max(axis=-1)

@@ -67,7 +67,7 @@ def _image_maps(img, srt, tail, alpha, margin):
     return omp, near
 
 
-def learned_fwer(eng, tfce_values, contrast, smoothness, E, alpha=0.05, margin=0.01, n_small=300,
+def learned_fwer(eng, tfce_values, contrast, smoothness, E, alpha=0.05, margin=0.02, n_small=300,
                  n_fallback=1200, seed=0, method="mlp", surrogate=None):
     """1-p(FWER) of `tfce_values` (observed TFCE image, host) for one contrast
     of a PermutationEngine; returns (map, info)."""
@@ -76,7 +76,7 @@ def learned_fwer(eng, tfce_values, contrast, smoothness, E, alpha=0.05, margin=0
     return maps[contrast], info
 
 
-def learned_fwer_maps(eng, images, smoothness, E, alpha=0.05, margin=0.01, n_small=300, n_fallback=1200,
+def learned_fwer_maps(eng, images, smoothness, E, alpha=0.05, margin=0.02, n_small=300, n_fallback=1200,
                       seed=0, method="mlp", surrogate=None):
     """1-p(FWER) maps of several observed TFCE images at once.  images:
     {contrast index: image or list of images (e.g. the + and - images)}; the
