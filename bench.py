@@ -18,9 +18,11 @@ import argparse
 import json
 import os
 import re
+import shutil
 import statistics
 import subprocess
 import sys
+import tempfile
 import threading
 import time
 
@@ -126,9 +128,9 @@ def dist_env():
 _W = {}
 
 
-def _cpu_init(study_args):
+def _cpu_init(study_args, stash=None):
     from tfce_mediation_gb300 import synth
-    st = synth.config2(**study_args)
+    st = _unstash_study(stash) if stash else synth.config2(**study_args)
     _W["st"] = st
     from oracle import oracle
     oracle.lib()
@@ -390,8 +392,28 @@ def _config_groups(st):
     return np.array([0] * (S - 1) + [1], np.int32)
 
 
-def _config_cpu_init(kind):
-    _W["cfg"] = (kind, _config_study(kind))
+def _stash_study(st, d):
+    """Write a study where the CPU-baseline worker can map it instead of
+    generating it again (the data as .npy, the rest pickled)."""
+    import pickle
+    os.makedirs(d, exist_ok=True)
+    np.save(os.path.join(d, "Y.npy"), st.Y)
+    rest = dict(st.__dict__)
+    rest.pop("Y")
+    with open(os.path.join(d, "study.pkl"), "wb") as fh:
+        pickle.dump(rest, fh)
+
+
+def _unstash_study(d):
+    import pickle
+    from tfce_mediation_gb300 import synth
+    with open(os.path.join(d, "study.pkl"), "rb") as fh:
+        rest = pickle.load(fh)
+    return synth.Study(Y=np.load(os.path.join(d, "Y.npy"), mmap_mode="r"), **rest)
+
+
+def _config_cpu_init(kind, stash=None):
+    _W["cfg"] = (kind, _unstash_study(stash) if stash else _config_study(kind))
     from oracle import oracle
     oracle.lib()
 
@@ -440,12 +462,12 @@ def _config_cpu_perm(p):
     return out
 
 
-def config_cpu_baseline(kind):
+def config_cpu_baseline(kind, stash=None):
     import multiprocessing as mp
     _one_thread_per_process()
     ctx = mp.get_context("spawn")
     n_cpu = CONFIG_CPU_PERMS[kind]
-    with ctx.Pool(1, initializer=_config_cpu_init, initargs=(kind,)) as pool:
+    with ctx.Pool(1, initializer=_config_cpu_init, initargs=(kind, stash)) as pool:
         pool.map(_config_cpu_perm, [10_000])  # warm: libraries loaded, caches filled
         t0 = time.perf_counter()
         pool.map(_config_cpu_perm, range(n_cpu))
@@ -464,7 +486,7 @@ def _sweep_bytes(st):
     return tot
 
 
-def run_config(kind, args):
+def run_config(kind, args, stash=None):
     """Sub-line of one configuration: whole-job rate through the engine's
     public loop with the data resident, the same through the pipelined entry
     with the data copied from pinned host memory every step (e2e), and the
@@ -474,6 +496,8 @@ def run_config(kind, args):
     from tfce_mediation_gb300.device import ptr
     from tfce_mediation_gb300.glm import DesignBatch
     st = _config_study(kind)
+    if stash:
+        _stash_study(st, stash)
     P = CONFIG_BATCH[kind]
     K = max(2, min(args.steps, 6))
     signs = 1 if kind == "config4a" else 2
@@ -603,12 +627,12 @@ def _one_thread_per_process():
         os.environ[var] = "1"
 
 
-def cpu_rate(n_perm, cores, study_args):
+def cpu_rate(n_perm, cores, study_args, stash=None):
     """perm/s of the oracle port over n_perm permutations on `cores` processes."""
     import multiprocessing as mp
     _one_thread_per_process()
     ctx = mp.get_context("spawn")
-    with ctx.Pool(cores, initializer=_cpu_init, initargs=(study_args,)) as pool:
+    with ctx.Pool(cores, initializer=_cpu_init, initargs=(study_args, stash)) as pool:
         pool.map(_cpu_perm, range(10_000, 10_000 + cores))  # warm: data built, libs loaded
         t0 = time.perf_counter()
         pool.map(_cpu_perm, range(n_perm))
@@ -659,6 +683,7 @@ def run_gpu(args):
     from tfce_mediation_gb300 import shard, synth
     from tfce_mediation_gb300.glm import DesignBatch
 
+    t_wall = time.perf_counter()
     ws, rank, local = dist_env()
     if ws > 1:
         dist.init_process_group("nccl")
@@ -867,21 +892,26 @@ def run_gpu(args):
         "glm": glm_info,
         "clocks": clocks,
     }
+    stash_root = tempfile.mkdtemp(prefix="tfgb_bench_")
     if not args.no_configs:
         line["time_to_fwer"] = time_to_fwer(eng, st)
         del eng
         torch.cuda.empty_cache()
         line["configs"] = {}
         for kind in CONFIGS:
-            line["configs"][kind] = run_config(kind, args)
+            line["configs"][kind] = run_config(kind, args, None if args.no_cpu_baseline else
+                                               os.path.join(stash_root, kind))
     if not args.no_cpu_baseline:
         cores = 1
-        v, dt = cpu_rate(args.cpu_perms, cores, {"n": args.n, "level": args.level})
+        _stash_study(st, os.path.join(stash_root, "config2"))
+        v, dt = cpu_rate(args.cpu_perms, cores, {"n": args.n, "level": args.level}, os.path.join(stash_root, "config2"))
         line["cpu_baseline"] = {"value": v, "unit": "perm/s", "cores": cores, "kind": "port",
                                 "sample": f"{args.cpu_perms} permutations of the same workload, "
                                           f"{dt:.1f} s, single process"}
         for kind in line.get("configs", {}):
-            line["configs"][kind]["cpu_baseline"] = config_cpu_baseline(kind)
+            line["configs"][kind]["cpu_baseline"] = config_cpu_baseline(kind, os.path.join(stash_root, kind))
+    shutil.rmtree(stash_root, ignore_errors=True)
+    line["bench_wall_s"] = round(time.perf_counter() - t_wall, 1)
     print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()

@@ -214,3 +214,33 @@ def test_multimodal_study_full_size():
     _assert_maxima(got, ref)
     # the study-wide value per permutation: max over surfaces
     _assert_maxima(got.max(axis=-1), ref.max(axis=-1))
+
+
+def test_mmr_lr_from_tmi_equals_per_surface_jobs(golden, case, tmp_path, monkeypatch):
+    """mmr-lr straight from the TMI file (all surfaces in one launch) writes
+    the same per-surface CSV values as the per-surface jobs that read the
+    tmi_temp/ hand-off, on the same seeded permutations."""
+    from tfce_mediation_gb300 import randomise as R
+    from tfce_mediation_gb300 import tmi
+    monkeypatch.chdir(tmp_path)
+    tmi.write_tm_filetype("study", image_array=case["y"].T, masking_array=list(case["masks"]),
+                          adjacency_array=list(case["adjs"]), checkname=False)
+    got = R.mmr_lr_tmi_run("study.tmi", (0, 7), 11, "out_tmi", tfce=(2.0, 1.0), pred_x=case["x"], noweight=True,
+                           batch=4)
+    os.makedirs("tmi_temp")
+    os.makedirs("out_jobs")
+    pos = case["pos"]
+    for s in range(3):
+        m = np.asarray(case["masks"][s])
+        mask = m[:, 0, 0] if m.shape[2] == 1 else m[m]
+        np.save(f"tmi_temp/{s}_mask_temp.npy", mask)
+        np.save(f"tmi_temp/{s}_adjacency_temp.npy", case["adjs"][s], allow_pickle=True)
+        np.save(f"tmi_temp/{s}_data_temp.npy", np.ascontiguousarray(case["y"][:, pos[s]:pos[s + 1]], np.float32))
+        np.save(f"tmi_temp/{s}_vdensity_temp.npy", np.array([1.0], np.float32))
+        R.mmr_lr_run(s, (0, 7), 11, "out_jobs", 2.0, 1.0, pred_x=case["x"], batch=4)
+    for s in range(3):
+        for c in (1, 2):
+            a = np.loadtxt(f"out_tmi/perm_maxTFCE_surf{s}_tcon{c}.csv")
+            b = np.loadtxt(f"out_jobs/perm_maxTFCE_surf{s}_tcon{c}.csv")
+            np.testing.assert_allclose(a, b, rtol=1e-6, atol=1e-6, err_msg=f"surface {s} contrast {c}")
+    assert got.shape == (8, 2, 2, 3)

@@ -13,6 +13,8 @@ appends the same CSV lines in the same order and format:
 * voxel_mediation_run  -- tmanalysis/voxel_tfce_mediation_randomise.py:42-77
 * mmr_lr_run           -- tm_multisurface/tm_mmr_rand_low_ram_parallel.py:166-207
   (tmi_temp/<s>_*_temp.npy, <path>/perm_maxTFCE_surf<s>_tcon<c>.csv, %f)
+* mmr_lr_tmi_run       -- mmr-lr from the TMI file itself (tm_mmr_rand_low_ram.py:140-201 builds the
+  tmi_temp/ hand-off the per-surface jobs read): every surface in one launch per batch
 * mmr_run              -- tm_multisurface/tm_multimodality_multisurface_regression.py:404-640
   (the in-memory multisurface driver: reads the TMI file; with -p the
   permutation loop of calculate_tfce / calc_mixed_tfce / calculate_mediation_tfce,
@@ -323,6 +325,68 @@ def mmr_lr_run(surf_num, perm_range, seed, path, H, E_, pred_x=None, mediation=N
                             vdensity=vd, floor_zero=floor, batch=batch)
     maxima = eng.run(perms=perms)[:, 0, 0, 0]
     _append(os.path.join(path, "perm_maxTFCE_surf%d_%s_zstat.csv" % (surf_num, medtype)), ["%f" % v for v in maxima])
+    return maxima
+
+
+def mmr_lr_tmi_run(tmifile, perm_range, seed, path, tfce=(2.0, 1.0), pred_x=None, mediation=None,
+                   covariates=None, subset=None, setadjacencyobjs=None, assigntfcesettings=None, noweight=False,
+                   batch=64):
+    """mmr-lr straight from the TMI file, every surface in one launch per
+    batch: the data, masks, adjacency sets and density weights that
+    tm_mmr_rand_low_ram.py:140-201 writes to tmi_temp/ for its per-surface
+    jobs (tm_mmr_rand_low_ram_parallel.py:166-207) are built in memory, and
+    each surface keeps its own threshold table and (H, E) (tfce: one pair, or
+    one pair per setting with assigntfcesettings), as the per-surface jobs
+    sweep them.  Writes <path>/perm_maxTFCE_surf<s>_tcon<c>.csv (or
+    _<m>_zstat.csv) for every surface, '%f'; permutation p of every surface is
+    RandomState(p + seed) (tm_func.py:147-151).  The zero-filled maximum of
+    the low-RAM scaling applies to every surface when any surface mask leaves
+    vertices out (it changes only the sign of a zero maximum of a surface
+    whose values are all negative).  Returns the maxima (P, C, signs, S)."""
+    from . import cynumstats
+    from .tmi import read_tm_filetype
+    _, image_array, masking_array, _, _, _, _, _, adjacency_array, _, _ = read_tm_filetype(tmifile, verbose=False)
+    n_surf = len(masking_array)
+    adjacent_range = list(setadjacencyobjs) if setadjacencyobjs else list(range(len(adjacency_array)))
+    tf = [float(v) for v in tfce]
+    if assigntfcesettings is not None:
+        assign = [int(a) for a in assigntfcesettings]
+        H = np.array([tf[2 * a] for a in assign], np.float32)
+        Es = np.array([tf[2 * a + 1] for a in assign], np.float32)
+    else:
+        H, Es = np.full(n_surf, tf[0], np.float32), np.full(n_surf, tf[1], np.float32)
+    off, idx, seg, vd = _mmr_layout(masking_array, adjacency_array, adjacent_range, noweight)
+    data = np.asarray(image_array[0])
+    if subset is not None:
+        data = data[:, np.isfinite(np.genfromtxt(str(subset), delimiter=","))]
+    if covariates is not None:
+        covars = np.genfromtxt(covariates, delimiter=",")
+        merge_y = cynumstats.resid_covars(np.column_stack([np.ones(len(covars)), covars]), data)
+    else:
+        merge_y = data.T
+    merge_y = np.ascontiguousarray(merge_y, np.float32)
+    n = merge_y.shape[0]
+    floor = any(np.asarray(m).shape[2] == 1 and not np.asarray(m).all() for m in masking_array)
+    perms = _perm_rows(n, perm_range[0], perm_range[1] + 1, seed)
+    os.makedirs(path, exist_ok=True)
+    if mediation is None:
+        eng = E.PermutationEngine(merge_y, pred_x, (off, idx), seg, H, Es, vdensity=vd, floor_zero=floor,
+                                  batch=batch)
+        maxima = eng.run(perms=perms)  # (P, C, 2, S)
+        for s_ in range(n_surf):
+            for c in range(maxima.shape[1]):
+                lines = []
+                for p in range(maxima.shape[0]):
+                    lines += ["%f" % maxima[p, c, 0, s_], "%f" % maxima[p, c, 1, s_]]
+                _append(os.path.join(path, "perm_maxTFCE_surf%d_tcon%d.csv" % (s_, c + 1)), lines)
+        return maxima
+    medtype, mx, dy = mediation
+    eng = E.MediationEngine(merge_y, mx, dy, medtype, (off, idx), seg, H, Es, vdensity=vd, floor_zero=floor,
+                            batch=batch)
+    maxima = eng.run(perms=perms)
+    for s_ in range(n_surf):
+        _append(os.path.join(path, "perm_maxTFCE_surf%d_%s_zstat.csv" % (s_, medtype)),
+                ["%f" % v for v in maxima[:, 0, 0, s_]])
     return maxima
 
 
