@@ -307,7 +307,12 @@ def mmr_lr_run(surf_num, perm_range, seed, path, H, E_, pred_x=None, mediation=N
     n = data.shape[0]
     m = np.asarray(mask).ravel() == 1
     off, idx = induced_csr(adjacency, m) if m.shape[0] == len(adjacency) and not m.all() else to_csr(adjacency)
-    vd = _vd(vdensity, np.ones(data.shape[1], bool)) if np.ndim(vdensity) else None
+    # --noweight saves a one-element array (tm_mmr_rand_low_ram.py:160-163); it broadcasts
+    vdensity = np.asarray(vdensity, np.float32)
+    if vdensity.size == 1:
+        vd = None if float(vdensity.ravel()[0]) == 1.0 else np.full(data.shape[1], vdensity.ravel()[0], np.float32)
+    else:
+        vd = _vd(vdensity, np.ones(data.shape[1], bool))
     perms = _perm_rows(n, perm_range[0], perm_range[1] + 1, seed)
     floor = not m.all()
     if mediation is None:

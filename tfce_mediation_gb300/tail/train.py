@@ -64,9 +64,12 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--out", default="weights.npz")
     ap.add_argument("--report", default=None)
+    ap.add_argument("--level-p", default="0.5,0.35,0.15",
+                    help="probabilities of icosphere levels 5, 6, 7 among the settings")
     a = ap.parse_args(argv)
     t0 = time.time()
-    settings = data.sample_settings(a.settings, a.seed)
+    level_p = tuple(float(x) for x in a.level_p.split(","))
+    settings = data.sample_settings(a.settings, a.seed, level_p=level_p)
     nulls = []
     for i, s in enumerate(settings):
         nulls.append(data.null_for_setting(s, a.full))
@@ -93,7 +96,7 @@ def main(argv=None):
     perr = p_errors(model, norm, ho_s, ho_n, a.small)
     model.save(a.out, feat_mean=fm, feat_std=fs, targ_mean=tm, targ_std=ts, quant=np.float64(gpd.QUANT),
                small=np.int64(a.small))
-    rep = {"settings": len(settings), "full_perms": a.full, "small_perms": a.small, "train_rows": int(X.shape[0]),
+    rep = {"settings": len(settings), "level_p": list(level_p), "full_perms": a.full, "small_perms": a.small, "train_rows": int(X.shape[0]),
            "heldout_rows": int(Xh.shape[0]), "gen_s": gen_s, "train_s": train_s, "final_train_loss": float(curve[-1]),
            "heldout_mse_normalised": held_mse, "classical_gpd_mse_normalised": base_mse,
            "heldout_max_abs_dp": perr}
