@@ -80,14 +80,6 @@ constexpr int kBitmapMaxBytes = 48 * 1024;
 #ifndef TFGB_ALANES
 #define TFGB_ALANES 1
 #endif
-// Per-component forms: the union phase in two passes -- (A) every new vertex
-// of the step, statically spread over the threads, reads its list and its
-// active neighbours' keys and stores their positions (independent loads, no
-// chains); (B) the walks and links from those positions, dynamically
-// balanced -- so a vertex's dependent chain loses the list and key rounds.
-#ifndef TFGB_UNION_2PASS
-#define TFGB_UNION_2PASS 0
-#endif
 // path halving in the maxima-only form (no potential chains to preserve)
 #ifndef TFGB_MAX_HALVE
 #define TFGB_MAX_HALVE 0
@@ -169,7 +161,6 @@ struct Slot {
   int32_t* roots_a;  // live roots after the previous threshold ...
   int32_t* roots_b;  // ... and after this one (swapped every step)
   Rec* rec;          // {W, extent} per position
-  int32_t* nbuf;     // two-pass union: 8 int32 per position of the current step
 };
 
 __host__ __device__ inline int64_t align_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
@@ -181,8 +172,7 @@ __host__ __device__ inline int64_t slot_bytes(int32_t vcap) {
 // Per-component accumulation adds two root lists and a 16-byte {W, extent}
 // record per vertex to the six int32/float arrays of the exact mode.
 __host__ __device__ inline int64_t slot_bytes_lazy(int32_t vcap) {
-  return 8 * align_up((int64_t)vcap * 4, 256) + align_up((int64_t)vcap * 16, 256) +
-         (TFGB_UNION_2PASS ? align_up((int64_t)vcap * 32, 256) : 0);
+  return 8 * align_up((int64_t)vcap * 4, 256) + align_up((int64_t)vcap * 16, 256);
 }
 
 __device__ inline Slot make_slot(char* base, int32_t vcap) {
@@ -191,7 +181,6 @@ __device__ inline Slot make_slot(char* base, int32_t vcap) {
   sl.roots_a = reinterpret_cast<int32_t*>(base + 6 * s);
   sl.roots_b = reinterpret_cast<int32_t*>(base + 7 * s);
   sl.rec = reinterpret_cast<Rec*>(base + 8 * s);
-  sl.nbuf = reinterpret_cast<int32_t*>(base + 8 * s + align_up((int64_t)vcap * 16, 256));
   sl.key = reinterpret_cast<uint32_t*>(base);
   sl.order = reinterpret_cast<int32_t*>(base + s);
   sl.parent = reinterpret_cast<int32_t*>(base + 2 * s);
@@ -600,74 +589,9 @@ __global__ void __launch_bounds__(kSweepThreads, kMinBlocks) tfce_sweep_kernel(S
         }
         return tgt;
       };
-#if TFGB_UNION_2PASS
-      static_assert(kUBatch == 6, "the two-pass union buffers 6 entries per vertex");
-      if constexpr (kLazy && !kChecked) {
-        // (A) positions of every new vertex's effective neighbours (statically
-        // spread, independent loads); -2 in the last word: more than kUBatch
-        // entries or a list outside the packed range -- the vertex takes the
-        // general path in (B)
-        for (int32_t p = s0 + tid; p < s1; p += nth) {
-          int4* nb = reinterpret_cast<int4*>(sl.nbuf + (int64_t)(p - s0) * 8);
-          const int32_t pk = reinterpret_cast<const int32_t*>(sl.acc)[p];
-          if (pk < 0 || (pk & 63) > kUBatch) {
-            nb[1] = make_int4(-1, -1, -1, -2);
-            continue;
-          }
-          const int64_t e0 = seg_e0 + (pk >> 6), e1 = e0 + (pk & 63);
-          uint32_t raw[kUBatch], ka[kUBatch];
-          int32_t an[kUBatch], cur[kUBatch];
-          int32_t v = -1;
-#pragma unroll
-          for (int k = 0; k < kUBatch; ++k) raw[k] = (e0 + k < e1) ? a.indices[e0 + k] : kIndexMask;
-#pragma unroll
-          for (int k = 0; k < kUBatch; ++k) {
-            const int64_t ag = static_cast<int64_t>(raw[k] & kIndexMask) - v0;
-            an[k] = static_cast<int32_t>(ag);
-            ka[k] = kInactiveKey;
-            if (e0 + k < e1) {
-              if (ag < 0 || ag >= Vs) set_err(a.err, kDevBadIndex);
-              else if (!use_bm || ((sAct[an[k] >> 5] >> (an[k] & 31)) & 1u)) ka[k] = sl.key[an[k]];
-            }
-          }
-#pragma unroll
-          for (int k = 0; k < kUBatch; ++k) {
-            cur[k] = -1;
-            if (ka[k] == kInactiveKey) continue;
-            const int la = static_cast<int>(ka[k] >> kPosBits);
-            if (la > i) continue;
-            if (la == i && (raw[k] & kOneWay)) {
-              if (v < 0) v = sl.order[p];
-              const float xa = sign * x[an[k]], xv = sign * x[v];
-              if (!(xa > xv || (xa == xv && an[k] < v))) continue;
-            }
-            cur[k] = static_cast<int32_t>(ka[k] & ((1u << kPosBits) - 1u));
-          }
-          nb[0] = make_int4(cur[0], cur[1], cur[2], cur[3]);
-          nb[1] = make_int4(cur[4], cur[5], -1, 0);
-        }
-        __syncthreads();
-      }
-#endif
       // each thread takes the next unprocessed vertex of the step from a
       // shared cursor, so threads with short walks do not wait for slow ones
       for (int32_t p = atomicAdd(&sGrab, 1); p < s1; p = atomicAdd(&sGrab, 1)) {
-#if TFGB_UNION_2PASS
-        if constexpr (kLazy && !kChecked) {
-          // (B) walks and links from the buffered positions
-          const int4* nb = reinterpret_cast<const int4*>(sl.nbuf + (int64_t)(p - s0) * 8);
-          const int4 q1 = nb[1];
-          if (q1.w != -2) {
-            const int4 q0 = nb[0];
-            int32_t cur[kUBatch] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y};
-            bool any = false;
-#pragma unroll
-            for (int k = 0; k < kUBatch; ++k) any |= (cur[k] >= 0);
-            if (any) walk_link(cur, p);
-            continue;
-          }
-        }
-#endif
         int32_t v = -1;  // the vertex: read when needed
         int64_t e0, e1;
         const int32_t pk = kLazy ? reinterpret_cast<const int32_t*>(sl.acc)[p] : -1;
