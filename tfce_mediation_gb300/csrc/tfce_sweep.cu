@@ -139,6 +139,8 @@ struct SweepArgs {
   // segment's own max / 100 (tm_func.py:84-91).
   const int32_t* thr_group;
   const float* seg_max;
+  // segments by decreasing size (nullable): the order items are handed out in
+  const int32_t* seg_rank;
 };
 
 // Per-component mode: the increments so far (root) or the potential to the
@@ -367,7 +369,11 @@ __global__ void __launch_bounds__(kSweepThreads, kMinBlocks) tfce_sweep_kernel(S
     const int32_t qi = sItem;
     __syncthreads();
     if (qi >= a.n_items) break;
-    const int32_t item = a.item_order ? a.item_order[qi] : qi;
+    int32_t item = a.item_order ? a.item_order[qi] : qi;
+    if (a.seg_rank) {  // largest segments first; n_items is a multiple of n_seg
+      const int32_t per_seg = a.n_items / a.n_seg;
+      item = (qi % per_seg) * a.n_seg + a.seg_rank[qi / per_seg];
+    }
     const int32_t seg = item % a.n_seg;
     const int32_t ms = item / a.n_seg;  // map * n_signs + sign
     const int32_t sgn = ms % a.n_signs;
@@ -978,6 +984,11 @@ struct tfce_adjset {
   // tfce_adjset_destroy.  Growth is geometric, so the retired total stays
   // below the live buffer's size.
   std::vector<void*> retired;
+  // Segments of uneven sizes: the segments by decreasing size, so items are
+  // handed out largest segment first (every map of the largest segment, then
+  // the next) and a launch does not end on a few long sweeps.  NULL when all
+  // segments have the same size.
+  int32_t* d_segrank = nullptr;
   std::mutex mu;
 };
 
@@ -999,6 +1010,7 @@ int release(tfce_adjset* h) {
   cudaFree(h->d_enh);
   cudaFree(h->d_group);
   cudaFree(h->d_segmax);
+  cudaFree(h->d_segrank);
   for (void* p : h->retired) cudaFree(p);
   h->retired.clear();
   cudaSetDevice(dev);
@@ -1083,6 +1095,7 @@ int launch_sweep(tfce_adjset* h, const float* stats, int64_t map_stride, int32_t
   a.err = h->d_ctrl + 1;
   a.n_items = items;
   a.item_order = nullptr;
+  a.seg_rank = h->d_segrank;
   const int bm = tfgb::bitmap_bytes(h->vmax_seg);
   a.bm_words = bm / 4;
   if (h->d_group) {
@@ -1247,6 +1260,16 @@ int tfce_adjset_create(const int64_t* offsets, const int32_t* indices, int32_t n
   TFGB_CUDA_H(cudaMemcpy(h->d_seg_off, seg.data(), sizeof(int64_t) * (n_seg + 1), cudaMemcpyHostToDevice));
   TFGB_CUDA_H(cudaMemcpy(h->d_H, H, sizeof(float) * n_seg, cudaMemcpyHostToDevice));
   TFGB_CUDA_H(cudaMemcpy(h->d_E, E, sizeof(float) * n_seg, cudaMemcpyHostToDevice));
+  bool uneven = false;
+  for (int s = 0; s + 1 < n_seg; ++s) uneven = uneven || (seg[s + 1] - seg[s] != seg[s + 2] - seg[s + 1]);
+  if (uneven) {
+    std::vector<int32_t> rank(n_seg);
+    for (int32_t s = 0; s < n_seg; ++s) rank[s] = s;
+    std::stable_sort(rank.begin(), rank.end(),
+                     [&](int32_t x, int32_t y) { return seg[x + 1] - seg[x] > seg[y + 1] - seg[y]; });
+    TFGB_CUDA_H(cudaMalloc(&h->d_segrank, sizeof(int32_t) * n_seg));
+    TFGB_CUDA_H(cudaMemcpy(h->d_segrank, rank.data(), sizeof(int32_t) * n_seg, cudaMemcpyHostToDevice));
+  }
 #undef TFGB_CUDA_H
   *out = h;
   return TFCE_OK;
