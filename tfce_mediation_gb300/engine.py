@@ -548,10 +548,39 @@ class MediationEngine:
         return out
 
     def run(self, n_perm=None, seed=0, start=0, stop=None, perms=None):
+        """Null maxima (n_perm, 1, 1, n_seg).  A batch's maxima are read back
+        after the next batch is queued, so the host forms the next batch's
+        path designs (FP64 inverses) while the GPU runs the current one."""
         if perms is None:
             stop = start + n_perm if stop is None else stop
             perms = permutations(self.n, seed, start, stop)
-        out = [self.run_batch(perms[b:b + self.batch]) for b in range(0, perms.shape[0], self.batch)]
+        t = self.t
+        if not hasattr(self, "_host_max"):
+            self._host_max = [t.empty(self.batch * self.n_seg, dtype=t.float32, pin_memory=True) for _ in range(2)]
+            self._max2 = [self._max.view(-1), t.empty_like(self._max.view(-1))]
+            self._done = [t.cuda.Event(), t.cuda.Event()]
+        out, prev = [], None
+
+        def collect(item):
+            k, P = item
+            self._done[k].synchronize()
+            out.append(self._host_max[k][: P * self.n_seg].numpy().reshape(P, 1, 1, self.n_seg).copy())
+
+        for i, b in enumerate(range(0, perms.shape[0], self.batch)):
+            rows = perms[b:b + self.batch]
+            P, k = len(rows), i % 2
+            z = self.zmaps(rows)
+            mx = self._max2[k][: P * self.n_seg]
+            self.inner.adj.sweep_batch(ptr(z), self.V, P, 1, ptr(self.inner.vd), int(self.inner.floor_zero),
+                                       ptr(mx), None, 0, stream_handle())
+            self._host_max[k][: P * self.n_seg].copy_(mx, non_blocking=True)
+            self._done[k].record()
+            if prev is not None:
+                collect(prev)
+            prev = (k, P)
+        if prev is not None:
+            collect(prev)
+        self.inner.status()
         return np.concatenate(out) if out else np.zeros((0, 1, 1, self.n_seg), np.float32)
 
     def observed(self):
