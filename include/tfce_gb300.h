@@ -315,6 +315,17 @@ int glm_tstat_tc(const void* y_tiles, const float* y_shift, const float* Y, int6
  *     holding it, is returned as 0). */
 int glm_col_center(const float* Y, int64_t ldy, int32_t n, int64_t V, const float* centre, float* out,
                    void* stream);
+/* glm_stat_tc with the tile's design count chosen: design_block 32 (N = 256
+ * MMA columns, kmax <= 5; the default there) or 16 (N = 128; the only choice
+ * for kmax > 5), 0 = the default (glm_tc_design_block).  p_tiles and x_rows
+ * must be laid out for the same design_block (row blocks of design_block * 8
+ * pseudoinverse rows; x_rows [ceil(G / design_block)][n_sc][kmax][design_block]).
+ * The autotuner times both for designs with kmax <= 5. */
+int glm_stat_tc_block(const void* y_tiles, const float* y_shift, const float* Y, const float* Y_centred,
+                      int64_t ldy, int32_t n, int32_t n_pad, int64_t V, const void* p_tiles, const float* u_rows,
+                      const float* x_rows, int32_t n_sc, const float* invdiag, const float* dof, int32_t G,
+                      int32_t kmax, int32_t design_block, int32_t mode, const int32_t* coef, int32_t n_coef,
+                      const float* wmat, int32_t w_stride, float* t_out, int64_t ldt, int32_t* err, void* stream);
 int glm_stat_tc(const void* y_tiles, const float* y_shift, const float* Y, const float* Y_centred, int64_t ldy,
                 int32_t n,
                 int32_t n_pad, int64_t V, const void* p_tiles, const float* u_rows, const float* x_rows,

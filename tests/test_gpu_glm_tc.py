@@ -136,3 +136,26 @@ def test_tc_no_intercept_design():
     t_tc = glm_tstat_tc(Y, DesignBatch(mats), [0, 1, 2]).cpu().numpy()
     for g, Xg in enumerate(mats):
         assert _err(t_tc[g], oracle.tval_fp64(Xg, Y)[[0, 1, 2]]) <= TOL
+
+
+
+@pytest.mark.parametrize("kmax", [3, 5])
+def test_design_block_16_equals_32(kmax):
+    """The tensor-core GLM with 16-design tiles (N = 128 MMA columns) gives the
+    t maps of the 32-design tiles (N = 256): the same products and sums per
+    design; both within the bar of the FP64 oracle."""
+    import torch
+    rng = np.random.default_rng(9)
+    n, V, G = 120, 700, 40
+    Y = rng.standard_normal((n, V)).astype(np.float32)
+    X = np.concatenate([np.ones((G, n, 1)), rng.standard_normal((G, n, kmax - 1))], axis=2)
+    coef = list(range(1, kmax))
+    res = []
+    for block in (32, 16):
+        ops = TensorCoreOperands(torch.from_numpy(Y).cuda())
+        ops.design_block = block
+        assert ops.block(kmax) == block
+        res.append(glm_tstat_tc(Y, DesignBatch(X), coef, ops=ops).cpu().numpy())
+    np.testing.assert_allclose(res[0], res[1], rtol=1e-6, atol=1e-6)
+    ref = np.stack([oracle.tval_fp64(X[g], Y)[coef] for g in range(G)])
+    assert _err(res[1], ref) <= TOL

@@ -84,6 +84,10 @@ SIGNATURES = {
                                    ctypes.c_int64, c_vp, c_vp, c_vp, ctypes.c_int32, c_vp, c_vp, ctypes.c_int32,
                                    ctypes.c_int32, ctypes.c_int32, c_vp, ctypes.c_int32, c_vp, ctypes.c_int32,
                                    c_vp, ctypes.c_int64, c_vp, c_vp]),
+    "glm_stat_tc_block": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
+                                         ctypes.c_int64, c_vp, c_vp, c_vp, ctypes.c_int32, c_vp, c_vp, ctypes.c_int32,
+                                         ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, c_vp, ctypes.c_int32, c_vp,
+                                         ctypes.c_int32, c_vp, ctypes.c_int64, c_vp, c_vp]),
     "sobel_combine": (ctypes.c_int, [c_vp, ctypes.c_int64, c_vp, c_vp, ctypes.c_int64,
                                      ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, c_vp,
                                      ctypes.c_int64, c_vp]),

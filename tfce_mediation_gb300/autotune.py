@@ -1,11 +1,13 @@
-"""Choice of P (permutations per launch) and of the sweep's CTA shape for a
-permutation engine.
+"""Choice of P (permutations per launch), of the sweep's CTA shape and of the
+tensor-core GLM's designs per tile for a permutation engine.
 
 Each candidate (P, CTAs per SM) is timed on the device (CUDA events, after a
 warm-up launch) for the GLM + sweep of one batch; the one with the highest
 permutations per second wins.  The sweep runs 3 CTAs of 512 threads per SM
 (40 registers, the most items in flight) or 2 (64 registers, no spills);
-which is faster depends on the segments' sizes and list lengths.  Good
+which is faster depends on the segments' sizes and list lengths.  The GLM
+tile holds 32 designs (N = 256 MMA columns) or 16 (N = 128); it is timed
+first, on the largest candidate batch.  Good
 values of P fill the persistent sweep grid evenly: one launch has P x
 contrasts x signs x segments sweep items spread over the resident CTAs
 (tfce_sweep_resident_slots), so P where that count is a multiple of the CTA
@@ -89,14 +91,51 @@ def time_batch(eng, P, seed=12345, repeats=3):
     return a.elapsed_time(b) / repeats
 
 
+def time_glm(eng, P, seed=12345, repeats=3):
+    """Milliseconds of the GLM of one batch of P permutations (device time)."""
+    import torch
+    from .engine import permutations
+    from .glm import DesignBatch
+    ops = DesignBatch(eng.X[permutations(eng.n, seed, 0, P)])
+    t = torch.empty((P, eng.C, eng.V), device="cuda", dtype=torch.float32)
+    eng.tmaps(ops, out=t)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(repeats):
+        eng.tmaps(ops, out=t)
+    b.record()
+    torch.cuda.synchronize()
+    eng.status()
+    return a.elapsed_time(b) / repeats
+
+
+def choose_design_block(eng, P):
+    """Designs per tensor-core GLM tile (32 or 16; only 16 exists for more
+    than 5 columns), timed on one batch; set on the engine's operands."""
+    tc = getattr(eng, "_tc", None)
+    if tc is None or eng.k > 5:
+        return None
+    ms = {}
+    for db in (32, 16):
+        tc.design_block = db
+        ms[db] = time_glm(eng, P)
+    tc.design_block = min(ms, key=ms.get)
+    return tc.design_block
+
+
 def choose_batch(eng, max_p=256, use_cache=True, shapes=(3, 2)):
-    """Best P and sweep CTA shape for this engine's problem (cached); the
-    shape is set on the engine's adjacency handle, P is returned."""
+    """Best P and sweep CTA shape for this engine's problem, and the GLM's
+    designs per tile (cached); the shape is set on the engine's adjacency
+    handle and the tile size on its GLM operands, P is returned."""
     key = _key(eng)
     cache = _load() if use_cache else {}
     if key in cache and "ctas_per_sm" in cache[key]:
         eng.adj.set_sweep_shape(int(cache[key]["ctas_per_sm"]))
+        if cache[key].get("design_block") and getattr(eng, "_tc", None) is not None:
+            eng._tc.design_block = int(cache[key]["design_block"])
         return int(cache[key]["P"])
+    design_block = choose_design_block(eng, max(candidates(eng, max_p)))
     results = {}
     for shape in shapes:
         eng.adj.set_sweep_shape(shape)
@@ -108,7 +147,7 @@ def choose_batch(eng, max_p=256, use_cache=True, shapes=(3, 2)):
             results[(shape, P)] = P / ms * 1000.0
     shape, best = max(results, key=results.get)
     eng.adj.set_sweep_shape(shape)
-    cache[key] = {"P": best, "ctas_per_sm": shape,
+    cache[key] = {"P": best, "ctas_per_sm": shape, "design_block": design_block,
                   "perm_per_s": {f"{s}x{p}": v for (s, p), v in results.items()}}
     if use_cache:
         _save(cache)

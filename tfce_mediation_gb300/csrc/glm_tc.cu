@@ -57,28 +57,31 @@ constexpr uint64_t kTcWaitNs = 2000000000ull;
 // output kinds of the programmed epilogue (mode 3)
 constexpr int kTcOutT = 0, kTcOutNegT = 1, kTcOutF = 2, kTcOutAmp = 3, kTcOutAcro = 4, kTcOutEss = 5;
 
-__host__ __device__ constexpr int tc_dpt(int kmax) { return kmax <= 5 ? 16 : 8; }  // designs per thread
-__host__ __device__ constexpr int tc_db(int kmax) { return 2 * tc_dpt(kmax); }     // designs per tile
-__host__ __device__ constexpr int tc_n(int kmax) { return tc_db(kmax) * kTcRowsPerDesign; }
+// designs per thread in the beta drain: 16 (32-design tiles, N = 256) or 8
+// (16-design tiles, N = 128); kmax > 5 always uses 8
+__host__ __device__ constexpr int tc_dpt(int kmax) { return kmax <= 5 ? 16 : 8; }
+__host__ __device__ constexpr int tc_db(int dpt) { return 2 * dpt; }     // designs per tile
+__host__ __device__ constexpr int tc_n(int dpt) { return tc_db(dpt) * kTcRowsPerDesign; }
 __host__ __device__ constexpr int tc_y_stage() { return kTcM * kTcK * 2 * 2; }          // 8 KB
-__host__ __device__ constexpr int tc_p_stage(int kmax) { return tc_n(kmax) * kTcK * 2 * 2; }
-__host__ __device__ constexpr int tc_stage(int kmax) { return tc_y_stage() + tc_p_stage(kmax); }
-__host__ __device__ constexpr int tc_xchunk(int kmax) { return kTcSubjChunk * kmax * tc_db(kmax) * 4; }
+__host__ __device__ constexpr int tc_p_stage(int dpt) { return tc_n(dpt) * kTcK * 2 * 2; }
+__host__ __device__ constexpr int tc_stage(int dpt) { return tc_y_stage() + tc_p_stage(dpt); }
+__host__ __device__ constexpr int tc_xchunk(int kmax, int dpt) { return kTcSubjChunk * kmax * tc_db(dpt) * 4; }
 __host__ __device__ constexpr int tc_ychunk() { return kTcSubjChunk * kTcM * 4; }
 constexpr int kTcBld = kTcM + 1;  // row stride (floats) of the drained betas
-__host__ __device__ constexpr int tc_beta_bytes(int kmax) { return tc_db(kmax) * kmax * kTcBld * 4; }
+__host__ __device__ constexpr int tc_beta_bytes(int kmax, int dpt) { return tc_db(dpt) * kmax * kTcBld * 4; }
 __host__ __device__ constexpr int tc_cmax(int a, int b) { return a > b ? a : b; }
 // partial-F epilogue: every thread's betas and RSS (DB/2 vertices x (kmax+1) floats)
-__host__ __device__ constexpr int tc_fslice_bytes(int kmax) { return 256 * (tc_db(kmax) / 2) * (kmax + 1) * 4; }
+__host__ __device__ constexpr int tc_fslice_bytes(int kmax, int dpt) { return 256 * (tc_db(dpt) / 2) * (kmax + 1) * 4; }
 // the stage ring, the drained betas, the subject chunks and the partial-F
 // slices share one area
-__host__ __device__ constexpr int tc_area(int kmax) {
-  return (tc_cmax(tc_cmax(tc_cmax(kTcStages * tc_stage(kmax), tc_beta_bytes(kmax)),
-                          2 * (tc_xchunk(kmax) + tc_ychunk())),
-                  tc_fslice_bytes(kmax)) + 127) / 128 * 128;
+__host__ __device__ constexpr int tc_area(int kmax, int dpt) {
+  return (tc_cmax(tc_cmax(tc_cmax(kTcStages * tc_stage(dpt), tc_beta_bytes(kmax, dpt)),
+                          2 * (tc_xchunk(kmax, dpt) + tc_ychunk())),
+                  tc_fslice_bytes(kmax, dpt)) + 127) / 128 * 128;
 }
-__host__ __device__ constexpr int tc_smem(int kmax) { return tc_area(kmax) + 128; }
-static_assert(tc_smem(5) <= 113 * 1024 && tc_smem(8) <= 113 * 1024 && tc_smem(4) <= 113 * 1024,
+__host__ __device__ constexpr int tc_smem(int kmax, int dpt) { return tc_area(kmax, dpt) + 128; }
+static_assert(tc_smem(5, 16) <= 113 * 1024 && tc_smem(8, 8) <= 113 * 1024 && tc_smem(4, 16) <= 113 * 1024 &&
+                  tc_smem(5, 8) <= 113 * 1024,
               "two CTAs per SM");
 
 
@@ -279,20 +282,20 @@ struct TcArgs {
   int32_t* err;
 };
 
-template <int KMAX, bool kCentred>
+template <int KMAX, bool kCentred, int DPT_ = tc_dpt(KMAX)>
 __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
   // centred form: r = (y - c) - Xc b[1..] for designs with an intercept
   // (column means removed from the other columns; c the data's centre)
   constexpr int J0 = kCentred ? 1 : 0;
-  constexpr int DPT = tc_dpt(KMAX);
-  constexpr int DB = tc_db(KMAX);
-  constexpr int N = tc_n(KMAX);
+  constexpr int DPT = DPT_;
+  constexpr int DB = tc_db(DPT);
+  constexpr int N = tc_n(DPT);
   constexpr int YS = tc_y_stage();
-  constexpr int PS = tc_p_stage(KMAX);
-  constexpr int ST = tc_stage(KMAX);
-  constexpr int XC = tc_xchunk(KMAX);
+  constexpr int PS = tc_p_stage(DPT);
+  constexpr int ST = tc_stage(DPT);
+  constexpr int XC = tc_xchunk(KMAX, DPT);
   extern __shared__ __align__(1024) unsigned char sm[];
-  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + tc_area(KMAX));  // full[4], empty[4], done
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + tc_area(KMAX, DPT));  // full[4], empty[4], done
   uint32_t* sTmem = reinterpret_cast<uint32_t*>(bars + 2 * kTcStages + 1);
   int* sFail = reinterpret_cast<int*>(sTmem + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -599,16 +602,18 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
   }
 }
 
-template <int KMAX>
+template <int KMAX, int DPT = tc_dpt(KMAX)>
 static int launch_tc(const TcArgs& a, int64_t n_vb, cudaStream_t stream) {
-  const int smem = tc_smem(KMAX);
+  const int smem = tc_smem(KMAX, DPT);
   const int64_t grid = n_vb * a.n_db;
   if (a.Yc != nullptr) {
-    TFGB_CUDA(cudaFuncSetAttribute(glm_tc_kernel<KMAX, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    glm_tc_kernel<KMAX, true><<<static_cast<unsigned>(grid), kTcThreads, smem, stream>>>(a);
+    TFGB_CUDA(cudaFuncSetAttribute(glm_tc_kernel<KMAX, true, DPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   smem));
+    glm_tc_kernel<KMAX, true, DPT><<<static_cast<unsigned>(grid), kTcThreads, smem, stream>>>(a);
   } else {
-    TFGB_CUDA(cudaFuncSetAttribute(glm_tc_kernel<KMAX, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    glm_tc_kernel<KMAX, false><<<static_cast<unsigned>(grid), kTcThreads, smem, stream>>>(a);
+    TFGB_CUDA(cudaFuncSetAttribute(glm_tc_kernel<KMAX, false, DPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   smem));
+    glm_tc_kernel<KMAX, false, DPT><<<static_cast<unsigned>(grid), kTcThreads, smem, stream>>>(a);
   }
   TFGB_CUDA(cudaGetLastError());
   return TFCE_OK;
@@ -620,7 +625,7 @@ extern "C" {
 
 int glm_tc_design_block(int32_t kmax) {
   if (kmax < 1 || kmax > tfgb::kTcRowsPerDesign) return -1;
-  return tfgb::tc_db(kmax);
+  return tfgb::tc_db(tfgb::tc_dpt(kmax));
 }
 
 int64_t glm_tile_bytes(int64_t rows, int32_t row_block, int32_t n_pad) {
@@ -672,13 +677,15 @@ int glm_tile_split(const float* src, int64_t ld_src, int32_t transpose, int64_t 
   return TFCE_OK;
 }
 
-int glm_stat_tc(const void* y_tiles, const float* y_shift, const float* Y, const float* Y_centred, int64_t ldy,
-                int32_t n,
-                int32_t n_pad, int64_t V, const void* p_tiles, const float* u_rows, const float* x_rows,
-                int32_t n_sc, const float* invdiag, const float* dof, int32_t G, int32_t kmax, int32_t mode,
-                const int32_t* coef, int32_t n_coef, const float* wmat, int32_t w_stride, float* t_out,
-                int64_t ldt, int32_t* err, void* stream) {
+int glm_stat_tc_block(const void* y_tiles, const float* y_shift, const float* Y, const float* Y_centred,
+                      int64_t ldy, int32_t n, int32_t n_pad, int64_t V, const void* p_tiles, const float* u_rows,
+                      const float* x_rows, int32_t n_sc, const float* invdiag, const float* dof, int32_t G,
+                      int32_t kmax, int32_t design_block, int32_t mode, const int32_t* coef, int32_t n_coef,
+                      const float* wmat, int32_t w_stride, float* t_out, int64_t ldt, int32_t* err, void* stream) {
   tfgb::clear_error();
+  if (design_block == 0 && kmax >= 1 && kmax <= tfgb::kTcRowsPerDesign) design_block = glm_tc_design_block(kmax);
+  TFGB_CHECK_ARG(design_block == 16 || (design_block == 32 && kmax <= 5),
+                 "design_block must be 32 (kmax <= 5) or 16");
   TFGB_CHECK_ARG(y_tiles && Y && p_tiles && t_out && err, "NULL pointer");
   TFGB_CHECK_ARG(mode == 4 || (x_rows && invdiag && dof), "x_rows / invdiag / dof are NULL");
   TFGB_CHECK_ARG(mode == 1 || coef != nullptr, "coef is NULL");
@@ -717,23 +724,33 @@ int glm_stat_tc(const void* y_tiles, const float* y_shift, const float* Y, const
   a.n_sc = n_sc;
   a.ks_count = n_pad / tfgb::kTcK;
   a.G = G;
-  a.n_db = (G + tfgb::tc_db(kmax) - 1) / tfgb::tc_db(kmax);
+  a.n_db = (G + design_block - 1) / design_block;
   a.n_coef = (mode == 1) ? 1 : n_coef;
   a.mode = mode;
   a.w_stride = w_stride;
   a.err = err;
   const int64_t n_vb = (V + tfgb::kTcM - 1) / tfgb::kTcM;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const bool small = (design_block == 16);
   switch (kmax) {
-    case 1: return tfgb::launch_tc<1>(a, n_vb, st);
-    case 2: return tfgb::launch_tc<2>(a, n_vb, st);
-    case 3: return tfgb::launch_tc<3>(a, n_vb, st);
-    case 4: return tfgb::launch_tc<4>(a, n_vb, st);
-    case 5: return tfgb::launch_tc<5>(a, n_vb, st);
+    case 1: return small ? tfgb::launch_tc<1, 8>(a, n_vb, st) : tfgb::launch_tc<1>(a, n_vb, st);
+    case 2: return small ? tfgb::launch_tc<2, 8>(a, n_vb, st) : tfgb::launch_tc<2>(a, n_vb, st);
+    case 3: return small ? tfgb::launch_tc<3, 8>(a, n_vb, st) : tfgb::launch_tc<3>(a, n_vb, st);
+    case 4: return small ? tfgb::launch_tc<4, 8>(a, n_vb, st) : tfgb::launch_tc<4>(a, n_vb, st);
+    case 5: return small ? tfgb::launch_tc<5, 8>(a, n_vb, st) : tfgb::launch_tc<5>(a, n_vb, st);
     case 6: return tfgb::launch_tc<6>(a, n_vb, st);
     case 7: return tfgb::launch_tc<7>(a, n_vb, st);
     default: return tfgb::launch_tc<8>(a, n_vb, st);
   }
+}
+
+int glm_stat_tc(const void* y_tiles, const float* y_shift, const float* Y, const float* Y_centred, int64_t ldy,
+                int32_t n, int32_t n_pad, int64_t V, const void* p_tiles, const float* u_rows, const float* x_rows,
+                int32_t n_sc, const float* invdiag, const float* dof, int32_t G, int32_t kmax, int32_t mode,
+                const int32_t* coef, int32_t n_coef, const float* wmat, int32_t w_stride, float* t_out,
+                int64_t ldt, int32_t* err, void* stream) {
+  return glm_stat_tc_block(y_tiles, y_shift, Y, Y_centred, ldy, n, n_pad, V, p_tiles, u_rows, x_rows, n_sc, invdiag,
+                           dof, G, kmax, 0, mode, coef, n_coef, wmat, w_stride, t_out, ldt, err, stream);
 }
 
 int glm_tstat_tc(const void* y_tiles, const float* y_shift, const float* Y, int64_t ldy, int32_t n,

@@ -261,6 +261,7 @@ class PermutationEngine:
         slot = {"P": P}
         if tc is not None:
             Gp, DB = tc.padded(P, kmax), tc.block(kmax)
+            slot["DB"] = DB
             keys = ("P8", "U", "Xt", "invd", "dof") + (("W",) if self._w_stride else ())
             if self._w_stride:
                 slot["h_W"] = t.zeros((P, self._w_stride), dtype=t.float32, pin_memory=True)
@@ -363,7 +364,8 @@ class PermutationEngine:
         Returns the per-batch maxima, (rows, C, signs, n_seg) each."""
         t = self.t
         P = self.batch
-        if not hasattr(self, "_slots") or self._slots[0]["P"] != P:
+        DB = None if self._tc is None else self._tc.block(self.k)
+        if not hasattr(self, "_slots") or self._slots[0]["P"] != P or self._slots[0].get("DB") != DB:
             self._slots = [self._graph_slot(P), self._graph_slot(P)]
         if not hasattr(self, "_up_stream"):
             self._up_stream = t.cuda.Stream()

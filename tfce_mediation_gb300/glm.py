@@ -234,6 +234,9 @@ class TensorCoreOperands:
         # the data minus its centre: residuals of intercept designs skip the intercept term
         self.Yc = t.empty_like(Yd) if centre else None
         self.err = t.zeros(1, dtype=t.int32, device="cuda")
+        # designs per tile: None = the library's default for kmax (32 for kmax <= 5, else 16);
+        # 16 or 32 to choose (the autotuner times both)
+        self.design_block = None
         self.retile()
 
     def retile(self):
@@ -246,6 +249,8 @@ class TensorCoreOperands:
                                            self.ROW_BLOCK, self.n_pad, ptr(self.yt), ptr(self.Yc), stream_handle()))
 
     def block(self, kmax):
+        if self.design_block is not None and (kmax <= 5 or self.design_block == 16):
+            return int(self.design_block)
         return int(self.lib.glm_tc_design_block(kmax))
 
     def padded(self, G, kmax):
@@ -307,11 +312,11 @@ class TensorCoreOperands:
         DesignBatch.program_weights.
         centred: x_rows came from host_operands(..., centred=True)."""
         w_stride = 0 if wmat is None else int(wmat.shape[-1])
-        _lib.check(self.lib.glm_stat_tc(ptr(self.yt), ptr(self.shift), ptr(self.Yd),
-                                        ptr(self.Yc) if centred else None, self.V, self.n, self.n_pad,
-                                        self.V, ptr(p_tiles), ptr(u_rows), ptr(x_rows), self.n_sc, ptr(invd),
-                                        ptr(dof), G, kmax, mode, ptr(coef_d), n_coef, ptr(wmat), w_stride,
-                                        ptr(out), ldt, ptr(self.err), stream_handle()))
+        _lib.check(self.lib.glm_stat_tc_block(ptr(self.yt), ptr(self.shift), ptr(self.Yd),
+                                              ptr(self.Yc) if centred else None, self.V, self.n, self.n_pad,
+                                              self.V, ptr(p_tiles), ptr(u_rows), ptr(x_rows), self.n_sc, ptr(invd),
+                                              ptr(dof), G, kmax, self.block(kmax), mode, ptr(coef_d), n_coef,
+                                              ptr(wmat), w_stride, ptr(out), ldt, ptr(self.err), stream_handle()))
 
     def status(self):
         e = int(self.err.item())
