@@ -871,6 +871,8 @@ def run_gpu(args):
         "config": {"workload": WORKLOAD, "perms_per_step": P, "sweeps_per_step": sweeps_per_launch,
                    "l2": "inputs larger than L2 (Y 459 MB, t maps %d MB per step)" % (P * C * V * 4 // 2 ** 20),
                    "parallelism": f"replicas over permutation ranges x{ws}",
+                   "sweep_ctas_per_sm": getattr(eng.adj, "ctas_per_sm", None),
+                   "glm_designs_per_tile": getattr(tc, "design_block", None) if tc is not None else None,
                    "data_gen_s": round(gen_s, 1)},
         "e2e": {"value": e2e_value, "unit": "perm/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,

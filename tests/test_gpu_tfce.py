@@ -264,6 +264,41 @@ def test_component_accumulation_segments_and_asymmetric(golden):
     np.testing.assert_allclose(e_c, e_e, rtol=COMPONENT_RTOL)
 
 
+def test_maxima_only_bit_exact_with_groups_and_asymmetric_lists(golden):
+    """The maxima-only form equals the exact mode bit for bit with threshold
+    groups (one table per group and sign), per-segment H/E, asymmetric lists,
+    a segment whose map has no positive values (an empty +x table),
+    floor_zero on and off, and both CTA shapes of the per-component kernels."""
+    off, idx = golden["sweep_off"], golden["sweep_idx"]
+    maps = golden["sweep_maps"]
+    O, I, seg = A.concat_csr([(off, idx), (off, idx), (off, idx)])
+    adj = A.AdjacencySet((O, I), [2.0, 1.5, 2.0], [1.0, 0.5, 0.67], seg)
+    n = off.shape[0] - 1
+    neg_only = -np.abs(maps[2])
+    stat = np.stack([np.concatenate([maps[0], maps[1], neg_only]),
+                     np.concatenate([maps[4], neg_only, maps[5]]),
+                     np.concatenate([maps[3], maps[3], maps[3]])]).astype(np.float32)
+    assert stat.shape[1] == 3 * n
+    for groups in (None, [0, 0, 1], [0, 1, 0]):
+        adj.set_threshold_groups(groups)
+        for fz in (0, 1):
+            adj.set_accumulation("exact")
+            mx_e, _ = _batch(adj, stat, floor_zero=fz)
+            adj.set_accumulation("component")
+            for shape in (3, 2):  # resident CTAs per SM of the per-component kernels
+                adj.set_sweep_shape(shape)
+                mx_c, _ = _batch(adj, stat, floor_zero=fz)
+                np.testing.assert_array_equal(mx_c, mx_e, err_msg=f"groups={groups} floor_zero={fz} shape={shape}")
+    adj.set_threshold_groups(None)
+    adj.set_sweep_shape(3)
+    # one sign only: the single-sign maxima-only items agree too
+    adj.set_accumulation("exact")
+    one_e, _ = _batch(adj, stat, signs=1, floor_zero=1)
+    adj.set_accumulation("component")
+    one_c, _ = _batch(adj, stat, signs=1, floor_zero=1)
+    np.testing.assert_array_equal(one_c, one_e)
+
+
 def test_large_segment_without_activity_bitmap():
     """A segment above the shared-memory activity bitmap's capacity (393,216
     vertices) sweeps without it: exact mode bit-identical to the oracle,
@@ -294,11 +329,13 @@ def test_large_segment_without_activity_bitmap():
 
 
 @pytest.mark.parametrize("E", [1.0, 0.5])
-def test_maxima_only_form_equals_potential_form(E):
-    """Maxima-only launches keep each component's largest sum instead of the
-    potentials; the maxima equal the potential form's (which resolves every
-    vertex) to the last float bit or two, on smooth maps of both signs and
-    two segments, and the oracle's to the float summation error."""
+def test_maxima_only_form_is_bit_exact(E):
+    """Maxima-only launches keep each component's largest float sum (rounding
+    is monotone, so that is the largest per-vertex float accumulation of its
+    members): the maxima equal the exact mode's and the oracle's (correctly
+    rounded HH) bit for bit, on smooth maps of both signs and two segments;
+    the potential form (double sums, one rounding) is within the float
+    summation error."""
     import torch
     from oracle import oracle
     from tfce_mediation_gb300 import adjacency as A
@@ -316,16 +353,18 @@ def test_maxima_only_form_equals_potential_form(E):
     adj = A.AdjacencySet((off, idx), 2.0, E, seg)
     d = torch.from_numpy(maps).cuda()
     res = {}
-    for mode in ("component", "component-chain"):
+    for mode in ("exact", "component", "component-chain"):
         adj.set_accumulation(mode)
         out = torch.empty((24, 2, 2), device="cuda")
         adj.sweep_batch(d.data_ptr(), V, 24, 2, None, 1, out.data_ptr())
         adj.status()
         res[mode] = out.cpu().numpy()
-    np.testing.assert_allclose(res["component"], res["component-chain"], rtol=2e-7, atol=0)
+    np.testing.assert_array_equal(res["component"], res["exact"])
+    np.testing.assert_allclose(res["component"], res["component-chain"], rtol=COMPONENT_RTOL, atol=0)
     Vh = V // 2
     for i in range(0, 24, 5):
         for si, s in enumerate((1.0, -1.0)):
             for h in range(2):
-                ref = oracle.tfce_max_batch(o1, i1, maps[i, h * Vh:(h + 1) * Vh], 2.0, E, sign=s, floor_zero=True)[0]
-                assert abs(res["component"][i, si, h] - ref) <= 1e-5 * abs(ref) + 1e-12, (i, s, h)
+                ref = oracle.tfce_max_batch(o1, i1, maps[i, h * Vh:(h + 1) * Vh], 2.0, E, sign=s,
+                                            floor_zero=True, hh_exact=True)[0]
+                assert res["component"][i, si, h] == ref, (i, s, h, res["component"][i, si, h], ref)

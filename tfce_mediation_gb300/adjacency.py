@@ -308,6 +308,9 @@ class AdjacencySet:
         self.n_seg = n_seg
         self.H = Hs.copy()
         self.E = Es.copy()
+        self.accumulation = "exact"  # the native handle's defaults
+        self.ctas_per_sm = 3
+        self.threshold_groups = None
 
     @property
     def handle(self):

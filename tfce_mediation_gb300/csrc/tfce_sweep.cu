@@ -84,6 +84,9 @@ constexpr int kBitmapMaxBytes = 48 * 1024;
 #ifndef TFGB_MAX_HALVE
 #define TFGB_MAX_HALVE 0
 #endif
+#ifndef TFGB_MAX_REC8  // maxima-only form: 8-byte {float sum, extent} records
+#define TFGB_MAX_REC8 1
+#endif
 constexpr int kSweepThreads = TFGB_SWEEP_THREADS;
 constexpr int kUBatch = TFGB_UBATCH;   // list entries of one vertex looked up together
 constexpr int kALanes = TFGB_ALANES;   // positions per thread per accumulation round
@@ -150,6 +153,16 @@ struct alignas(16) Rec {
   double w;
   int32_t size;
   int32_t pad;
+};
+
+// Maxima-only form: {sum, extent} of a position in 8 bytes (in the Rec region
+// of the slot; four records per sector).  The sum is a float: rounding is
+// monotone, so fl(max(a, b) + x) = max(fl(a + x), fl(b + x)), and the largest
+// float sum kept per component equals the largest per-vertex float
+// accumulation of its members (fast_tfce.hpp:77-82) bit for bit.
+struct alignas(8) Rec8 {
+  float w;  // >= 0: ordered as its bit pattern
+  int32_t size;
 };
 
 struct Slot {
@@ -359,6 +372,9 @@ __global__ void __launch_bounds__(kSweepThreads, kMinBlocks) tfce_sweep_kernel(S
   // (no path halving), so parent[] is also the chain of the potentials; the
   // exact mode halves paths.
   constexpr bool kHalve = !kLazy || (kMaxOnly && TFGB_MAX_HALVE);
+  // Maxima-only form: float sums and extents in 8-byte records
+  constexpr bool kR8 = kMaxOnly && TFGB_MAX_REC8;
+  Rec8* const rec8 = reinterpret_cast<Rec8*>(sl.rec);
 #ifdef TFGB_PHASE_PROFILE
   long long _pt = clock64();
 #endif
@@ -498,7 +514,8 @@ __global__ void __launch_bounds__(kSweepThreads, kMinBlocks) tfce_sweep_kernel(S
         sl.order[p] = v;
         sl.parent[p] = p;
         if constexpr (kLazy) {
-          sl.rec[p] = Rec{0.0, 1, 0};
+          if constexpr (kR8) rec8[p] = Rec8{0.0f, 1};
+          else sl.rec[p] = Rec{0.0, 1, 0};
           // the vertex's list (start relative to the segment's, degree) by
           // position, so the union phase reads it without a dependent load;
           // -1: out of the packed range, read the offsets
@@ -715,6 +732,20 @@ __global__ void __launch_bounds__(kSweepThreads, kMinBlocks) tfce_sweep_kernel(S
             }
           }
         }
+        if constexpr (kR8) {
+#pragma unroll
+          for (int k = 0; k < kSLanes; ++k) {
+            if (d[k] < 0) continue;
+            // d is no longer a root: no other thread writes its record in this
+            // phase.  Atomics on the final root: extent, and the largest sum
+            // (sums are >= 0, so their bit patterns order as the values do).
+            const Rec8 rd = rec8[d[k]];
+            atomicAdd(&rec8[c[k]].size, rd.size);
+            if (c[k] != pd[k]) st_state(sl.parent + d[k], c[k]);
+            atomicMax(reinterpret_cast<unsigned int*>(&rec8[c[k]].w), __float_as_uint(rd.w));
+          }
+          continue;
+        }
         int32_t sz[kSLanes];
         double wd[kSLanes], wr[kSLanes];
 #pragma unroll
@@ -771,20 +802,32 @@ __global__ void __launch_bounds__(kSweepThreads, kMinBlocks) tfce_sweep_kernel(S
             const int32_t q = q0 + k;
             c[k] = (q >= n_cand) ? -1 : (q < n_old) ? cur_roots[q] : s0 + (q - n_old);
           }
+          if constexpr (kR8) {
+            // no thread writes a record in this phase but its own root's sum
 #pragma unroll
-          for (int k = 0; k < kALanes; ++k) is_root[k] = (c[k] >= 0) && (ld_state(sl.parent + c[k]) == c[k]);
-          int32_t sz[kALanes];
-          double w[kALanes];
+            for (int k = 0; k < kALanes; ++k) is_root[k] = (c[k] >= 0) && (ld_state(sl.parent + c[k]) == c[k]);
 #pragma unroll
-          for (int k = 0; k < kALanes; ++k) {
-            if (!is_root[k]) continue;
-            const Rec rc = sl.rec[c[k]];
-            sz[k] = rc.size;
-            w[k] = rc.w;
+            for (int k = 0; k < kALanes; ++k) {
+              if (!is_root[k]) continue;
+              const Rec8 rc = rec8[c[k]];
+              rec8[c[k]].w = __fadd_rn(rc.w, increment(rc.size, E, e_mode, HHl));
+            }
+          } else {
+#pragma unroll
+            for (int k = 0; k < kALanes; ++k) is_root[k] = (c[k] >= 0) && (ld_state(sl.parent + c[k]) == c[k]);
+            int32_t sz[kALanes];
+            double w[kALanes];
+#pragma unroll
+            for (int k = 0; k < kALanes; ++k) {
+              if (!is_root[k]) continue;
+              const Rec rc = sl.rec[c[k]];
+              sz[k] = rc.size;
+              w[k] = rc.w;
+            }
+#pragma unroll
+            for (int k = 0; k < kALanes; ++k)
+              if (is_root[k]) sl.rec[c[k]].w = w[k] + static_cast<double>(increment(sz[k], E, e_mode, HHl));
           }
-#pragma unroll
-          for (int k = 0; k < kALanes; ++k)
-            if (is_root[k]) sl.rec[c[k]].w = w[k] + static_cast<double>(increment(sz[k], E, e_mode, HHl));
           const unsigned mask = __activemask();
           const int lane = tid & 31;
 #pragma unroll
@@ -859,7 +902,7 @@ __global__ void __launch_bounds__(kSweepThreads, kMinBlocks) tfce_sweep_kernel(S
       float best = (n_act < Vs) ? __fmul_rn(0.0f, scale) : -INFINITY;
       const int32_t nr = sNRoots;
       for (int32_t q = tid; q < nr; q += nth)
-        best = fmaxf(best, __fmul_rn(__double2float_rn(sl.rec[cur_roots[q]].w), scale));
+        best = fmaxf(best, __fmul_rn(kR8 ? rec8[cur_roots[q]].w : __double2float_rn(sl.rec[cur_roots[q]].w), scale));
       best = block_max(best, sRed);
       if (tid == 0 && a.out_max) a.out_max[item] = (best == -INFINITY) ? 0.0f : best;
       __syncthreads();
