@@ -176,6 +176,9 @@ NEXT = {
                 "vertices), 120 subjects x 3 intervals: F_a, F_s, F_sa = 3 maps x 2 hemispheres",
     "gd_fwhm": "geodesic FWHM smoothing, one icosphere-L7 hemisphere (163,842 vertices), vertex pairs within "
                "chord 0.038 (~60 per vertex), batches of 64 images",
+    "geodesic": "exact geodesic distance lists (adjacency.compute_distance_parallel for every source), one "
+                "icosphere-L7 hemisphere (163,842 vertices) scaled to a 0.9 mm mean edge with 0.15 mm radial "
+                "noise (saddle vertices), radius 9 mm",
 }
 
 
@@ -206,6 +209,12 @@ def _next_study(kind):
         dist = np.linalg.norm(v[pairs[:, 0]] - v[pairs[:, 1]], axis=1).astype(np.float32)
         imgs = rng.standard_normal((64, v.shape[0])).astype(np.float32)
         return dict(pairs=pairs, dist=dist, imgs=imgs, V=v.shape[0], sigma=4e-4)
+    if kind == "geodesic":
+        v, f = synth.icosphere(7)
+        e = np.linalg.norm(v[f[:, 0]] - v[f[:, 1]], axis=1).mean()
+        r = 0.9 / e
+        v = v * r * (1.0 + (0.15 / r) * rng.standard_normal((v.shape[0], 1)))
+        return dict(v=np.ascontiguousarray(v, np.float32), f=np.ascontiguousarray(f, np.int32), radius=9.0)
     raise ValueError(kind)
 
 
@@ -245,6 +254,9 @@ def _next_cpu_perm(p):
         F = oracle.rm_ancova_one(d["Y"].reshape(s, n, -1), d["f1"], d["subj"], dmy_covariates=d["cov"],
                                  rand_array=ra, shuffle=sh)
         return [_segment_max(st, np.asarray(m, np.float32)) for m in F]
+    if kind == "geodesic":
+        oracle.geodesic_lists(d["v"], d["f"], d["radius"], True, p * 100, (p + 1) * 100)
+        return []
     sl = slice(p * 20_000, (p + 1) * 20_000)
     oracle.calc_gd_fwhm(d["pairs"][sl], d["dist"][sl], d["imgs"][0], d["sigma"])
     return []
@@ -271,6 +283,11 @@ def run_next(args):
             per_img = dt / (n_cpu * 20_000) * M
             cpu = {"value": 1.0 / per_img, "unit": "images/s", "cores": 1, "kind": "port",
                    "sample": f"{n_cpu} x 20,000 of {M:,} pairs of one image, extrapolated per pair"}
+        elif kind == "geodesic":
+            cpu = {"value": n_cpu * 100 / dt, "unit": "sources/s", "cores": 1, "kind": "port",
+                   "sample": f"{n_cpu} x 100 sources of the same mesh and radius, {dt:.1f} s (the oracle's "
+                             "window propagation; the reference's own library runs this propagation and then "
+                             "queries every vertex j > i)"}
         else:
             cpu = {"value": n_cpu / dt, "unit": "perm/s", "cores": 1, "kind": "port",
                    "sample": f"{n_cpu} permutations of the same workload, {dt:.1f} s"}
@@ -321,6 +338,37 @@ def run_next(args):
                              "frac": achieved / hbm, "peak_source": peak_kind + " hbm_gbs",
                              "note": "16 B per gather entry (index, pair, weight, value; every image re-reads "
                                      "the list)"},
+                "cpu_baseline": cpu, "gpu_launches": K, "data": "synthetic"}
+        print(json.dumps(line), flush=True)
+        return
+    if kind == "geodesic":
+        from tfce_mediation_gb300.geodesic import GeodesicMesh
+        t0 = time.perf_counter()
+        m = GeodesicMesh(d["v"], d["f"])
+        setup_s = time.perf_counter() - t0
+        V = d["v"].shape[0]
+        for _ in range(args.warmup):
+            m.lists(3.0, True, 0, min(V, 4096))
+        times, n_pairs = [], 0
+        for _ in range(K):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            i, j, dist = m.lists(d["radius"], True)
+            times.append(time.perf_counter() - t0)
+            n_pairs = int(i.shape[0])
+        dt = float(np.median(times))
+        t0 = time.perf_counter()
+        n3 = int(m.lists(3.0, True)[0].shape[0])
+        dt3 = time.perf_counter() - t0
+        line = {"metric": "sources/s", "value": V / dt, "unit": "sources/s", "workload": kind,
+                "config": {"workload": NEXT[kind], "sources": V, "saddle_vertices": m.n_saddle,
+                           "pairs_below_radius": n_pairs},
+                "seconds_per_mesh": dt, "mesh_setup_s": setup_s, "steps": K, "warmup": args.warmup,
+                "higher_is_better": True,
+                "radius_3mm": {"seconds_per_mesh": dt3, "pairs": n3},
+                "note": "whole call through GeodesicMesh.lists (propagation of every source on the GPU, lists "
+                        "copied back and ordered by (i, j) on the host); latency-bound: one thread per source "
+                        "walks its own heap and distance table",
                 "cpu_baseline": cpu, "gpu_launches": K, "data": "synthetic"}
         print(json.dumps(line), flush=True)
         return

@@ -28,6 +28,8 @@
  *   reg_rm_ancova_one_bs_factor / _two_bs_factor  tfce_mediation/pyfunc.py:1712-2280
  *                                                     -> glm_stat_tc (mode 4), rm_anova_combine
  *   calc_gd_fwhm  tfce_mediation/cynumstats.pyx:76-107  -> gd_fwhm_weights, gd_fwhm_smooth
+ *   adjacency.compute / compute_distance_parallel  tfce_mediation/adjacency.pyx:44-106
+ *                                                     -> geodesic_mesh_*, geodesic_distance_lists
  */
 #ifndef TFCE_GB300_H_
 #define TFCE_GB300_H_
@@ -387,6 +389,36 @@ int gd_fwhm_weights(const float* dist, int64_t M, float scale, float* w, void* s
 int gd_fwhm_smooth(const int64_t* off, const int32_t* src, const int32_t* pidx, const float* w, int64_t M,
                    const float* data, int64_t ld, int32_t B, int32_t V, float* out, int64_t ldo, int32_t* err,
                    void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Exact geodesic distance lists (adjacency.compute / compute_distance_parallel,
+ * tfce_mediation/adjacency.pyx:44-106, over the exact geodesic library in
+ * tfce_mediation/lib/geodesic).  For every source vertex i of a triangle mesh,
+ * the vertices j whose exact geodesic distance along the surface is below a
+ * threshold.  Propagation runs from each source up to threshold + 1e-10, as
+ * the reference propagates (adjacency.pyx:54, :94).
+ *   geodesic_mesh_create: host pts [n_vertices][3] float32 and faces
+ *     [n_faces][3] int32; rejects (TFCE_EINVAL) out-of-range or repeated face
+ *     vertices, zero-length edges, zero-area faces and edges shared by more
+ *     than two faces.  Vertices whose total angle exceeds 2 pi - 1e-5, and
+ *     boundary vertices, are the pseudo-sources geodesics may bend around
+ *     (the reference's rule, lib/geodesic/geodesic_mesh.h:335-344);
+ *     geodesic_mesh_saddles returns their count.
+ *   geodesic_distance_lists: sources [src_lo, src_hi); keeps (i, j, distance)
+ *     for every j != i with distance < threshold (only j > i when
+ *     only_greater, the pairs compute_distance_parallel returns), sorted by i
+ *     then j; *n_out gets their number.  Synchronous.  TFCE_ERANGE when a
+ *     source's propagation outgrows 16384 queued windows or reached vertices.
+ *   geodesic_take_lists: copies the kept lists into host arrays of at least
+ *     *n_out entries and releases them. */
+typedef struct geodesic_mesh geodesic_mesh;
+int geodesic_mesh_create(const float* pts, int32_t n_vertices, const int32_t* faces, int32_t n_faces,
+                         geodesic_mesh** out);
+void geodesic_mesh_destroy(geodesic_mesh* m);
+int geodesic_mesh_saddles(geodesic_mesh* m, int32_t* n_saddle);
+int geodesic_distance_lists(geodesic_mesh* m, double threshold, int32_t only_greater, int32_t src_lo,
+                            int32_t src_hi, int64_t* n_out);
+int geodesic_take_lists(geodesic_mesh* m, int32_t* out_i, int32_t* out_j, double* out_d, int64_t cap);
 
 /* ---------------------------------------------------------------------------
  * FWER.  fwer_sort sorts n doubles ascending in place (device).  fwer_lookup

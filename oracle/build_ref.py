@@ -7,9 +7,12 @@ checkout is ``$TFCE_REFERENCE_ROOT`` when that is set, else a directory named
 
 * ``oracle/_ref/libref_tfce.so`` -- ``tfce_mediation/lib/fast_tfce.hpp``
   (the reference sweep) behind the C-ABI shim ``oracle/ref_tfce_shim.cpp``;
-* ``oracle/_ref/tfce_mediation/{tfce,cynumstats}*.so`` -- the reference's
-  Cython operator modules ``tfce_mediation/tfce.pyx`` and
-  ``tfce_mediation/cynumstats.pyx``, cythonized with language_level 2 (they use
+* ``oracle/_ref/libref_geodesic.so`` -- the header-only exact geodesic library
+  ``tfce_mediation/lib/geodesic/`` behind ``oracle/ref_geodesic_shim.cpp``;
+* ``oracle/_ref/tfce_mediation/{tfce,cynumstats,adjacency}*.so`` -- the
+  reference's Cython modules ``tfce_mediation/tfce.pyx``,
+  ``tfce_mediation/cynumstats.pyx`` and ``tfce_mediation/adjacency.pyx`` (the
+  exact geodesic neighbour lists over ``lib/geodesic``), cythonized with language_level 2 (they use
   ``xrange``) into ``oracle/_ref/cython/`` and compiled as C++11, the flags
   ``tfce_mediation/setup.py:25-41`` gives them.
 
@@ -49,6 +52,22 @@ def build_shim(ref: str) -> str | None:
     return so
 
 
+def build_geodesic_shim(ref: str) -> str | None:
+    """oracle/_ref/libref_geodesic.so: the reference's header-only exact
+    geodesic library (tfce_mediation/lib/geodesic) behind
+    oracle/ref_geodesic_shim.cpp."""
+    lib = os.path.join(ref, "tfce_mediation", "lib", "geodesic")
+    if not os.path.isfile(os.path.join(lib, "geodesic_algorithm_exact.h")):
+        return None
+    os.makedirs(OUT, exist_ok=True)
+    so = os.path.join(OUT, "libref_geodesic.so")
+    src = os.path.join(HERE, "ref_geodesic_shim.cpp")
+    if os.path.exists(so) and os.path.getmtime(so) >= os.path.getmtime(src):
+        return so
+    subprocess.check_call(["g++", "-O2", "-std=c++11", "-shared", "-fPIC", "-w", "-I", lib, src, "-o", so])
+    return so
+
+
 def build_cython(ref: str) -> bool:
     pkg = os.path.join(ref, "tfce_mediation")
     if not os.path.isfile(os.path.join(pkg, "tfce.pyx")):
@@ -66,7 +85,7 @@ def build_cython(ref: str) -> bool:
     if not os.path.exists(init):
         open(init, "w").close()
     have = [f for f in os.listdir(dst) if f.endswith(".so")]
-    if any(f.startswith("tfce.") for f in have) and any(f.startswith("cynumstats.") for f in have):
+    if all(any(f.startswith(m + ".") for f in have) for m in ("tfce", "cynumstats", "adjacency")):
         return True
     exts = [
         Extension("tfce_mediation.tfce", [os.path.join(pkg, "tfce.pyx")],
@@ -74,6 +93,9 @@ def build_cython(ref: str) -> bool:
                   language="c++", extra_compile_args=["-std=c++11", "-O2", "-w"]),
         Extension("tfce_mediation.cynumstats", [os.path.join(pkg, "cynumstats.pyx")],
                   include_dirs=[numpy.get_include()],
+                  language="c++", extra_compile_args=["-std=c++11", "-O2", "-w"]),
+        Extension("tfce_mediation.adjacency", [os.path.join(pkg, "adjacency.pyx")],
+                  include_dirs=[os.path.join(pkg, "lib"), numpy.get_include()],
                   language="c++", extra_compile_args=["-std=c++11", "-O2", "-w"]),
     ]
     exts = cythonize(exts, build_dir=os.path.join(OUT, "cython"), quiet=True,
@@ -94,6 +116,10 @@ def build() -> dict:
     if not os.path.isdir(ref):
         return out
     out["shim"] = build_shim(ref)
+    try:
+        out["geodesic"] = build_geodesic_shim(ref)
+    except Exception as exc:  # pins the geodesic oracle only
+        print(f"oracle/build_ref.py: geodesic shim not built: {exc}", file=sys.stderr)
     try:
         out["cython"] = build_cython(ref)
     except Exception as exc:  # the shim alone still pins the sweep

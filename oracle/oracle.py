@@ -38,10 +38,10 @@ def build() -> str:
     same recipe works on x86_64 and aarch64)."""
     os.makedirs(_BUILD, exist_ok=True)
     so = os.path.join(_BUILD, "libtfce_oracle.so")
-    src = os.path.join(HERE, "tfce_oracle.c")
-    if not (os.path.exists(so) and os.path.getmtime(so) >= os.path.getmtime(src)):
+    srcs = [os.path.join(HERE, "tfce_oracle.c"), os.path.join(HERE, "geodesic_oracle.c")]
+    if not (os.path.exists(so) and all(os.path.getmtime(so) >= os.path.getmtime(x) for x in srcs)):
         tmp = so + f".{os.getpid()}.tmp"
-        subprocess.check_call(["gcc", "-O2", "-std=c11", "-shared", "-fPIC", src, "-o", tmp, "-lm"])
+        subprocess.check_call(["gcc", "-O2", "-std=c11", "-shared", "-fPIC"] + srcs + ["-o", tmp, "-lm"])
         os.replace(tmp, so)
     return so
 
@@ -62,8 +62,73 @@ def lib():
                                             ctypes.c_int, _f32p, ctypes.c_int]
         l.oracle_threshold_table.restype = ctypes.c_int
         l.oracle_threshold_table.argtypes = [ctypes.c_float, _f32p, ctypes.c_int]
+        l.oracle_geodesic_lists.restype = ctypes.c_int
+        l.oracle_geodesic_lists.argtypes = _GEO_ARGS
         _LIB = l
     return _LIB
+
+
+_GEO_ARGS = [ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_double, ctypes.c_int32,
+             ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+             ctypes.c_void_p]
+_REF_GEO = None
+
+
+def _geo_call(fn, v, f, threshold, only_greater, src_lo, src_hi, cap):
+    v = np.ascontiguousarray(v, np.float32)
+    f = np.ascontiguousarray(f, np.int32)
+    src_hi = v.shape[0] if src_hi is None else int(src_hi)
+    if cap is None:
+        cap = 4096 + 256 * (src_hi - int(src_lo))
+    while True:
+        oi = np.empty(cap, np.int32)
+        oj = np.empty(cap, np.int32)
+        od = np.empty(cap, np.float64)
+        n = ctypes.c_int64()
+        rc = fn(v.shape[0], v.ctypes.data, f.shape[0], f.ctypes.data, float(threshold), int(bool(only_greater)),
+                int(src_lo), src_hi, cap, oi.ctypes.data, oj.ctypes.data, od.ctypes.data, ctypes.byref(n))
+        if rc == -4:
+            cap *= 4
+            continue
+        if rc:
+            raise ValueError(f"geodesic lists failed ({rc})")
+        k = n.value
+        return oi[:k].copy(), oj[:k].copy(), od[:k].copy()
+
+
+def geodesic_lists(v, f, threshold, only_greater=True, src_lo=0, src_hi=None, cap=None):
+    """Exact geodesic (i, j, d) for sources i in [src_lo, src_hi) and vertices
+    j != i with d < threshold (j > i when only_greater), sorted by i then j:
+    the pairs tfce_mediation/adjacency.pyx:83-106 lists, by the window
+    propagation restated in oracle/geodesic_oracle.c."""
+    return _geo_call(lib().oracle_geodesic_lists, v, f, threshold, only_greater, src_lo, src_hi, cap)
+
+
+def ref_geodesic_lib():
+    """The reference's exact geodesic library behind oracle/ref_geodesic_shim.cpp
+    (oracle/_ref/libref_geodesic.so), when it was built from a reference
+    checkout on this machine; otherwise None."""
+    global _REF_GEO
+    if _REF_GEO is None:
+        so = os.path.join(HERE, "_ref", "libref_geodesic.so")
+        if not os.path.exists(so):
+            return None
+        try:
+            l = ctypes.CDLL(so)
+        except OSError:
+            return None
+        l.ref_geodesic_lists.restype = ctypes.c_int
+        l.ref_geodesic_lists.argtypes = _GEO_ARGS
+        _REF_GEO = l
+    return _REF_GEO
+
+
+def ref_geodesic_lists(v, f, threshold, only_greater=True, src_lo=0, src_hi=None, cap=None):
+    """The same lists from the reference's own library (None when it is not built)."""
+    l = ref_geodesic_lib()
+    if l is None:
+        return None
+    return _geo_call(l.ref_geodesic_lists, v, f, threshold, only_greater, src_lo, src_hi, cap)
 
 
 def ref_lib():

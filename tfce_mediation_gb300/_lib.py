@@ -59,6 +59,12 @@ SIGNATURES = {
                                                 ctypes.c_int32, ctypes.c_int32, c_vp, c_vp, c_vp,
                                                 ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, c_vp,
                                                 ctypes.c_int32, c_vp, c_vp]),
+    "geodesic_mesh_create": (ctypes.c_int, [c_f32p, ctypes.c_int32, c_i32p, ctypes.c_int32, ctypes.POINTER(c_vp)]),
+    "geodesic_mesh_destroy": (None, [c_vp]),
+    "geodesic_mesh_saddles": (ctypes.c_int, [c_vp, c_i32p]),
+    "geodesic_distance_lists": (ctypes.c_int, [c_vp, ctypes.c_double, ctypes.c_int32, ctypes.c_int32,
+                                               ctypes.c_int32, c_i64p]),
+    "geodesic_take_lists": (ctypes.c_int, [c_vp, c_i32p, c_i32p, c_f64p, ctypes.c_int64]),
     "glm_tstat": (ctypes.c_int, [c_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int64, c_vp, c_vp,
                                  c_vp, c_vp, ctypes.c_int32, ctypes.c_int32, c_vp, ctypes.c_int32,
                                  c_vp, ctypes.c_int64, c_vp]),

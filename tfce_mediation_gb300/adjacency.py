@@ -13,6 +13,11 @@ same quirks), vectorised with numpy instead of per-vertex Python loops:
   (keeps self entries and voxel 0's outgoing list, so it is asymmetric);
 * ``merge_adjacency_array`` -- tfce_mediation/tm_func.py:521-540.
 
+``compute`` and ``compute_distance_parallel`` (the reference's own
+``tfce_mediation.adjacency`` module, adjacency.pyx:44-106: exact geodesic
+neighbour lists) are the GPU drop-ins of ``geodesic.py``, importable from here
+under the reference's module name.
+
 ``AdjacencySet`` owns the device CSR (the C-ABI ``tfce_adjset`` handle).
 """
 from __future__ import annotations
@@ -23,6 +28,7 @@ import itertools
 import numpy as np
 
 from . import _lib
+from .geodesic import compute, compute_distance_parallel  # noqa: F401  (adjacency.pyx:44-106)
 
 
 # ---------------------------------------------------------------------------
