@@ -629,6 +629,50 @@ def run_config(kind, args, stash=None):
     return line
 
 
+def dropin_rate(st, P, n_perm=2048):
+    """The reference-facing drop-in, timed as a user of the reference's CLI
+    would run it: randomise.vertex_regress_run (the
+    vertex_tfce_multiple_regression_randomise.py replacement) reading the
+    python_temp_<surface> hand-off files of the headline study (Y, masks,
+    adjacency lists, per-vertex density weights) and appending the
+    per-permutation maxima to the CSVs.  Wall clock of one call over n_perm
+    permutations, files, engine set-up and CSV writing included."""
+    from types import SimpleNamespace
+
+    from tfce_mediation_gb300 import adjacency as A
+    from tfce_mediation_gb300 import randomise
+    Vh = st.segments[1] - st.segments[0]
+    off, idx = st.offsets[:Vh + 1], st.indices[:st.offsets[Vh]]
+    adj = np.empty(Vh, dtype=object)
+    for v, l in enumerate(A.from_csr(off, idx)):
+        adj[v] = l
+    vd = A.vertex_density((off, idx))
+    cwd = os.getcwd()
+    with tempfile.TemporaryDirectory() as root:
+        d = os.path.join(root, "python_temp_area")
+        os.makedirs(d)
+        mask = np.ones(Vh, bool)
+        for name, val in (("merge_y", st.Y), ("num_vertex", st.Y.shape[1]), ("num_vertex_lh", Vh),
+                          ("all_vertex", Vh), ("bin_mask_lh", mask), ("bin_mask_rh", mask), ("num_subjects", st.n),
+                          ("pred_x", st.pred_x), ("adjac_lh", adj), ("adjac_rh", adj),
+                          ("optstfce", np.array([2.0, 1.0])), ("vdensity_lh", vd), ("vdensity_rh", vd)):
+            np.save(os.path.join(d, f"{name}.npy"), val, allow_pickle=True)
+        os.chdir(root)
+        try:
+            opts = SimpleNamespace(range=[0, n_perm - 1], surface=["area"], seed=[SEED], specifyvars=None,
+                                   exchangeblock=None, batch=P)
+            t0 = time.perf_counter()
+            randomise.vertex_regress_run(opts)
+            dt = time.perf_counter() - t0
+            lines = sum(1 for _ in open("output_area/perm_Tstat_area/perm_tstat_con1_TFCE_maxVertex.csv"))
+        finally:
+            os.chdir(cwd)
+    return {"value": n_perm / dt, "unit": "perm/s", "perms": n_perm, "seconds": dt, "csv_lines_per_contrast": lines,
+            "note": "randomise.vertex_regress_run (drop-in for vertex_tfce_multiple_regression_randomise.py): "
+                    "hand-off files read, engine built, maxima appended to the CSVs, all inside the timed call; "
+                    "per-vertex density weights on, so the sweep keeps its potential form"}
+
+
 def time_to_fwer(eng, st, n_perm=10_000, seed=99):
     """Wall time from the resident data to the 1-p(FWER) maps of every
     contrast and sign: the plain path (n_perm permutations) and the learned
@@ -845,6 +889,7 @@ def run_gpu(args):
     h2d = st.Y.nbytes + sum(v.numel() * v.element_size() for k_, v in slot.items()
                             if k_.startswith("h_") and k_ != "h_max")
     d2h = P * C * 2 * S * 4
+    dropin = dropin_rate(st, P) if (rank == 0 and not args.no_configs) else None
 
     if rank != 0:
         dist.destroy_process_group() if ws > 1 else None
@@ -927,6 +972,7 @@ def run_gpu(args):
                 "note": "PermutationEngine.run_stream; per step: Y (pinned host) -> HBM and re-tiled, host "
                         "FP64 design inverses (overlapped with the previous step), captured GLM + sweep, "
                         "maxima -> host"},
+        "dropin": dropin,
         "job_api": {"value": job_value, "unit": "perm/s",
                     "note": "PermutationEngine.run_graph over %d permutations, Y resident" % (8 * P)},
         "gpu_launches": launches,
