@@ -32,6 +32,7 @@
 // with four times the capacity; every loop is bounded.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <numeric>
@@ -43,7 +44,7 @@ namespace tfgb {
 namespace geo {
 
 constexpr int kThreads = 128;
-constexpr int64_t kIterLimit = int64_t(1) << 22;  // heap pops per source
+constexpr int64_t kIterLimit = int64_t(1) << 22;  // heap pops / rounds per source
 
 struct Mesh {
   const int32_t* face;    // [nf][3]
@@ -55,10 +56,134 @@ struct Mesh {
   const uint8_t* saddle;  // [nv]
 };
 
-// Per-thread scratch, element k of thread t at k * T + t.
+// A queued item: a window (tag = face << 2 | edge) or a pseudo-source
+// (tag = -1 - v, key = its distance).
+struct Item {
+  double key;
+  int32_t tag;
+  double b0, b1, sx, sy, sig;
+};
+
+// The window geometry, shared by both kernels.  St supplies the queue and
+// the table of reached vertices: push(Item), dist(v), reach(v, d).
+template <class St>
+struct Geometry {
+  const Mesh& m;
+  St& st;
+  double max_dist;
+
+  // a window on local edge e of face f, entering f
+  __device__ void window(int32_t f, int32_t e, double b0, double b1, double sx, double sy, double sig) {
+    const double L = m.len[3 * f + e];
+    b0 = fmax(b0, 0.0);
+    b1 = fmin(b1, L);
+    if (!(b1 - b0 > 1e-12 * L)) return;
+    const double x = sx < b0 ? b0 - sx : (sx > b1 ? sx - b1 : 0.0);
+    const double key = sig + sqrt(x * x + sy * sy);
+    if (key > max_dist) return;
+    // end-vertex filter: P = f_e at 0, Q = f_{e+1} at L
+    const double dP = st.dist(m.face[3 * f + e]);
+    const double dQ = st.dist(m.face[3 * f + (e + 1) % 3]);
+    const double far = sig + hypot(sx - b1, sy), near = sig + hypot(sx - b0, sy);
+    if (far > dP + b1 || near > dQ + (L - b0)) return;
+    st.push(Item{key, (f << 2) | e, b0, b1, sx, sy, sig});
+  }
+
+  // the child crossing face f over its local edge le, from 2-D point pa (the
+  // edge's first vertex in f) to pb, covering [q0, q1]; pthird is f's third
+  // vertex, on the far side of the edge from the face beyond it
+  __device__ void child(int32_t f, int32_t le, double2 pa, double2 pb, double2 pthird, double2 q0, double2 q1,
+                        double sx, double sy, double sig) {
+    const int32_t nb = m.nbr[3 * f + le];
+    if (nb < 0) return;
+    const int32_t g = nb >> 2, ge = nb & 3;
+    const bool same = (m.face[3 * g + ge] == m.face[3 * f + le]);
+    const double2 P = same ? pa : pb, Q = same ? pb : pa;
+    double ux = Q.x - P.x, uy = Q.y - P.y;
+    const double ul = hypot(ux, uy);
+    ux /= ul;
+    uy /= ul;
+    double nx = -uy, ny = ux;
+    if (nx * (pthird.x - P.x) + ny * (pthird.y - P.y) > 0.0) {
+      nx = -nx;
+      ny = -ny;
+    }
+    const double s2x = (sx - P.x) * ux + (sy - P.y) * uy;
+    const double s2y = (sx - P.x) * nx + (sy - P.y) * ny;
+    if (!(s2y < 0.0)) return;  // the image lies on the edge's line
+    double t0 = (q0.x - P.x) * ux + (q0.y - P.y) * uy;
+    double t1 = (q1.x - P.x) * ux + (q1.y - P.y) * uy;
+    if (t0 > t1) {
+      const double x = t0;
+      t0 = t1;
+      t1 = x;
+    }
+    window(g, ge, t0, t1, s2x, s2y, sig);
+  }
+
+  // where the line from s through (x, 0) meets segment a -> b (clamped)
+  __device__ static double2 hit(double sx, double sy, double x, double2 a, double2 b) {
+    const double dx = x - sx, dy = -sy;
+    const double ex = b.x - a.x, ey = b.y - a.y;
+    const double mu = ((sx - a.x) * dy - (sy - a.y) * dx) / (ex * dy - ey * dx);
+    const double c = fmin(fmax(mu, 0.0), 1.0);
+    return make_double2(a.x + c * ex, a.y + c * ey);
+  }
+
+  __device__ void propagate(const Item& w) {
+    const int32_t f = w.tag >> 2, e = w.tag & 3;
+    const double L = m.len[3 * f + e];
+    const double2 C = m.third[3 * f + e];
+    const double2 A = make_double2(0.0, 0.0), B = make_double2(L, 0.0);
+    const double sx = w.sx, sy = w.sy;
+    const double xc = sx + (C.x - sx) * (-sy) / (C.y - sy);  // line s -> C at y = 0
+    if (xc >= w.b0 && xc <= w.b1) st.reach(m.face[3 * f + (e + 2) % 3], w.sig + hypot(C.x - sx, C.y - sy));
+    if (w.b0 < xc) {  // edge C -> A: local edge e + 2
+      const double2 q0 = hit(sx, sy, w.b0, A, C);
+      const double2 q1 = (w.b1 < xc) ? hit(sx, sy, w.b1, A, C) : C;
+      child(f, (e + 2) % 3, C, A, B, q0, q1, sx, sy, w.sig);
+    }
+    if (w.b1 > xc) {  // edge B -> C: local edge e + 1
+      const double2 q0 = (w.b0 > xc) ? hit(sx, sy, w.b0, B, C) : C;
+      const double2 q1 = hit(sx, sy, w.b1, B, C);
+      child(f, (e + 1) % 3, B, C, A, q0, q1, sx, sy, w.sig);
+    }
+  }
+
+  // a (pseudo-)source u at distance du: its neighbours along the edges, and a
+  // window on the edge opposite u in every face around it, entering the face
+  // beyond that edge
+  __device__ void expand(int32_t u, double du) {
+    for (int32_t k = m.vf_off[u]; k < m.vf_off[u + 1]; ++k) {
+      const int32_t f = m.vf[k] >> 2, c = m.vf[k] & 3;
+      const int32_t e = (c + 1) % 3;  // opposite edge f_{c+1} -> f_{c+2}
+      const int32_t v1 = m.face[3 * f + e], v2 = m.face[3 * f + (e + 1) % 3];
+      const double l1 = m.len[3 * f + c];            // u -> v1
+      const double l2 = m.len[3 * f + (c + 2) % 3];  // v2 -> u
+      st.reach(v1, du + l1);
+      st.reach(v2, du + l2);
+      const int32_t nb = m.nbr[3 * f + e];
+      if (nb < 0) continue;
+      const int32_t g = nb >> 2, ge = nb & 3;
+      const double L = m.len[3 * f + e];
+      const bool p_is_v1 = (m.face[3 * g + ge] == v1);
+      const double dP = p_is_v1 ? l1 : l2, dQ = p_is_v1 ? l2 : l1;
+      const double x = (L * L + dP * dP - dQ * dQ) / (2.0 * L);
+      const double y2 = dP * dP - x * x;
+      const double y = -(y2 > 0.0 ? sqrt(y2) : 0.0);
+      if (y < 0.0) window(g, ge, 0.0, L, x, y, du);
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// One thread per source: a binary heap and an open-addressing table of reached
+// vertices in global scratch, element k of thread t at k * T + t.  Used for
+// the sources whose propagation outgrows a warp's shared-memory queue.
+// ---------------------------------------------------------------------------
 struct Scratch {
   double* hkey;   // heap: smallest distance of the item
-  int32_t* htag;  // face << 2 | edge of a window, or -1 - v for a pseudo-source v
+  int32_t* htag;
   double* hb0;
   double* hb1;
   double* hsx;
@@ -72,20 +197,14 @@ struct Scratch {
   int32_t tbits;    // table capacity per thread = 1 << tbits
 };
 
-struct Item {
-  double key;
-  int32_t tag;
-  double b0, b1, sx, sy, sig;
-};
-
-struct Ctx {
+struct ThreadState {
   const Mesh& m;
   const Scratch& s;
   int64_t t, T;
   int32_t nh = 0, nocc = 0;
   bool fail = false;
   double max_dist;
-  __device__ Ctx(const Mesh& m_, const Scratch& s_, int64_t t_, int64_t T_, double md)
+  __device__ ThreadState(const Mesh& m_, const Scratch& s_, int64_t t_, int64_t T_, double md)
       : m(m_), s(s_), t(t_), T(T_), max_dist(md) {}
   __device__ int64_t ix(int32_t k) const { return static_cast<int64_t>(k) * T + t; }
 
@@ -162,7 +281,6 @@ struct Ctx {
     const int32_t k = slot(v, false);
     return k < 0 ? static_cast<double>(INFINITY) : s.td[ix(k)];
   }
-
   // d(v) = min(d(v), dv); a pseudo-source whose distance fell is queued
   __device__ void reach(int32_t v, double dv) {
     const int32_t k = slot(v, true);
@@ -171,119 +289,17 @@ struct Ctx {
     if (m.saddle[v] && dv <= max_dist) push(Item{dv, -1 - v, 0.0, 0.0, 0.0, 0.0, 0.0});
   }
 
-  // a window on local edge e of face f, entering f
-  __device__ void window(int32_t f, int32_t e, double b0, double b1, double sx, double sy, double sig) {
-    const double L = m.len[3 * f + e];
-    b0 = fmax(b0, 0.0);
-    b1 = fmin(b1, L);
-    if (!(b1 - b0 > 1e-12 * L)) return;
-    const double x = sx < b0 ? b0 - sx : (sx > b1 ? sx - b1 : 0.0);
-    const double key = sig + sqrt(x * x + sy * sy);
-    if (key > max_dist) return;
-    // end-vertex filter: P = f_e at 0, Q = f_{e+1} at L
-    const double dP = dist(m.face[3 * f + e]);
-    const double dQ = dist(m.face[3 * f + (e + 1) % 3]);
-    const double far = sig + hypot(sx - b1, sy), near = sig + hypot(sx - b0, sy);
-    if (far > dP + b1 || near > dQ + (L - b0)) return;
-    push(Item{key, (f << 2) | e, b0, b1, sx, sy, sig});
-  }
-
-  // the child crossing face f over its local edge le, from 2-D point pa (the
-  // edge's first vertex in f) to pb, covering [q0, q1]; pthird is f's third
-  // vertex, on the far side of the edge from the face beyond it
-  __device__ void child(int32_t f, int32_t le, double2 pa, double2 pb, double2 pthird, double2 q0, double2 q1,
-                        double sx, double sy, double sig) {
-    const int32_t nb = m.nbr[3 * f + le];
-    if (nb < 0) return;
-    const int32_t g = nb >> 2, ge = nb & 3;
-    const bool same = (m.face[3 * g + ge] == m.face[3 * f + le]);
-    const double2 P = same ? pa : pb, Q = same ? pb : pa;
-    double ux = Q.x - P.x, uy = Q.y - P.y;
-    const double ul = hypot(ux, uy);
-    ux /= ul;
-    uy /= ul;
-    double nx = -uy, ny = ux;
-    if (nx * (pthird.x - P.x) + ny * (pthird.y - P.y) > 0.0) {
-      nx = -nx;
-      ny = -ny;
-    }
-    const double s2x = (sx - P.x) * ux + (sy - P.y) * uy;
-    const double s2y = (sx - P.x) * nx + (sy - P.y) * ny;
-    if (!(s2y < 0.0)) return;  // the image lies on the edge's line
-    double t0 = (q0.x - P.x) * ux + (q0.y - P.y) * uy;
-    double t1 = (q1.x - P.x) * ux + (q1.y - P.y) * uy;
-    if (t0 > t1) {
-      const double x = t0;
-      t0 = t1;
-      t1 = x;
-    }
-    window(g, ge, t0, t1, s2x, s2y, sig);
-  }
-
-  // where the line from s through (x, 0) meets segment a -> b (clamped)
-  __device__ static double2 hit(double sx, double sy, double x, double2 a, double2 b) {
-    const double dx = x - sx, dy = -sy;
-    const double ex = b.x - a.x, ey = b.y - a.y;
-    const double mu = ((sx - a.x) * dy - (sy - a.y) * dx) / (ex * dy - ey * dx);
-    const double c = fmin(fmax(mu, 0.0), 1.0);
-    return make_double2(a.x + c * ex, a.y + c * ey);
-  }
-
-  __device__ void propagate(const Item& w) {
-    const int32_t f = w.tag >> 2, e = w.tag & 3;
-    const double L = m.len[3 * f + e];
-    const double2 C = m.third[3 * f + e];
-    const double2 A = make_double2(0.0, 0.0), B = make_double2(L, 0.0);
-    const double sx = w.sx, sy = w.sy;
-    const double xc = sx + (C.x - sx) * (-sy) / (C.y - sy);  // line s -> C at y = 0
-    if (xc >= w.b0 && xc <= w.b1) reach(m.face[3 * f + (e + 2) % 3], w.sig + hypot(C.x - sx, C.y - sy));
-    if (w.b0 < xc) {  // edge C -> A: local edge e + 2
-      const double2 q0 = hit(sx, sy, w.b0, A, C);
-      const double2 q1 = (w.b1 < xc) ? hit(sx, sy, w.b1, A, C) : C;
-      child(f, (e + 2) % 3, C, A, B, q0, q1, sx, sy, w.sig);
-    }
-    if (w.b1 > xc) {  // edge B -> C: local edge e + 1
-      const double2 q0 = (w.b0 > xc) ? hit(sx, sy, w.b0, B, C) : C;
-      const double2 q1 = hit(sx, sy, w.b1, B, C);
-      child(f, (e + 1) % 3, B, C, A, q0, q1, sx, sy, w.sig);
-    }
-  }
-
-  // a (pseudo-)source u at distance du: its neighbours along the edges, and a
-  // window on the edge opposite u in every face around it, entering the face
-  // beyond that edge
-  __device__ void expand(int32_t u, double du) {
-    for (int32_t k = m.vf_off[u]; k < m.vf_off[u + 1] && !fail; ++k) {
-      const int32_t f = m.vf[k] >> 2, c = m.vf[k] & 3;
-      const int32_t e = (c + 1) % 3;  // opposite edge f_{c+1} -> f_{c+2}
-      const int32_t v1 = m.face[3 * f + e], v2 = m.face[3 * f + (e + 1) % 3];
-      const double l1 = m.len[3 * f + c];            // u -> v1
-      const double l2 = m.len[3 * f + (c + 2) % 3];  // v2 -> u
-      reach(v1, du + l1);
-      reach(v2, du + l2);
-      const int32_t nb = m.nbr[3 * f + e];
-      if (nb < 0) continue;
-      const int32_t g = nb >> 2, ge = nb & 3;
-      const double L = m.len[3 * f + e];
-      const bool p_is_v1 = (m.face[3 * g + ge] == v1);
-      const double dP = p_is_v1 ? l1 : l2, dQ = p_is_v1 ? l2 : l1;
-      const double x = (L * L + dP * dP - dQ * dQ) / (2.0 * L);
-      const double y2 = dP * dP - x * x;
-      const double y = -(y2 > 0.0 ? sqrt(y2) : 0.0);
-      if (y < 0.0) window(g, ge, 0.0, L, x, y, du);
-    }
-  }
-
   __device__ void run(int32_t src) {
     for (int32_t k = 0; k < nocc; ++k) s.tv[ix(s.occ[ix(k)])] = -1;
     nocc = 0;
     nh = 0;
     fail = false;
+    Geometry<ThreadState> geo{m, *this, max_dist};
     const int32_t k0 = slot(src, true);
     if (k0 < 0) return;
     s.td[ix(k0)] = 0.0;
     s.tdone[ix(k0)] = 0.0;
-    expand(src, 0.0);
+    geo.expand(src, 0.0);
     for (int64_t it = 0; nh > 0 && !fail; ++it) {
       if (it >= kIterLimit) {
         fail = true;
@@ -296,37 +312,139 @@ struct Ctx {
         const int32_t k = slot(v, false);
         if (k < 0 || w.key > s.td[ix(k)] || s.tdone[ix(k)] <= w.key) continue;  // stale or done
         s.tdone[ix(k)] = w.key;
-        expand(v, w.key);
+        geo.expand(v, w.key);
       } else {
-        propagate(w);
+        geo.propagate(w);
       }
     }
   }
 };
 
+// ---------------------------------------------------------------------------
+// One warp per source.  The keys of the pending items and the table of
+// reached vertices live in the warp's shared memory, the item bodies in
+// global memory (per warp, contiguous).  Each round the warp takes up to 32
+// items whose key lies within delta of the smallest pending key (one per
+// lane), moves the last items into their places, and the lanes propagate
+// them together, pushing children and reaching vertices with shared-memory
+// atomics.  The filters are sound in any order, so the distances are the
+// same exact ones; delta trades a little extra work for 32-wide rounds.
+// ---------------------------------------------------------------------------
+constexpr int kWarpPool = 2048;            // pending items per warp
+constexpr int kWarpTabBits = 10;           // reached-vertex table: 1024 slots
+constexpr int kWarpTab = 1 << kWarpTabBits;
+constexpr int kWarpTabMax = 3 * kWarpTab / 4;
+constexpr int kWarpsPerCta = 4;
+
+struct WarpShared {
+  double key[kWarpPool];
+  unsigned long long td[kWarpTab];     // distance bits (non-negative doubles order as their bits)
+  unsigned long long tdone[kWarpTab];  // distance a pseudo-source was expanded at
+  int32_t tv[kWarpTab];                // vertex id, -1 empty
+  int32_t occ[kWarpTab];               // occupied slots
+  int32_t sel[32];
+  int32_t srcpos[32];
+  int32_t n_pool;
+  int32_t n_occ;
+  int32_t fail;
+};
+
+struct WarpBodies {  // per warp [kWarpPool]
+  int32_t* tag;
+  double* b0;
+  double* b1;
+  double* sx;
+  double* sy;
+  double* sig;
+};
+
+struct WarpState {
+  const Mesh& m;
+  WarpShared& w;
+  WarpBodies b;
+  double max_dist;
+
+  __device__ void push(const Item& it) {
+    const int32_t i = atomicAdd(&w.n_pool, 1);
+    if (i >= kWarpPool) {
+      w.fail = 1;
+      return;
+    }
+    w.key[i] = it.key;
+    b.tag[i] = it.tag;
+    b.b0[i] = it.b0;
+    b.b1[i] = it.b1;
+    b.sx[i] = it.sx;
+    b.sy[i] = it.sy;
+    b.sig[i] = it.sig;
+  }
+  // slot of v (claimed with a CAS when absent and insert is set), or -1
+  __device__ int32_t slot(int32_t v, bool insert) {
+    const uint32_t h = (static_cast<uint32_t>(v) * 2654435761u) >> (32 - kWarpTabBits);
+    volatile int32_t* tv = w.tv;
+    for (uint32_t p = 0; p < kWarpTab; ++p) {
+      const int32_t k = static_cast<int32_t>((h + p) & (kWarpTab - 1));
+      int32_t key = tv[k];
+      if (key == v) return k;
+      if (key < 0) {
+        if (!insert) return -1;
+        key = atomicCAS(&w.tv[k], -1, v);
+        if (key == -1) {
+          const int32_t n = atomicAdd(&w.n_occ, 1);
+          w.occ[n] = k;  // n < kWarpTab: every claim is one slot
+          if (n >= kWarpTabMax) w.fail = 1;
+          return k;
+        }
+        if (key == v) return k;
+      }
+    }
+    w.fail = 1;
+    return -1;
+  }
+  __device__ double dist(int32_t v) {
+    const int32_t k = slot(v, false);
+    if (k < 0) return static_cast<double>(INFINITY);
+    return __longlong_as_double(static_cast<long long>(reinterpret_cast<volatile unsigned long long*>(w.td)[k]));
+  }
+  __device__ void reach(int32_t v, double dv) {
+    const int32_t k = slot(v, true);
+    if (k < 0) return;
+    const unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(dv));
+    const unsigned long long old = atomicMin(&w.td[k], bits);
+    if (bits < old && m.saddle[v] && dv <= max_dist) push(Item{dv, -1 - v, 0.0, 0.0, 0.0, 0.0, 0.0});
+  }
+};
+
 struct LaunchArgs {
   Mesh m;
-  Scratch s;
-  const int32_t* src_list;  // sources (nullable: src_lo + q)
+  Scratch s;                 // thread-per-source kernel
+  WarpBodies wb;             // warp kernel: bodies of warp gw at gw * kWarpPool
+  const int32_t* src_list;   // sources (nullable: src_lo + q)
   int32_t src_lo;
   int32_t n_src;
   double threshold;
   double max_dist;
+  double delta;              // warp kernel: window of keys taken per round
   int32_t only_greater;
   int64_t cap;               // output entries
   int32_t* out_j;
   double* out_d;
   unsigned long long* cursor;
+  int32_t* queue;            // warp kernel: next source
   int64_t* src_base;         // [n_src] first output entry of each source (-1: failed)
   int32_t* src_count;        // [n_src]
   int32_t* failed;           // [n_src] sources to run again with more capacity
   int32_t* n_failed;
 };
 
+__device__ inline bool keep_pair(const LaunchArgs& a, int32_t src, int32_t v, double d) {
+  return v != src && (!a.only_greater || v > src) && d < a.threshold;
+}
+
 __global__ void __launch_bounds__(kThreads) geodesic_lists_kernel(LaunchArgs a) {
   const int64_t T = static_cast<int64_t>(gridDim.x) * blockDim.x;
   const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  Ctx c(a.m, a.s, t, T, a.max_dist);
+  ThreadState c(a.m, a.s, t, T, a.max_dist);
   for (int64_t q = t; q < a.n_src; q += T) {
     const int32_t src = a.src_list ? a.src_list[q] : a.src_lo + static_cast<int32_t>(q);
     c.run(src);
@@ -339,8 +457,7 @@ __global__ void __launch_bounds__(kThreads) geodesic_lists_kernel(LaunchArgs a) 
     int32_t n = 0;
     for (int32_t k = 0; k < c.nocc; ++k) {
       const int64_t i = c.ix(a.s.occ[c.ix(k)]);
-      const int32_t v = a.s.tv[i];
-      if (v != src && (!a.only_greater || v > src) && a.s.td[i] < a.threshold) ++n;
+      n += keep_pair(a, src, a.s.tv[i], a.s.td[i]);
     }
     const unsigned long long base = atomicAdd(a.cursor, static_cast<unsigned long long>(n));
     a.src_base[q] = static_cast<int64_t>(base);
@@ -348,16 +465,187 @@ __global__ void __launch_bounds__(kThreads) geodesic_lists_kernel(LaunchArgs a) 
     int64_t w = static_cast<int64_t>(base);
     for (int32_t k = 0; k < c.nocc; ++k) {
       const int64_t i = c.ix(a.s.occ[c.ix(k)]);
-      const int32_t v = a.s.tv[i];
-      const double d = a.s.td[i];
-      if (v != src && (!a.only_greater || v > src) && d < a.threshold) {
-        if (w < a.cap) {
-          a.out_j[w] = v;
-          a.out_d[w] = d;
-        }
-        ++w;
+      if (!keep_pair(a, src, a.s.tv[i], a.s.td[i])) continue;
+      if (w < a.cap) {
+        a.out_j[w] = a.s.tv[i];
+        a.out_d[w] = a.s.td[i];
+      }
+      ++w;
+    }
+  }
+}
+
+__device__ inline double warp_min(double x) {
+  for (int o = 16; o > 0; o >>= 1) x = fmin(x, __shfl_xor_sync(0xffffffffu, x, o));
+  return x;
+}
+
+__global__ void __launch_bounds__(32 * kWarpsPerCta) geodesic_warp_kernel(LaunchArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  WarpShared& w = reinterpret_cast<WarpShared*>(smem_raw)[wid];
+  const int64_t gw = static_cast<int64_t>(blockIdx.x) * kWarpsPerCta + wid;
+  WarpBodies b = a.wb;
+  b.tag += gw * kWarpPool;
+  b.b0 += gw * kWarpPool;
+  b.b1 += gw * kWarpPool;
+  b.sx += gw * kWarpPool;
+  b.sy += gw * kWarpPool;
+  b.sig += gw * kWarpPool;
+  WarpState st{a.m, w, b, a.max_dist};
+  Geometry<WarpState> geo{a.m, st, a.max_dist};
+  const unsigned all = 0xffffffffu;
+  const unsigned lt = (1u << lane) - 1u;
+  for (int k = lane; k < kWarpTab; k += 32) {
+    w.tv[k] = -1;
+    w.td[k] = static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(INFINITY)));
+    w.tdone[k] = w.td[k];
+  }
+  if (lane == 0) w.n_occ = 0;
+  __syncwarp();
+  for (;;) {
+    int32_t q = 0;
+    if (lane == 0) q = atomicAdd(a.queue, 1);
+    q = __shfl_sync(all, q, 0);
+    if (q >= a.n_src) break;
+    const int32_t src = a.src_list ? a.src_list[q] : a.src_lo + q;
+    // clear the previous source's slots
+    const int32_t nocc = w.n_occ;
+    __syncwarp();
+    for (int32_t k = lane; k < nocc; k += 32) {
+      const int32_t s = w.occ[k];
+      w.tv[s] = -1;
+      w.td[s] = static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(INFINITY)));
+      w.tdone[s] = w.td[s];
+    }
+    if (lane == 0) {
+      w.n_occ = 0;
+      w.n_pool = 0;
+      w.fail = 0;
+    }
+    __syncwarp();
+    if (lane == 0) {
+      const int32_t k0 = st.slot(src, true);
+      if (k0 >= 0) {
+        w.td[k0] = 0ull;
+        w.tdone[k0] = 0ull;
+        geo.expand(src, 0.0);
       }
     }
+    __syncwarp();
+    const volatile WarpShared& vw = w;
+    for (int64_t round = 0;; ++round) {
+      const int32_t n = vw.n_pool;
+      if (vw.fail || round >= kIterLimit) {
+        if (lane == 0) w.fail = 1;
+        break;
+      }
+      double kmin = static_cast<double>(INFINITY);
+      for (int32_t k = lane; k < n; k += 32) kmin = fmin(kmin, w.key[k]);
+      kmin = warp_min(kmin);
+      if (n == 0 || kmin > a.max_dist) break;
+      const double thr = kmin + a.delta;
+      // take up to 32 items with key <= thr, in pool order
+      int32_t taken = 0;
+      for (int32_t base = 0; base < n && taken < 32; base += 32) {
+        const int32_t idx = base + lane;
+        const bool qual = idx < n && w.key[idx] <= thr;
+        const unsigned mk = __ballot_sync(all, qual);
+        const int r = __popc(mk & lt);
+        if (qual && taken + r < 32) w.sel[taken + r] = idx;
+        taken = min(32, taken + __popc(mk));
+      }
+      __syncwarp();
+      Item it{};
+      const int32_t my = (lane < taken) ? w.sel[lane] : -1;
+      if (my >= 0) it = Item{w.key[my], b.tag[my], b.b0[my], b.b1[my], b.sx[my], b.sy[my], b.sig[my]};
+      __syncwarp();
+      if (my >= 0) w.key[my] = -1.0;  // taken
+      __syncwarp();
+      // the items beyond the new end that were not taken move into the holes below it
+      const int32_t n_new = n - taken;
+      const int32_t pos = n_new + lane;
+      const bool is_src = lane < taken && w.key[pos] >= 0.0;
+      const unsigned ms = __ballot_sync(all, is_src);
+      if (is_src) w.srcpos[__popc(ms & lt)] = pos;
+      const bool is_hole = my >= 0 && my < n_new;
+      const unsigned mh = __ballot_sync(all, is_hole);
+      __syncwarp();
+      if (is_hole) {
+        const int32_t from = w.srcpos[__popc(mh & lt)];
+        w.key[my] = w.key[from];
+        b.tag[my] = b.tag[from];
+        b.b0[my] = b.b0[from];
+        b.b1[my] = b.b1[from];
+        b.sx[my] = b.sx[from];
+        b.sy[my] = b.sy[from];
+        b.sig[my] = b.sig[from];
+      }
+      __syncwarp();
+      if (lane == 0) w.n_pool = n_new;
+      __syncwarp();
+      if (my >= 0) {
+        if (it.tag < 0) {
+          const int32_t v = -1 - it.tag;
+          const int32_t k = st.slot(v, false);
+          const unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(it.key));
+          if (k >= 0 && bits <= reinterpret_cast<volatile unsigned long long*>(w.td)[k] &&
+              atomicMin(&w.tdone[k], bits) > bits)
+            geo.expand(v, it.key);
+        } else {
+          geo.propagate(it);
+        }
+      }
+      __syncwarp();
+    }
+    __syncwarp();
+    if (vw.fail) {
+      if (lane == 0) {
+        a.src_base[q] = -1;
+        a.src_count[q] = 0;
+        a.failed[atomicAdd(a.n_failed, 1)] = src;
+      }
+      __syncwarp();
+      continue;
+    }
+    // output: the reached vertices below the threshold
+    const int32_t no = min(w.n_occ, kWarpTab);
+    int32_t cnt = 0;
+    for (int32_t k = lane; k < no; k += 32) {
+      const int32_t s = w.occ[k];
+      cnt += keep_pair(a, src, w.tv[s], __longlong_as_double(static_cast<long long>(w.td[s])));
+    }
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(all, cnt, o);
+    unsigned long long base = 0;
+    if (lane == 0) {
+      base = atomicAdd(a.cursor, static_cast<unsigned long long>(cnt));
+      a.src_base[q] = static_cast<int64_t>(base);
+      a.src_count[q] = cnt;
+    }
+    base = __shfl_sync(all, base, 0);
+    int64_t wpos = static_cast<int64_t>(base);
+    for (int32_t k0 = 0; k0 < no; k0 += 32) {
+      const int32_t k = k0 + lane;
+      bool keep = false;
+      int32_t v = -1;
+      double d = 0.0;
+      if (k < no) {
+        const int32_t s = w.occ[k];
+        v = w.tv[s];
+        d = __longlong_as_double(static_cast<long long>(w.td[s]));
+        keep = keep_pair(a, src, v, d);
+      }
+      const unsigned mk = __ballot_sync(all, keep);
+      if (keep) {
+        const int64_t o = wpos + __popc(mk & lt);
+        if (o < a.cap) {
+          a.out_j[o] = v;
+          a.out_d[o] = d;
+        }
+      }
+      wpos += __popc(mk);
+    }
+    __syncwarp();
   }
 }
 
@@ -375,6 +663,7 @@ struct geodesic_mesh {
   int32_t* d_vf = nullptr;
   uint8_t* d_saddle = nullptr;
   int32_t n_saddle = 0;
+  double mean_edge = 0.0;
   // results of the last geodesic_distance_lists call, sorted by (i, j)
   std::vector<int32_t> ri, rj;
   std::vector<double> rd;
@@ -412,28 +701,59 @@ int upload(T** dst, const std::vector<T>& src) {
 // One launch over n_src sources (src_list on the device, or src_lo + q) with
 // the given per-thread capacities; appends the output of every source that
 // finished and returns the ones that did not in `again`.
+// One launch over n_src sources (src_list on the device, or src_lo + q):
+// warp mode (hcap == 0) runs one warp per source with its queue keys and
+// vertex table in shared memory; otherwise one thread per source with the
+// given heap and table capacities in global scratch.  Appends the output of
+// every source that finished and returns the ones that did not in `again`.
 int launch_chunk(geodesic_mesh* m, const int32_t* h_src, int32_t src_lo, int32_t n_src, double threshold,
-                 int32_t only_greater, int32_t hcap, int32_t tbits, std::vector<int32_t>& out_i,
+                 int32_t only_greater, int32_t hcap, int32_t tbits, double delta, std::vector<int32_t>& out_i,
                  std::vector<int32_t>& out_j, std::vector<double>& out_d, std::vector<int32_t>& again) {
   int sms = 0;
   TFGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device));
-  const int64_t tcap = int64_t(1) << tbits;
+  const bool warp_mode = (hcap == 0);
+  const int64_t tcap = warp_mode ? 0 : int64_t(1) << tbits;
   const int64_t per_thread = hcap * (8 + 4 + 5 * 8) + tcap * (4 + 8 + 8 + 4);
   const int64_t budget = int64_t(3) << 30;  // scratch bytes
   constexpr int64_t kB = tfgb::geo::kThreads;
-  int64_t T = std::min<int64_t>(static_cast<int64_t>(sms) * 256, budget / per_thread) / kB * kB;
-  T = std::min<int64_t>(std::max<int64_t>(T, kB), (n_src + kB - 1) / kB * kB);
+  int64_t T = kB;
+  int warp_ctas = 0;
+  const size_t warp_smem = sizeof(tfgb::geo::WarpShared) * tfgb::geo::kWarpsPerCta;
+  if (warp_mode) {
+    TFGB_CUDA(cudaFuncSetAttribute(tfgb::geo::geodesic_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(warp_smem)));
+    int per_sm = 0;
+    TFGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tfgb::geo::geodesic_warp_kernel,
+                                                            32 * tfgb::geo::kWarpsPerCta, warp_smem));
+    warp_ctas = sms * std::max(per_sm, 1);
+  } else {
+    T = std::min<int64_t>(static_cast<int64_t>(sms) * 256, budget / per_thread) / kB * kB;
+    T = std::min<int64_t>(std::max<int64_t>(T, kB), (n_src + kB - 1) / kB * kB);
+  }
   Buf scratch, srcs, base, count, failed, ctrl, oj, od;
-  TFGB_CUDA(cudaMalloc(&scratch.p, per_thread * T + 16 * 256));  // + the 256-byte alignment of 11 arrays
+  const int64_t n_warps = static_cast<int64_t>(warp_ctas) * tfgb::geo::kWarpsPerCta;
+  const int64_t scratch_bytes = warp_mode ? n_warps * tfgb::geo::kWarpPool * (4 + 5 * 8) : per_thread * T;
+  TFGB_CUDA(cudaMalloc(&scratch.p, scratch_bytes + 16 * 256));  // + the 256-byte alignment of the arrays
   char* sp = static_cast<char*>(scratch.p);
   tfgb::geo::Scratch s{};
+  tfgb::geo::WarpBodies wb{};
   auto take = [&](int64_t bytes) {
     char* p = sp;
     sp += (bytes + 255) / 256 * 256;
     return p;
   };
+  if (warp_mode) {
+    const int64_t nb = n_warps * tfgb::geo::kWarpPool;
+    wb.b0 = reinterpret_cast<double*>(take(8 * nb));
+    wb.b1 = reinterpret_cast<double*>(take(8 * nb));
+    wb.sx = reinterpret_cast<double*>(take(8 * nb));
+    wb.sy = reinterpret_cast<double*>(take(8 * nb));
+    wb.sig = reinterpret_cast<double*>(take(8 * nb));
+    wb.tag = reinterpret_cast<int32_t*>(take(4 * nb));
+  }
   s.hcap = hcap;
   s.tbits = tbits;
+  if (!warp_mode) {
   s.hkey = reinterpret_cast<double*>(take(8 * hcap * T));
   s.hb0 = reinterpret_cast<double*>(take(8 * hcap * T));
   s.hb1 = reinterpret_cast<double*>(take(8 * hcap * T));
@@ -445,7 +765,7 @@ int launch_chunk(geodesic_mesh* m, const int32_t* h_src, int32_t src_lo, int32_t
   s.htag = reinterpret_cast<int32_t*>(take(4 * hcap * T));
   s.tv = reinterpret_cast<int32_t*>(take(4 * tcap * T));
   s.occ = reinterpret_cast<int32_t*>(take(4 * tcap * T));
-  (void)sp;
+  }
   if (h_src) {
     TFGB_CUDA(cudaMalloc(&srcs.p, 4 * std::max(n_src, 1)));
     TFGB_CUDA(cudaMemcpy(srcs.p, h_src, 4 * static_cast<size_t>(n_src), cudaMemcpyHostToDevice));
@@ -453,7 +773,7 @@ int launch_chunk(geodesic_mesh* m, const int32_t* h_src, int32_t src_lo, int32_t
   TFGB_CUDA(cudaMalloc(&base.p, 8 * std::max(n_src, 1)));
   TFGB_CUDA(cudaMalloc(&count.p, 4 * std::max(n_src, 1)));
   TFGB_CUDA(cudaMalloc(&failed.p, 4 * std::max(n_src, 1)));
-  TFGB_CUDA(cudaMalloc(&ctrl.p, 16));
+  TFGB_CUDA(cudaMalloc(&ctrl.p, 16));  // cursor (8 bytes), failed count, warp queue
   int64_t cap = std::max<int64_t>(int64_t(n_src) * 256, 4096);  // output entries; relaunched larger when short
   for (int attempt = 0; attempt < 2; ++attempt) {
     cudaFree(oj.p);
@@ -463,8 +783,9 @@ int launch_chunk(geodesic_mesh* m, const int32_t* h_src, int32_t src_lo, int32_t
     TFGB_CUDA(cudaMalloc(&od.p, 8 * cap));
     TFGB_CUDA(cudaMemset(ctrl.p, 0, 16));
     // every table slot empty (-1): a thread clears only the slots its own
-    // sources filled, so a relaunch starts from a cleared table too
-    TFGB_CUDA(cudaMemset(s.tv, 0xff, 4 * tcap * T));
+    // sources filled, so a relaunch starts from a cleared table too (the
+    // warp kernel clears its shared-memory table itself)
+    if (!warp_mode) TFGB_CUDA(cudaMemset(s.tv, 0xff, 4 * tcap * T));
     tfgb::geo::LaunchArgs a{};
     a.m.face = m->d_face;
     a.m.nbr = m->d_nbr;
@@ -474,6 +795,9 @@ int launch_chunk(geodesic_mesh* m, const int32_t* h_src, int32_t src_lo, int32_t
     a.m.vf = m->d_vf;
     a.m.saddle = m->d_saddle;
     a.s = s;
+    a.wb = wb;
+    a.delta = delta;
+    a.queue = reinterpret_cast<int32_t*>(static_cast<char*>(ctrl.p) + 12);
     a.src_list = static_cast<const int32_t*>(srcs.p);
     a.src_lo = src_lo;
     a.n_src = n_src;
@@ -488,7 +812,10 @@ int launch_chunk(geodesic_mesh* m, const int32_t* h_src, int32_t src_lo, int32_t
     a.src_base = static_cast<int64_t*>(base.p);
     a.src_count = static_cast<int32_t*>(count.p);
     a.failed = static_cast<int32_t*>(failed.p);
-    tfgb::geo::geodesic_lists_kernel<<<static_cast<unsigned>(T / tfgb::geo::kThreads), tfgb::geo::kThreads>>>(a);
+    if (warp_mode)
+      tfgb::geo::geodesic_warp_kernel<<<warp_ctas, 32 * tfgb::geo::kWarpsPerCta, warp_smem>>>(a);
+    else
+      tfgb::geo::geodesic_lists_kernel<<<static_cast<unsigned>(T / tfgb::geo::kThreads), tfgb::geo::kThreads>>>(a);
     TFGB_CUDA(cudaGetLastError());
     TFGB_CUDA(cudaDeviceSynchronize());
     unsigned long long used = 0;
@@ -620,6 +947,7 @@ int geodesic_mesh_create(const float* pts, int32_t n_vertices, const int32_t* fa
   m->nv = n_vertices;
   m->nf = n_faces;
   m->n_saddle = n_saddle;
+  m->mean_edge = std::accumulate(len.begin(), len.end(), 0.0) / static_cast<double>(len.size());
   int rc = upload(&m->d_face, std::vector<int32_t>(faces, faces + 3 * nf));
   if (!rc) rc = upload(&m->d_nbr, nbr);
   if (!rc) rc = upload(&m->d_len, len);
@@ -664,16 +992,20 @@ int geodesic_distance_lists(geodesic_mesh* m, double threshold, int32_t only_gre
   std::vector<double> cd;
   int rc = TFCE_OK;
   constexpr int32_t kChunk = 1 << 16;
+  // keys within delta of the frontier are taken together: one mean edge length
+  double delta = m->mean_edge;
+  if (const char* env = std::getenv("TFCE_GEODESIC_DELTA_EDGES")) delta = std::atof(env) * m->mean_edge;
   for (int32_t lo = src_lo; lo < src_hi && !rc; lo += kChunk) {
     const int32_t n = std::min(kChunk, src_hi - lo);
-    rc = launch_chunk(m, nullptr, lo, n, threshold, only_greater, 1024, 10, ci, cj, cd, again);
+    rc = launch_chunk(m, nullptr, lo, n, threshold, only_greater, 0, 0, delta, ci, cj, cd, again);
   }
-  // sources that outgrew the heap or the distance table: four times the room
+  // sources that outgrew a warp's queue or table: one thread each, with 4096
+  // and then 16384 heap entries and table slots in global scratch
   for (int round = 1; round <= 2 && !rc && !again.empty(); ++round) {
     std::vector<int32_t> todo;
     todo.swap(again);
     rc = launch_chunk(m, todo.data(), 0, static_cast<int32_t>(todo.size()), threshold, only_greater,
-                      1024 << (2 * round), 10 + 2 * round, ci, cj, cd, again);
+                      1024 << (2 * round), 10 + 2 * round, delta, ci, cj, cd, again);
   }
   cudaSetDevice(dev);
   if (rc) return rc;
