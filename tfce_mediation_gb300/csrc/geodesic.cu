@@ -46,14 +46,22 @@ namespace geo {
 constexpr int kThreads = 128;
 constexpr int64_t kIterLimit = int64_t(1) << 22;  // heap pops / rounds per source
 
+// Everything a window crossing needs about local edge e of face f, in one
+// 48-byte record, so that a crossing is a few dependent loads, not a dozen.
+struct alignas(16) FaceEdge {
+  double len;      // |f_e f_{e+1}|
+  double cx, cy;   // the third vertex f_{e+2} in this edge's frame (cy > 0)
+  int32_t a, b, c; // f_e, f_{e+1}, f_{e+2}
+  int32_t nbr;     // face beyond this edge << 2 | its local edge, -1 at the boundary
+  int32_t flags;   // pseudo-source bits: 1 = a, 2 = b, 4 = c
+  int32_t pad;
+};
+static_assert(sizeof(FaceEdge) == 48, "face-edge record");
+
 struct Mesh {
-  const int32_t* face;    // [nf][3]
-  const int32_t* nbr;     // [nf][3] face beyond local edge e << 2 | its local edge, -1 at the boundary
-  const double* len;      // [nf][3] length of local edge e (f_e -> f_{e+1})
-  const double2* third;   // [nf][3] third vertex in the frame of local edge e
+  const FaceEdge* fe;     // [nf][3]
   const int32_t* vf_off;  // [nv + 1]
   const int32_t* vf;      // incident faces: face << 2 | the vertex's corner
-  const uint8_t* saddle;  // [nv]
 };
 
 // A queued item: a window (tag = face << 2 | edge) or a pseudo-source
@@ -72,32 +80,33 @@ struct Geometry {
   St& st;
   double max_dist;
 
-  // a window on local edge e of face f, entering f
-  __device__ void window(int32_t f, int32_t e, double b0, double b1, double sx, double sy, double sig) {
-    const double L = m.len[3 * f + e];
+  // a window on the edge of record E (local edge e of face f), entering f
+  __device__ void window(int32_t f, int32_t e, const FaceEdge& E, double b0, double b1, double sx, double sy,
+                         double sig) {
+    const double L = E.len;
     b0 = fmax(b0, 0.0);
     b1 = fmin(b1, L);
     if (!(b1 - b0 > 1e-12 * L)) return;
     const double x = sx < b0 ? b0 - sx : (sx > b1 ? sx - b1 : 0.0);
     const double key = sig + sqrt(x * x + sy * sy);
     if (key > max_dist) return;
-    // end-vertex filter: P = f_e at 0, Q = f_{e+1} at L
-    const double dP = st.dist(m.face[3 * f + e]);
-    const double dQ = st.dist(m.face[3 * f + (e + 1) % 3]);
+    // end-vertex filter: P = E.a at 0, Q = E.b at L
+    const double dP = st.dist(E.a);
+    const double dQ = st.dist(E.b);
     const double far = sig + hypot(sx - b1, sy), near = sig + hypot(sx - b0, sy);
     if (far > dP + b1 || near > dQ + (L - b0)) return;
     st.push(Item{key, (f << 2) | e, b0, b1, sx, sy, sig});
   }
 
-  // the child crossing face f over its local edge le, from 2-D point pa (the
-  // edge's first vertex in f) to pb, covering [q0, q1]; pthird is f's third
-  // vertex, on the far side of the edge from the face beyond it
-  __device__ void child(int32_t f, int32_t le, double2 pa, double2 pb, double2 pthird, double2 q0, double2 q1,
+  // the child crossing face f over its edge of record X (from 2-D point pa,
+  // X.a, to pb), covering [q0, q1]; pthird is f's third vertex, on the far
+  // side of the edge from the face beyond it
+  __device__ void child(const FaceEdge& X, double2 pa, double2 pb, double2 pthird, double2 q0, double2 q1,
                         double sx, double sy, double sig) {
-    const int32_t nb = m.nbr[3 * f + le];
-    if (nb < 0) return;
-    const int32_t g = nb >> 2, ge = nb & 3;
-    const bool same = (m.face[3 * g + ge] == m.face[3 * f + le]);
+    if (X.nbr < 0) return;
+    const int32_t g = X.nbr >> 2, ge = X.nbr & 3;
+    const FaceEdge G = m.fe[3 * g + ge];
+    const bool same = (G.a == X.a);
     const double2 P = same ? pa : pb, Q = same ? pb : pa;
     double ux = Q.x - P.x, uy = Q.y - P.y;
     const double ul = hypot(ux, uy);
@@ -118,7 +127,7 @@ struct Geometry {
       t0 = t1;
       t1 = x;
     }
-    window(g, ge, t0, t1, s2x, s2y, sig);
+    window(g, ge, G, t0, t1, s2x, s2y, sig);
   }
 
   // where the line from s through (x, 0) meets segment a -> b (clamped)
@@ -132,21 +141,25 @@ struct Geometry {
 
   __device__ void propagate(const Item& w) {
     const int32_t f = w.tag >> 2, e = w.tag & 3;
-    const double L = m.len[3 * f + e];
-    const double2 C = m.third[3 * f + e];
+    // the face's three edge records, loaded together
+    const FaceEdge E = m.fe[3 * f + e];
+    const FaceEdge Eb = m.fe[3 * f + (e + 1) % 3];  // B -> C
+    const FaceEdge Ea = m.fe[3 * f + (e + 2) % 3];  // C -> A
+    const double L = E.len;
+    const double2 C = make_double2(E.cx, E.cy);
     const double2 A = make_double2(0.0, 0.0), B = make_double2(L, 0.0);
     const double sx = w.sx, sy = w.sy;
     const double xc = sx + (C.x - sx) * (-sy) / (C.y - sy);  // line s -> C at y = 0
-    if (xc >= w.b0 && xc <= w.b1) st.reach(m.face[3 * f + (e + 2) % 3], w.sig + hypot(C.x - sx, C.y - sy));
+    if (xc >= w.b0 && xc <= w.b1) st.reach(E.c, w.sig + hypot(C.x - sx, C.y - sy), (E.flags & 4) != 0);
     if (w.b0 < xc) {  // edge C -> A: local edge e + 2
       const double2 q0 = hit(sx, sy, w.b0, A, C);
       const double2 q1 = (w.b1 < xc) ? hit(sx, sy, w.b1, A, C) : C;
-      child(f, (e + 2) % 3, C, A, B, q0, q1, sx, sy, w.sig);
+      child(Ea, C, A, B, q0, q1, sx, sy, w.sig);
     }
     if (w.b1 > xc) {  // edge B -> C: local edge e + 1
       const double2 q0 = (w.b0 > xc) ? hit(sx, sy, w.b0, B, C) : C;
       const double2 q1 = hit(sx, sy, w.b1, B, C);
-      child(f, (e + 1) % 3, B, C, A, q0, q1, sx, sy, w.sig);
+      child(Eb, B, C, A, q0, q1, sx, sy, w.sig);
     }
   }
 
@@ -156,22 +169,22 @@ struct Geometry {
   __device__ void expand(int32_t u, double du) {
     for (int32_t k = m.vf_off[u]; k < m.vf_off[u + 1]; ++k) {
       const int32_t f = m.vf[k] >> 2, c = m.vf[k] & 3;
-      const int32_t e = (c + 1) % 3;  // opposite edge f_{c+1} -> f_{c+2}
-      const int32_t v1 = m.face[3 * f + e], v2 = m.face[3 * f + (e + 1) % 3];
-      const double l1 = m.len[3 * f + c];            // u -> v1
-      const double l2 = m.len[3 * f + (c + 2) % 3];  // v2 -> u
-      st.reach(v1, du + l1);
-      st.reach(v2, du + l2);
-      const int32_t nb = m.nbr[3 * f + e];
-      if (nb < 0) continue;
-      const int32_t g = nb >> 2, ge = nb & 3;
-      const double L = m.len[3 * f + e];
-      const bool p_is_v1 = (m.face[3 * g + ge] == v1);
+      const FaceEdge U1 = m.fe[3 * f + c];            // u -> v1
+      const FaceEdge O = m.fe[3 * f + (c + 1) % 3];   // opposite edge v1 -> v2
+      const FaceEdge U2 = m.fe[3 * f + (c + 2) % 3];  // v2 -> u
+      const double l1 = U1.len, l2 = U2.len;
+      st.reach(O.a, du + l1, (O.flags & 1) != 0);
+      st.reach(O.b, du + l2, (O.flags & 2) != 0);
+      if (O.nbr < 0) continue;
+      const int32_t g = O.nbr >> 2, ge = O.nbr & 3;
+      const FaceEdge G = m.fe[3 * g + ge];
+      const double L = O.len;
+      const bool p_is_v1 = (G.a == O.a);
       const double dP = p_is_v1 ? l1 : l2, dQ = p_is_v1 ? l2 : l1;
       const double x = (L * L + dP * dP - dQ * dQ) / (2.0 * L);
       const double y2 = dP * dP - x * x;
       const double y = -(y2 > 0.0 ? sqrt(y2) : 0.0);
-      if (y < 0.0) window(g, ge, 0.0, L, x, y, du);
+      if (y < 0.0) window(g, ge, G, 0.0, L, x, y, du);
     }
   }
 };
@@ -282,11 +295,11 @@ struct ThreadState {
     return k < 0 ? static_cast<double>(INFINITY) : s.td[ix(k)];
   }
   // d(v) = min(d(v), dv); a pseudo-source whose distance fell is queued
-  __device__ void reach(int32_t v, double dv) {
+  __device__ void reach(int32_t v, double dv, bool pseudo) {
     const int32_t k = slot(v, true);
     if (k < 0 || !(dv < s.td[ix(k)])) return;
     s.td[ix(k)] = dv;
-    if (m.saddle[v] && dv <= max_dist) push(Item{dv, -1 - v, 0.0, 0.0, 0.0, 0.0, 0.0});
+    if (pseudo && dv <= max_dist) push(Item{dv, -1 - v, 0.0, 0.0, 0.0, 0.0, dv});
   }
 
   __device__ void run(int32_t src) {
@@ -334,10 +347,10 @@ constexpr int kWarpPool = 2048;            // pending items per warp
 constexpr int kWarpTabBits = 10;           // reached-vertex table: 1024 slots
 constexpr int kWarpTab = 1 << kWarpTabBits;
 constexpr int kWarpTabMax = 3 * kWarpTab / 4;
-constexpr int kWarpsPerCta = 4;
+constexpr int kWarpsPerCta = 6;
 
 struct WarpShared {
-  double key[kWarpPool];
+  float key[kWarpPool];  // smallest distance of the item, rounded down (orders and bounds only)
   unsigned long long td[kWarpTab];     // distance bits (non-negative doubles order as their bits)
   unsigned long long tdone[kWarpTab];  // distance a pseudo-source was expanded at
   int32_t tv[kWarpTab];                // vertex id, -1 empty
@@ -370,7 +383,7 @@ struct WarpState {
       w.fail = 1;
       return;
     }
-    w.key[i] = it.key;
+    w.key[i] = __double2float_rd(it.key);
     b.tag[i] = it.tag;
     b.b0[i] = it.b0;
     b.b1[i] = it.b1;
@@ -406,12 +419,12 @@ struct WarpState {
     if (k < 0) return static_cast<double>(INFINITY);
     return __longlong_as_double(static_cast<long long>(reinterpret_cast<volatile unsigned long long*>(w.td)[k]));
   }
-  __device__ void reach(int32_t v, double dv) {
+  __device__ void reach(int32_t v, double dv, bool pseudo) {
     const int32_t k = slot(v, true);
     if (k < 0) return;
     const unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(dv));
     const unsigned long long old = atomicMin(&w.td[k], bits);
-    if (bits < old && m.saddle[v] && dv <= max_dist) push(Item{dv, -1 - v, 0.0, 0.0, 0.0, 0.0, 0.0});
+    if (bits < old && pseudo && dv <= max_dist) push(Item{dv, -1 - v, 0.0, 0.0, 0.0, 0.0, dv});
   }
 };
 
@@ -541,15 +554,15 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) geodesic_warp_kernel(Launch
         break;
       }
       double kmin = static_cast<double>(INFINITY);
-      for (int32_t k = lane; k < n; k += 32) kmin = fmin(kmin, w.key[k]);
+      for (int32_t k = lane; k < n; k += 32) kmin = fmin(kmin, static_cast<double>(w.key[k]));
       kmin = warp_min(kmin);
-      if (n == 0 || kmin > a.max_dist) break;
+      if (n == 0 || kmin > a.max_dist) break;  // keys are rounded down: nothing left within the radius
       const double thr = kmin + a.delta;
       // take up to 32 items with key <= thr, in pool order
       int32_t taken = 0;
       for (int32_t base = 0; base < n && taken < 32; base += 32) {
         const int32_t idx = base + lane;
-        const bool qual = idx < n && w.key[idx] <= thr;
+        const bool qual = idx < n && static_cast<double>(w.key[idx]) <= thr;
         const unsigned mk = __ballot_sync(all, qual);
         const int r = __popc(mk & lt);
         if (qual && taken + r < 32) w.sel[taken + r] = idx;
@@ -558,14 +571,14 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) geodesic_warp_kernel(Launch
       __syncwarp();
       Item it{};
       const int32_t my = (lane < taken) ? w.sel[lane] : -1;
-      if (my >= 0) it = Item{w.key[my], b.tag[my], b.b0[my], b.b1[my], b.sx[my], b.sy[my], b.sig[my]};
+      if (my >= 0) it = Item{0.0, b.tag[my], b.b0[my], b.b1[my], b.sx[my], b.sy[my], b.sig[my]};
       __syncwarp();
-      if (my >= 0) w.key[my] = -1.0;  // taken
+      if (my >= 0) w.key[my] = -1.0f;  // taken
       __syncwarp();
       // the items beyond the new end that were not taken move into the holes below it
       const int32_t n_new = n - taken;
       const int32_t pos = n_new + lane;
-      const bool is_src = lane < taken && w.key[pos] >= 0.0;
+      const bool is_src = lane < taken && w.key[pos] >= 0.0f;
       const unsigned ms = __ballot_sync(all, is_src);
       if (is_src) w.srcpos[__popc(ms & lt)] = pos;
       const bool is_hole = my >= 0 && my < n_new;
@@ -585,13 +598,13 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) geodesic_warp_kernel(Launch
       if (lane == 0) w.n_pool = n_new;
       __syncwarp();
       if (my >= 0) {
-        if (it.tag < 0) {
+        if (it.tag < 0) {  // a pseudo-source: its exact distance is in sig
           const int32_t v = -1 - it.tag;
           const int32_t k = st.slot(v, false);
-          const unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(it.key));
+          const unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(it.sig));
           if (k >= 0 && bits <= reinterpret_cast<volatile unsigned long long*>(w.td)[k] &&
               atomicMin(&w.tdone[k], bits) > bits)
-            geo.expand(v, it.key);
+            geo.expand(v, it.sig);
         } else {
           geo.propagate(it);
         }
@@ -655,13 +668,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) geodesic_warp_kernel(Launch
 struct geodesic_mesh {
   int device = 0;
   int32_t nv = 0, nf = 0;
-  int32_t* d_face = nullptr;
-  int32_t* d_nbr = nullptr;
-  double* d_len = nullptr;
-  double2* d_third = nullptr;
+  tfgb::geo::FaceEdge* d_fe = nullptr;
   int32_t* d_vf_off = nullptr;
   int32_t* d_vf = nullptr;
-  uint8_t* d_saddle = nullptr;
+  double pairs_per_src = 256.0;  // output entries per source seen so far (sizes the output buffers)
   int32_t n_saddle = 0;
   double mean_edge = 0.0;
   // results of the last geodesic_distance_lists call, sorted by (i, j)
@@ -676,13 +686,9 @@ void free_mesh(geodesic_mesh* m) {
   int dev = 0;
   cudaGetDevice(&dev);
   cudaSetDevice(m->device);
-  cudaFree(m->d_face);
-  cudaFree(m->d_nbr);
-  cudaFree(m->d_len);
-  cudaFree(m->d_third);
+  cudaFree(m->d_fe);
   cudaFree(m->d_vf_off);
   cudaFree(m->d_vf);
-  cudaFree(m->d_saddle);
   cudaSetDevice(dev);
 }
 
@@ -774,7 +780,9 @@ int launch_chunk(geodesic_mesh* m, const int32_t* h_src, int32_t src_lo, int32_t
   TFGB_CUDA(cudaMalloc(&count.p, 4 * std::max(n_src, 1)));
   TFGB_CUDA(cudaMalloc(&failed.p, 4 * std::max(n_src, 1)));
   TFGB_CUDA(cudaMalloc(&ctrl.p, 16));  // cursor (8 bytes), failed count, warp queue
-  int64_t cap = std::max<int64_t>(int64_t(n_src) * 256, 4096);  // output entries; relaunched larger when short
+  // output entries, from the largest count per source seen on this mesh; a
+  // launch that outgrows it runs again with the exact size
+  int64_t cap = std::max<int64_t>(static_cast<int64_t>(n_src * m->pairs_per_src * 1.25), 4096);
   for (int attempt = 0; attempt < 2; ++attempt) {
     cudaFree(oj.p);
     cudaFree(od.p);
@@ -787,13 +795,9 @@ int launch_chunk(geodesic_mesh* m, const int32_t* h_src, int32_t src_lo, int32_t
     // warp kernel clears its shared-memory table itself)
     if (!warp_mode) TFGB_CUDA(cudaMemset(s.tv, 0xff, 4 * tcap * T));
     tfgb::geo::LaunchArgs a{};
-    a.m.face = m->d_face;
-    a.m.nbr = m->d_nbr;
-    a.m.len = m->d_len;
-    a.m.third = m->d_third;
+    a.m.fe = m->d_fe;
     a.m.vf_off = m->d_vf_off;
     a.m.vf = m->d_vf;
-    a.m.saddle = m->d_saddle;
     a.s = s;
     a.wb = wb;
     a.delta = delta;
@@ -820,6 +824,7 @@ int launch_chunk(geodesic_mesh* m, const int32_t* h_src, int32_t src_lo, int32_t
     TFGB_CUDA(cudaDeviceSynchronize());
     unsigned long long used = 0;
     TFGB_CUDA(cudaMemcpy(&used, ctrl.p, 8, cudaMemcpyDeviceToHost));
+    m->pairs_per_src = std::max(m->pairs_per_src, static_cast<double>(used) / std::max(n_src, 1));
     if (static_cast<int64_t>(used) <= cap) break;
     cap = static_cast<int64_t>(used);  // run the chunk again with room for all of it
   }
@@ -948,13 +953,24 @@ int geodesic_mesh_create(const float* pts, int32_t n_vertices, const int32_t* fa
   m->nf = n_faces;
   m->n_saddle = n_saddle;
   m->mean_edge = std::accumulate(len.begin(), len.end(), 0.0) / static_cast<double>(len.size());
-  int rc = upload(&m->d_face, std::vector<int32_t>(faces, faces + 3 * nf));
-  if (!rc) rc = upload(&m->d_nbr, nbr);
-  if (!rc) rc = upload(&m->d_len, len);
-  if (!rc) rc = upload(&m->d_third, third);
+  std::vector<tfgb::geo::FaceEdge> fe(3 * nf);
+  for (int64_t f = 0; f < nf; ++f) {
+    for (int e = 0; e < 3; ++e) {
+      tfgb::geo::FaceEdge& r = fe[3 * f + e];
+      r.len = len[3 * f + e];
+      r.cx = third[3 * f + e].x;
+      r.cy = third[3 * f + e].y;
+      r.a = faces[3 * f + e];
+      r.b = faces[3 * f + (e + 1) % 3];
+      r.c = faces[3 * f + (e + 2) % 3];
+      r.nbr = nbr[3 * f + e];
+      r.flags = (saddle[r.a] ? 1 : 0) | (saddle[r.b] ? 2 : 0) | (saddle[r.c] ? 4 : 0);
+      r.pad = 0;
+    }
+  }
+  int rc = upload(&m->d_fe, fe);
   if (!rc) rc = upload(&m->d_vf_off, vf_off);
   if (!rc) rc = upload(&m->d_vf, vf);
-  if (!rc) rc = upload(&m->d_saddle, saddle);
   if (rc) {
     free_mesh(m);
     delete m;
