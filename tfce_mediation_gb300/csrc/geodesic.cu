@@ -47,16 +47,17 @@ constexpr int kThreads = 128;
 constexpr int64_t kIterLimit = int64_t(1) << 22;  // heap pops / rounds per source
 
 // Everything a window crossing needs about local edge e of face f, in one
-// 48-byte record, so that a crossing is a few dependent loads, not a dozen.
+// 64-byte record, so that a crossing is a few dependent loads, not a dozen.
 struct alignas(16) FaceEdge {
   double len;      // |f_e f_{e+1}|
+  double inv_len;  // 1 / len
   double cx, cy;   // the third vertex f_{e+2} in this edge's frame (cy > 0)
   int32_t a, b, c; // f_e, f_{e+1}, f_{e+2}
   int32_t nbr;     // face beyond this edge << 2 | its local edge, -1 at the boundary
   int32_t flags;   // pseudo-source bits: 1 = a, 2 = b, 4 = c
-  int32_t pad;
+  int32_t pad[3];
 };
-static_assert(sizeof(FaceEdge) == 48, "face-edge record");
+static_assert(sizeof(FaceEdge) == 64, "face-edge record");
 
 struct Mesh {
   const FaceEdge* fe;     // [nf][3]
@@ -72,13 +73,27 @@ struct Item {
   double b0, b1, sx, sy, sig;
 };
 
+// The radius a window's FP32 key is compared with.
+__host__ __device__ inline float max_key(double max_dist) {
+  return static_cast<float>(max_dist * (1.0 + 1.0 / 65536.0));
+}
+
 // The window geometry, shared by both kernels.  St supplies the queue and
 // the table of reached vertices: push(Item), dist(v), reach(v, d).
+//
+// GB300's FP64 rate is about 1/64 of its FP32 rate, so the FP64 work per
+// window is kept small: the smallest distance of a window (which only orders
+// the queue and bounds the radius) is taken in FP32 and compared with the
+// radius widened by 2^-16; the end-vertex filter compares squares instead of
+// taking square roots; an edge's unit vector uses the stored 1 / length.
+// Distances to vertices stay FP64.  (Divisions through one FP64 Newton step
+// from the FP32 reciprocal measured no faster.)
 template <class St>
 struct Geometry {
   const Mesh& m;
   St& st;
   double max_dist;
+  float max_key;  // max_dist widened by 2^-16 (a window's FP32 key errs by ~1e-7)
 
   // a window on the edge of record E (local edge e of face f), entering f
   __device__ void window(int32_t f, int32_t e, const FaceEdge& E, double b0, double b1, double sx, double sy,
@@ -88,14 +103,16 @@ struct Geometry {
     b1 = fmin(b1, L);
     if (!(b1 - b0 > 1e-12 * L)) return;
     const double x = sx < b0 ? b0 - sx : (sx > b1 ? sx - b1 : 0.0);
-    const double key = sig + sqrt(x * x + sy * sy);
-    if (key > max_dist) return;
-    // end-vertex filter: P = E.a at 0, Q = E.b at L
-    const double dP = st.dist(E.a);
-    const double dQ = st.dist(E.b);
-    const double far = sig + hypot(sx - b1, sy), near = sig + hypot(sx - b0, sy);
-    if (far > dP + b1 || near > dQ + (L - b0)) return;
-    st.push(Item{key, (f << 2) | e, b0, b1, sx, sy, sig});
+    const float key = static_cast<float>(sig) + sqrtf(static_cast<float>(x * x + sy * sy));
+    if (key > max_key) return;
+    // end-vertex filter, squared: sig + |s - (b1, 0)| > d(P) + b1, and the
+    // same at b0 for Q = E.b at L
+    const double rP = st.dist(E.a) + b1 - sig;
+    const double rQ = st.dist(E.b) + (L - b0) - sig;
+    const double fx = sx - b1, nx0 = sx - b0, sy2 = sy * sy;
+    if (rP < 0.0 || fx * fx + sy2 > rP * rP) return;
+    if (rQ < 0.0 || nx0 * nx0 + sy2 > rQ * rQ) return;
+    st.push(Item{static_cast<double>(key), (f << 2) | e, b0, b1, sx, sy, sig});
   }
 
   // the child crossing face f over its edge of record X (from 2-D point pa,
@@ -108,10 +125,7 @@ struct Geometry {
     const FaceEdge G = m.fe[3 * g + ge];
     const bool same = (G.a == X.a);
     const double2 P = same ? pa : pb, Q = same ? pb : pa;
-    double ux = Q.x - P.x, uy = Q.y - P.y;
-    const double ul = hypot(ux, uy);
-    ux /= ul;
-    uy /= ul;
+    const double ux = (Q.x - P.x) * G.inv_len, uy = (Q.y - P.y) * G.inv_len;
     double nx = -uy, ny = ux;
     if (nx * (pthird.x - P.x) + ny * (pthird.y - P.y) > 0.0) {
       nx = -nx;
@@ -150,7 +164,10 @@ struct Geometry {
     const double2 A = make_double2(0.0, 0.0), B = make_double2(L, 0.0);
     const double sx = w.sx, sy = w.sy;
     const double xc = sx + (C.x - sx) * (-sy) / (C.y - sy);  // line s -> C at y = 0
-    if (xc >= w.b0 && xc <= w.b1) st.reach(E.c, w.sig + hypot(C.x - sx, C.y - sy), (E.flags & 4) != 0);
+    if (xc >= w.b0 && xc <= w.b1) {
+      const double dx = C.x - sx, dy = C.y - sy;
+      st.reach(E.c, w.sig + sqrt(dx * dx + dy * dy), (E.flags & 4) != 0);
+    }
     if (w.b0 < xc) {  // edge C -> A: local edge e + 2
       const double2 q0 = hit(sx, sy, w.b0, A, C);
       const double2 q1 = (w.b1 < xc) ? hit(sx, sy, w.b1, A, C) : C;
@@ -181,7 +198,7 @@ struct Geometry {
       const double L = O.len;
       const bool p_is_v1 = (G.a == O.a);
       const double dP = p_is_v1 ? l1 : l2, dQ = p_is_v1 ? l2 : l1;
-      const double x = (L * L + dP * dP - dQ * dQ) / (2.0 * L);
+      const double x = (L * L + dP * dP - dQ * dQ) * (0.5 * O.inv_len);
       const double y2 = dP * dP - x * x;
       const double y = -(y2 > 0.0 ? sqrt(y2) : 0.0);
       if (y < 0.0) window(g, ge, G, 0.0, L, x, y, du);
@@ -307,7 +324,7 @@ struct ThreadState {
     nocc = 0;
     nh = 0;
     fail = false;
-    Geometry<ThreadState> geo{m, *this, max_dist};
+    Geometry<ThreadState> geo{m, *this, max_dist, max_key(max_dist)};
     const int32_t k0 = slot(src, true);
     if (k0 < 0) return;
     s.td[ix(k0)] = 0.0;
@@ -319,7 +336,7 @@ struct ThreadState {
         return;
       }
       const Item w = pop();
-      if (w.key > max_dist) break;
+      if (w.key > max_key(max_dist)) break;
       if (w.tag < 0) {
         const int32_t v = -1 - w.tag;
         const int32_t k = slot(v, false);
@@ -506,7 +523,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) geodesic_warp_kernel(Launch
   b.sy += gw * kWarpPool;
   b.sig += gw * kWarpPool;
   WarpState st{a.m, w, b, a.max_dist};
-  Geometry<WarpState> geo{a.m, st, a.max_dist};
+  Geometry<WarpState> geo{a.m, st, a.max_dist, max_key(a.max_dist)};
   const unsigned all = 0xffffffffu;
   const unsigned lt = (1u << lane) - 1u;
   for (int k = lane; k < kWarpTab; k += 32) {
@@ -556,7 +573,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) geodesic_warp_kernel(Launch
       double kmin = static_cast<double>(INFINITY);
       for (int32_t k = lane; k < n; k += 32) kmin = fmin(kmin, static_cast<double>(w.key[k]));
       kmin = warp_min(kmin);
-      if (n == 0 || kmin > a.max_dist) break;  // keys are rounded down: nothing left within the radius
+      if (n == 0 || kmin > static_cast<double>(geo.max_key)) break;  // nothing left within the radius
       const double thr = kmin + a.delta;
       // take up to 32 items with key <= thr, in pool order
       int32_t taken = 0;
@@ -958,6 +975,7 @@ int geodesic_mesh_create(const float* pts, int32_t n_vertices, const int32_t* fa
     for (int e = 0; e < 3; ++e) {
       tfgb::geo::FaceEdge& r = fe[3 * f + e];
       r.len = len[3 * f + e];
+      r.inv_len = 1.0 / len[3 * f + e];
       r.cx = third[3 * f + e].x;
       r.cy = third[3 * f + e].y;
       r.a = faces[3 * f + e];
@@ -965,7 +983,7 @@ int geodesic_mesh_create(const float* pts, int32_t n_vertices, const int32_t* fa
       r.c = faces[3 * f + (e + 2) % 3];
       r.nbr = nbr[3 * f + e];
       r.flags = (saddle[r.a] ? 1 : 0) | (saddle[r.b] ? 2 : 0) | (saddle[r.c] ? 4 : 0);
-      r.pad = 0;
+      r.pad[0] = r.pad[1] = r.pad[2] = 0;
     }
   }
   int rc = upload(&m->d_fe, fe);
