@@ -673,6 +673,26 @@ def dropin_rate(st, P, n_perm=2048):
                     "per-vertex density weights on, so the sweep keeps its potential form"}
 
 
+def geodesic_sub_line():
+    """The exact geodesic neighbour lists (adjacency.compute_distance_parallel
+    for every source of one L7 hemisphere, the "geodesic" workload) at the
+    3 mm and 9 mm radii the reference's scripts use, through GeodesicMesh.lists;
+    wall clock of each whole call.  The one-core rate of the oracle's window
+    propagation on this mesh and radius is in bench.py --workload geodesic."""
+    from tfce_mediation_gb300.geodesic import GeodesicMesh
+    d = _next_study("geodesic")
+    m = GeodesicMesh(d["v"], d["f"])
+    V = d["v"].shape[0]
+    m.lists(3.0, True, 0, min(V, 4096))  # warm-up
+    out = {"workload": NEXT["geodesic"], "sources": V, "saddle_vertices": m.n_saddle}
+    for r in (3.0, 9.0):
+        t0 = time.perf_counter()
+        n = int(m.lists(r, True)[0].shape[0])
+        dt = time.perf_counter() - t0
+        out[f"radius_{r:g}mm"] = {"seconds": dt, "sources_per_s": V / dt, "pairs": n}
+    return out
+
+
 def time_to_fwer(eng, st, n_perm=10_000, seed=99):
     """Wall time from the resident data to the 1-p(FWER) maps of every
     contrast and sign: the plain path (n_perm permutations) and the learned
@@ -997,6 +1017,7 @@ def run_gpu(args):
         for kind in CONFIGS:
             line["configs"][kind] = run_config(kind, args, None if args.no_cpu_baseline else
                                                os.path.join(stash_root, kind))
+        line["geodesic_lists"] = geodesic_sub_line()
     if not args.no_cpu_baseline:
         cores = 1
         _stash_study(st, os.path.join(stash_root, "config2"))
