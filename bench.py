@@ -367,8 +367,8 @@ def run_next(args):
                 "higher_is_better": True,
                 "radius_3mm": {"seconds_per_mesh": dt3, "pairs": n3},
                 "note": "whole call through GeodesicMesh.lists (propagation of every source on the GPU, lists "
-                        "copied back and ordered by (i, j) on the host); latency-bound: one thread per source "
-                        "walks its own heap and distance table",
+                        "copied back and ordered by (i, j) on the host); one warp per source; bound by the FP64 "
+                        "pipe (76% active, profiles/geodesic_warp_lists.md)",
                 "cpu_baseline": cpu, "gpu_launches": K, "data": "synthetic"}
         print(json.dumps(line), flush=True)
         return
