@@ -19,17 +19,18 @@
 // boundary vertices, are pseudo-sources (the reference's rule,
 // geodesic_mesh.h:335-344).  A window is dropped when an end vertex of its
 // edge gives a shorter path to every point of the interval, or when it lies
-// beyond the radius.  Windows and pseudo-sources are taken in order of their
-// smallest distance from a binary heap until it exceeds the radius.
+// beyond the radius.
 //
-// GPU mapping: sources are independent, so each thread runs the propagation
-// of one source at a time (a grid-stride loop over the sources).  Its heap
-// (windows stored inline) and its open-addressing table of vertex distances
-// live in global scratch laid out [slot][thread], so the threads of a warp
-// touching the same heap level or table slot coalesce.  The mesh tables are
-// read-only and shared by all threads (L2-resident: ~100 bytes per face).
-// A source whose heap or table outgrows its capacity is listed and run again
-// with four times the capacity; every loop is bounded.
+// GPU mapping: sources are independent.  geodesic_warp_kernel gives each
+// source a warp: the keys of its pending windows and pseudo-sources and its
+// table of reached vertices sit in the warp's shared memory, and each round
+// the 32 lanes propagate the items within one edge length of the smallest
+// pending key (the filters are sound in any order, so the distances are the
+// same exact ones).  A source that outgrows the warp's queue or table runs
+// again in geodesic_lists_kernel, one thread per source with a binary heap
+// and a table in global scratch laid out [slot][thread], with four and then
+// sixteen times the room.  The mesh tables are read-only face-edge records
+// shared by all (L2-resident).  Every loop is bounded.
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>

@@ -4,9 +4,9 @@
 The reference propagates its exact geodesic library (tfce_mediation/lib/geodesic)
 from one source vertex at a time on one CPU core and then asks for the
 distance of every vertex j > i.  Here every source of the mesh is propagated
-in one launch (``csrc/geodesic.cu``: one thread per source, window propagation
-in double precision) and only the vertices reached within the radius are
-listed.
+in one launch (``csrc/geodesic.cu``: one warp per source, exact window
+propagation with double-precision distances) and only the vertices reached
+within the radius are listed.
 
 * ``compute(v, f, thresholds)`` -- adjacency.pyx:44-80: for every threshold,
   the list of vertices within that geodesic distance of each vertex (Python
