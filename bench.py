@@ -821,8 +821,16 @@ def run_gpu(args):
     perms = [E.permutations(n, SEED, base + s * P, base + (s + 1) * P) for s in range(total_steps)]
     # device-resident design operators (inputs resident before the timed region)
     tc = eng._tc
+    qf = eng._graph_qf()
     from tfce_mediation_gb300.device import dev
-    if tc is not None:
+    if qf:
+        ops = []
+        for p in perms:
+            db = DesignBatch(eng.X[p])
+            XR, GI = tc.host_operands_qf(db)
+            ops.append((dev(XR), dev(GI), dev(db.invdiag64.astype(np.float32)), dev(db.dof.astype(np.float32))))
+        xt_buf = tc.tile_designs_qf(ops[0][0], P, eng.k)
+    elif tc is not None:
         ops = []
         for p in perms:
             db = DesignBatch(eng.X[p])
@@ -841,7 +849,11 @@ def run_gpu(args):
     def step(s, ev=None):
         if ev is not None:
             ev[0].record(stream)
-        if tc is not None:
+        if qf:
+            XRd, GId, invd, dof = ops[s]
+            tc.tile_designs_qf(XRd, P, eng.k, out=xt_buf)
+            tc.tstat_qf(xt_buf, GId, invd, dof, P, eng.k, eng._coef, C, eng._tbuf, V)
+        elif tc is not None:
             P8d, Ud, Xtd, invd, dof = ops[s]
             tc.tile_designs(P8d, P, eng.k, out=pt_buf)
             tc.stat(0, pt_buf, Ud, Xtd, invd, dof, P, eng.k, eng._coef, C, eng._tbuf, V, centred=eng._centred)
@@ -956,7 +968,22 @@ def run_gpu(args):
     per_sweep, traffic_note = profile_traffic("tfce_sweep")
     traffic = None if per_sweep is None else per_sweep * sweeps_per_launch
     clocks = clk.summary()
-    if tc is not None:
+    if qf:
+        # split-BF16 GEMM: 3 MMAs of M=V, N=R rows per design (the k-1 centred
+        # columns padded to 4 or 8), K=n_pad; epilogue O(k^2) per vertex and design
+        R = tc.qf_rows(eng.k)
+        mma_flop = 2.0 * 3 * V * R * tc.qf_padded(P, eng.k) * tc.n_pad
+        glm_info = {"precision": "bf16x3", "kernels": "tile_split_kernel + glm_tc_qf_kernel<%d>" % (eng.k - 1),
+                    "form": "quadratic (RSS = yy - c'inv(Xc'Xc)c)",
+                    "ms_per_launch": glm_avg,
+                    "tensor_tflops_issued": mma_flop / (glm_avg / 1000) / 1e12,
+                    "tensor_peak_tflops": bf16_sus,
+                    "tensor_frac": mma_flop / (glm_avg / 1000) / 1e12 / bf16_sus,
+                    "peak_source": f"{peak_kind} bf16_tflops_sustained (kernel timed inside a long step)",
+                    "glm_ms_by_form": getattr(tc, "glm_timings", None),
+                    "note": "tensor FLOPs count the three split-BF16 products on %d rows per design" % R}
+        launches = 3 * args.steps
+    elif tc is not None:
         # split-BF16 GEMM: 3 MMAs of M=V, N=8 rows per design, K=n_pad; residual
         # epilogue: (k+1) FP32 FMAs per vertex, design and subject (k with the
         # centred form)
@@ -969,6 +996,7 @@ def run_gpu(args):
                     "tensor_frac": mma_flop / (glm_avg / 1000) / 1e12 / bf16_sus,
                     "peak_source": f"{peak_kind} bf16_tflops_sustained (kernel timed inside a long step)",
                     "epilogue_fp32_tflops": epi_flop / (glm_avg / 1000) / 1e12,
+                    "glm_ms_by_form": getattr(tc, "glm_timings", None),
                     "note": "tensor FLOPs count the three split-BF16 products on 8 padded rows per design"}
         launches = 3 * args.steps
     else:
@@ -985,7 +1013,9 @@ def run_gpu(args):
                    "l2": "inputs larger than L2 (Y 459 MB, t maps %d MB per step)" % (P * C * V * 4 // 2 ** 20),
                    "parallelism": f"replicas over permutation ranges x{ws}",
                    "sweep_ctas_per_sm": getattr(eng.adj, "ctas_per_sm", None),
-                   "glm_designs_per_tile": getattr(tc, "design_block", None) if tc is not None else None,
+                   "glm_designs_per_tile": (int(tc.lib.glm_qf_design_block(eng.k)) if qf else
+                                            getattr(tc, "design_block", None) if tc is not None else None),
+                   "glm_form": "quadratic" if qf else "residual" if tc is not None else "fp32",
                    "data_gen_s": round(gen_s, 1)},
         "e2e": {"value": e2e_value, "unit": "perm/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,

@@ -328,6 +328,31 @@ int glm_stat_tc_block(const void* y_tiles, const float* y_shift, const float* Y,
                       const float* x_rows, int32_t n_sc, const float* invdiag, const float* dof, int32_t G,
                       int32_t kmax, int32_t design_block, int32_t mode, const int32_t* coef, int32_t n_coef,
                       const float* wmat, int32_t w_stride, float* t_out, int64_t ldt, int32_t* err, void* stream);
+/* Quadratic-form tensor-core GLM: t of coefficients >= 1 of designs whose
+ * first column is all ones (the same t as cynumstats.pyx:28-64 / glm_tstat).
+ * By Frisch-Waugh, with Xc the other columns minus their means and c =
+ * Xc'(y - centre) from one split-BF16 GEMM (M = 128 vertices, N = 256: R = 4
+ * rows per design for kmax <= 5, 8 for kmax <= 8):
+ *   b = inv(Xc'Xc) c,  RSS = yy - c'b,  t_j = b_j / sqrt(RSS / dof * invdiag_j);
+ * no residual pass over the subjects.
+ *   glm_qf_design_block(kmax): designs per tile (64 for kmax <= 5, 32 for
+ *     kmax <= 8); -1 for kmax outside [2, 8];
+ *   glm_col_sumsq: yy[v] = sum_i (Yc[i][v] - mean_v)^2 over the n rows of the
+ *     centred data (glm_tile_split's `shifted` output), FP64 accumulation;
+ *   glm_tstat_tc_qf: y_tiles as glm_tstat_tc (centred); x_tiles from
+ *     glm_tile_split of the centred design columns stacked [G_pad*R][n_pad]
+ *     (design d, column j >= 1 at row d*R + j - 1, other rows zero) in row
+ *     blocks of 256; ginv [G_pad][kmax-1][kmax-1] = inv(X'X) without its
+ *     first row and column (= inv(Xc'Xc)); invdiag [G][kmax] and dof [G] as
+ *     glm_tstat; coef[0..n_coef) in [1, kmax) (another index yields NaN);
+ *     err as glm_tstat_tc.  RSS is clamped at 0 (a perfect fit gives +-inf
+ *     or NaN, as 0/0).  Tiles 16-byte aligned. */
+int glm_qf_design_block(int32_t kmax);
+int glm_col_sumsq(const float* Y_centred, int64_t ldy, int32_t n, int64_t V, float* yy, void* stream);
+int glm_tstat_tc_qf(const void* y_tiles, const float* yy, int32_t n, int32_t n_pad, int64_t V,
+                    const void* x_tiles, const float* ginv, const float* invdiag, const float* dof, int32_t G,
+                    int32_t kmax, const int32_t* coef, int32_t n_coef, float* t_out, int64_t ldt, int32_t* err,
+                    void* stream);
 int glm_stat_tc(const void* y_tiles, const float* y_shift, const float* Y, const float* Y_centred, int64_t ldy,
                 int32_t n,
                 int32_t n_pad, int64_t V, const void* p_tiles, const float* u_rows, const float* x_rows,

@@ -47,7 +47,10 @@ def _seg(st, h):
     return off, idx, v0, v1
 
 
-def test_config2_fwer_maps_vs_fp64_oracle():
+@pytest.mark.parametrize("quadratic_form", [True, False])
+def test_config2_fwer_maps_vs_fp64_oracle(quadratic_form):
+    """The headline study, with the GLM in its quadratic form and with the
+    residual epilogue (the two forms the autotuner chooses from)."""
     fx = np.load(NULL)
     null_ref = fx["null"]  # (N, 4 contrasts, 2 signs)
     N = null_ref.shape[0]
@@ -55,6 +58,8 @@ def test_config2_fwer_maps_vs_fp64_oracle():
     st = synth.config2(seed=int(fx["study_seed"]))
     eng = E.PermutationEngine(st.Y, st.pred_x, (st.offsets, st.indices), st.segments, 2.0, 1.0, batch=256,
                               floor_zero=True)
+    eng._tc.quadratic_form = quadratic_form
+    assert eng._graph_qf() == quadratic_form
     perms = E.permutations(st.n, int(fx["seed"]), 0, N)
     got = eng.run_graph(perms=perms)  # (N, C, 2, S)
     null_gpu = np.vectorize(lambda v: float("%.4f" % v))(got.max(axis=-1))

@@ -43,11 +43,16 @@ def ref100(config1):
     return perms, oracle_maxima(config1, perms)
 
 
-@pytest.fixture(scope="module", params=["bf16x3", "fp32"])
+@pytest.fixture(scope="module", params=["bf16x3", "bf16x3-residual", "fp32"])
 def run100(config1, ref100, request):
+    """bf16x3: the tensor-core GLM in its quadratic form (the engines'
+    default here); bf16x3-residual: with the residual epilogue."""
     st = config1
     eng = E.PermutationEngine(st.Y, st.pred_x, (st.offsets, st.indices), st.segments, 2.0, 1.0, batch=32,
-                              precision=request.param)
+                              precision=request.param.split("-")[0])
+    if request.param.endswith("residual"):
+        eng._tc.quadratic_form = False
+    assert eng._graph_qf() == (request.param == "bf16x3")
     perms, ref = ref100
     gpu = E.reduce_vertex(eng.run(perms=perms))
     return st, eng, perms, gpu, ref

@@ -1,8 +1,12 @@
-"""tcgen05 split-BF16 GLM (glm_tstat_tc) against the FP64 oracle.
+"""tcgen05 split-BF16 GLM against the FP64 oracle: the residual epilogue
+(glm_tstat_tc) and the quadratic form (glm_tstat_tc_qf: t of coefficients
+>= 1 of intercept designs from c = Xc'(y - centre), RSS = yy - c'inv(Xc'Xc)c).
 
 Bar: |t_tc - t_fp64| <= 2e-4 * max(1, |t|).  Split BF16 represents each
 operand to ~2^-17 relative and drops the lo.lo product, so the betas carry
-~1e-5 relative error; the residual pass reads the FP32 data."""
+~1e-5 relative error; the residual pass reads the FP32 data, and the
+quadratic form's RSS carries the cross products' split error scaled by
+R^2 / (1 - R^2) of the fit."""
 import numpy as np
 import pytest
 
@@ -61,8 +65,9 @@ def test_tile_layout_matches_definition():
         np.testing.assert_array_equal(got, exp)
 
 
+@pytest.mark.parametrize("form", ["quadratic", "residual"])
 @pytest.mark.parametrize("n,V,G", [(100, 10242, 40), (350, 4000, 33), (57, 777, 16), (350, 20000, 64)])
-def test_tc_vs_fp64(n, V, G):
+def test_tc_vs_fp64(n, V, G, form):
     rng = np.random.default_rng(n + V)
     Y = rng.standard_normal((n, V)).astype(np.float32)
     Y[:, : V // 3] += 0.4 * rng.standard_normal(n)[:, None].astype(np.float32)
@@ -71,14 +76,14 @@ def test_tc_vs_fp64(n, V, G):
     perms = np.stack([rng.permutation(n) for _ in range(G)])
     db = DesignBatch(X[perms])
     coef = [1, 2, 3, 4]
-    t_tc = glm_tstat_tc(Y, db, coef).cpu().numpy()
+    t_tc = glm_tstat_tc(Y, db, coef, quadratic_form=form == "quadratic").cpu().numpy()
     t_32 = glm_stat(Y, db, WHAT_T, coef=coef).cpu().numpy()
     e_tc, e_32 = 0.0, 0.0
     for g in range(G):
         ref = oracle.tval_fp64(X[perms[g]], Y)[coef]
         e_tc = max(e_tc, _err(t_tc[g], ref))
         e_32 = max(e_32, _err(t_32[g], ref))
-    print(f"n={n} V={V} G={G}: tc {e_tc:.2e}  fp32 {e_32:.2e}")
+    print(f"n={n} V={V} G={G} {form}: tc {e_tc:.2e}  fp32 {e_32:.2e}")
     assert e_tc <= TOL, e_tc
 
 
@@ -155,7 +160,70 @@ def test_design_block_16_equals_32(kmax):
         ops = TensorCoreOperands(torch.from_numpy(Y).cuda())
         ops.design_block = block
         assert ops.block(kmax) == block
-        res.append(glm_tstat_tc(Y, DesignBatch(X), coef, ops=ops).cpu().numpy())
+        res.append(glm_tstat_tc(Y, DesignBatch(X), coef, ops=ops, quadratic_form=False).cpu().numpy())
     np.testing.assert_allclose(res[0], res[1], rtol=1e-6, atol=1e-6)
     ref = np.stack([oracle.tval_fp64(X[g], Y)[coef] for g in range(G)])
     assert _err(res[1], ref) <= TOL
+
+
+@pytest.mark.parametrize("kmax", [2, 3, 4, 5, 6, 7, 8])
+def test_quadratic_form_every_kmax(kmax):
+    """Every column count: 4 rows per design (64-design tiles) up to kmax 5,
+    8 rows (32-design tiles) above; 70 designs leave a partial design tile
+    and 1,000 vertices a partial vertex tile."""
+    import torch
+    rng = np.random.default_rng(40 + kmax)
+    n, V, G = 97, 1000, 70
+    Y = (2.0 + rng.standard_normal((n, V))).astype(np.float32)
+    X = np.column_stack([np.ones(n), rng.standard_normal((n, kmax - 1))])
+    perms = np.stack([rng.permutation(n) for _ in range(G)])
+    db = DesignBatch(X[perms])
+    coef = list(range(1, kmax))
+    ops = TensorCoreOperands(torch.from_numpy(Y).cuda())
+    assert ops.qf_ok(db, coef)
+    t_qf = glm_tstat_tc(Y, db, coef, ops=ops).cpu().numpy()
+    assert int(ops.err.item()) == 0
+    ref = np.stack([oracle.tval_fp64(X[perms[g]], Y)[coef] for g in range(G)])
+    assert _err(t_qf, ref) <= TOL, _err(t_qf, ref)
+
+
+@pytest.mark.parametrize("r2", [0.5, 0.9, 0.97])
+def test_quadratic_form_strong_fits(r2):
+    """Vertices whose data the design explains to R^2 = 0.5 .. 0.97 (the
+    unpermuted design, t up to ~100): the quadratic form's RSS = yy - c'b
+    loses relative precision as R^2 / (1 - R^2); within the bar up to 0.97."""
+    rng = np.random.default_rng(int(r2 * 100))
+    n, V, G = 350, 2048, 8
+    X = np.column_stack([np.ones(n), rng.integers(0, 2, n), rng.standard_normal((n, 3))])
+    fit = X[:, 1:] @ rng.standard_normal((4, V))
+    fit /= fit.std(axis=0, keepdims=True)
+    noise = rng.standard_normal((n, V))
+    noise /= noise.std(axis=0, keepdims=True)
+    Y = (10.0 + np.sqrt(r2) * fit + np.sqrt(1.0 - r2) * noise).astype(np.float32)
+    designs = np.stack([X] + [X[rng.permutation(n)] for _ in range(G - 1)])
+    coef = [1, 2, 3, 4]
+    t_qf = glm_tstat_tc(Y, DesignBatch(designs), coef, quadratic_form=True).cpu().numpy()
+    e = max(_err(t_qf[g], oracle.tval_fp64(designs[g], Y)[coef]) for g in range(G))
+    print(f"R^2 {r2}: quadratic form {e:.2e}")
+    assert e <= TOL, e
+
+
+def test_quadratic_form_mixed_k_designs():
+    """The mediation engine's batches: designs [1, x] and [1, x, m] padded to
+    kmax 3; the shorter design's missing column has zero cross products and
+    inverse rows."""
+    rng = np.random.default_rng(77)
+    n, V = 150, 1500
+    Y = rng.standard_normal((n, V)).astype(np.float32)
+    x, m = rng.standard_normal(n), rng.standard_normal(n)
+    mats = []
+    for g in range(24):
+        p = rng.permutation(n)
+        mats.append(np.column_stack([np.ones(n), x[p]]) if g % 2 == 0 else np.column_stack([np.ones(n), x[p], m]))
+    db = DesignBatch(mats, kmax=3)
+    t_qf = glm_tstat_tc(Y, db, [1], quadratic_form=True).cpu().numpy()
+    t_res = glm_tstat_tc(Y, db, [1], quadratic_form=False).cpu().numpy()
+    for g, Xg in enumerate(mats):
+        ref = oracle.tval_fp64(Xg, Y)[[1]]
+        assert _err(t_qf[g], ref) <= TOL, (g, _err(t_qf[g], ref))
+    assert _err(t_qf, t_res.astype(np.float64)) <= TOL

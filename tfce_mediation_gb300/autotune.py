@@ -6,8 +6,10 @@ warm-up launch) for the GLM + sweep of one batch; the one with the highest
 permutations per second wins.  The sweep runs 3 CTAs of 512 threads per SM
 (40 registers, the most items in flight) or 2 (64 registers, no spills);
 which is faster depends on the segments' sizes and list lengths.  The GLM
-tile holds 32 designs (N = 256 MMA columns) or 16 (N = 128); it is timed
-first, on the largest candidate batch.  Good
+runs as the quadratic form (t from the cross products of the centred
+designs with the data, where it applies) or with the residual epilogue, whose
+tile holds 32 designs (N = 256 MMA columns) or 16 (N = 128); the forms are
+timed first, on the largest candidate batch.  Good
 values of P fill the persistent sweep grid evenly: one launch has P x
 contrasts x signs x segments sweep items spread over the resident CTAs
 (tfce_sweep_resident_slots), so P where that count is a multiple of the CTA
@@ -111,31 +113,44 @@ def time_glm(eng, P, seed=12345, repeats=3):
 
 
 def choose_design_block(eng, P):
-    """Designs per tensor-core GLM tile (32 or 16; only 16 exists for more
-    than 5 columns), timed on one batch; set on the engine's operands."""
+    """The tensor-core GLM's form, timed on one batch and set on the engine's
+    operands: the quadratic form where the engine's GLM allows it, or the
+    residual epilogue with 32 or 16 designs per tile (only 16 exists for more
+    than 5 columns).  Returns (design_block, quadratic_form); the timings
+    (ms per batch) are kept as the operands' glm_timings."""
     tc = getattr(eng, "_tc", None)
-    if tc is None or eng.k > 5:
-        return None
+    if tc is None:
+        return None, False
     ms = {}
-    for db in (32, 16):
+    tc.quadratic_form = True
+    if eng._graph_qf():
+        ms["qf"] = time_glm(eng, P)
+    tc.quadratic_form = False
+    res = {}
+    for db in ((32, 16) if eng.k <= 5 else (16,)):
         tc.design_block = db
-        ms[db] = time_glm(eng, P)
-    tc.design_block = min(ms, key=ms.get)
-    return tc.design_block
+        res[db] = ms[f"res{db}"] = time_glm(eng, P)
+    tc.glm_timings = ms
+    tc.design_block = min(res, key=res.get)
+    tc.quadratic_form = "qf" in ms and ms["qf"] <= res[tc.design_block]
+    return tc.design_block, tc.quadratic_form
 
 
 def choose_batch(eng, max_p=256, use_cache=True, shapes=(3, 2)):
     """Best P and sweep CTA shape for this engine's problem, and the GLM's
-    designs per tile (cached); the shape is set on the engine's adjacency
-    handle and the tile size on its GLM operands, P is returned."""
+    form and designs per tile (cached); the shape is set on the engine's
+    adjacency handle and the GLM's choice on its operands, P is returned."""
     key = _key(eng)
     cache = _load() if use_cache else {}
     if key in cache and "ctas_per_sm" in cache[key]:
         eng.adj.set_sweep_shape(int(cache[key]["ctas_per_sm"]))
-        if cache[key].get("design_block") and getattr(eng, "_tc", None) is not None:
-            eng._tc.design_block = int(cache[key]["design_block"])
+        if getattr(eng, "_tc", None) is not None:
+            if cache[key].get("design_block"):
+                eng._tc.design_block = int(cache[key]["design_block"])
+            eng._tc.quadratic_form = bool(cache[key].get("quadratic_form", True))
+            eng._tc.glm_timings = cache[key].get("glm_ms")
         return int(cache[key]["P"])
-    design_block = choose_design_block(eng, max(candidates(eng, max_p)))
+    design_block, quadratic_form = choose_design_block(eng, max(candidates(eng, max_p)))
     results = {}
     for shape in shapes:
         eng.adj.set_sweep_shape(shape)
@@ -147,7 +162,8 @@ def choose_batch(eng, max_p=256, use_cache=True, shapes=(3, 2)):
             results[(shape, P)] = P / ms * 1000.0
     shape, best = max(results, key=results.get)
     eng.adj.set_sweep_shape(shape)
-    cache[key] = {"P": best, "ctas_per_sm": shape, "design_block": design_block,
+    cache[key] = {"P": best, "ctas_per_sm": shape, "design_block": design_block, "quadratic_form": quadratic_form,
+                  "glm_ms": getattr(getattr(eng, "_tc", None), "glm_timings", None),
                   "perm_per_s": {f"{s}x{p}": v for (s, p), v in results.items()}}
     if use_cache:
         _save(cache)

@@ -190,6 +190,18 @@ __device__ inline void tmem_ld8(uint32_t taddr, float* out) {
   for (int i = 0; i < 8; ++i) out[i] = __uint_as_float(r[i]);
 }
 
+__device__ inline void tmem_ld16(uint32_t taddr, float* out) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) out[i] = __uint_as_float(r[i]);
+}
+
 // --- operand pre-tiling -------------------------------------------------------
 // dst = the split-BF16 tiles of a [rows][cols] FP32 matrix (row stride ld_src;
 // transpose: the source is stored [cols][rows], e.g. the data n x V):
@@ -261,6 +273,28 @@ __global__ void col_center_kernel(const float* __restrict__ Y, int64_t ldy, int 
   }
 }
 
+// Centred sum of squares of every column of Yc [n][ldy] (the data minus its
+// per-vertex centre): sum (y - m)^2 with m the column's mean, as
+// S2 - S1^2 / n from FP32 sums of 16-row blocks accumulated in FP64.
+__global__ void col_sumsq_kernel(const float* __restrict__ Yc, int64_t ldy, int n, int64_t V,
+                                 float* __restrict__ yy) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (int64_t)gridDim.x * blockDim.x) {
+    double s1 = 0.0, s2 = 0.0;
+    for (int i0 = 0; i0 < n; i0 += 16) {
+      float b1 = 0.0f, b2 = 0.0f;
+      const int i1 = min(n, i0 + 16);
+      for (int i = i0; i < i1; ++i) {
+        const float x = __ldg(Yc + (int64_t)i * ldy + v);
+        b1 += x;
+        b2 = fmaf(x, x, b2);
+      }
+      s1 += static_cast<double>(b1);
+      s2 += static_cast<double>(b2);
+    }
+    yy[v] = static_cast<float>(fmax(s2 - s1 * s1 / n, 0.0));
+  }
+}
+
 // --- the GEMM + residual epilogue -----------------------------------------------
 struct TcArgs {
   const __nv_bfloat16* yt;  // pre-tiled data, 128-vertex row blocks
@@ -282,28 +316,12 @@ struct TcArgs {
   int32_t* err;
 };
 
-template <int KMAX, bool kCentred, int DPT_ = tc_dpt(KMAX)>
-__global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
-  // centred form: r = (y - c) - Xc b[1..] for designs with an intercept
-  // (column means removed from the other columns; c the data's centre)
-  constexpr int J0 = kCentred ? 1 : 0;
-  constexpr int DPT = DPT_;
-  constexpr int DB = tc_db(DPT);
-  constexpr int N = tc_n(DPT);
-  constexpr int YS = tc_y_stage();
-  constexpr int PS = tc_p_stage(DPT);
-  constexpr int ST = tc_stage(DPT);
-  constexpr int XC = tc_xchunk(KMAX, DPT);
-  extern __shared__ __align__(1024) unsigned char sm[];
-  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + tc_area(KMAX, DPT));  // full[4], empty[4], done
-  uint32_t* sTmem = reinterpret_cast<uint32_t*>(bars + 2 * kTcStages + 1);
-  int* sFail = reinterpret_cast<int*>(sTmem + 1);
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int64_t vb = blockIdx.x / a.n_db;
-  const int db = static_cast<int>(blockIdx.x % a.n_db);
-  const uint32_t sbase = smem_addr(sm);
-  const uint32_t full0 = smem_addr(bars), empty0 = full0 + 8 * kTcStages, done = full0 + 16 * kTcStages;
-
+// Tensor memory for N accumulator columns (warp 0) and the pipeline's
+// barriers (thread 0: full[4], empty[4], done); returns the TMEM address.
+// Every thread of the CTA calls it (it synchronises the CTA).
+template <int N>
+__device__ __forceinline__ uint32_t tc_setup(uint32_t* sTmem, uint32_t full0, uint32_t empty0, uint32_t done,
+                                             int* sFail, int warp, int tid) {
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(sTmem)),
                  "n"(N)
@@ -322,62 +340,102 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  const uint32_t tmem = *sTmem;
-  const int KS = a.ks_count;
+  return *sTmem;
+}
 
-  // ---- copy / MMA pipeline (one thread) ----
-  if (tid == 0) {
-    const unsigned char* ysrc = reinterpret_cast<const unsigned char*>(a.yt) + (vb * KS) * (int64_t)YS;
-    const unsigned char* psrc = reinterpret_cast<const unsigned char*>(a.pt) + ((int64_t)db * KS) * (int64_t)PS;
-    const uint32_t idesc = make_idesc(kTcM, N);
-    int issued = 0;  // K steps whose copies were issued
-    bool ok = true;
-    for (; issued < kTcStages && issued < KS; ++issued) {
-      const uint32_t dst = sbase + issued * ST, fb = full0 + 8 * issued;
+// ---- copy / MMA pipeline, run by one thread ----
+// K steps of D[128][N] += A . B over the pre-tiled operands: a 4-stage ring of
+// one cp.async.bulk per operand per stage (completing on the stage's full
+// barrier); the three split products of a step are committed to the stage's
+// empty barrier, and a stage is refilled one step behind the MMA issue.
+// Commits `done` after the last step.  On a wait that ran out: records
+// kDevLoopLimit, sets *sFail and waits (bounded) for the copies in flight.
+template <int N>
+__device__ __forceinline__ void tc_gemm_pipeline(const unsigned char* ysrc, const unsigned char* psrc,
+                                                 uint32_t sbase, uint32_t full0, uint32_t empty0, uint32_t done,
+                                                 uint32_t tmem, int KS, int32_t* err, int* sFail) {
+  constexpr int YS = tc_y_stage();
+  constexpr int PS = N * kTcK * 2 * 2;
+  constexpr int ST = YS + PS;
+  const uint32_t idesc = make_idesc(kTcM, N);
+  int issued = 0;  // K steps whose copies were issued
+  bool ok = true;
+  for (; issued < kTcStages && issued < KS; ++issued) {
+    const uint32_t dst = sbase + issued * ST, fb = full0 + 8 * issued;
+    mbar_expect_tx(fb, YS + PS);
+    bulk_g2s(dst, ysrc + (int64_t)issued * YS, YS, fb);
+    bulk_g2s(dst + YS, psrc + (int64_t)issued * PS, PS, fb);
+  }
+  int ks = 0;  // K steps whose copies were consumed
+  for (; ks < KS; ++ks) {
+    const int s = ks % kTcStages;
+    if (!mbar_wait(full0 + 8 * s, (ks / kTcStages) & 1)) {
+      ok = false;
+      break;
+    }
+    tc_fence_after();
+    const uint32_t st = sbase + s * ST;
+    const uint64_t ah = make_desc(st, kTcM * 16, 128);
+    const uint64_t al = make_desc(st + YS / 2, kTcM * 16, 128);
+    const uint64_t bh = make_desc(st + YS, N * 16, 128);
+    const uint64_t bl = make_desc(st + YS + PS / 2, N * 16, 128);
+    mma_bf16(tmem, ah, bh, idesc, ks > 0 ? 1u : 0u);
+    mma_bf16(tmem, ah, bl, idesc, 1u);
+    mma_bf16(tmem, al, bh, idesc, 1u);
+    mma_commit(empty0 + 8 * s);
+    // refill the stage of step ks-1 (its MMAs are queued ahead of this step's)
+    if (ks >= 1 && issued < KS) {
+      const int kp = ks - 1, sp = kp % kTcStages;
+      if (!mbar_wait(empty0 + 8 * sp, (kp / kTcStages) & 1)) {
+        ok = false;
+        ++ks;
+        break;
+      }
+      const uint32_t dst = sbase + sp * ST, fb = full0 + 8 * sp;
       mbar_expect_tx(fb, YS + PS);
       bulk_g2s(dst, ysrc + (int64_t)issued * YS, YS, fb);
       bulk_g2s(dst + YS, psrc + (int64_t)issued * PS, PS, fb);
-    }
-    int ks = 0;  // K steps whose copies were consumed
-    for (; ks < KS; ++ks) {
-      const int s = ks % kTcStages;
-      if (!mbar_wait(full0 + 8 * s, (ks / kTcStages) & 1)) {
-        ok = false;
-        break;
-      }
-      tc_fence_after();
-      const uint32_t st = sbase + s * ST;
-      const uint64_t ah = make_desc(st, kTcM * 16, 128);
-      const uint64_t al = make_desc(st + YS / 2, kTcM * 16, 128);
-      const uint64_t bh = make_desc(st + YS, N * 16, 128);
-      const uint64_t bl = make_desc(st + YS + PS / 2, N * 16, 128);
-      mma_bf16(tmem, ah, bh, idesc, ks > 0 ? 1u : 0u);
-      mma_bf16(tmem, ah, bl, idesc, 1u);
-      mma_bf16(tmem, al, bh, idesc, 1u);
-      mma_commit(empty0 + 8 * s);
-      // refill the stage of step ks-1 (its MMAs are queued ahead of this step's)
-      if (ks >= 1 && issued < KS) {
-        const int kp = ks - 1, sp = kp % kTcStages;
-        if (!mbar_wait(empty0 + 8 * sp, (kp / kTcStages) & 1)) {
-          ok = false;
-          ++ks;
-          break;
-        }
-        const uint32_t dst = sbase + sp * ST, fb = full0 + 8 * sp;
-        mbar_expect_tx(fb, YS + PS);
-        bulk_g2s(dst, ysrc + (int64_t)issued * YS, YS, fb);
-        bulk_g2s(dst + YS, psrc + (int64_t)issued * PS, PS, fb);
-        ++issued;
-      }
-    }
-    mma_commit(done);
-    if (!ok) {
-      atomicCAS(a.err, 0, kDevLoopLimit);
-      *sFail = 1;
-      // copies issued but not consumed: wait (bounded) until they have landed
-      for (int qq = ks; qq < issued; ++qq) mbar_wait(full0 + 8 * (qq % kTcStages), (qq / kTcStages) & 1);
+      ++issued;
     }
   }
+  mma_commit(done);
+  if (!ok) {
+    atomicCAS(err, 0, kDevLoopLimit);
+    *sFail = 1;
+    // copies issued but not consumed: wait (bounded) until they have landed
+    for (int qq = ks; qq < issued; ++qq) mbar_wait(full0 + 8 * (qq % kTcStages), (qq / kTcStages) & 1);
+  }
+}
+
+template <int KMAX, bool kCentred, int DPT_ = tc_dpt(KMAX)>
+__global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
+  // centred form: r = (y - c) - Xc b[1..] for designs with an intercept
+  // (column means removed from the other columns; c the data's centre)
+  constexpr int J0 = kCentred ? 1 : 0;
+  constexpr int DPT = DPT_;
+  constexpr int DB = tc_db(DPT);
+  constexpr int N = tc_n(DPT);
+  constexpr int YS = tc_y_stage();
+  constexpr int PS = tc_p_stage(DPT);
+  constexpr int XC = tc_xchunk(KMAX, DPT);
+  extern __shared__ __align__(1024) unsigned char sm[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + tc_area(KMAX, DPT));  // full[4], empty[4], done
+  uint32_t* sTmem = reinterpret_cast<uint32_t*>(bars + 2 * kTcStages + 1);
+  int* sFail = reinterpret_cast<int*>(sTmem + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int64_t vb = blockIdx.x / a.n_db;
+  const int db = static_cast<int>(blockIdx.x % a.n_db);
+  const uint32_t sbase = smem_addr(sm);
+  const uint32_t full0 = smem_addr(bars), empty0 = full0 + 8 * kTcStages, done = full0 + 16 * kTcStages;
+
+  const uint32_t tmem = tc_setup<N>(sTmem, full0, empty0, done, sFail, warp, tid);
+  const int KS = a.ks_count;
+
+  // ---- copy / MMA pipeline (one thread) ----
+  if (tid == 0)
+    tc_gemm_pipeline<N>(reinterpret_cast<const unsigned char*>(a.yt) + (vb * KS) * (int64_t)YS,
+                        reinterpret_cast<const unsigned char*>(a.pt) + ((int64_t)db * KS) * (int64_t)PS, sbase,
+                        full0, empty0, done, tmem, KS, a.err, sFail);
   __syncwarp();
   if (!mbar_wait(done, 0)) {
     if (lane == 0) atomicCAS(a.err, 0, kDevLoopLimit);
@@ -602,6 +660,132 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
   }
 }
 
+
+// --- the quadratic-form GLM (centred designs, t of coefficients >= 1) ---------
+// For designs whose first column is all ones, and t of the other coefficients
+// only (the permutation engines' case), everything follows from the cross
+// products of the centred design columns with the centred data,
+// c_d(v) = Xc_d' (y(v) - centre(v)), by Frisch-Waugh (the intercept drops out):
+//   b   = inv(Xc'Xc) c                         the betas of columns 1..k-1
+//   RSS = yy - c'b, yy = sum_i (y_i - mean)^2  the residual sum of squares
+//   t_j = b_j / sqrt(RSS / dof * inv(X'X)_jj)  (cynumstats.pyx:47-64)
+// One GEMM D[v][d*R + j] = sum_i (y_i(v) - centre(v)) Xc_d[i][j] -- R = 4 rows
+// per design for k <= 5 (64 designs per 256-column tile), 8 for k <= 8 (32)
+// -- and an epilogue of O(k^2) FMAs per (vertex, design) replace the
+// residual pass's (k+1) n.  RSS = yy - c'b is first-order in the split error
+// of c, scaled by R^2 / (1 - R^2) of the fit; the split error of a cross
+// product is a sum of independent roundings while the product itself is
+// coherent, so at the fits a permutation null produces (R^2 ~ k / n) the t
+// error stays that of the betas.
+constexpr int kQfN = 256;  // accumulator columns (MMA N)
+__host__ __device__ constexpr int qf_rows(int kc) { return kc <= 4 ? 4 : 8; }  // B rows per design
+__host__ __device__ constexpr int qf_db(int kc) { return kQfN / qf_rows(kc); }  // designs per tile
+__host__ __device__ constexpr int qf_stage() { return tc_y_stage() + kQfN * kTcK * 2 * 2; }
+__host__ __device__ constexpr int qf_smem() { return kTcStages * qf_stage() + 128; }
+static_assert(qf_smem() <= 113 * 1024, "two CTAs per SM");
+
+struct QfArgs {
+  const __nv_bfloat16* yt;  // pre-tiled centred data, 128-vertex row blocks
+  const __nv_bfloat16* xt;  // pre-tiled centred design columns, R rows per design, 256-row blocks
+  const float* yy;          // [V] centred sum of squares of each vertex's data
+  const float* ginv;        // [G_pad][KC][KC] inv(Xc'Xc) = inv(X'X) without its first row and column
+  const float* invdiag;     // [G][KC + 1] SE factors
+  const float* dof;         // [G]
+  const int32_t* coef;      // coefficient indices in [1, KC]
+  float* t_out;             // [G][n_coef][ldt]
+  int64_t ldt, V;
+  int32_t ks_count, G, n_db, n_coef;
+  int32_t* err;
+};
+
+template <int KC>
+__global__ void __launch_bounds__(kTcThreads, 2) glm_tc_qf_kernel(QfArgs a) {
+  constexpr int R = qf_rows(KC), DB = qf_db(KC), N = kQfN;
+  constexpr int YS = tc_y_stage(), PS = N * kTcK * 2 * 2;
+  extern __shared__ __align__(1024) unsigned char sm[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + kTcStages * qf_stage());  // full[4], empty[4], done
+  uint32_t* sTmem = reinterpret_cast<uint32_t*>(bars + 2 * kTcStages + 1);
+  int* sFail = reinterpret_cast<int*>(sTmem + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int64_t vb = blockIdx.x / a.n_db;
+  const int db = static_cast<int>(blockIdx.x % a.n_db);
+  const uint32_t sbase = smem_addr(sm);
+  const uint32_t full0 = smem_addr(bars), empty0 = full0 + 8 * kTcStages, done = full0 + 16 * kTcStages;
+  const uint32_t tmem = tc_setup<N>(sTmem, full0, empty0, done, sFail, warp, tid);
+  const int KS = a.ks_count;
+
+  if (tid == 0)
+    tc_gemm_pipeline<N>(reinterpret_cast<const unsigned char*>(a.yt) + (vb * KS) * (int64_t)YS,
+                        reinterpret_cast<const unsigned char*>(a.xt) + ((int64_t)db * KS) * (int64_t)PS, sbase,
+                        full0, empty0, done, tmem, KS, a.err, sFail);
+  __syncwarp();
+  if (!mbar_wait(done, 0)) {
+    if (lane == 0) atomicCAS(a.err, 0, kDevLoopLimit);
+    *sFail = 1;
+  }
+  tc_fence_after();
+  __syncthreads();
+
+  if (*sFail == 0) {
+    // warp w reads TMEM lanes 32*(w%4).. (its 32 vertices) for the designs of
+    // tile half w/4; every lane of a warp works on the same design at a time,
+    // so the per-design constants are warp-uniform loads and the t stores
+    // coalesce over the vertices
+    const int q = warp & 3, half = warp >> 2;
+    const int64_t v = vb * kTcM + q * 32 + lane;
+    const bool live = v < a.V;
+    const float yyv = live ? __ldg(a.yy + v) : 0.0f;
+    constexpr int DPW = DB / 2;  // designs per warp
+    constexpr int DPL = 16 / R;  // designs per 16-column load
+#pragma unroll 1
+    for (int d0 = 0; d0 < DPW; d0 += DPL) {
+      float cc[16];
+      tmem_ld16(tmem + (static_cast<uint32_t>(q * 32) << 16) + (half * DPW + d0) * R, cc);
+#pragma unroll
+      for (int dd = 0; dd < DPL; ++dd) {
+        const int g = db * DB + half * DPW + d0 + dd;
+        if (g >= a.G) break;
+        const float* gi = a.ginv + (int64_t)g * KC * KC;
+        float b[KC];
+        float qf = 0.0f;
+#pragma unroll
+        for (int i = 0; i < KC; ++i) {
+          float s = 0.0f;
+#pragma unroll
+          for (int j = 0; j < KC; ++j) s = fmaf(__ldg(gi + i * KC + j), cc[dd * R + j], s);
+          b[i] = s;
+          qf = fmaf(cc[dd * R + i], s, qf);
+        }
+        const float rss = fmaxf(yyv - qf, 0.0f);
+        const float inv_dof = 1.0f / __ldg(a.dof + g);
+        for (int ci = 0; ci < a.n_coef; ++ci) {
+          const int j = __ldg(a.coef + ci);
+          float bj = __int_as_float(0x7fc00000);  // NaN for a coefficient outside [1, KC]
+#pragma unroll
+          for (int jj = 0; jj < KC; ++jj)
+            if (jj + 1 == j) bj = b[jj];
+          const float dj = (j >= 1 && j <= KC) ? __ldg(a.invdiag + (int64_t)g * (KC + 1) + j) : 1.0f;
+          if (live) a.t_out[((int64_t)g * a.n_coef + ci) * a.ldt + v] = bj / sqrtf(rss * inv_dof * dj);
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(N) : "memory");
+  }
+}
+
+template <int KC>
+static int launch_tc_qf(const QfArgs& a, int64_t n_vb, cudaStream_t stream) {
+  const int smem = qf_smem();
+  TFGB_CUDA(cudaFuncSetAttribute(glm_tc_qf_kernel<KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  glm_tc_qf_kernel<KC><<<static_cast<unsigned>(n_vb * a.n_db), kTcThreads, smem, stream>>>(a);
+  TFGB_CUDA(cudaGetLastError());
+  return TFCE_OK;
+}
+
 template <int KMAX, int DPT = tc_dpt(KMAX)>
 static int launch_tc(const TcArgs& a, int64_t n_vb, cudaStream_t stream) {
   const int smem = tc_smem(KMAX, DPT);
@@ -626,6 +810,64 @@ extern "C" {
 int glm_tc_design_block(int32_t kmax) {
   if (kmax < 1 || kmax > tfgb::kTcRowsPerDesign) return -1;
   return tfgb::tc_db(tfgb::tc_dpt(kmax));
+}
+
+int glm_qf_design_block(int32_t kmax) {
+  if (kmax < 2 || kmax > tfgb::kTcRowsPerDesign) return -1;
+  return tfgb::qf_db(kmax - 1);
+}
+
+int glm_col_sumsq(const float* Y_centred, int64_t ldy, int32_t n, int64_t V, float* yy, void* stream) {
+  tfgb::clear_error();
+  TFGB_CHECK_ARG(Y_centred && yy, "NULL pointer");
+  TFGB_CHECK_ARG(n > 0 && V >= 0 && ldy >= V, "bad sizes");
+  if (V == 0) return TFCE_OK;
+  const unsigned blocks = static_cast<unsigned>(std::min<int64_t>((V + 255) / 256, 152 * 16));
+  tfgb::col_sumsq_kernel<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(Y_centred, ldy, n, V, yy);
+  TFGB_CUDA(cudaGetLastError());
+  return TFCE_OK;
+}
+
+int glm_tstat_tc_qf(const void* y_tiles, const float* yy, int32_t n, int32_t n_pad, int64_t V,
+                    const void* x_tiles, const float* ginv, const float* invdiag, const float* dof, int32_t G,
+                    int32_t kmax, const int32_t* coef, int32_t n_coef, float* t_out, int64_t ldt, int32_t* err,
+                    void* stream) {
+  tfgb::clear_error();
+  TFGB_CHECK_ARG(y_tiles && yy && x_tiles && ginv && invdiag && dof && coef && t_out && err, "NULL pointer");
+  TFGB_CHECK_ARG(kmax >= 2 && kmax <= tfgb::kTcRowsPerDesign, "kmax must be in [2, 8]");
+  TFGB_CHECK_ARG(n > kmax && n_pad >= n && n_pad % tfgb::kTcK == 0, "n_pad must be >= n and a multiple of 16");
+  TFGB_CHECK_ARG(n_coef >= 1, "n_coef must be >= 1");
+  TFGB_CHECK_ARG(V >= 0 && G >= 0 && ldt >= V, "bad sizes");
+  TFGB_CHECK_ARG(reinterpret_cast<uintptr_t>(y_tiles) % 16 == 0 && reinterpret_cast<uintptr_t>(x_tiles) % 16 == 0,
+                 "tiles must be 16-byte aligned");
+  if (V == 0 || G == 0) return TFCE_OK;
+  tfgb::QfArgs a{};
+  a.yt = static_cast<const __nv_bfloat16*>(y_tiles);
+  a.xt = static_cast<const __nv_bfloat16*>(x_tiles);
+  a.yy = yy;
+  a.ginv = ginv;
+  a.invdiag = invdiag;
+  a.dof = dof;
+  a.coef = coef;
+  a.t_out = t_out;
+  a.ldt = ldt;
+  a.V = V;
+  a.ks_count = n_pad / tfgb::kTcK;
+  a.G = G;
+  a.n_db = (G + glm_qf_design_block(kmax) - 1) / glm_qf_design_block(kmax);
+  a.n_coef = n_coef;
+  a.err = err;
+  const int64_t n_vb = (V + tfgb::kTcM - 1) / tfgb::kTcM;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  switch (kmax - 1) {
+    case 1: return tfgb::launch_tc_qf<1>(a, n_vb, st);
+    case 2: return tfgb::launch_tc_qf<2>(a, n_vb, st);
+    case 3: return tfgb::launch_tc_qf<3>(a, n_vb, st);
+    case 4: return tfgb::launch_tc_qf<4>(a, n_vb, st);
+    case 5: return tfgb::launch_tc_qf<5>(a, n_vb, st);
+    case 6: return tfgb::launch_tc_qf<6>(a, n_vb, st);
+    default: return tfgb::launch_tc_qf<7>(a, n_vb, st);
+  }
 }
 
 int64_t glm_tile_bytes(int64_t rows, int32_t row_block, int32_t n_pad) {

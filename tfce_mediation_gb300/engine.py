@@ -179,6 +179,12 @@ class PermutationEngine:
         if (precision or self.precision) == "bf16x3":
             tc = self._tc if self._tc is not None else TensorCoreOperands(self.Yd)
             self._tc = tc
+            if self.outputs is None and tc.qf_ok(designs, self.contrasts):
+                XR, GI = tc.host_operands_qf(designs)
+                xt = tc.tile_designs_qf(dev(XR), G, designs.kmax)
+                tc.tstat_qf(xt, dev(GI), dev(designs.invdiag64.astype(np.float32)),
+                            dev(designs.dof.astype(np.float32)), G, designs.kmax, self._coef, self.C, out, self.V)
+                return out
             centred = self._centred and tc.centred_ok(designs)
             P8, U, Xt = tc.host_operands(designs, centred=centred)
             pt = tc.tile_designs(dev(P8), G, designs.kmax)
@@ -252,6 +258,14 @@ class PermutationEngine:
         return np.concatenate(out) if out else np.zeros((0, self.C, self.signs, self.n_seg), np.float32)
 
     # -- CUDA-graph path ----------------------------------------------------
+    def _graph_qf(self):
+        """Whether the captured batches run the quadratic-form GLM: t of
+        coefficients >= 1 of the intercept designs [1, pred_x], no output
+        program, and the operands' setting on."""
+        tc = self._tc
+        return (tc is not None and self.outputs is None and self._centred and tc.quadratic_form
+                and tc.yy is not None and 2 <= self.k <= 8 and min(self.contrasts) >= 1)
+
     def _graph_slot(self, P):
         """One captured batch: pinned design operators -> device, glm_tstat,
         the sweep (counter reset included), maxima -> pinned host memory."""
@@ -259,7 +273,16 @@ class PermutationEngine:
         n, kmax = self.n, self.k
         tc = self._tc
         slot = {"P": P}
-        if tc is not None:
+        qf = self._graph_qf()
+        slot["QF"] = qf
+        if qf:
+            R, Gp = tc.qf_rows(kmax), tc.qf_padded(P, kmax)
+            keys = ("XR", "GI", "invd", "dof")
+            slot["h_XR"] = t.zeros((Gp * R, tc.n_pad), dtype=t.float32, pin_memory=True)
+            slot["h_GI"] = t.zeros((Gp, kmax - 1, kmax - 1), dtype=t.float32, pin_memory=True)
+            slot["d_xt"] = t.empty(int(self.lib.glm_tile_bytes(Gp * R, 256, tc.n_pad)), dtype=t.uint8,
+                                   device="cuda")
+        elif tc is not None:
             Gp, DB = tc.padded(P, kmax), tc.block(kmax)
             slot["DB"] = DB
             keys = ("P8", "U", "Xt", "invd", "dof") + (("W",) if self._w_stride else ())
@@ -286,7 +309,11 @@ class PermutationEngine:
         def body_glm():
             for key in keys:
                 slot["d_" + key].copy_(slot["h_" + key], non_blocking=True)
-            if tc is not None:
+            if qf:
+                tc.tile_designs_qf(slot["d_XR"], P, kmax, out=slot["d_xt"])
+                tc.tstat_qf(slot["d_xt"], slot["d_GI"], slot["d_invd"], slot["d_dof"], P, kmax, self._coef, self.C,
+                            slot["d_t"], self.V)
+            elif tc is not None:
                 tc.tile_designs(slot["d_P8"], P, kmax, out=slot["d_pt"])
                 tc.stat(3 if self.outputs is not None else 0, slot["d_pt"], slot["d_U"], slot["d_Xt"],
                         slot["d_invd"], slot["d_dof"], P, kmax, self._coef, self.C, slot["d_t"], self.V,
@@ -326,7 +353,9 @@ class PermutationEngine:
     def _fill(self, slot, perms):
         db = DesignBatch(self.X[perms])
         P = perms.shape[0]
-        if self._tc is not None:
+        if slot["QF"]:
+            self._tc.host_operands_qf(db, XR=slot["h_XR"].numpy(), GI=slot["h_GI"].numpy())
+        elif self._tc is not None:
             self._tc.host_operands(db, P8=slot["h_P8"].numpy(), U=slot["h_U"].numpy(), Xt=slot["h_Xt"].numpy(),
                                    centred=self._centred)
             if self._w_stride:
@@ -365,7 +394,8 @@ class PermutationEngine:
         t = self.t
         P = self.batch
         DB = None if self._tc is None else self._tc.block(self.k)
-        if not hasattr(self, "_slots") or self._slots[0]["P"] != P or self._slots[0].get("DB") != DB:
+        if (not hasattr(self, "_slots") or self._slots[0]["P"] != P or self._slots[0].get("DB") != DB
+                or self._slots[0]["QF"] != self._graph_qf()):
             self._slots = [self._graph_slot(P), self._graph_slot(P)]
         if not hasattr(self, "_up_stream"):
             self._up_stream = t.cuda.Stream()

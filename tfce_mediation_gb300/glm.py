@@ -78,6 +78,7 @@ class DesignBatch:
         pinv = np.zeros((G, kmax, n), np.float64)
         Xp = np.zeros((G, n, kmax), np.float64)
         invdiag = np.zeros((G, kmax), np.float64)
+        inv_p = np.zeros((G, kmax, kmax), np.float64)  # inv(X'X), zero padded
         same_k = len(set(ks)) == 1
         if same_k:
             Xs = np.stack(mats).astype(np.float64)
@@ -87,26 +88,23 @@ class DesignBatch:
             Xp[:, :, :k] = Xs
             di = np.diagonal(inv if invXX is None else np.asarray(invXX, np.float64), axis1=1, axis2=2)
             invdiag[:, :k] = di
+            inv_p[:, :k, :k] = inv
         else:
             for g, m in enumerate(mats):
                 k = m.shape[1]
                 inv = np.linalg.inv(m.T @ m)
+                inv_p[g, :k, :k] = inv
                 pinv[g, :k] = inv @ m.T
                 Xp[g, :, :k] = m
                 invdiag[g, :k] = np.diag(inv if invXX is None else np.asarray(invXX[g], np.float64))
         self.G, self.n, self.kmax, self.ks = G, n, kmax, ks
         self.pinv64, self.X64, self.invdiag64 = pinv, Xp, invdiag
         self._mats = mats
+        self._inv64 = inv_p
         self.dof = np.asarray([n - k for k in ks], np.float64)
 
     def inverse(self):
         """(G, kmax, kmax) inv(X'X) per design (zero padded), FP64."""
-        if getattr(self, "_inv64", None) is None:
-            inv = np.zeros((self.G, self.kmax, self.kmax), np.float64)
-            for g, m in enumerate(self._mats):
-                k = m.shape[1]
-                inv[g, :k, :k] = np.linalg.inv(m.T @ m)
-            self._inv64 = inv
         return self._inv64
 
     def group_blocks(self, groups):
@@ -216,7 +214,13 @@ class TensorCoreOperands:
     design batch: the stacked pseudoinverse rows [G_pad*8][n_pad] (tiled on
     the device), u = pinv(X_d).1 [G_pad][kmax] (restores the betas of the
     uncentred data) and the negated design rows [G_pad/DB][n_sc][kmax][DB]
-    for the residual epilogue."""
+    for the residual epilogue.
+
+    The quadratic form (glm_tstat_tc_qf) serves t of coefficients >= 1 of
+    designs whose first column is all ones: its operands are the centred
+    design columns [G_pad*R][n_pad] (tiled on the device) and inv(Xc'Xc)
+    [G_pad][k-1][k-1], with the data's centred sum of squares yy [V] kept
+    beside the tiles."""
 
     ROW_BLOCK = 128
 
@@ -233,7 +237,11 @@ class TensorCoreOperands:
         self.shift = t.empty(self.V, dtype=t.float32, device="cuda") if centre else None
         # the data minus its centre: residuals of intercept designs skip the intercept term
         self.Yc = t.empty_like(Yd) if centre else None
+        self.yy = t.empty(self.V, dtype=t.float32, device="cuda") if centre else None
         self.err = t.zeros(1, dtype=t.int32, device="cuda")
+        # t of coefficients >= 1 of intercept designs through the quadratic
+        # form (False: the residual epilogue; the autotuner times both)
+        self.quadratic_form = True
         # designs per tile: None = the library's default for kmax (32 for kmax <= 5, else 16);
         # 16 or 32 to choose (the autotuner times both)
         self.design_block = None
@@ -247,6 +255,8 @@ class TensorCoreOperands:
         # tiles of the centred data, and the centred FP32 copy in the same pass
         _lib.check(self.lib.glm_tile_split(ptr(self.Yd), self.V, 1, self.V, self.n, ptr(self.shift),
                                            self.ROW_BLOCK, self.n_pad, ptr(self.yt), ptr(self.Yc), stream_handle()))
+        if self.yy is not None:
+            _lib.check(self.lib.glm_col_sumsq(ptr(self.Yc), self.V, self.n, self.V, ptr(self.yy), stream_handle()))
 
     def block(self, kmax):
         if self.design_block is not None and (kmax <= 5 or self.design_block == 16):
@@ -262,6 +272,53 @@ class TensorCoreOperands:
         exists, every design's first column is all ones, and no requested
         output uses coefficient 0."""
         return self.Yc is not None and not first_column_used and bool(np.all(db.X64[:, :, 0] == 1.0))
+
+    def qf_ok(self, db: DesignBatch, coef):
+        """Whether the quadratic form serves t of `coef` for these designs:
+        centred data, every design's first column all ones, kmax in [2, 8]
+        and no coefficient 0 (designs with fewer columns are zero padded:
+        their missing columns get zero cross products and inverse rows)."""
+        return (self.quadratic_form and self.yy is not None and 2 <= db.kmax <= 8
+                and min(int(c) for c in coef) >= 1 and self.centred_ok(db))
+
+    def qf_rows(self, kmax):
+        return 4 if kmax <= 5 else 8
+
+    def qf_padded(self, G, kmax):
+        DB = int(self.lib.glm_qf_design_block(kmax))
+        return (G + DB - 1) // DB * DB
+
+    def host_operands_qf(self, db: DesignBatch, XR=None, GI=None):
+        """Host float32 operands of the quadratic form: the centred design
+        columns 1..k-1 stacked [G_pad*R][n_pad] (design d, column j at row
+        d*R + j - 1) and inv(Xc'Xc) = inv(X'X)[1:, 1:] [G_pad][k-1][k-1];
+        written into XR / GI when given (e.g. pinned buffers of those sizes)."""
+        G, k, n = db.G, db.kmax, db.n
+        R, Gp = self.qf_rows(k), self.qf_padded(G, k)
+        xr = np.zeros((Gp, R, self.n_pad), np.float32) if XR is None else XR.reshape(Gp, R, self.n_pad)
+        gi = np.zeros((Gp, k - 1, k - 1), np.float32) if GI is None else GI.reshape(Gp, k - 1, k - 1)
+        if XR is not None:
+            xr[...] = 0.0
+        xc = db.X64[:, :, 1:] - db.X64[:, :, 1:].mean(axis=1, keepdims=True)
+        xr[:G, :k - 1, :n] = xc.transpose(0, 2, 1)
+        gi[G:] = 0.0
+        gi[:G] = db.inverse()[:, 1:, 1:]
+        return xr.reshape(Gp * R, self.n_pad), gi
+
+    def tile_designs_qf(self, XR_dev, G, kmax, out=None):
+        """Device tiles of the stacked centred design columns XR_dev (G_pad*R, n_pad)."""
+        t = self.t
+        rows = self.qf_padded(G, kmax) * self.qf_rows(kmax)
+        nbytes = int(self.lib.glm_tile_bytes(rows, 256, self.n_pad))
+        out = t.empty(nbytes, dtype=t.uint8, device="cuda") if out is None else out
+        _lib.check(self.lib.glm_tile_split(ptr(XR_dev), self.n_pad, 0, rows, self.n_pad, None, 256, self.n_pad,
+                                           ptr(out), None, stream_handle()))
+        return out
+
+    def tstat_qf(self, x_tiles, ginv, invd, dof, G, kmax, coef_d, n_coef, out, ldt):
+        _lib.check(self.lib.glm_tstat_tc_qf(ptr(self.yt), ptr(self.yy), self.n, self.n_pad, self.V, ptr(x_tiles),
+                                            ptr(ginv), ptr(invd), ptr(dof), G, kmax, ptr(coef_d), n_coef, ptr(out),
+                                            ldt, ptr(self.err), stream_handle()))
 
     def host_operands(self, db: DesignBatch, P8=None, U=None, Xt=None, centred=False):
         """Host float32 operands of a DesignBatch: stacked pseudoinverse rows
@@ -325,11 +382,29 @@ class TensorCoreOperands:
             raise RuntimeError("tensor-core GLM: a copy or MMA completion wait ran out (device code %d)" % e)
 
 
-def glm_tstat_tc(Y, designs, coef, ops=None, centre=True):
-    """t maps (G, n_coef, V) through the tcgen05 split-BF16 GLM (glm_tstat_tc)."""
+def glm_tstat_tc(Y, designs, coef, ops=None, centre=True, quadratic_form=None):
+    """t maps (G, n_coef, V) through the tcgen05 split-BF16 GLM: the quadratic
+    form (glm_tstat_tc_qf) where it applies and quadratic_form is not False
+    (None: the operands' setting), else the residual epilogue (glm_tstat_tc)."""
     t = require_cuda()
     db = designs if isinstance(designs, DesignBatch) else DesignBatch(designs)
     ops = ops or TensorCoreOperands(dev(Y, t.float32), centre=centre)
+    keep = ops.quadratic_form
+    if quadratic_form is not None:
+        ops.quadratic_form = bool(quadratic_form)
+    try:
+        use_qf = ops.qf_ok(db, coef)
+    finally:
+        ops.quadratic_form = keep
+    if use_qf:
+        XR, GI = ops.host_operands_qf(db)
+        xt = ops.tile_designs_qf(dev(XR), db.G, db.kmax)
+        out = t.empty((db.G, len(coef), ops.V), device="cuda", dtype=t.float32)
+        ops.tstat_qf(xt, dev(GI), dev(db.invdiag64.astype(np.float32)), dev(db.dof.astype(np.float32)), db.G,
+                     db.kmax, dev(np.asarray(coef, np.int32)), len(coef), out, ops.V)
+        t.cuda.synchronize()
+        ops.status()
+        return out
     centred = ops.centred_ok(db, first_column_used=0 in list(coef))
     P8, U, Xt = ops.host_operands(db, centred=centred)
     pt = ops.tile_designs(dev(P8), db.G, db.kmax)
