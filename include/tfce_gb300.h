@@ -342,11 +342,12 @@ int glm_stat_tc_block(const void* y_tiles, const float* y_shift, const float* Y,
  *   glm_tstat_tc_qf: y_tiles as glm_tstat_tc (centred); x_tiles from
  *     glm_tile_split of the centred design columns stacked [G_pad*R][n_pad]
  *     (design d, column j >= 1 at row d*R + j - 1, other rows zero) in row
- *     blocks of 256; ginv [G_pad][kmax-1][kmax-1] = inv(X'X) without its
- *     first row and column (= inv(Xc'Xc)); invdiag [G][kmax] and dof [G] as
- *     glm_tstat; coef[0..n_coef) in [1, kmax) (another index yields NaN);
- *     err as glm_tstat_tc.  RSS is clamped at 0 (a perfect fit gives +-inf
- *     or NaN, as 0/0).  Tiles 16-byte aligned. */
+ *     blocks of 256; ginv [G_pad][R][R] = inv(X'X) without its first row
+ *     and column (= inv(Xc'Xc)), zero padded to R x R; invdiag [G][kmax]
+ *     and dof [G] as glm_tstat; coef[0..n_coef), n_coef <= 8, in [1, kmax)
+ *     (another index yields NaN); err as glm_tstat_tc.  RSS is clamped at 0
+ *     (a perfect fit gives +-inf or NaN, as 0/0).  Tiles and ginv 16-byte
+ *     aligned. */
 int glm_qf_design_block(int32_t kmax);
 int glm_col_sumsq(const float* Y_centred, int64_t ldy, int32_t n, int64_t V, float* yy, void* stream);
 int glm_tstat_tc_qf(const void* y_tiles, const float* yy, int32_t n, int32_t n_pad, int64_t V,

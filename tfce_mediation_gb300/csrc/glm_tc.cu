@@ -432,18 +432,22 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
   const int KS = a.ks_count;
 
   // ---- copy / MMA pipeline (one thread) ----
-  if (tid == 0)
+  // the producer thread alone waits for the accumulator; the other warps
+  // wait at the CTA barrier (no issue slots spent polling)
+  if (tid == 0) {
     tc_gemm_pipeline<N>(reinterpret_cast<const unsigned char*>(a.yt) + (vb * KS) * (int64_t)YS,
                         reinterpret_cast<const unsigned char*>(a.pt) + ((int64_t)db * KS) * (int64_t)PS, sbase,
                         full0, empty0, done, tmem, KS, a.err, sFail);
-  __syncwarp();
-  if (!mbar_wait(done, 0)) {
-    if (lane == 0) atomicCAS(a.err, 0, kDevLoopLimit);
-    *sFail = 1;
+    if (!mbar_wait(done, 0)) {
+      atomicCAS(a.err, 0, kDevLoopLimit);
+      *sFail = 1;
+    }
+    fence_proxy_async();
+    tc_fence_before();
   }
+  __syncthreads();
   tc_fence_after();
   fence_proxy_async();
-  __syncthreads();
   const bool failed = *sFail != 0;
 
   // ---- drain: TMEM lane = vertex -> sB[(d*KMAX + j)*kTcBld + vertex] ----
@@ -677,7 +681,8 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_kernel(TcArgs a) {
 // product is a sum of independent roundings while the product itself is
 // coherent, so at the fits a permutation null produces (R^2 ~ k / n) the t
 // error stays that of the betas.
-constexpr int kQfN = 256;  // accumulator columns (MMA N)
+constexpr int kQfN = 256;       // accumulator columns (MMA N)
+constexpr int kQfMaxCoef = 8;   // coefficients per design
 __host__ __device__ constexpr int qf_rows(int kc) { return kc <= 4 ? 4 : 8; }  // B rows per design
 __host__ __device__ constexpr int qf_db(int kc) { return kQfN / qf_rows(kc); }  // designs per tile
 __host__ __device__ constexpr int qf_stage() { return tc_y_stage() + kQfN * kTcK * 2 * 2; }
@@ -688,7 +693,7 @@ struct QfArgs {
   const __nv_bfloat16* yt;  // pre-tiled centred data, 128-vertex row blocks
   const __nv_bfloat16* xt;  // pre-tiled centred design columns, R rows per design, 256-row blocks
   const float* yy;          // [V] centred sum of squares of each vertex's data
-  const float* ginv;        // [G_pad][KC][KC] inv(Xc'Xc) = inv(X'X) without its first row and column
+  const float* ginv;        // [G_pad][R][R] inv(Xc'Xc) = inv(X'X) without its first row and column, zero padded
   const float* invdiag;     // [G][KC + 1] SE factors
   const float* dof;         // [G]
   const int32_t* coef;      // coefficient indices in [1, KC]
@@ -714,17 +719,20 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_qf_kernel(QfArgs a) {
   const uint32_t tmem = tc_setup<N>(sTmem, full0, empty0, done, sFail, warp, tid);
   const int KS = a.ks_count;
 
-  if (tid == 0)
+  // the producer thread alone waits for the accumulator; the other warps
+  // wait at the CTA barrier (no issue slots spent polling)
+  if (tid == 0) {
     tc_gemm_pipeline<N>(reinterpret_cast<const unsigned char*>(a.yt) + (vb * KS) * (int64_t)YS,
                         reinterpret_cast<const unsigned char*>(a.xt) + ((int64_t)db * KS) * (int64_t)PS, sbase,
                         full0, empty0, done, tmem, KS, a.err, sFail);
-  __syncwarp();
-  if (!mbar_wait(done, 0)) {
-    if (lane == 0) atomicCAS(a.err, 0, kDevLoopLimit);
-    *sFail = 1;
+    if (!mbar_wait(done, 0)) {
+      atomicCAS(a.err, 0, kDevLoopLimit);
+      *sFail = 1;
+    }
+    tc_fence_before();
   }
-  tc_fence_after();
   __syncthreads();
+  tc_fence_after();
 
   if (*sFail == 0) {
     // warp w reads TMEM lanes 32*(w%4).. (its 32 vertices) for the designs of
@@ -735,6 +743,9 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_qf_kernel(QfArgs a) {
     const int64_t v = vb * kTcM + q * 32 + lane;
     const bool live = v < a.V;
     const float yyv = live ? __ldg(a.yy + v) : 0.0f;
+    int jc[kQfMaxCoef];  // the requested coefficients (uniform)
+#pragma unroll
+    for (int ci = 0; ci < kQfMaxCoef; ++ci) jc[ci] = (ci < a.n_coef) ? __ldg(a.coef + ci) : 0;
     constexpr int DPW = DB / 2;  // designs per warp
     constexpr int DPL = 16 / R;  // designs per 16-column load
 #pragma unroll 1
@@ -745,27 +756,39 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_qf_kernel(QfArgs a) {
       for (int dd = 0; dd < DPL; ++dd) {
         const int g = db * DB + half * DPW + d0 + dd;
         if (g >= a.G) break;
-        const float* gi = a.ginv + (int64_t)g * KC * KC;
+        // b = inv(Xc'Xc) c from the padded R x R inverse, rows as float4
+        const float4* gi = reinterpret_cast<const float4*>(a.ginv + (int64_t)g * R * R);
         float b[KC];
         float qf = 0.0f;
 #pragma unroll
         for (int i = 0; i < KC; ++i) {
+          float row[R];
+#pragma unroll
+          for (int r4 = 0; r4 < (KC + 3) / 4; ++r4) {
+            const float4 x4 = __ldg(gi + i * (R / 4) + r4);
+            row[4 * r4] = x4.x;
+            row[4 * r4 + 1] = x4.y;
+            row[4 * r4 + 2] = x4.z;
+            row[4 * r4 + 3] = x4.w;
+          }
           float s = 0.0f;
 #pragma unroll
-          for (int j = 0; j < KC; ++j) s = fmaf(__ldg(gi + i * KC + j), cc[dd * R + j], s);
+          for (int j = 0; j < KC; ++j) s = fmaf(row[j], cc[dd * R + j], s);
           b[i] = s;
           qf = fmaf(cc[dd * R + i], s, qf);
         }
-        const float rss = fmaxf(yyv - qf, 0.0f);
-        const float inv_dof = 1.0f / __ldg(a.dof + g);
-        for (int ci = 0; ci < a.n_coef; ++ci) {
-          const int j = __ldg(a.coef + ci);
+        // sigma^2 = RSS / dof; t_j = b_j / sqrt(sigma^2 inv(X'X)_jj)
+        const float s2 = fmaxf(yyv - qf, 0.0f) / __ldg(a.dof + g);
+#pragma unroll
+        for (int ci = 0; ci < kQfMaxCoef; ++ci) {
+          if (ci >= a.n_coef) break;
+          const int j = jc[ci];
           float bj = __int_as_float(0x7fc00000);  // NaN for a coefficient outside [1, KC]
 #pragma unroll
           for (int jj = 0; jj < KC; ++jj)
             if (jj + 1 == j) bj = b[jj];
           const float dj = (j >= 1 && j <= KC) ? __ldg(a.invdiag + (int64_t)g * (KC + 1) + j) : 1.0f;
-          if (live) a.t_out[((int64_t)g * a.n_coef + ci) * a.ldt + v] = bj / sqrtf(rss * inv_dof * dj);
+          if (live) a.t_out[((int64_t)g * a.n_coef + ci) * a.ldt + v] = bj * rsqrtf(s2 * dj);
         }
       }
     }
@@ -836,10 +859,11 @@ int glm_tstat_tc_qf(const void* y_tiles, const float* yy, int32_t n, int32_t n_p
   TFGB_CHECK_ARG(y_tiles && yy && x_tiles && ginv && invdiag && dof && coef && t_out && err, "NULL pointer");
   TFGB_CHECK_ARG(kmax >= 2 && kmax <= tfgb::kTcRowsPerDesign, "kmax must be in [2, 8]");
   TFGB_CHECK_ARG(n > kmax && n_pad >= n && n_pad % tfgb::kTcK == 0, "n_pad must be >= n and a multiple of 16");
-  TFGB_CHECK_ARG(n_coef >= 1, "n_coef must be >= 1");
+  TFGB_CHECK_ARG(n_coef >= 1 && n_coef <= tfgb::kQfMaxCoef, "n_coef must be in [1, 8]");
   TFGB_CHECK_ARG(V >= 0 && G >= 0 && ldt >= V, "bad sizes");
-  TFGB_CHECK_ARG(reinterpret_cast<uintptr_t>(y_tiles) % 16 == 0 && reinterpret_cast<uintptr_t>(x_tiles) % 16 == 0,
-                 "tiles must be 16-byte aligned");
+  TFGB_CHECK_ARG(reinterpret_cast<uintptr_t>(y_tiles) % 16 == 0 && reinterpret_cast<uintptr_t>(x_tiles) % 16 == 0 &&
+                     reinterpret_cast<uintptr_t>(ginv) % 16 == 0,
+                 "tiles and ginv must be 16-byte aligned");
   if (V == 0 || G == 0) return TFCE_OK;
   tfgb::QfArgs a{};
   a.yt = static_cast<const __nv_bfloat16*>(y_tiles);

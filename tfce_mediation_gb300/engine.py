@@ -279,7 +279,7 @@ class PermutationEngine:
             R, Gp = tc.qf_rows(kmax), tc.qf_padded(P, kmax)
             keys = ("XR", "GI", "invd", "dof")
             slot["h_XR"] = t.zeros((Gp * R, tc.n_pad), dtype=t.float32, pin_memory=True)
-            slot["h_GI"] = t.zeros((Gp, kmax - 1, kmax - 1), dtype=t.float32, pin_memory=True)
+            slot["h_GI"] = t.zeros((Gp, R, R), dtype=t.float32, pin_memory=True)
             slot["d_xt"] = t.empty(int(self.lib.glm_tile_bytes(Gp * R, 256, tc.n_pad)), dtype=t.uint8,
                                    device="cuda")
         elif tc is not None:

@@ -278,7 +278,7 @@ class TensorCoreOperands:
         centred data, every design's first column all ones, kmax in [2, 8]
         and no coefficient 0 (designs with fewer columns are zero padded:
         their missing columns get zero cross products and inverse rows)."""
-        return (self.quadratic_form and self.yy is not None and 2 <= db.kmax <= 8
+        return (self.quadratic_form and self.yy is not None and 2 <= db.kmax <= 8 and 1 <= len(coef) <= 8
                 and min(int(c) for c in coef) >= 1 and self.centred_ok(db))
 
     def qf_rows(self, kmax):
@@ -291,18 +291,19 @@ class TensorCoreOperands:
     def host_operands_qf(self, db: DesignBatch, XR=None, GI=None):
         """Host float32 operands of the quadratic form: the centred design
         columns 1..k-1 stacked [G_pad*R][n_pad] (design d, column j at row
-        d*R + j - 1) and inv(Xc'Xc) = inv(X'X)[1:, 1:] [G_pad][k-1][k-1];
-        written into XR / GI when given (e.g. pinned buffers of those sizes)."""
+        d*R + j - 1) and inv(Xc'Xc) = inv(X'X)[1:, 1:] zero padded to
+        [G_pad][R][R]; written into XR / GI when given (e.g. pinned buffers of
+        those sizes)."""
         G, k, n = db.G, db.kmax, db.n
         R, Gp = self.qf_rows(k), self.qf_padded(G, k)
         xr = np.zeros((Gp, R, self.n_pad), np.float32) if XR is None else XR.reshape(Gp, R, self.n_pad)
-        gi = np.zeros((Gp, k - 1, k - 1), np.float32) if GI is None else GI.reshape(Gp, k - 1, k - 1)
+        gi = np.zeros((Gp, R, R), np.float32) if GI is None else GI.reshape(Gp, R, R)
         if XR is not None:
             xr[...] = 0.0
+            gi[...] = 0.0
         xc = db.X64[:, :, 1:] - db.X64[:, :, 1:].mean(axis=1, keepdims=True)
         xr[:G, :k - 1, :n] = xc.transpose(0, 2, 1)
-        gi[G:] = 0.0
-        gi[:G] = db.inverse()[:, 1:, 1:]
+        gi[:G, :k - 1, :k - 1] = db.inverse()[:, 1:, 1:]
         return xr.reshape(Gp * R, self.n_pad), gi
 
     def tile_designs_qf(self, XR_dev, G, kmax, out=None):
