@@ -900,7 +900,7 @@ def run_gpu(args):
     # public API, pipelined: each step hands the engine new pinned host data
     # and its permutations (PermutationEngine.run_stream: captured batch
     # graphs, host preparation of a batch overlapped with the previous one)
-    e2e_steps = max(2, min(args.steps, 8))
+    e2e_steps = max(2, min(args.steps, 30))
     pr_all = E.permutations(n, SEED, 10 ** 6 + base, 10 ** 6 + base + e2e_steps * P)
     eng.run_stream([(Yh, pr_all[:P])])  # capture outside the timed region
     torch.cuda.synchronize()

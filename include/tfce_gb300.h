@@ -328,6 +328,15 @@ int glm_stat_tc_block(const void* y_tiles, const float* y_shift, const float* Y,
                       const float* x_rows, int32_t n_sc, const float* invdiag, const float* dof, int32_t G,
                       int32_t kmax, int32_t design_block, int32_t mode, const int32_t* coef, int32_t n_coef,
                       const float* wmat, int32_t w_stride, float* t_out, int64_t ldt, int32_t* err, void* stream);
+/* Permutation index streams of the mmr-lr convention (tm_func.py:147-151):
+ * out[(p - start) * n + i] = numpy.random.RandomState(seed + p).permutation(n)[i]
+ * for p in [start, stop), bit for bit (MT19937 seeded from one 32-bit
+ * integer, Fisher-Yates from the last element with masked-rejection draws).
+ * Host work only, split over `threads` threads (0 = the hardware count).
+ * TFCE_EINVAL when a seed + p falls outside [0, 2^32 - 1] (RandomState's
+ * own range). */
+int perm_stream(int64_t n, int64_t seed, int64_t start, int64_t stop, int64_t* out, int32_t threads);
+
 /* Quadratic-form tensor-core GLM: t of coefficients >= 1 of designs whose
  * first column is all ones (the same t as cynumstats.pyx:28-64 / glm_tstat).
  * By Frisch-Waugh, with Xc the other columns minus their means and c =

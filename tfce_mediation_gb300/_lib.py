@@ -85,6 +85,8 @@ SIGNATURES = {
     "glm_tstat_tc": (ctypes.c_int, [c_vp, c_vp, c_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
                                     ctypes.c_int64, c_vp, c_vp, c_vp, ctypes.c_int32, c_vp, c_vp, ctypes.c_int32,
                                     ctypes.c_int32, c_vp, ctypes.c_int32, c_vp, ctypes.c_int64, c_vp, c_vp]),
+    "perm_stream": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, c_vp,
+                                   ctypes.c_int32]),
     "glm_qf_design_block": (ctypes.c_int, [ctypes.c_int32]),
     "glm_col_sumsq": (ctypes.c_int, [c_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int64, c_vp, c_vp]),
     "glm_tstat_tc_qf": (ctypes.c_int, [c_vp, c_vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, c_vp, c_vp,

@@ -21,7 +21,8 @@ OUTDIR = os.path.join(PKG, "_native")
 LIB = os.path.join(OUTDIR, "libtfce_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["capi.cu", "tfce_sweep.cu", "glm.cu", "glm_tc.cu", "fwer.cu", "mlp.cu", "rm_anova.cu", "gd_fwhm.cu", "geodesic.cu"]
+SOURCES = ["capi.cu", "tfce_sweep.cu", "glm.cu", "glm_tc.cu", "fwer.cu", "mlp.cu", "rm_anova.cu", "gd_fwhm.cu", "geodesic.cu",
+           "perm_stream.cu"]
 
 
 def nvcc() -> str:

@@ -21,6 +21,8 @@ operators go up and P x C x 2 x S maxima come down.
 """
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 
 from . import _lib
@@ -30,10 +32,15 @@ from .glm import OUT_NEG_T, OUT_T, DesignBatch, TensorCoreOperands, output_colum
 
 
 def permutations(n, seed, start, stop):
-    """Index streams of the mmr-lr convention (tm_func.py:147-151)."""
+    """Index streams of the mmr-lr convention (tm_func.py:147-151): row p is
+    numpy.random.RandomState(seed + p).permutation(n), generated by the
+    native library (perm_stream, bit-identical to numpy's)."""
     if stop <= start:
         return np.zeros((0, n), np.int64)
-    return np.stack([np.random.RandomState(seed + p).permutation(n) for p in range(start, stop)])
+    out = np.empty((stop - start, n), np.int64)
+    _lib.check(_lib.load().perm_stream(int(n), int(seed), int(start), int(stop),
+                                       out.ctypes.data_as(ctypes.c_void_p), 0))
+    return out
 
 
 class PermutationEngine:

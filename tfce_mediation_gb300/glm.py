@@ -66,30 +66,41 @@ class DesignBatch:
 
     def __init__(self, designs, invXX=None, kmax=None):
         if isinstance(designs, np.ndarray) and designs.ndim == 3:
-            mats = [designs[g] for g in range(designs.shape[0])]
+            Xs = np.array(designs, np.float64)
+            mats = None
+            G, n = Xs.shape[0], Xs.shape[1]
+            ks = [Xs.shape[2]] * G
         else:
             mats = [np.asarray(d, np.float64) for d in designs]
-        G = len(mats)
-        n = mats[0].shape[0]
-        ks = [m.shape[1] for m in mats]
+            G = len(mats)
+            n = mats[0].shape[0]
+            ks = [m.shape[1] for m in mats]
         kmax = kmax or max(ks)
         if kmax > 8:
             raise ValueError("at most 8 regressors per design")
-        pinv = np.zeros((G, kmax, n), np.float64)
-        Xp = np.zeros((G, n, kmax), np.float64)
         invdiag = np.zeros((G, kmax), np.float64)
         inv_p = np.zeros((G, kmax, kmax), np.float64)  # inv(X'X), zero padded
         same_k = len(set(ks)) == 1
+        self._pinv64 = None
         if same_k:
-            Xs = np.stack(mats).astype(np.float64)
-            inv = np.linalg.inv(np.einsum("gsi,gsj->gij", Xs, Xs))
+            if mats is not None:
+                Xs = np.stack(mats)
             k = ks[0]
-            pinv[:, :k, :] = np.einsum("gij,gsj->gis", inv, Xs)
-            Xp[:, :, :k] = Xs
+            inv = np.linalg.inv(np.einsum("gsi,gsj->gij", Xs, Xs))
+            # the stacked pseudoinverses are formed on first use (the
+            # quadratic-form GLM does not need them)
+            self._pinv_src = (inv, Xs, k)
+            if k == kmax:
+                Xp = Xs
+            else:
+                Xp = np.zeros((G, n, kmax), np.float64)
+                Xp[:, :, :k] = Xs
             di = np.diagonal(inv if invXX is None else np.asarray(invXX, np.float64), axis1=1, axis2=2)
             invdiag[:, :k] = di
             inv_p[:, :k, :k] = inv
         else:
+            pinv = np.zeros((G, kmax, n), np.float64)
+            Xp = np.zeros((G, n, kmax), np.float64)
             for g, m in enumerate(mats):
                 k = m.shape[1]
                 inv = np.linalg.inv(m.T @ m)
@@ -97,11 +108,21 @@ class DesignBatch:
                 pinv[g, :k] = inv @ m.T
                 Xp[g, :, :k] = m
                 invdiag[g, :k] = np.diag(inv if invXX is None else np.asarray(invXX[g], np.float64))
+            self._pinv64 = pinv
         self.G, self.n, self.kmax, self.ks = G, n, kmax, ks
-        self.pinv64, self.X64, self.invdiag64 = pinv, Xp, invdiag
-        self._mats = mats
+        self.X64, self.invdiag64 = Xp, invdiag
         self._inv64 = inv_p
         self.dof = np.asarray([n - k for k in ks], np.float64)
+
+    @property
+    def pinv64(self):
+        """(G, kmax, n) pinv(X_d) = inv(X'X) X' per design (zero padded), FP64."""
+        if self._pinv64 is None:
+            inv, Xs, k = self._pinv_src
+            pinv = np.zeros((self.G, self.kmax, self.n), np.float64)
+            pinv[:, :k, :] = np.einsum("gij,gsj->gis", inv, Xs)
+            self._pinv64 = pinv
+        return self._pinv64
 
     def inverse(self):
         """(G, kmax, kmax) inv(X'X) per design (zero padded), FP64."""
