@@ -699,7 +699,8 @@ def time_to_fwer(eng, st, n_perm=10_000, seed=99):
     tail (300 permutations + the margin fallback), and how far apart the
     two maps are where the plain p <= 0.05."""
     import torch
-    from tfce_mediation_gb300.tail import data, gpd
+    from tfce_mediation_gb300 import fwer
+    from tfce_mediation_gb300.tail import data
     from tfce_mediation_gb300.tail.surrogate import TailSurrogate, learned_fwer_maps
     _, maps, _ = eng.observed()
     V1 = int(st.segments[1])
@@ -711,7 +712,9 @@ def time_to_fwer(eng, st, n_perm=10_000, seed=99):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     mx = eng.run_graph(n_perm=n_perm, seed=seed).max(axis=-1)
-    plain = {c: [gpd.one_minus_p(maps[c, s_], mx[:, c, :].reshape(-1)) for s_ in range(2)] for c in range(eng.C)}
+    # the plain GPU path's own 1-p maps: one device sort of each contrast's null, device lookups
+    srt = {c: fwer.sorted_null(mx[:, c, :].reshape(-1)) for c in range(eng.C)}
+    plain = {c: [fwer.fwep_presorted(srt[c], maps[c, s_]) for s_ in range(2)] for c in range(eng.C)}
     torch.cuda.synchronize()
     plain_s = time.perf_counter() - t0
     m, info = learned_fwer_maps(eng, images, rho, 1.0, seed=seed, surrogate=sur)
@@ -728,7 +731,7 @@ def time_to_fwer(eng, st, n_perm=10_000, seed=99):
                              "max_abs_dp_where_p_le_0.05": worst, "vertices_p_le_0.05": nsig},
             "note": "1-p(FWER) maps of 4 contrasts x (+,-) of the observed study (calculate_fweP formula); "
                     "learned tail: MLP GPD tail from 300 permutations; vertices whose surrogate or small-sample p lies within "
-                    "0.02 of alpha get 1,200 more permutations"}
+                    "0.02 of alpha get at least 1,200 more permutations (rounded up to whole batches)"}
 
 
 def _one_thread_per_process():

@@ -384,7 +384,7 @@ class PermutationEngine:
         res = self.run_stream((None, perms[b:b + P]) for b in range(0, perms.shape[0], P))
         return np.concatenate(res) if res else np.zeros((0, self.C, self.signs, self.n_seg), np.float32)
 
-    def run_stream(self, steps):
+    def run_stream(self, steps, on_batch=None):
         """The pipelined public entry: one batch per item of `steps`, each a
         pair (data, perms) -- data: new (n, V) host data in the caller's
         vertex order (pinned memory keeps the copy asynchronous) or None to
@@ -397,6 +397,9 @@ class PermutationEngine:
         batch's GLM waits for it; each batch's maxima come back when its slot
         is reused or at the end.  A short batch is padded with its last row
         inside the captured graph and the padding discarded.
+        on_batch (optional): called as on_batch(i, maxima) as soon as step i's
+        maxima are back on the host, while later steps run on the device --
+        host work placed there overlaps the device.
         Returns the per-batch maxima, (rows, C, signs, n_seg) each."""
         t = self.t
         P = self.batch
@@ -415,6 +418,8 @@ class PermutationEngine:
             slot["event"].synchronize()
             results[slot["order"]] = slot["h_max"].numpy()[: slot["rows"]].copy()
             slot["busy"] = False
+            if on_batch is not None:
+                on_batch(slot["order"], results[slot["order"]])
 
         n_steps = 0
         for s_, (data, perms) in enumerate(steps):

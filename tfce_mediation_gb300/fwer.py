@@ -38,6 +38,17 @@ def fwep(tfce_image, null):
     return _lookup(sorted_null(null), tfce_image, 0).cpu().numpy()
 
 
+def fwep_presorted(srt, tfce_image):
+    """fwep against a null already sorted on the device (sorted_null), so
+    that several images share one sort; host float64."""
+    return _lookup(srt, tfce_image, 0).cpu().numpy()
+
+
+def lookup_presorted(srt, tfce_image):
+    """fwep_presorted left on the device (float64 tensor)."""
+    return _lookup(srt, tfce_image, 0)
+
+
 def nearest(values, null):
     return _lookup(sorted_null(null), values, 1).cpu().numpy()
 

@@ -17,6 +17,8 @@ import time
 
 import numpy as np
 
+from .. import fwer
+from ..device import dev
 from . import gpd
 from .mlp import MLP
 
@@ -30,41 +32,40 @@ class TailSurrogate:
         self.tm, self.ts = extra["targ_mean"], extra["targ_std"]
 
     def tail(self, null_small, n_vertices, smoothness, E, n, k):
-        f, m = gpd.features(null_small, n_vertices, smoothness, E, n, k)
-        pred = self.model.predict_bf16(((f - self.fm) / self.fs)[None])[0] * self.ts + self.tm
-        return gpd.decode(pred, m)
+        return self.tails([gpd.features(null_small, n_vertices, smoothness, E, n, k)])[0]
 
-
-def _maxima(eng, start, count, seed):
-    """(count, C, signs) per-permutation maxima (max over segments): whole
-    batches through the captured graphs, the remainder as one short batch
-    (no padding to a full batch)."""
-    P = eng.batch
-    full = count // P * P
-    parts = []
-    if full:
-        parts.append(eng.run_graph(start=start, stop=start + full, seed=seed))
-    if count > full:
-        parts.append(eng.run(start=start + full, stop=start + count, seed=seed))
-    return np.concatenate(parts).max(axis=-1)
+    def tails(self, feats):
+        """(u, xi, sigma) of several null samples in one BF16 inference:
+        feats = [(features, median), ...] from gpd.features (host work that
+        can run while permutations are still on the device)."""
+        F = np.stack([(f - self.fm) / self.fs for f, _ in feats])
+        pred = self.model.predict_bf16(F) * self.ts + self.tm
+        return [gpd.decode(pred[i], m) for i, (_, m) in enumerate(feats)]
 
 
 def _image_maps(img, srt, tail, alpha, margin):
-    """1-p of one image from a sorted null (model tail where given) and the
-    vertices to send back: the model's p or the sample's own empirical p
-    within `margin` of alpha.  Taking the union keeps a surrogate whose tail
-    is biased from moving a vertex across alpha unchecked: the empirical p of
-    the same sample flags it too."""
-    v = np.asarray(img, np.float64)
-    pos = v > 0
-    vp = v[pos]
-    emp = np.maximum(np.searchsorted(srt, vp, side="left") - 1, 0) / srt.shape[0]
-    model = emp if tail is None else gpd.apply_tail(emp.copy(), vp, *tail)
-    omp = np.zeros(v.shape[0])
-    omp[pos] = model
-    near = np.zeros(v.shape[0], bool)
-    near[pos] = (np.abs((1.0 - model) - alpha) <= margin) | (np.abs((1.0 - emp) - alpha) <= margin)
-    return omp, near
+    """1-p of one image from a null sorted on the device (fwer.sorted_null;
+    model tail where given) and the vertices to send back: the model's p or
+    the sample's own empirical p within `margin` of alpha.  Taking the union
+    keeps a surrogate whose tail is biased from moving a vertex across alpha
+    unchecked: the empirical p of the same sample flags it too.  Computed on
+    the device: the empirical p is the calculate_fweP lookup (fwer_lookup),
+    the tail and the flags elementwise."""
+    import torch
+    v = dev(np.ascontiguousarray(img, np.float32)).double()
+    emp = fwer.lookup_presorted(srt, v)
+    model = emp
+    if tail is not None:
+        u, xi, sigma = tail
+        y = (v - u) / sigma
+        if abs(xi) < 1e-9:
+            sf = torch.exp(-y)
+        else:
+            base = torch.clamp(1.0 + xi * y, min=0.0)
+            sf = torch.where(base > 0, base.pow(-1.0 / xi), torch.zeros_like(base))
+        model = torch.where(v > u, 1.0 - (1.0 - gpd.QUANT) * sf, emp)
+    near = (v > 0) & (((1.0 - model) - alpha).abs().le(margin) | ((1.0 - emp) - alpha).abs().le(margin))
+    return model.cpu().numpy(), near.cpu().numpy()
 
 
 def learned_fwer(eng, tfce_values, contrast, smoothness, E, alpha=0.05, margin=0.02, n_small=300,
@@ -81,25 +82,68 @@ def learned_fwer_maps(eng, images, smoothness, E, alpha=0.05, margin=0.02, n_sma
     """1-p(FWER) maps of several observed TFCE images at once.  images:
     {contrast index: image or list of images (e.g. the + and - images)}; the
     null of a contrast holds both signs' maxima of every permutation, as the
-    reference's CSV does.  One small permutation run serves every contrast;
-    one fallback run serves every vertex near alpha.  Returns ({contrast:
-    map or list of maps}, info)."""
+    reference's CSV does.  One permutation run serves every contrast: its
+    first n_small permutations give the model tails, and all of them (at
+    least n_small + n_fallback, rounded up to whole batches of the engine)
+    the empirical p of every vertex near alpha.  Returns ({contrast: map or list
+    of maps}, info)."""
     import torch
+    from ..engine import permutations
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    small = _maxima(eng, 0, n_small, seed)  # (n_small, C, signs)
+    # the fallback permutations run with the small sample, as one pipelined
+    # run: a whole-study map nearly always has vertices near alpha, and one
+    # run (one pipeline fill) costs less than two.  The fallback is rounded
+    # up to whole batches of the engine: a short last batch costs a full one
+    # on the device, so its permutations are used rather than padded away.
+    P = eng.batch
+    n_fallback = max(n_fallback, 0)
+    if n_fallback:
+        n_fallback = -(-(n_small + n_fallback) // P) * P - n_small
+    total = n_small + n_fallback
+    perms = permutations(eng.n, seed, 0, total)
+    need = -(-n_small // P)  # batches holding the small sample
+    got, fit = {}, {}
+
+    def small_sample():
+        return np.concatenate([got[i] for i in range(need)])[:n_small].max(axis=-1)  # (n_small, C, signs)
+
+    def host_fits():
+        # the tail fits of the small sample: host work
+        small = small_sample()
+        for c in images:
+            null = small[:, c, :].reshape(-1).astype(np.float64)
+            if method == "mlp":
+                fit[c] = gpd.features(null, eng.V, smoothness, E, eng.n, eng.k)
+            elif method == "gpd":
+                fit[c] = gpd.tail_params(null)
+            else:
+                fit[c] = None
+
+    def on_batch(i, maxima):
+        # once the small sample is back, its fits run while the fallback
+        # permutations are still on the device
+        got[i] = maxima
+        if not fit and all(j in got for j in range(need)):
+            host_fits()
+
+    res = eng.run_stream(((None, perms[b:b + P]) for b in range(0, total, P)), on_batch=on_batch)
+    both = np.concatenate(res).max(axis=-1)  # (total, C, signs)
+    small, more = both[:n_small], both[n_small:]
+    if not fit:
+        host_fits()
     sur = surrogate or (TailSurrogate() if method == "mlp" else None)
+    cs = list(images)
+    if method == "mlp":
+        tl = dict(zip(cs, sur.tails([fit[c] for c in cs])))
+    else:
+        tl = {c: fit[c] for c in cs}
     out, near_any, tails = {}, {}, {}
     for c, imgs in images.items():
-        null = small[:, c, :].reshape(-1).astype(np.float64)
-        tail = None
-        if method == "mlp":
-            tail = sur.tail(null, eng.V, smoothness, E, eng.n, eng.k)
-        elif method == "gpd":
-            tail = gpd.tail_params(null)
+        tail = tl[c]
         tails[c] = None if tail is None else [float(x) for x in tail]
         lst = imgs if isinstance(imgs, (list, tuple)) else [imgs]
-        srt = np.sort(null)
+        srt = fwer.sorted_null(small[:, c, :].reshape(-1))
         maps, nears = [], []
         for img in lst:
             omp, nr = _image_maps(img, srt, tail, alpha, margin)
@@ -108,9 +152,8 @@ def learned_fwer_maps(eng, images, smoothness, E, alpha=0.05, margin=0.02, n_sma
         out[c] = maps
         near_any[c] = nears
     n_near = int(sum(int(n.sum()) for v in near_any.values() for n in v))
-    used = n_small
+    used = n_small + n_fallback
     if n_near and n_fallback > 0:
-        more = _maxima(eng, n_small, n_fallback, seed)
         for c, imgs in images.items():
             srt = np.sort(np.concatenate([small[:, c, :].reshape(-1), more[:, c, :].reshape(-1)]).astype(np.float64))
             lst = imgs if isinstance(imgs, (list, tuple)) else [imgs]
@@ -118,7 +161,6 @@ def learned_fwer_maps(eng, images, smoothness, E, alpha=0.05, margin=0.02, n_sma
                 nr = near_any[c][i]
                 if nr.any():
                     out[c][i][nr] = gpd.one_minus_p(np.asarray(img)[nr], srt, presorted=True)
-        used += n_fallback
     torch.cuda.synchronize()
     res = {c: (m if isinstance(images[c], (list, tuple)) else m[0]) for c, m in out.items()}
     return res, {"perms": used, "seconds": time.perf_counter() - t0, "near_alpha": n_near, "tail": tails,
