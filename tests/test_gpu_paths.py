@@ -62,6 +62,25 @@ def test_mediation_engine_vs_oracle(med_study, medtype):
     _assert_maxima(got, ref)
 
 
+def test_mediation_run_stream_uploads_match_serial_runs(med_study):
+    """MediationEngine.run_stream with new data every step (uploads on a side
+    stream after the previous batch's GLM) returns exactly what upload + run
+    per step returns."""
+    import torch
+    st, x, dy = med_study
+    eng = E.MediationEngine(st.Y, x, dy, "M", (st.offsets, st.indices), st.segments, 2.0, 1.0,
+                            floor_zero=True, batch=8)
+    perms = E.permutations(st.n, 41, 0, 21)
+    rng = np.random.default_rng(12)
+    datas = [torch.from_numpy((st.Y + 0.3 * rng.standard_normal(st.Y.shape)).astype(np.float32)).pin_memory()
+             for _ in range(3)]
+    steps = [(datas[0], perms[:8]), (datas[1], perms[8:16]), (datas[2], perms[16:])]
+    got = eng.run_stream(steps)
+    for (d, pr), g in zip(steps, got):
+        eng.inner.upload(d)
+        np.testing.assert_array_equal(g, eng.run(perms=pr))
+
+
 def test_voxel_engine_E_half_vs_oracle():
     st = synth.config3(seed=3, n=48, shape=(26, 30, 24), semi=(11.0, 13.0, 10.0), fwhm=2.0)
     eng = E.PermutationEngine(st.Y, st.pred_x, (st.offsets, st.indices), None, 2.0, 0.5, batch=8)

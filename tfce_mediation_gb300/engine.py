@@ -559,24 +559,32 @@ class MediationEngine:
             ta.append(tas)
         return A, B, ta
 
-    def zmaps(self, perms, out=None):
-        """Indirect-effect z maps (P, V) on the device for permutation rows."""
-        P = len(perms)
+    def _designs(self, perms):
+        """Host work of a batch: the path designs (FP64 inverses) of the
+        permutation rows, as (DesignBatch, path-a t of medtype 'Y' or None)."""
         A, B, ta = self._paths(perms)
+        if self.medtype == "Y":
+            return DesignBatch(B, kmax=self.kmax), np.asarray(ta, np.float32)
+        return DesignBatch([m for pair in zip(A, B) for m in pair], kmax=self.kmax), None
+
+    def _zmaps_from(self, db, ta, P, out=None):
         inner = self.inner
         z = self._z[:P] if out is None else out
         lib = inner.lib
-        if self.medtype == "Y":
-            tm = inner.tmaps(DesignBatch(B, kmax=self.kmax))  # (P, 1, V)
-            tas = dev(np.asarray(ta, np.float32))
+        tm = inner.tmaps(db)
+        if self.medtype == "Y":  # tm (P, 1, V): path b
+            tas = dev(ta)
             _lib.check(lib.sobel_combine(None, self.V, ptr(tas), ptr(tm), self.V, P, self.V, self.alg_code,
                                          ptr(z), self.V, stream_handle()))
-        else:
-            designs = [m for pair in zip(A, B) for m in pair]
-            tm = inner.tmaps(DesignBatch(designs, kmax=self.kmax))  # (2P, 1, V): a, b, a, b ...
+        else:  # tm (2P, 1, V): a, b, a, b ...
             _lib.check(lib.sobel_combine(ptr(tm), 2 * self.V, None, ptr(tm) + 4 * self.V, 2 * self.V, P,
                                          self.V, self.alg_code, ptr(z), self.V, stream_handle()))
         return z
+
+    def zmaps(self, perms, out=None):
+        """Indirect-effect z maps (P, V) on the device for permutation rows."""
+        db, ta = self._designs(perms)
+        return self._zmaps_from(db, ta, len(perms), out)
 
     def run_batch(self, perms):
         """Maxima (P, 1, 1, n_seg) for the permutation index rows `perms`."""
@@ -598,11 +606,30 @@ class MediationEngine:
         if perms is None:
             stop = start + n_perm if stop is None else stop
             perms = permutations(self.n, seed, start, stop)
+        res = self.run_stream((None, perms[b:b + self.batch]) for b in range(0, perms.shape[0], self.batch))
+        return np.concatenate(res) if res else np.zeros((0, 1, 1, self.n_seg), np.float32)
+
+    def run_stream(self, steps):
+        """The pipelined public entry, as PermutationEngine.run_stream: one
+        batch per item (data, perms) of `steps` -- data: new (n, V) mediator
+        data from the host (pinned memory keeps the copy asynchronous) or None
+        to keep the resident data; perms: at most `batch` permutation rows.
+        A batch's path designs are formed on the host while the previous batch
+        runs on the device; new data is copied and re-tiled on a side stream
+        once the previous batch's GLM (the last reader of the resident data)
+        is done, and this batch's GLM waits for it; each batch's maxima are
+        read back after the next batch is queued.  Returns the per-batch
+        maxima, (rows, 1, 1, n_seg) each."""
         t = self.t
+        inner = self.inner
         if not hasattr(self, "_host_max"):
             self._host_max = [t.empty(self.batch * self.n_seg, dtype=t.float32, pin_memory=True) for _ in range(2)]
             self._max2 = [self._max.view(-1), t.empty_like(self._max.view(-1))]
             self._done = [t.cuda.Event(), t.cuda.Event()]
+            self._glm_done = [t.cuda.Event(), t.cuda.Event()]
+            self._up_stream = t.cuda.Stream()
+            self._up_done = t.cuda.Event()
+        main = t.cuda.current_stream()
         out, prev = [], None
 
         def collect(item):
@@ -610,22 +637,36 @@ class MediationEngine:
             self._done[k].synchronize()
             out.append(self._host_max[k][: P * self.n_seg].numpy().reshape(P, 1, 1, self.n_seg).copy())
 
-        for i, b in enumerate(range(0, perms.shape[0], self.batch)):
-            rows = perms[b:b + self.batch]
+        for i, (data, rows) in enumerate(steps):
+            rows = np.asarray(rows)
             P, k = len(rows), i % 2
-            z = self.zmaps(rows)
+            if P > self.batch:
+                raise ValueError("a step has more permutations than the engine's batch")
+            if P == 0:
+                out.append(np.zeros((0, 1, 1, self.n_seg), np.float32))
+                continue
+            db, ta = self._designs(rows)  # host work, overlapping the previous batch
+            if data is not None:
+                up = self._up_stream
+                up.wait_stream(main) if prev is None else up.wait_event(self._glm_done[prev[0]])
+                with t.cuda.stream(up):
+                    inner.upload(data)
+                self._up_done.record(up)
+                main.wait_event(self._up_done)
+            z = self._zmaps_from(db, ta, P)
+            self._glm_done[k].record(main)
             mx = self._max2[k][: P * self.n_seg]
-            self.inner.adj.sweep_batch(ptr(z), self.V, P, 1, ptr(self.inner.vd), int(self.inner.floor_zero),
-                                       ptr(mx), None, 0, stream_handle())
+            inner.adj.sweep_batch(ptr(z), self.V, P, 1, ptr(inner.vd), int(inner.floor_zero),
+                                  ptr(mx), None, 0, stream_handle())
             self._host_max[k][: P * self.n_seg].copy_(mx, non_blocking=True)
-            self._done[k].record()
+            self._done[k].record(main)
             if prev is not None:
                 collect(prev)
             prev = (k, P)
         if prev is not None:
             collect(prev)
-        self.inner.status()
-        return np.concatenate(out) if out else np.zeros((0, 1, 1, self.n_seg), np.float32)
+        inner.status()
+        return out
 
     def observed(self):
         """Unpermuted z map (V,) and scaled TFCE map (V,) on the host."""
