@@ -83,3 +83,22 @@ def test_new_entries_reject_invalid_arguments_on_host():
     assert lib.glm_stat_tc(one, None, one, None, 16, 16, 16, 16, one, None, one, 32, one, one, 1, 5, 9, one, 1,
                            None, 0, one, 16, one, None) == E
     assert b"mode" in lib.tfce_last_error()
+
+
+def test_quadratic_form_glm_arguments_are_rejected_on_host():
+    """glm_tstat_tc_qf checks its sizes and pointers before any device work:
+    kmax outside [2, 8], more than 8 coefficients, n_pad not a multiple of 16
+    or below n, and NULL operands are TFCE_EINVAL."""
+    lib = _lib.load()
+    assert lib.glm_qf_design_block(5) == 64 and lib.glm_qf_design_block(8) == 32
+    assert lib.glm_qf_design_block(1) == -1 and lib.glm_qf_design_block(9) == -1
+    fake = ctypes.c_void_p(256)  # never dereferenced: every call below fails its host checks
+
+    def call(n=100, n_pad=112, V=10, G=4, kmax=5, n_coef=2, ptrs=True, ldt=10):
+        p = fake if ptrs else None
+        return lib.glm_tstat_tc_qf(p, p, n, n_pad, V, p, p, p, p, G, kmax, p, n_coef, p, ldt, p, None)
+
+    for kw in ({"kmax": 1}, {"kmax": 9}, {"n_coef": 0}, {"n_coef": 9}, {"n_pad": 100}, {"n_pad": 96},
+               {"ptrs": False}, {"ldt": 5}, {"n": 5, "n_pad": 16}):
+        assert call(**kw) == _lib.TFCE_EINVAL, kw
+    assert lib.glm_col_sumsq(None, 10, 5, 10, None, None) == _lib.TFCE_EINVAL

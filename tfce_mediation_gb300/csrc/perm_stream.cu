@@ -106,11 +106,18 @@ extern "C" int perm_stream(int64_t n, int64_t seed, int64_t start, int64_t stop,
   }
   std::vector<std::thread> pool;
   const int64_t per = (rows + nt - 1) / nt;
+  int64_t done = 0;  // rows handed to threads
   for (int64_t t = 0; t < nt; ++t) {
     const int64_t r0 = t * per, r1 = std::min(rows, r0 + per);
     if (r0 >= r1) break;
-    pool.emplace_back(tfgb::fill_rows, n, first, r0, r1, out);
+    try {
+      pool.emplace_back(tfgb::fill_rows, n, first, r0, r1, out);
+    } catch (...) {
+      break;  // no more threads: the calling thread fills the rest
+    }
+    done = r1;
   }
+  if (done < rows) tfgb::fill_rows(n, first, done, rows, out);
   for (auto& th : pool) th.join();
   return TFCE_OK;
 }

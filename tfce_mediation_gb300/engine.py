@@ -410,6 +410,10 @@ class PermutationEngine:
         if not hasattr(self, "_up_stream"):
             self._up_stream = t.cuda.Stream()
             self._up_done = t.cuda.Event()
+        for slot in self._slots:
+            if slot.get("busy"):  # left by a call that raised: drain it, its maxima are not this call's
+                slot["event"].synchronize()
+                slot["busy"] = False
         main = t.cuda.current_stream()
         results = {}
         prev = None
