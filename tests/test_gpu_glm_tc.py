@@ -227,3 +227,25 @@ def test_quadratic_form_mixed_k_designs():
         ref = oracle.tval_fp64(Xg, Y)[[1]]
         assert _err(t_qf[g], ref) <= TOL, (g, _err(t_qf[g], ref))
     assert _err(t_qf, t_res.astype(np.float64)) <= TOL
+
+
+def test_quadratic_form_coefficient_outside_design_is_nan():
+    """A requested coefficient outside [1, kmax) gives a NaN row through the
+    C ABI (the documented behaviour), the other rows unaffected."""
+    import torch
+    from tfce_mediation_gb300.device import dev
+    rng = np.random.default_rng(3)
+    n, V, G, k = 80, 600, 10, 4
+    Y = rng.standard_normal((n, V)).astype(np.float32)
+    X = np.column_stack([np.ones(n), rng.standard_normal((n, k - 1))])
+    db = DesignBatch(np.stack([X[rng.permutation(n)] for _ in range(G)]))
+    ops = TensorCoreOperands(torch.from_numpy(Y).cuda())
+    XR, GI = ops.host_operands_qf(db)
+    xt = ops.tile_designs_qf(dev(XR), G, k)
+    out = torch.empty((G, 2, V), device="cuda")
+    ops.tstat_qf(xt, dev(GI), dev(db.invdiag64.astype(np.float32)), dev(db.dof.astype(np.float32)), G, k,
+                 dev(np.array([2, 7], np.int32)), 2, out, V)
+    got = out.cpu().numpy()
+    assert np.isnan(got[:, 1]).all()
+    ref = np.stack([oracle.tval_fp64(db.X64[g], Y)[2] for g in range(G)])
+    assert _err(got[:, 0], ref) <= TOL
