@@ -703,6 +703,67 @@ struct QfArgs {
   int32_t* err;
 };
 
+// The quadratic-form epilogue of one warp: the DB/2 designs of the tile from
+// design `dfirst` on (global index gbase + dfirst + ...), read from the TMEM
+// accumulator columns at `tacc` (lane quarter included) for vertex v of this
+// lane.  Every lane works on the same design at a time, so the per-design
+// constants are warp-uniform loads and the t stores coalesce over the vertices.
+template <int KC>
+__device__ __forceinline__ void qf_epilogue_warp(const QfArgs& a, uint32_t tacc, int dfirst, int gbase, int64_t v) {
+  constexpr int R = qf_rows(KC), DB = qf_db(KC);
+  const bool live = v < a.V;
+  const float yyv = live ? __ldg(a.yy + v) : 0.0f;
+  int jc[kQfMaxCoef];  // the requested coefficients (uniform)
+#pragma unroll
+  for (int ci = 0; ci < kQfMaxCoef; ++ci) jc[ci] = (ci < a.n_coef) ? __ldg(a.coef + ci) : 0;
+  constexpr int DPW = DB / 2;  // designs per warp
+  constexpr int DPL = 16 / R;  // designs per 16-column load
+#pragma unroll 1
+  for (int d0 = 0; d0 < DPW; d0 += DPL) {
+    float cc[16];
+    tmem_ld16(tacc + d0 * R, cc);
+#pragma unroll
+    for (int dd = 0; dd < DPL; ++dd) {
+      const int g = gbase + dfirst + d0 + dd;
+      if (g >= a.G) break;
+      // b = inv(Xc'Xc) c from the padded R x R inverse, rows as float4
+      const float4* gi = reinterpret_cast<const float4*>(a.ginv + (int64_t)g * R * R);
+      float b[KC];
+      float qf = 0.0f;
+#pragma unroll
+      for (int i = 0; i < KC; ++i) {
+        float row[R];
+#pragma unroll
+        for (int r4 = 0; r4 < (KC + 3) / 4; ++r4) {
+          const float4 x4 = __ldg(gi + i * (R / 4) + r4);
+          row[4 * r4] = x4.x;
+          row[4 * r4 + 1] = x4.y;
+          row[4 * r4 + 2] = x4.z;
+          row[4 * r4 + 3] = x4.w;
+        }
+        float s = 0.0f;
+#pragma unroll
+        for (int j = 0; j < KC; ++j) s = fmaf(row[j], cc[dd * R + j], s);
+        b[i] = s;
+        qf = fmaf(cc[dd * R + i], s, qf);
+      }
+      // sigma^2 = RSS / dof; t_j = b_j / sqrt(sigma^2 inv(X'X)_jj)
+      const float s2 = fmaxf(yyv - qf, 0.0f) / __ldg(a.dof + g);
+#pragma unroll
+      for (int ci = 0; ci < kQfMaxCoef; ++ci) {
+        if (ci >= a.n_coef) break;
+        const int j = jc[ci];
+        float bj = __int_as_float(0x7fc00000);  // NaN for a coefficient outside [1, KC]
+#pragma unroll
+        for (int jj = 0; jj < KC; ++jj)
+          if (jj + 1 == j) bj = b[jj];
+        const float dj = (j >= 1 && j <= KC) ? __ldg(a.invdiag + (int64_t)g * (KC + 1) + j) : 1.0f;
+        if (live) a.t_out[((int64_t)g * a.n_coef + ci) * a.ldt + v] = bj * rsqrtf(s2 * dj);
+      }
+    }
+  }
+}
+
 template <int KC>
 __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_qf_kernel(QfArgs a) {
   constexpr int R = qf_rows(KC), DB = qf_db(KC), N = kQfN;
@@ -735,63 +796,9 @@ __global__ void __launch_bounds__(kTcThreads, 2) glm_tc_qf_kernel(QfArgs a) {
   tc_fence_after();
 
   if (*sFail == 0) {
-    // warp w reads TMEM lanes 32*(w%4).. (its 32 vertices) for the designs of
-    // tile half w/4; every lane of a warp works on the same design at a time,
-    // so the per-design constants are warp-uniform loads and the t stores
-    // coalesce over the vertices
     const int q = warp & 3, half = warp >> 2;
-    const int64_t v = vb * kTcM + q * 32 + lane;
-    const bool live = v < a.V;
-    const float yyv = live ? __ldg(a.yy + v) : 0.0f;
-    int jc[kQfMaxCoef];  // the requested coefficients (uniform)
-#pragma unroll
-    for (int ci = 0; ci < kQfMaxCoef; ++ci) jc[ci] = (ci < a.n_coef) ? __ldg(a.coef + ci) : 0;
-    constexpr int DPW = DB / 2;  // designs per warp
-    constexpr int DPL = 16 / R;  // designs per 16-column load
-#pragma unroll 1
-    for (int d0 = 0; d0 < DPW; d0 += DPL) {
-      float cc[16];
-      tmem_ld16(tmem + (static_cast<uint32_t>(q * 32) << 16) + (half * DPW + d0) * R, cc);
-#pragma unroll
-      for (int dd = 0; dd < DPL; ++dd) {
-        const int g = db * DB + half * DPW + d0 + dd;
-        if (g >= a.G) break;
-        // b = inv(Xc'Xc) c from the padded R x R inverse, rows as float4
-        const float4* gi = reinterpret_cast<const float4*>(a.ginv + (int64_t)g * R * R);
-        float b[KC];
-        float qf = 0.0f;
-#pragma unroll
-        for (int i = 0; i < KC; ++i) {
-          float row[R];
-#pragma unroll
-          for (int r4 = 0; r4 < (KC + 3) / 4; ++r4) {
-            const float4 x4 = __ldg(gi + i * (R / 4) + r4);
-            row[4 * r4] = x4.x;
-            row[4 * r4 + 1] = x4.y;
-            row[4 * r4 + 2] = x4.z;
-            row[4 * r4 + 3] = x4.w;
-          }
-          float s = 0.0f;
-#pragma unroll
-          for (int j = 0; j < KC; ++j) s = fmaf(row[j], cc[dd * R + j], s);
-          b[i] = s;
-          qf = fmaf(cc[dd * R + i], s, qf);
-        }
-        // sigma^2 = RSS / dof; t_j = b_j / sqrt(sigma^2 inv(X'X)_jj)
-        const float s2 = fmaxf(yyv - qf, 0.0f) / __ldg(a.dof + g);
-#pragma unroll
-        for (int ci = 0; ci < kQfMaxCoef; ++ci) {
-          if (ci >= a.n_coef) break;
-          const int j = jc[ci];
-          float bj = __int_as_float(0x7fc00000);  // NaN for a coefficient outside [1, KC]
-#pragma unroll
-          for (int jj = 0; jj < KC; ++jj)
-            if (jj + 1 == j) bj = b[jj];
-          const float dj = (j >= 1 && j <= KC) ? __ldg(a.invdiag + (int64_t)g * (KC + 1) + j) : 1.0f;
-          if (live) a.t_out[((int64_t)g * a.n_coef + ci) * a.ldt + v] = bj * rsqrtf(s2 * dj);
-        }
-      }
-    }
+    qf_epilogue_warp<KC>(a, tmem + (static_cast<uint32_t>(q * 32) << 16) + half * (DB / 2) * R, half * (DB / 2),
+                         db * DB, vb * kTcM + q * 32 + lane);
   }
   tc_fence_before();
   __syncthreads();
