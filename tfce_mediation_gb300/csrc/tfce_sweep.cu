@@ -739,10 +739,13 @@ __global__ void __launch_bounds__(kSweepThreads, kMinBlocks) tfce_sweep_kernel(S
             // d is no longer a root: no other thread writes its record in this
             // phase.  Atomics on the final root: extent, and the largest sum
             // (sums are >= 0, so their bit patterns order as the values do).
-            const Rec8 rd = rec8[d[k]];
+            // A position of this step still holds its bucketing record {0, 1}:
+            // records change only on final roots, and sums only from (A') on.
+            const bool fresh = q0 + k >= nd;
+            const Rec8 rd = fresh ? Rec8{0.0f, 1} : rec8[d[k]];
             atomicAdd(&rec8[c[k]].size, rd.size);
             if (c[k] != pd[k]) st_state(sl.parent + d[k], c[k]);
-            atomicMax(reinterpret_cast<unsigned int*>(&rec8[c[k]].w), __float_as_uint(rd.w));
+            if (rd.w > 0.0f) atomicMax(reinterpret_cast<unsigned int*>(&rec8[c[k]].w), __float_as_uint(rd.w));
           }
           continue;
         }
