@@ -512,10 +512,11 @@ __global__ void __launch_bounds__(kSweepThreads, kMinBlocks) tfce_sweep_kernel(S
         key = (static_cast<uint32_t>(lv) << kPosBits) | static_cast<uint32_t>(p);
         if (use_bm && lv == 0) atomicOr(&sAct[v >> 5], 1u << (v & 31));
         sl.order[p] = v;
-        sl.parent[p] = p;
+        // maxima-only form: parents and records are set one step ahead, for
+        // a step's contiguous positions at once (below and in (A'))
+        if constexpr (!kR8) sl.parent[p] = p;
         if constexpr (kLazy) {
-          if constexpr (kR8) rec8[p] = Rec8{0.0f, 1};
-          else sl.rec[p] = Rec{0.0, 1, 0};
+          if constexpr (!kR8) sl.rec[p] = Rec{0.0, 1, 0};
           // the vertex's list (start relative to the segment's, degree) by
           // position, so the union phase reads it without a dependent load;
           // -1: out of the packed range, read the offsets
@@ -528,6 +529,13 @@ __global__ void __launch_bounds__(kSweepThreads, kMinBlocks) tfce_sweep_kernel(S
         }
       }
       sl.key[v] = key;
+    }
+    if constexpr (kR8) {
+      if (L > 0)  // the first step's positions (sStart was set before the last barrier)
+        for (int32_t q = sStart[0] + tid; q < sStart[1]; q += nth) {
+          sl.parent[q] = q;
+          rec8[q] = Rec8{0.0f, 1};
+        }
     }
     __syncthreads();
     TFGB_PHASE_MARK(1);
@@ -844,6 +852,15 @@ __global__ void __launch_bounds__(kSweepThreads, kMinBlocks) tfce_sweep_kernel(S
               if (is_root[k]) nxt_roots[base + __popc(roots & ((1u << lane) - 1u))] = c[k];
             }
           }
+        }
+        if constexpr (kR8) {
+          // the next step's positions: read first by its union phase, after
+          // this phase's barrier
+          if (i + 1 < L)
+            for (int32_t q = s1 + tid; q < sStart[i + 2]; q += nth) {
+              sl.parent[q] = q;
+              rec8[q] = Rec8{0.0f, 1};
+            }
         }
         __syncthreads();
         if (tid == 0) sNRoots = sNext;
