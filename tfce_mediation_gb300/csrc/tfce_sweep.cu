@@ -375,6 +375,9 @@ __global__ void __launch_bounds__(kSweepThreads, kMinBlocks) tfce_sweep_kernel(S
   // Maxima-only form: float sums and extents in 8-byte records
   constexpr bool kR8 = kMaxOnly && TFGB_MAX_REC8;
   Rec8* const rec8 = reinterpret_cast<Rec8*>(sl.rec);
+  // and {vertex, packed list} of a position in one 8-byte record (the second
+  // half of the Rec region), so that bucketing scatters one store per vertex
+  int2* const vtx8 = reinterpret_cast<int2*>(sl.rec) + a.vcap;
 #ifdef TFGB_PHASE_PROFILE
   long long _pt = clock64();
 #endif
@@ -511,7 +514,7 @@ __global__ void __launch_bounds__(kSweepThreads, kMinBlocks) tfce_sweep_kernel(S
         const int32_t p = sStart[lv] + base + __popc(peers & ((1u << lane) - 1u));
         key = (static_cast<uint32_t>(lv) << kPosBits) | static_cast<uint32_t>(p);
         if (use_bm && lv == 0) atomicOr(&sAct[v >> 5], 1u << (v & 31));
-        sl.order[p] = v;
+        if constexpr (!kR8) sl.order[p] = v;
         // maxima-only form: parents and records are set one step ahead, for
         // a step's contiguous positions at once (below and in (A'))
         if constexpr (!kR8) sl.parent[p] = p;
@@ -521,8 +524,10 @@ __global__ void __launch_bounds__(kSweepThreads, kMinBlocks) tfce_sweep_kernel(S
           // position, so the union phase reads it without a dependent load;
           // -1: out of the packed range, read the offsets
           const int64_t e0 = a.offsets[v0 + v], deg = a.offsets[v0 + v + 1] - e0, rel = e0 - seg_e0;
-          reinterpret_cast<int32_t*>(sl.acc)[p] =
+          const int32_t packed =
               (deg <= 63 && rel >= 0 && rel < (int64_t(1) << 25)) ? static_cast<int32_t>((rel << 6) | deg) : -1;
+          if constexpr (kR8) vtx8[p] = make_int2(v, packed);
+          else reinterpret_cast<int32_t*>(sl.acc)[p] = packed;
         } else {
           sl.size[p] = 1;
           sl.acc[p] = (a.out_mode == 2 && omap) ? omap[v] : 0.0f;
@@ -625,12 +630,19 @@ __global__ void __launch_bounds__(kSweepThreads, kMinBlocks) tfce_sweep_kernel(S
       for (int32_t p = atomicAdd(&sGrab, 1); p < s1; p = atomicAdd(&sGrab, 1)) {
         int32_t v = -1;  // the vertex: read when needed
         int64_t e0, e1;
-        const int32_t pk = kLazy ? reinterpret_cast<const int32_t*>(sl.acc)[p] : -1;
+        int32_t pk = -1;
+        if constexpr (kR8) {
+          const int2 r = vtx8[p];
+          v = r.x;
+          pk = r.y;
+        } else if constexpr (kLazy) {
+          pk = reinterpret_cast<const int32_t*>(sl.acc)[p];
+        }
         if (pk >= 0) {
           e0 = seg_e0 + (pk >> 6);
           e1 = e0 + (pk & 63);
         } else {
-          v = sl.order[p];
+          if (v < 0) v = sl.order[p];
           e0 = a.offsets[v0 + v];
           e1 = a.offsets[v0 + v + 1];
         }
@@ -673,7 +685,7 @@ __global__ void __launch_bounds__(kSweepThreads, kMinBlocks) tfce_sweep_kernel(S
             if (la == i && (kChecked || (raw[k] & kOneWay))) {
               // one-directional entry: effective only if the neighbour was
               // inserted first (larger value; ties by smaller index)
-              if (v < 0) v = sl.order[p];
+              if (v < 0) v = sl.order[p];  // (set above in the maxima-only form)
               const float xa = sign * x[an[k]], xv = sign * x[v];
               if (!(xa > xv || (xa == xv && an[k] < v))) continue;
             }
@@ -692,7 +704,7 @@ __global__ void __launch_bounds__(kSweepThreads, kMinBlocks) tfce_sweep_kernel(S
         // the next step's vertices become active (read after two more barriers)
         const int32_t s2 = sStart[i + 2];
         for (int32_t q = s1 + tid; q < s2; q += nth) {
-          const int32_t vq = sl.order[q];
+          const int32_t vq = kR8 ? vtx8[q].x : sl.order[q];
           atomicOr(&sAct[vq >> 5], 1u << (vq & 31));
         }
       }
