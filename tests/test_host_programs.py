@@ -381,3 +381,30 @@ def test_cosinor_closed_forms_random(seed):
         t_acro = a2 / (sigma * np.sqrt(inv[c_, c_] * b[s_] ** 2 + cr + inv[s_, s_] * b[c_] ** 2))
         np.testing.assert_allclose(t_amp, res[9][i], rtol=1e-6)
         np.testing.assert_allclose(t_acro, res[10][i], rtol=1e-6)
+
+
+def test_design_batch_operators():
+    """DesignBatch's host operators: inv(X'X) zero padded for designs of fewer
+    columns, pinv = inv(X'X) X' (formed on first use for same-k batches),
+    diag and dof, and the quadratic form's inv(Xc'Xc) = inv(X'X)[1:, 1:]."""
+    import numpy as np
+    from tfce_mediation_gb300.glm import DesignBatch
+    rng = np.random.default_rng(4)
+    n = 40
+    X = np.column_stack([np.ones(n), rng.standard_normal((n, 3))])
+    same = DesignBatch(np.stack([X[rng.permutation(n)] for _ in range(5)]))
+    assert same._pinv64 is None  # not formed until asked for
+    for g in range(5):
+        Xg = same.X64[g]
+        inv = np.linalg.inv(Xg.T @ Xg)
+        np.testing.assert_allclose(same.inverse()[g], inv, rtol=1e-12, atol=1e-14)
+        np.testing.assert_allclose(same.pinv64[g], inv @ Xg.T, rtol=1e-10, atol=1e-13)
+        np.testing.assert_allclose(same.invdiag64[g], np.diag(inv), rtol=1e-12)
+        Xc = Xg[:, 1:] - Xg[:, 1:].mean(axis=0)
+        np.testing.assert_allclose(same.inverse()[g][1:, 1:], np.linalg.inv(Xc.T @ Xc), rtol=1e-10, atol=1e-14)
+    assert same.dof.tolist() == [n - 4] * 5
+    mixed = DesignBatch([X[:, :2], X, X[:, :3]], kmax=4)
+    assert mixed.kmax == 4 and mixed.dof.tolist() == [n - 2, n - 4, n - 3]
+    assert np.all(mixed.inverse()[0, 2:, :] == 0) and np.all(mixed.inverse()[0, :, 2:] == 0)
+    assert np.all(mixed.X64[2, :, 3] == 0) and np.all(mixed.pinv64[0, 2:] == 0)
+    np.testing.assert_allclose(mixed.inverse()[2, :3, :3], np.linalg.inv(X[:, :3].T @ X[:, :3]), rtol=1e-12)
