@@ -4,7 +4,9 @@ Workload (the headline configuration): two icosphere-L7 hemispheres
 (2 x 163,842 = 327,684 vertices, triangle-edge adjacency), n = 350 subjects,
 k = 5 regressors (intercept, group, age, sex, covariate), 4 contrasts x (+,-)
 x 2 hemispheres = 16 TFCE sweeps per permutation, H = 2, E = 1.  A step is one
-batch of P permutations: one glm_tstat launch and one tfce_sweep_batch launch.
+batch of P permutations: the tiling of the batch's centred design columns, one
+tensor-core GLM launch (glm_tstat_tc_qf, or the form the autotuner keeps) and
+one tfce_sweep_batch launch.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--batch P]
   python bench.py --impl reference ...   # the reference's CPU algorithm (oracle port)
